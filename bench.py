@@ -1,0 +1,380 @@
+#!/usr/bin/env python3
+"""Benchmark of the semi-Lagrangian stream + collide step on GB300.
+
+Workload (one "step" = one fused stream + collide time step over the whole
+field): 3-D Taylor-Green vortex, D3Q19, BGK, semi-Lagrangian streaming on a
+periodic cube [0, 2 pi)^3 with 16^3 hexahedra and FE_DGQ order 4 (125
+nodes / cell, 512,000 nodes x 19), Ma = 0.1, Re = 1600, CFL = 0.4;
+synthetic analytic initial state, equilibrium-initialised.
+
+value:   node updates/s of the FP32-deviation path with f resident in HBM
+         (device time from CUDA events around each step; L2 flushed by a
+         256 MiB write between timed steps, outside the events).
+e2e:     the same metric through the C ABI with host buffers: each step
+         uploads f (FP64, pinned host memory), runs the step and reads rho
+         and u back.
+fp64_plain: the plain FP64 path on the same workload.
+roofline: algorithmic bytes per step = 2 Q s_f per node (f read once,
+         written once) over the measured HBM copy bandwidth.
+cpu_baseline: the CPU oracle (FP64 restatement of the reference algorithm:
+         copy + per-direction CSR SpMV + collide sweep, OpenMP) on a bounded
+         sample of the same workload.
+
+--impl reference: the reference's CPU path cannot be built (deal.II,
+Trilinos, p4est, Boost, MPI absent); its algorithm restated in the oracle
+is timed on all host threads on the same workload instead.
+
+Multi-GPU (torchrun): replicas only -- every rank runs the same solve on its
+own GPU, value = total node updates / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(
+    name="tgv3d_d3q19_bgk_sl_dg_p4_16x16x16",
+    stencil="D3Q19", cells=(16, 16, 16), order=4, topology="dg", collision="BGK_STANDARD",
+    Ma=0.1, Re=1600.0, cfl=0.4, L=2 * math.pi,
+)
+METRIC = "node updates/s (semi-Lagrangian stream + collide)"
+UNIT = "node_updates/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def spec_for(precision: str):
+    import natrium_gb300 as N
+    w = WORKLOAD
+    scaling = math.sqrt(3) / w["Ma"]
+    nu = 1.0 / w["Re"]  # U = 1, characteristic length 1 (TaylorGreenVortex3D.cpp:21)
+    return N.SolverSpec(stencil=w["stencil"], order=w["order"], cells=w["cells"], length=(w["L"],) * 3,
+                        scaling=scaling, viscosity=nu, cfl=w["cfl"], collision=w["collision"],
+                        precision=precision, topology=w["topology"])
+
+
+def initial_state(spec):
+    from natrium_gb300 import problems as P
+    X = P.node_coords(spec.cells, spec.order, spec.length, spec.topology)
+    rho, u = P.taylor_green_3d(X, WORKLOAD["Ma"])
+    return P.equilibrium(spec.stencil, spec.scaling, rho, u * 1.0)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def time_device(sol, torch, stream, flush, steps: int, warmup: int):
+    """Per-step CUDA-event timing on the solver's stream, L2 flushed between
+    steps outside the events.  Returns (per-step ms list, launches)."""
+    for _ in range(warmup):
+        sol.step_async(1, write_macro=False)
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    l0 = sol.launches
+    for k in range(steps):
+        ev[k][0].record(stream)
+        sol.step_async(1, write_macro=False)
+        ev[k][1].record(stream)
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)
+    torch.cuda.synchronize()
+    sol.status()
+    return [a.elapsed_time(b) for a, b in ev], sol.launches - l0
+
+
+def time_e2e(sol, torch, f_host, rho_h, u_h, steps: int):
+    """C-ABI calls with host buffers: upload f, one step, read rho/u."""
+    sol.upload_f(f_host)
+    sol.step(1)
+    sol.download_macro()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sol.upload_f(f_host)
+        sol.step(1)
+        r, u = sol.download_macro()
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / steps
+
+
+def traffic_from_profile():
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            d = json.load(fh)
+        return d
+    except Exception:
+        return None
+
+
+def cpu_baseline(sample_cells=(8, 8, 8), steps=5):
+    """Oracle (FP64 restatement of the reference algorithm) on a bounded
+    sample of the workload: same stencil / order / topology, fewer cells."""
+    import oracle as O
+    w = WORKLOAD
+    st = O.stencil(w["stencil"], math.sqrt(3) / w["Ma"])
+    mesh = O.Mesh(3, sample_cells, w["order"], w["topology"] == "dg", (w["L"],) * 3)
+    dt = O.time_step(mesh.h_min(), w["order"], st.max_speed, w["cfl"])
+    tau = (1.0 / w["Re"]) / (dt * st.cs2) + 0.5
+    rho, u = O.tgv3d_init(mesh.coords(), w["Ma"])
+    f = O.equilibrium(st, rho, np.ascontiguousarray(u))
+    S = O.SLOperator(mesh, st, dt)
+    threads = O.max_threads()
+    S.step_bgk(f, tau, 1, threads)
+    t0 = time.perf_counter()
+    S.step_bgk(f, tau, steps, threads)
+    el = (time.perf_counter() - t0) / steps
+    return {"value": mesh.n_nodes / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{w['stencil']} BGK FE_DGQ p={w['order']}, {sample_cells[0]}^3 cells "
+                      f"({mesh.n_nodes} nodes), {steps} timed steps of copy + CSR SpMV + collide, FP64, "
+                      f"{threads} OpenMP threads"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    import oracle as O
+    w = WORKLOAD
+    st = O.stencil(w["stencil"], math.sqrt(3) / w["Ma"])
+    mesh = O.Mesh(3, w["cells"], w["order"], w["topology"] == "dg", (w["L"],) * 3)
+    dt = O.time_step(mesh.h_min(), w["order"], st.max_speed, w["cfl"])
+    tau = (1.0 / w["Re"]) / (dt * st.cs2) + 0.5
+    rho, u = O.tgv3d_init(mesh.coords(), w["Ma"])
+    f = O.equilibrium(st, rho, np.ascontiguousarray(u))
+    S = O.SLOperator(mesh, st, dt)
+    threads = O.max_threads()
+    S.step_bgk(f, tau, max(args.warmup, 1), threads)
+    t0 = time.perf_counter()
+    S.step_bgk(f, tau, args.steps, threads)
+    el = (time.perf_counter() - t0) / args.steps
+    v = mesh.n_nodes / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic TGV3D state)",
+        "config": {"workload": w["name"], "nodes": mesh.n_nodes, "stencil": w["stencil"], "order": w["order"],
+                   "topology": w["topology"], "cells": list(w["cells"])},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"full workload, {args.steps} steps; the reference (deal.II/Trilinos) cannot "
+                                   "be built, its algorithm is restated in oracle/natoracle.c"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import natrium_gb300 as N
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.Stream()
+    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+
+    # --- FP32-deviation path (headline) -------------------------------------
+    spec = spec_for("fp32dev")
+    f0 = initial_state(spec)
+    sol = N.Solver(spec)
+    sol.set_stream(stream.cuda_stream)
+    sol.upload_f(f0)
+    ncand, chosen = sol.autotune(10)
+    kinfo = sol.kernel_info()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    try:
+        smi_index = int(vis.split(",")[local]) if vis else local
+    except (ValueError, IndexError):
+        smi_index = local
+    if args.profile:
+        per, launches = time_device(sol, torch, stream, flush, args.steps, args.warmup)
+        print(json.dumps({"profile_run": True, "ms_per_step": sum(per) / args.steps, "launches": launches,
+                          "kernel": kinfo}))
+        sol.close()
+        return 0
+    with ClockSampler(smi_index) as clk:
+        per, launches = time_device(sol, torch, stream, flush, args.steps, args.warmup)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    total_ms = sum(per)
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms = total_ms / args.steps
+    nodes = sol.n_dev
+    value = ws * nodes * args.steps / (total_ms * 1e-3)
+    Q = sol.Q
+
+    # --- e2e through the C ABI with host buffers -------------------------------
+    f_host = torch.from_numpy(f0).pin_memory().numpy()
+    e2e_steps = max(5, min(50, args.steps // 20))
+    e2e_s = time_e2e(sol, torch, f_host, None, None, e2e_steps)
+    h2d = f0.nbytes
+    d2h = 8 * (1 + sol.D) * sol.n_ref
+    # correctness guard on the measured state: finite, mass near 1
+    rho, u = sol.download_macro()
+    ok = bool(np.all(np.isfinite(rho)) and abs(float(np.mean(rho)) - 1.0) < 1e-2)
+    sol.close()
+
+    # --- plain FP64 path ---------------------------------------------------------
+    spec64 = spec_for("fp64")
+    sol64 = N.Solver(spec64)
+    sol64.set_stream(stream.cuda_stream)
+    sol64.upload_f(f0)
+    sol64.autotune(3)
+    kinfo64 = sol64.kernel_info()
+    steps64 = max(3, args.steps // 4)
+    per64, _ = time_device(sol64, torch, stream, flush, steps64, args.warmup)
+    ms64 = sum(per64) / steps64
+    sol64.close()
+
+    hbm, peak_kind = peaks()
+    alg_bytes = 2 * Q * 4 * nodes
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    alg64 = 2 * Q * 8 * nodes
+    ach64 = alg64 / (ms64 * 1e-3) / 1e9
+    tr = traffic_from_profile()
+    traffic = None
+    if tr and tr.get("workload") == WORKLOAD["name"]:
+        traffic = tr.get("dram_bytes_per_launch")
+
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+    cpu = cpu_baseline() if ws == 1 else None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (analytic Taylor-Green initial state, equilibrium-initialised)",
+        "config": {"workload": WORKLOAD["name"], "nodes": nodes, "stencil": WORKLOAD["stencil"],
+                   "collision": WORKLOAD["collision"], "order": WORKLOAD["order"], "topology": WORKLOAD["topology"],
+                   "cells": list(WORKLOAD["cells"]), "storage": "fp32 deviation f - w_i",
+                   "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
+                   "parallelism": f"replicas x{ws}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "kernel": ("k_sl_step_v2" if kinfo["variant"] == 2 else "k_sl_step") + "<D3Q19,float,BGK>",
+                     "tile_nodes": kinfo["tile_nodes"], "threads": kinfo["threads"],
+                     "autotune": {"candidates": ncand, "chosen": chosen}},
+        "cpu_baseline": cpu,
+        "e2e": {"value": ws * nodes / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "fp64_plain": {"value": ws * nodes / (ms64 * 1e-3), "ms_per_step": ms64, "steps": steps64,
+                       "roofline_frac": ach64 / hbm, "achieved_gbs": ach64, "kernel": kinfo64},
+        "speedup_vs_fp64_plain": ms64 / ms,
+        "state_ok": ok,
+    }
+    print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--profile", action="store_true",
+                    help="lean run for ncu: FP32 device timing only (no e2e, FP64 leg, CPU baseline or clocks)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,198 @@
+/*
+ * natgpu.h -- C ABI of the GB300-native semi-Lagrangian stream + collide
+ * engine (libnatgpu.so).
+ *
+ * The entry points replace, for one CFDSolver-style time loop, the two
+ * operator interfaces of NATriuM that carry the hot path:
+ *
+ *   advection/AdvectionOperator.h:151-152 (virtual double stream(f_old, f, t)),
+ *   implemented by advection/SemiLagrangian.h:150-161 and inlined in
+ *   solver/CFDSolver.cpp:658-754 (copy f, BlockSparseMatrix::vmult, boundaries);
+ *
+ *   collision/CollisionModel.h:74-78 (virtual void collideAll(f, rho, u,
+ *   owned, inInitializationProcedure)), run in the time loop through
+ *   collision_advanced/CollisionSelection.h:60-232 -> CollisionOperator.h:26-111.
+ *
+ * Plain C: plain pointers and sizes, no C++ or torch types.  Every call
+ * returns an int status (NAT_OK == 0); no exception crosses the ABI.  The
+ * text of the last error of a handle is available from nat_last_error().
+ * A handle is thread-compatible, not thread-safe: one CUDA stream per handle.
+ *
+ * Distribution-function layout on the host (reference layout): Q blocks of
+ * n_ref doubles, block 0 = f_0 (the rest population, never streamed), blocks
+ * 1..Q-1 = the streamed directions in the stencil's own order (this is the
+ * order of DistributionFunctions::at(i), solver/DistributionFunctions.h:47-300).
+ * Inside a block the nodes are numbered lexicographically over the node
+ * lattice of the Cartesian mesh, x fastest:
+ *   NAT_TOPO_FEQ: (N_a * p + 1) nodes per axis (continuous FE_Q on
+ *                 Gauss-Lobatto points, the reference's semi-Lagrangian element,
+ *                 advection/SemiLagrangian.cpp:43-44; periodic duplicates kept);
+ *   NAT_TOPO_DG:  N_a * (p + 1) nodes per axis (FE_DGQArbitraryNodes).
+ * Macroscopic fields: rho[n_ref], u[D][n_ref] with u scaled (u_lattice *
+ * scaling), as the reference stores them (CollisionOperator.h:79-82).
+ */
+#ifndef NATGPU_H
+#define NATGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define NAT_OK 0
+#define NAT_ERR_INVALID_ARG 1
+#define NAT_ERR_OOM 2
+/* rho < 1e-10 in a collision: the reference throws CollisionException /
+ * DensityZeroException (collision_advanced/AuxiliaryCollisionFunctions.h:53-56,
+ * CollisionOperator.h:106-109) */
+#define NAT_ERR_DENSITY_UNDERFLOW 3
+#define NAT_ERR_NAN 4
+#define NAT_ERR_TIMEOUT 5
+#define NAT_ERR_CUDA 6
+#define NAT_ERR_UNSUPPORTED 7
+
+/* ---- stencils (stencils/*.cpp of the reference) ------------------------ */
+#define NAT_D2Q9 0
+#define NAT_D3Q19 1
+#define NAT_D3Q27 2
+#define NAT_D2Q25H 3
+
+/* ---- collision models (utilities/ConfigNames.h CollisionSchemeName) ---- */
+#define NAT_BGK_STANDARD 0      /* BGKCollision + BGKEquilibrium */
+#define NAT_BGK_INCOMPRESSIBLE 1 /* collision/BGKIncompressible.cpp (D2Q9) */
+#define NAT_KBC_STANDARD 2      /* collision/KBCStandard.cpp (D2Q9); D3Q27 extension */
+
+/* ---- node topology ----------------------------------------------------- */
+#define NAT_TOPO_FEQ 0
+#define NAT_TOPO_DG 1
+
+/* ---- storage precision ------------------------------------------------- */
+#define NAT_FP64 0     /* plain: f stored and computed in double */
+#define NAT_FP32_DEV 1 /* f - w_i stored in float, float arithmetic,
+                          compensated moment sums */
+
+/* Solver description.  Replaces the subset of SolverConfiguration /
+ * ProblemDescription that the stream + collide path reads. */
+typedef struct nat_spec {
+  int dim;          /* 2 or 3 */
+  int stencil;      /* NAT_D2Q9 ... */
+  int order;        /* FE order p (1..6) */
+  int topology;     /* NAT_TOPO_FEQ or NAT_TOPO_DG */
+  int cells[3];     /* uniform Cartesian cells per axis (unused axes: 1) */
+  double length[3]; /* box edge lengths; the box is [0, L_a) */
+  int periodic[3];  /* must be 1 on every used axis */
+  double scaling;   /* stencil scaling (e = scaling * unit vectors) */
+  double viscosity; /* kinematic viscosity nu */
+  double cfl;       /* used when dt <= 0: dt = CFL h_min / (sqrt(2) scaling p^2)
+                       (utilities/CFDSolverUtilities.cpp:92-100) */
+  double dt;        /* time step; <= 0 selects the CFL rule */
+  int collision;    /* NAT_BGK_STANDARD ... */
+  int precision;    /* NAT_FP64 or NAT_FP32_DEV */
+} nat_spec;
+
+typedef struct nat_solver nat_solver;
+
+/* Create a solver: allocates device buffers on the current CUDA device and
+ * assembles the streaming operator for dt (SemiLagrangian::setDeltaT ->
+ * updateSparsityPattern/reassemble, advection/SemiLagrangian.h:175-179). */
+int nat_create(const nat_spec* spec, nat_solver** out);
+int nat_destroy(nat_solver* s);
+
+/* Sizes: n_ref = nodes per block in the reference layout; n_dev = nodes per
+ * block on the device (periodic duplicates folded); Q, D. */
+int nat_sizes(const nat_solver* s, int64_t* n_ref, int64_t* n_dev, int* Q,
+              int* D);
+/* Time step and relaxation time tau = nu / (dt c_s^2) + 1/2
+ * (collision_advanced/AuxiliaryCollisionFunctions.h:63-68). */
+int nat_get_dt(const nat_solver* s, double* dt, double* tau);
+
+/* setDeltaT: rebuild the operator for a new time step
+ * (advection/SemiLagrangian.h:175-179). */
+int nat_set_dt(nat_solver* s, double dt);
+
+/* Bind the handle to a CUDA stream (cudaStream_t passed as void*); NULL =
+ * the legacy default stream. */
+int nat_set_stream(nat_solver* s, void* cuda_stream);
+
+/* Copy f (host, reference layout, Q * n_ref doubles) to the device. */
+int nat_upload_f(nat_solver* s, const double* f_host);
+/* Copy f back to the host (reference layout; periodic duplicates filled). */
+int nat_download_f(nat_solver* s, double* f_host);
+/* Copy rho (n_ref) and u (D * n_ref, scaled) of the last collision. */
+int nat_download_macro(nat_solver* s, double* rho_host, double* u_host);
+/* Copy rho and scaled u from the host to the device (the input of a
+ * collision with in_init != 0). */
+int nat_upload_macro(nat_solver* s, const double* rho_host,
+                     const double* u_host);
+
+/* AdvectionOperator::stream(f_old, f, t): f <- A f (semi-Lagrangian
+ * streaming of directions 1..Q-1, f_0 unchanged); writes dt to *dt_out when
+ * dt_out != NULL (the interface returns dt). */
+int nat_stream(nat_solver* s, double t, double* dt_out);
+
+/* CollisionModel::collideAll(f, rho, u, owned, inInitializationProcedure):
+ * in-place collision of every node; writes rho and (unless in_init) u.  With
+ * in_init != 0 the velocity is taken from the device copy of u. */
+int nat_collide(nat_solver* s, int in_init);
+
+/* n_steps of the CFDSolver loop body {stream(); collide();} fused into one
+ * kernel per step.  rho and u are written by the last step only.  Checks the
+ * device status word once at the end (synchronises the stream). */
+int nat_step(nat_solver* s, int n_steps);
+
+/* Same as nat_step but only enqueues the work (no synchronisation, no status
+ * check); pair with nat_status(). */
+int nat_step_async(nat_solver* s, int n_steps, int write_macro);
+
+/* Synchronise the handle's stream and return the device status
+ * (NAT_OK, NAT_ERR_DENSITY_UNDERFLOW, NAT_ERR_NAN); clears it. */
+int nat_status(nat_solver* s);
+
+/* Copy the text of the last error into buf (always NUL terminated). */
+int nat_last_error(const nat_solver* s, char* buf, size_t len);
+
+/* FP64 global reductions over the device state (mass = sum of rho over the
+ * lattice nodes with Gauss-Lobatto quadrature weights; kinetic energy
+ * 0.5 sum rho |u|^2 with the same weights, solver/PhysicalProperties.cpp:29-79);
+ * they use the macroscopic fields of the last collision. */
+int nat_mass_energy(nat_solver* s, double* mass, double* kinetic_energy);
+
+/* Device pointers of the current distribution buffer (Q blocks of n_dev
+ * values, double for NAT_FP64 and float (f - w_i) for NAT_FP32_DEV). */
+int nat_device_f(nat_solver* s, void** f_dev);
+
+/* Kernel choice for the fused step: 0 = automatic (the specialised kernel
+ * when an instantiation for this order / topology / tile exists and every
+ * departure point lies in the node's own or the adjacent upwind cell, the
+ * generic kernel otherwise), 1 = generic kernel only, 2 = specialised kernel
+ * required (NAT_ERR_UNSUPPORTED when none applies). */
+int nat_set_kernel_variant(nat_solver* s, int variant);
+/* The fused-step kernel in use: 1 generic, 2 specialised. */
+int nat_kernel_variant(const nat_solver* s);
+
+/* Autotuner: times `steps` fused steps with every kernel that applies to
+ * this configuration (each specialised tile shape and the generic kernel),
+ * keeps the fastest, and restores f and the status word afterwards.  Writes
+ * the number of candidates and the index of the chosen one (the generic
+ * kernel is the last) when the pointers are not NULL.  Synchronises. */
+int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen);
+
+/* The fused-step kernel in use: variant (1 generic, 2 specialised), tile
+ * extent in nodes, threads per CTA, dynamic shared memory per CTA. */
+int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* threads,
+                    int64_t* smem_bytes);
+
+/* Number of kernels this handle has launched (for launch accounting). */
+int64_t nat_launch_count(const nat_solver* s);
+
+/* Library version string. */
+const char* nat_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NATGPU_H */

@@ -1,0 +1,394 @@
+"""natrium_gb300 -- GB300-native semi-Lagrangian stream + collide for NATriuM.
+
+Python host mirror of the reference's operator interfaces for the hot path,
+on top of the C ABI of ``libnatgpu.so`` (``include/natgpu.h``):
+
+* :class:`Solver` -- one device-resident solve (the state a ``CFDSolver``
+  keeps in ``m_f``, ``m_density``, ``m_velocity``).
+* :class:`SemiLagrangian` -- ``AdvectionOperator::stream(f_old, f, t)``
+  (advection/SemiLagrangian.h:150-161) and ``setDeltaT`` (:175-179).
+* :class:`BGKStandard`, :class:`BGKIncompressible`, :class:`KBCStandard` --
+  ``CollisionModel::collideAll(f, rho, u, owned, inInitializationProcedure)``
+  (collision/CollisionModel.h:74-78).
+* :class:`DistributionFunctions` -- host mirror of
+  solver/DistributionFunctions.h: Q blocks of n doubles, block 0 = f_0.
+
+There is no CPU fallback: importing the package raises if the CUDA library is
+missing, and every call goes through the CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libnatgpu.so")
+
+# status codes (include/natgpu.h)
+NAT_OK = 0
+NAT_ERR_INVALID_ARG = 1
+NAT_ERR_OOM = 2
+NAT_ERR_DENSITY_UNDERFLOW = 3
+NAT_ERR_NAN = 4
+NAT_ERR_TIMEOUT = 5
+NAT_ERR_CUDA = 6
+NAT_ERR_UNSUPPORTED = 7
+
+STENCILS = {"D2Q9": 0, "D3Q19": 1, "D3Q27": 2, "D2Q25H": 3}
+STENCIL_DQ = {"D2Q9": (2, 9), "D3Q19": (3, 19), "D3Q27": (3, 27), "D2Q25H": (2, 25)}
+COLLISIONS = {"BGK_STANDARD": 0, "BGK_INCOMPRESSIBLE": 1, "KBC_STANDARD": 2}
+TOPOLOGIES = {"feq": 0, "dg": 1}
+PRECISIONS = {"fp64": 0, "fp32dev": 1}
+
+# every symbol include/natgpu.h declares
+EXPORTS = [
+    "nat_create", "nat_destroy", "nat_sizes", "nat_get_dt", "nat_set_dt", "nat_set_stream",
+    "nat_upload_f", "nat_download_f", "nat_download_macro", "nat_upload_macro", "nat_stream",
+    "nat_collide", "nat_step", "nat_step_async", "nat_status", "nat_last_error",
+    "nat_mass_energy", "nat_device_f", "nat_launch_count", "nat_version", "nat_set_kernel_variant",
+    "nat_kernel_variant", "nat_autotune", "nat_kernel_info",
+]
+
+
+class NatError(RuntimeError):
+    """Error returned through the C ABI (code + text of nat_last_error)."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class CollisionException(NatError):
+    """rho < 1e-10 in a collision (the reference's CollisionException /
+    DensityZeroException, collision_advanced/AuxiliaryCollisionFunctions.h:53-56)."""
+
+
+class _Spec(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int), ("stencil", C.c_int), ("order", C.c_int), ("topology", C.c_int),
+        ("cells", C.c_int * 3), ("length", C.c_double * 3), ("periodic", C.c_int * 3),
+        ("scaling", C.c_double), ("viscosity", C.c_double), ("cfl", C.c_double), ("dt", C.c_double),
+        ("collision", C.c_int), ("precision", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Load libnatgpu.so (fails loudly when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise ImportError(f"libnatgpu.so not found at {path}; build it with "
+                          "`python -m natrium_gb300.build` (nvcc, sm_103a)")
+    L = C.CDLL(path)
+    vp, dp, i64p = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)
+    L.nat_create.argtypes = [C.POINTER(_Spec), C.POINTER(vp)]
+    L.nat_destroy.argtypes = [vp]
+    L.nat_sizes.argtypes = [vp, i64p, i64p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.nat_get_dt.argtypes = [vp, dp, dp]
+    L.nat_set_dt.argtypes = [vp, C.c_double]
+    L.nat_set_stream.argtypes = [vp, vp]
+    L.nat_upload_f.argtypes = [vp, dp]
+    L.nat_download_f.argtypes = [vp, dp]
+    L.nat_download_macro.argtypes = [vp, dp, dp]
+    L.nat_upload_macro.argtypes = [vp, dp, dp]
+    L.nat_stream.argtypes = [vp, C.c_double, dp]
+    L.nat_collide.argtypes = [vp, C.c_int]
+    L.nat_step.argtypes = [vp, C.c_int]
+    L.nat_step_async.argtypes = [vp, C.c_int, C.c_int]
+    L.nat_status.argtypes = [vp]
+    L.nat_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+    L.nat_mass_energy.argtypes = [vp, dp, dp]
+    L.nat_device_f.argtypes = [vp, C.POINTER(vp)]
+    L.nat_launch_count.argtypes = [vp]
+    L.nat_launch_count.restype = C.c_int64
+    L.nat_version.restype = C.c_char_p
+    L.nat_set_kernel_variant.argtypes = [vp, C.c_int]
+    L.nat_kernel_variant.argtypes = [vp]
+    L.nat_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.nat_kernel_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), i64p]
+    _lib = L
+    return L
+
+
+def _dp(a: np.ndarray):
+    if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+        raise TypeError("expected a C-contiguous float64 array")
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+@dataclass
+class SolverSpec:
+    """Problem + numerics of one stream-collide solve (a plain struct in
+    place of SolverConfiguration / ProblemDescription)."""
+    stencil: str = "D2Q9"
+    order: int = 4
+    cells: tuple = (8, 8)
+    length: tuple = (2 * np.pi, 2 * np.pi)
+    scaling: float = 1.0
+    viscosity: float = 1e-3
+    cfl: float = 0.4
+    dt: float = 0.0
+    collision: str = "BGK_STANDARD"
+    precision: str = "fp64"
+    topology: str = "feq"
+
+    @property
+    def dim(self) -> int:
+        return STENCIL_DQ[self.stencil][0]
+
+    def c(self) -> _Spec:
+        s = _Spec()
+        s.dim = self.dim
+        s.stencil = STENCILS[self.stencil]
+        s.order = int(self.order)
+        s.topology = TOPOLOGIES[self.topology]
+        for a in range(3):
+            s.cells[a] = int(self.cells[a]) if a < self.dim else 1
+            s.length[a] = float(self.length[a]) if a < self.dim else 1.0
+            s.periodic[a] = 1
+        s.scaling = float(self.scaling)
+        s.viscosity = float(self.viscosity)
+        s.cfl = float(self.cfl)
+        s.dt = float(self.dt)
+        s.collision = COLLISIONS[self.collision]
+        s.precision = PRECISIONS[self.precision]
+        return s
+
+
+class Solver:
+    """One device-resident solve driven through the C ABI."""
+
+    def __init__(self, spec: SolverSpec):
+        self.spec = spec
+        self._L = load_library()
+        self._h = C.c_void_p()
+        cs = spec.c()
+        rc = self._L.nat_create(C.byref(cs), C.byref(self._h))
+        if rc != NAT_OK:
+            msg = self._err()
+            self._L.nat_destroy(self._h)
+            self._h = C.c_void_p()
+            raise NatError(rc, msg)
+        nr, nd = C.c_int64(), C.c_int64()
+        q, d = C.c_int(), C.c_int()
+        self._L.nat_sizes(self._h, C.byref(nr), C.byref(nd), C.byref(q), C.byref(d))
+        self.n_ref, self.n_dev, self.Q, self.D = nr.value, nd.value, q.value, d.value
+
+    # -- plumbing ----------------------------------------------------------
+    def _err(self) -> str:
+        buf = C.create_string_buffer(512)
+        self._L.nat_last_error(self._h, buf, 512)
+        return buf.value.decode()
+
+    def _check(self, rc: int):
+        if rc == NAT_OK:
+            return
+        msg = self._err()
+        if rc in (NAT_ERR_DENSITY_UNDERFLOW, NAT_ERR_NAN):
+            raise CollisionException(rc, msg)
+        raise NatError(rc, msg)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.nat_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- properties ----------------------------------------------------------
+    @property
+    def dt(self) -> float:
+        dt, tau = C.c_double(), C.c_double()
+        self._L.nat_get_dt(self._h, C.byref(dt), C.byref(tau))
+        return dt.value
+
+    @property
+    def tau(self) -> float:
+        dt, tau = C.c_double(), C.c_double()
+        self._L.nat_get_dt(self._h, C.byref(dt), C.byref(tau))
+        return tau.value
+
+    @property
+    def launches(self) -> int:
+        return int(self._L.nat_launch_count(self._h))
+
+    # -- state transfer -------------------------------------------------------
+    def upload_f(self, f: np.ndarray):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        if f.shape != (self.Q, self.n_ref):
+            raise ValueError(f"f must have shape {(self.Q, self.n_ref)}")
+        self._check(self._L.nat_upload_f(self._h, _dp(f)))
+
+    def download_f(self) -> np.ndarray:
+        out = np.empty((self.Q, self.n_ref))
+        self._check(self._L.nat_download_f(self._h, _dp(out)))
+        return out
+
+    def download_macro(self):
+        rho = np.empty(self.n_ref)
+        u = np.empty((self.D, self.n_ref))
+        self._check(self._L.nat_download_macro(self._h, _dp(rho), _dp(u)))
+        return rho, u
+
+    def upload_macro(self, rho: np.ndarray, u: np.ndarray):
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        self._check(self._L.nat_upload_macro(self._h, _dp(rho), _dp(u)))
+
+    # -- operators --------------------------------------------------------------
+    def set_dt(self, dt: float):
+        self._check(self._L.nat_set_dt(self._h, dt))
+
+    def set_stream(self, cuda_stream_ptr: int):
+        self._check(self._L.nat_set_stream(self._h, C.c_void_p(cuda_stream_ptr)))
+
+    def stream(self, t: float = 0.0) -> float:
+        dt = C.c_double()
+        self._check(self._L.nat_stream(self._h, t, C.byref(dt)))
+        return dt.value
+
+    def collide(self, in_init: bool = False):
+        self._check(self._L.nat_collide(self._h, int(in_init)))
+
+    def step(self, n: int = 1):
+        self._check(self._L.nat_step(self._h, int(n)))
+
+    def step_async(self, n: int = 1, write_macro: bool = True):
+        self._check(self._L.nat_step_async(self._h, int(n), int(write_macro)))
+
+    def status(self):
+        self._check(self._L.nat_status(self._h))
+
+    def mass_energy(self):
+        m, e = C.c_double(), C.c_double()
+        self._check(self._L.nat_mass_energy(self._h, C.byref(m), C.byref(e)))
+        return m.value, e.value
+
+    def set_kernel_variant(self, variant: int):
+        """0 automatic, 1 generic kernel, 2 specialised kernel required."""
+        self._check(self._L.nat_set_kernel_variant(self._h, int(variant)))
+
+    @property
+    def kernel_variant(self) -> int:
+        return int(self._L.nat_kernel_variant(self._h))
+
+    def autotune(self, steps: int = 5):
+        """Time every applicable kernel for `steps` steps and keep the
+        fastest (the state is restored).  Returns (n_candidates, chosen)."""
+        nc, ch = C.c_int(), C.c_int()
+        self._check(self._L.nat_autotune(self._h, int(steps), C.byref(nc), C.byref(ch)))
+        return nc.value, ch.value
+
+    def kernel_info(self) -> dict:
+        v, th = C.c_int(), C.c_int()
+        tile = (C.c_int * 3)()
+        sm = C.c_int64()
+        self._check(self._L.nat_kernel_info(self._h, C.byref(v), tile, C.byref(th), C.byref(sm)))
+        return {"variant": v.value, "tile_nodes": list(tile), "threads": th.value, "smem_bytes": sm.value}
+
+    def device_f_ptr(self) -> int:
+        p = C.c_void_p()
+        self._check(self._L.nat_device_f(self._h, C.byref(p)))
+        return p.value or 0
+
+
+# ---------------------------------------------------------------------------
+# mirrors of the reference interfaces
+# ---------------------------------------------------------------------------
+
+@dataclass
+class DistributionFunctions:
+    """Host mirror of solver/DistributionFunctions.h: f.at(i) is block i."""
+    f: np.ndarray = field(default_factory=lambda: np.zeros((0, 0)))
+
+    def at(self, i: int) -> np.ndarray:
+        return self.f[i]
+
+    def getFStream(self) -> np.ndarray:
+        return self.f[1:]
+
+    def size(self) -> int:
+        return self.f.shape[0]
+
+    def copy(self) -> "DistributionFunctions":
+        return DistributionFunctions(self.f.copy())
+
+
+class SemiLagrangian:
+    """advection/SemiLagrangian.h: stream(f_old, f, t) on the device."""
+
+    def __init__(self, solver: Solver):
+        self.solver = solver
+
+    def setDeltaT(self, dt: float):
+        self.solver.set_dt(dt)
+
+    def getDeltaT(self) -> float:
+        return self.solver.dt
+
+    def stream(self, f_old: DistributionFunctions, f: DistributionFunctions, t: float = 0.0) -> float:
+        if f_old is f:
+            raise ValueError("f_old and f must be different objects (SemiLagrangian.h:153)")
+        f_old.f = f.f.copy()
+        self.solver.upload_f(f_old.f)
+        dt = self.solver.stream(t)
+        f.f = self.solver.download_f()
+        return dt
+
+
+class _CollisionModel:
+    MODEL = "BGK_STANDARD"
+
+    def __init__(self, solver: Solver):
+        if solver.spec.collision != self.MODEL:
+            raise ValueError(f"solver was created for {solver.spec.collision}, not {self.MODEL}")
+        self.solver = solver
+
+    def collideAll(self, f: DistributionFunctions, densities: np.ndarray, velocities: np.ndarray,
+                   locally_owned_dofs=None, inInitializationProcedure: bool = False):
+        """In-place collision of every node; densities and (unless in init)
+        velocities are overwritten like the reference's vectors."""
+        s = self.solver
+        s.upload_f(f.f)
+        if inInitializationProcedure:
+            s.upload_macro(np.ascontiguousarray(densities), np.ascontiguousarray(velocities))
+        s.collide(inInitializationProcedure)
+        f.f[...] = s.download_f()
+        rho, u = s.download_macro()
+        densities[...] = rho
+        if not inInitializationProcedure:
+            velocities[...] = u
+
+
+class BGKStandard(_CollisionModel):
+    MODEL = "BGK_STANDARD"
+
+
+class BGKIncompressible(_CollisionModel):
+    MODEL = "BGK_INCOMPRESSIBLE"
+
+
+class KBCStandard(_CollisionModel):
+    MODEL = "KBC_STANDARD"
+
+
+def version() -> str:
+    return load_library().nat_version().decode()

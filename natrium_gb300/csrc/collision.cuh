@@ -1,0 +1,312 @@
+// Collision epilogues of the fused stream + collide kernel.
+//
+// Two storage modes:
+//   DEV == false (plain FP64): v holds f.
+//   DEV == true  (FP32 deviation): v holds g = f - r, where r is the model's
+//       rest state (the equilibrium at rho = 1, u = 0: r_i = w_i for BGK and
+//       KBC; the incompressible equilibrium at rho = 1 for BGK_INCOMPRESSIBLE).
+//       Every quantity is computed in deviation form so that float keeps the
+//       small non-equilibrium part accurate.
+// u is the unscaled velocity (lattice units, c_s^2 = 1/3); the reference
+// stores scaling * u (CollisionOperator.h:79-82).
+#pragma once
+
+#include <math.h>
+
+#include "stencils.cuh"
+
+namespace natgpu {
+
+// Neumaier-compensated running sum (float moments of the FP32 path).
+template <class Real>
+struct CSum {
+  Real s = Real(0), c = Real(0);
+  __device__ __forceinline__ void add(Real x) {
+    Real t = s + x;
+    c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+    s = t;
+  }
+  __device__ __forceinline__ Real value() const { return s + c; }
+};
+
+// Moments: density (or its deviation) and momentum.  COMP selects
+// compensated summation (used for the float path).
+template <class S, bool COMP, class Real>
+__device__ __forceinline__ void moments(const Real (&v)[S::Q], Real& m0,
+                                        Real (&j)[3]) {
+  if constexpr (COMP) {
+    CSum<Real> a0, ax, ay, az;
+    static_for<0, S::Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      a0.add(v[i]);
+      if constexpr (S::e(i, 0) > 0) ax.add(v[i]);
+      if constexpr (S::e(i, 0) < 0) ax.add(-v[i]);
+      if constexpr (S::e(i, 1) > 0) ay.add(v[i]);
+      if constexpr (S::e(i, 1) < 0) ay.add(-v[i]);
+      if constexpr (S::e(i, 2) > 0) az.add(v[i]);
+      if constexpr (S::e(i, 2) < 0) az.add(-v[i]);
+    });
+    m0 = a0.value();
+    j[0] = ax.value();
+    j[1] = ay.value();
+    j[2] = az.value();
+  } else {
+    Real a0 = 0, ax = 0, ay = 0, az = 0;
+    static_for<0, S::Q>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      a0 += v[i];
+      if constexpr (S::e(i, 0) > 0) ax += v[i];
+      if constexpr (S::e(i, 0) < 0) ax -= v[i];
+      if constexpr (S::e(i, 1) > 0) ay += v[i];
+      if constexpr (S::e(i, 1) < 0) ay -= v[i];
+      if constexpr (S::e(i, 2) > 0) az += v[i];
+      if constexpr (S::e(i, 2) < 0) az -= v[i];
+    });
+    m0 = a0;
+    j[0] = ax;
+    j[1] = ay;
+    j[2] = az;
+  }
+}
+
+// e_i . u with compile-time e
+template <class S, int i, class Real>
+__device__ __forceinline__ Real edot(const Real (&u)[3]) {
+  Real r = Real(0);
+  if constexpr (S::e(i, 0) == 1) r += u[0];
+  if constexpr (S::e(i, 0) == -1) r -= u[0];
+  if constexpr (S::e(i, 1) == 1) r += u[1];
+  if constexpr (S::e(i, 1) == -1) r -= u[1];
+  if constexpr (S::D == 3) {
+    if constexpr (S::e(i, 2) == 1) r += u[2];
+    if constexpr (S::e(i, 2) == -1) r -= u[2];
+  }
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// BGK with the second-order equilibrium
+// (collision_advanced/CollisionSchemes.h:28-41, Equilibria.h:33-83).
+// Returns the density.  If given_u, u is input (inInitializationProcedure).
+// ---------------------------------------------------------------------------
+template <class S, bool DEV, bool COMP, class Real>
+__device__ __forceinline__ Real collide_bgk(Real (&v)[S::Q], Real inv_tau,
+                                            Real (&u)[3], bool given_u) {
+  Real m0, j[3];
+  moments<S, COMP>(v, m0, j);
+  const Real rho = DEV ? (Real(1) + m0) : m0;
+  if (!given_u) {
+    const Real inv = Real(1) / rho;
+    u[0] = j[0] * inv;
+    u[1] = j[1] * inv;
+    u[2] = (S::D == 3) ? j[2] * inv : Real(0);
+  }
+  const Real uu = Real(1.5) * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  static_for<0, S::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    const Real ue = Real(3) * edot<S, i>(u);
+    const Real poly = ue * (Real(1) + Real(0.5) * ue) - uu;
+    Real eq;
+    if constexpr (DEV)
+      eq = Real(S::w(i)) * (m0 + rho * poly);
+    else
+      eq = Real(S::w(i)) * rho * (Real(1) + poly);
+    v[i] = v[i] - inv_tau * (v[i] - eq);
+  });
+  return rho;
+}
+
+// ---------------------------------------------------------------------------
+// BGK incompressible, D2Q9 only (collision/BGKIncompressible.cpp:62-190):
+// feq_0 = -4 sigma rho + 4/9 (1 + usq), feq_1..4 = lambda rho + 1/9 (1 + ...),
+// feq_5..8 = gamma rho + rho/36 (1 + ...), lambda = 1/3, gamma = 1/12,
+// sigma = lambda + gamma.  (The reference weights directions 5-8 with rho and
+// 0-4 without; kept as written.)
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr double inc_c(int i) {
+  return i == 0 ? -4.0 * (1.0 / 3.0 + 1.0 / 12.0) : (i <= 4 ? 1.0 / 3.0 : 1.0 / 12.0);
+}
+__host__ __device__ constexpr double inc_w(int i) {
+  return i == 0 ? 4.0 / 9.0 : (i <= 4 ? 1.0 / 9.0 : 1.0 / 36.0);
+}
+// rest state of the incompressible model (rho = 1, u = 0)
+__host__ __device__ constexpr double inc_rest(int i) { return inc_c(i) + inc_w(i); }
+
+template <bool DEV, bool COMP, class Real>
+__device__ __forceinline__ Real collide_bgk_inc(Real (&v)[9], Real inv_tau,
+                                                Real (&u)[3], bool given_u) {
+  using S = SD2Q9;
+  Real m0, j[3];
+  moments<S, COMP>(v, m0, j);
+  const Real rho = DEV ? (Real(1) + m0) : m0;
+  if (!given_u) {
+    const Real inv = Real(1) / rho;
+    u[0] = j[0] * inv;
+    u[1] = j[1] * inv;
+    u[2] = Real(0);
+  }
+  const Real usq = -Real(1.5) * (u[0] * u[0] + u[1] * u[1]);
+  static_for<0, 9>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    const Real ue = Real(3) * edot<S, i>(u);
+    const Real poly = ue * (Real(1) + Real(0.5) * ue) + usq;
+    Real eq;
+    if constexpr (DEV) {
+      // feq - rest, written so float keeps the small part
+      if constexpr (i >= 5)
+        eq = Real(inc_c(i)) * m0 + Real(inc_w(i)) * (m0 + rho * poly);
+      else
+        eq = Real(inc_c(i)) * m0 + Real(inc_w(i)) * poly;
+    } else {
+      if constexpr (i >= 5)
+        eq = Real(inc_c(i)) * rho + Real(inc_w(i)) * rho * (Real(1) + poly);
+      else
+        eq = Real(inc_c(i)) * rho + Real(inc_w(i)) * (Real(1) + poly);
+    }
+    v[i] = v[i] - inv_tau * (v[i] - eq);
+  });
+  return rho;
+}
+
+// ---------------------------------------------------------------------------
+// KBC (entropic multi-relaxation), D2Q9 as collision/KBCStandard.cpp:88-497
+// (KBC_C: the shear part keeps the trace), extended to D3Q27 with the same
+// construction (no reference implementation for D3Q27).  Equilibrium in the
+// product form of KBCStandard.cpp:26-63 / :250-271.
+//   ds_i: shear part of f - feq (from the second-moment differences),
+//   dh_i = (f_i - feq_i) - ds_i,
+//   gamma = 1/beta - (2 - 1/beta) <ds|dh> / <dh|dh>, <x|y> = sum x y / feq,
+//   gamma = 2 when <dh|dh> < 1e-16,  f_i -= beta (2 ds_i + gamma dh_i),
+//   beta = 1 / (2 tau).
+// ---------------------------------------------------------------------------
+template <class S, int i, class Real>
+__device__ __forceinline__ Real kbc_shear(const Real (&M)[3][3]) {
+  constexpr int ex = S::e(i, 0), ey = S::e(i, 1), ez = S::e(i, 2);
+  constexpr int nz = (ex != 0) + (ey != 0) + (ez != 0);
+  if constexpr (nz == 0) {
+    return -(M[0][0] + M[1][1] + M[2][2]);
+  } else if constexpr (nz == 1) {
+    constexpr int a = ex != 0 ? 0 : (ey != 0 ? 1 : 2);
+    return Real(0.5) * M[a][a];
+  } else if constexpr (nz == 2) {
+    constexpr int a = ex != 0 ? 0 : 1;
+    constexpr int b = ez != 0 ? 2 : 1;
+    constexpr int sgn = S::e(i, a) * S::e(i, b);
+    return Real(0.25 * sgn) * M[a][b];
+  } else {
+    return Real(0);
+  }
+}
+
+template <class S, bool DEV, bool COMP, class Real>
+__device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
+                                            Real (&u)[3], bool given_u) {
+  Real m0, j[3];
+  moments<S, COMP>(v, m0, j);
+  const Real rho = DEV ? (Real(1) + m0) : m0;
+  if (!given_u) {
+    const Real inv = Real(1) / rho;
+    u[0] = j[0] * inv;
+    u[1] = j[1] * inv;
+    u[2] = (S::D == 3) ? j[2] * inv : Real(0);
+  }
+  // per axis: factor - 1 for c = -1, 0, +1 (stable small-number form of
+  // base = 2 - sqrt(1 + 3u^2), post = (2u + sqrt(1+3u^2)) / (1 - u))
+  Real dm[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const Real ua = u[a];
+    const Real s = sqrt(Real(1) + Real(3) * ua * ua);
+    const Real sm1 = Real(3) * ua * ua / (Real(1) + s);  // s - 1
+    const Real pm1 = (Real(3) * ua + sm1) / (Real(1) - ua);  // post - 1
+    dm[a][1] = -sm1;                                       // base - 1
+    dm[a][2] = pm1 - sm1 - sm1 * pm1;                      // base*post - 1
+    dm[a][0] = (-sm1 - pm1) / (Real(1) + pm1);             // base/post - 1
+  }
+  Real feq[S::Q], df[S::Q];
+  static_for<0, S::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    Real q = Real(0);  // prod_a (1 + d_a) - 1
+#pragma unroll
+    for (int a = 0; a < S::D; ++a) {
+      const int c = (a == 0 ? S::e(i, 0) : (a == 1 ? S::e(i, 1) : S::e(i, 2))) + 1;
+      const Real d = dm[a][c];
+      q = q + d + q * d;
+    }
+    const Real w = Real(S::w(i));
+    feq[i] = w * rho * (Real(1) + q);
+    if constexpr (DEV)
+      df[i] = v[i] - w * (m0 * (Real(1) + q) + q);
+    else
+      df[i] = v[i] - feq[i];
+  });
+  // second-moment differences of f - feq
+  Real M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  static_for<0, S::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr int ex = S::e(i, 0), ey = S::e(i, 1), ez = S::e(i, 2);
+    if constexpr (ex != 0) M[0][0] += df[i];
+    if constexpr (ey != 0) M[1][1] += df[i];
+    if constexpr (ez != 0) M[2][2] += df[i];
+    if constexpr (ex * ey != 0) M[0][1] += Real(ex * ey) * df[i];
+    if constexpr (ex * ez != 0) M[0][2] += Real(ex * ez) * df[i];
+    if constexpr (ey * ez != 0) M[1][2] += Real(ey * ez) * df[i];
+  });
+  M[1][0] = M[0][1];
+  M[2][0] = M[0][2];
+  M[2][1] = M[1][2];
+  Real ss = Real(0), sh = Real(0);
+  Real ds[S::Q];
+  static_for<0, S::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    ds[i] = kbc_shear<S, i>(M);
+    const Real dh = df[i] - ds[i];
+    const Real inv = Real(1) / feq[i];
+    ss += ds[i] * dh * inv;
+    sh += dh * dh * inv;
+  });
+  const Real beta = Real(0.5) / tau;
+  const Real ib = Real(1) / beta;
+  Real gamma = ib - (Real(2) - ib) * (ss / sh);
+  if (sh < Real(1e-16)) gamma = Real(2);
+  static_for<0, S::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    const Real dh = df[i] - ds[i];
+    v[i] = v[i] - beta * (Real(2) * ds[i] + gamma * dh);
+  });
+  return rho;
+}
+
+// Mass / momentum projection of the FP32 collision: removes the float
+// rounding defect of the conserved moments (post - pre) through the rest and
+// the axis populations, so that the collision conserves them exactly up to
+// the (unbiased) rounding of small differences.
+template <class S, class Real>
+__device__ __forceinline__ void conserve(Real (&v)[S::Q], const Real (&pre)[S::Q]) {
+  Real dm = 0, dj[3] = {0, 0, 0};
+  static_for<0, S::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    const Real d = v[i] - pre[i];
+    dm += d;
+    if constexpr (S::e(i, 0) > 0) dj[0] += d;
+    if constexpr (S::e(i, 0) < 0) dj[0] -= d;
+    if constexpr (S::e(i, 1) > 0) dj[1] += d;
+    if constexpr (S::e(i, 1) < 0) dj[1] -= d;
+    if constexpr (S::e(i, 2) > 0) dj[2] += d;
+    if constexpr (S::e(i, 2) < 0) dj[2] -= d;
+  });
+  // axis populations: +a and -a; changing them by -+dj/2 removes the
+  // momentum defect and leaves the mass unchanged
+  static_for<1, S::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    constexpr int nz = (S::e(i, 0) != 0) + (S::e(i, 1) != 0) + (S::e(i, 2) != 0);
+    if constexpr (nz == 1) {
+      constexpr int a = S::e(i, 0) != 0 ? 0 : (S::e(i, 1) != 0 ? 1 : 2);
+      constexpr int sg = S::e(i, 0) + S::e(i, 1) + S::e(i, 2);
+      if constexpr (a < S::D) v[i] -= Real(0.5 * sg) * dj[a];
+    }
+  });
+  v[0] -= dm;
+}
+
+}  // namespace natgpu

@@ -1,0 +1,47 @@
+// Launcher table shared by the per-stencil translation units and the API.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "natgpu_common.h"
+
+namespace natgpu {
+
+// collision selector values (match sl_step.cuh)
+enum { L_COLL_NONE = 0, L_COLL_BGK = 1, L_COLL_BGK_INC = 2, L_COLL_KBC = 3 };
+
+struct KernelSet {
+  const void* step;     // fused stream(+collide) kernel, NULL if unsupported
+  const void* collide;  // collide-only kernel, NULL for COLL_NONE
+};
+
+// prec: 0 = FP64, 1 = FP32 deviation
+KernelSet kernels_d2q9(int coll, int prec);
+KernelSet kernels_d3q19(int coll, int prec);
+KernelSet kernels_d3q27(int coll, int prec);
+
+// threads per CTA of the fused kernel and nodes per thread
+constexpr int STEP_THREADS = 256;
+constexpr int STEP_NPT = 2;
+
+// dynamic shared memory of the fused kernel
+size_t step_smem_bytes(int prec, const int Rmax[3], const int B[3]);
+
+// Specialised fused kernel (sl_step_v2.cuh): compile-time order, topology
+// and tile shape.
+struct V2Launch {
+  int stencil, coll, prec, P;
+  bool dg;
+  int cells[3];  // tile shape in cells
+  int B[3];      // tile shape in nodes
+  int nth;       // threads per CTA
+  const void* fn;
+  size_t smem;
+};
+// every instantiation that applies, in order of preference
+std::vector<V2Launch> find_v2(int stencil, int coll, int prec, int P, bool dg, const int cells[3], int dim,
+                              int nx);
+
+}  // namespace natgpu

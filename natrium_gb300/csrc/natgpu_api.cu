@@ -1,0 +1,1012 @@
+// Host side of libnatgpu.so: the C ABI declared in include/natgpu.h.
+//
+// Owns the device state of one solve (distribution functions in HBM,
+// macroscopic fields, streaming tables, status word) and enqueues the
+// kernels on the handle's CUDA stream.  Operator assembly (the reference's
+// SemiLagrangian::updateSparsityPattern + reassemble,
+// advection/SemiLagrangian.cpp:93-141, 145-522) reduces on a Cartesian box to
+// the per-axis 1-D tables built in build_tables(): departure point of every
+// node class, the cell that holds it, and the Lagrange weights there, in FP64.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/natgpu.h"
+#include "collision.cuh"
+#include "launch.h"
+#include "natgpu_common.h"
+#include "sl_step.cuh"
+#include "sl_step_v2.cuh"
+
+using namespace natgpu;
+
+struct nat_solver {
+  nat_spec spec;
+  int D = 0, Q = 0;
+  int period = 0;
+  int n_ax[3] = {1, 1, 1};      // device lattice per axis
+  int n_ref_ax[3] = {1, 1, 1};  // reference layout per axis
+  long long n_dev = 0, n_ref = 0;
+  double dt = 0, tau = 0, h[3] = {1, 1, 1};
+  double cs2_scaled = 0;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  void* f[2] = {nullptr, nullptr};
+  int cur = 0;
+  double* rho = nullptr;
+  double* u = nullptr;
+  double* staging = nullptr;  // Q * n_ref doubles
+  double* red = nullptr;      // reduction results (2 doubles)
+  int* status = nullptr;
+  SLTables* d_tab = nullptr;
+  SLTables h_tab;
+  int B[3] = {1, 1, 1};
+  int ntiles = 0;
+  size_t smem_step = 0;
+  KernelSet ks_coll, ks_stream;
+  std::string err;
+  long long launches = 0;
+  double rest[32];
+  // specialised kernel (sl_step_v2.cuh)
+  int variant = 0;  // 0 auto, 1 generic only, 2 specialised required
+  bool use_v2 = false;
+  V2Launch v2;
+  SpecWeights<double> w64;
+  SpecWeights<float> w32;
+};
+
+namespace {
+
+int fail(nat_solver* s, int code, const char* fmt, ...) {
+  if (s) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    s->err = buf;
+  }
+  return code;
+}
+
+int cuda_fail(nat_solver* s, cudaError_t e, const char* what) {
+  return fail(s, NAT_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                              \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return cuda_fail(s, e_, what); \
+  } while (0)
+
+// ---- stencil metadata (host) ---------------------------------------------
+struct HostStencil {
+  int D, Q;
+  double e[32][3];  // unit velocities
+  double w[32];
+};
+
+template <class S>
+HostStencil host_stencil() {
+  HostStencil h;
+  h.D = S::D;
+  h.Q = S::Q;
+  for (int i = 0; i < S::Q; ++i) {
+    for (int a = 0; a < 3; ++a) h.e[i][a] = S::e(i, a);
+    h.w[i] = S::w(i);
+  }
+  return h;
+}
+
+bool get_host_stencil(int id, HostStencil* out) {
+  switch (id) {
+    case NAT_D2Q9: *out = host_stencil<SD2Q9>(); return true;
+    case NAT_D3Q19: *out = host_stencil<SD3Q19>(); return true;
+    case NAT_D3Q27: *out = host_stencil<SD3Q27>(); return true;
+    default: return false;
+  }
+}
+
+// ---- 1-D Gauss-Lobatto points and Lagrange basis ----------------------------
+// Points: the end points and the roots of P_p' (Newton iteration on the
+// Legendre ODE, long double), mapped to [0, 1].
+void gl_points(int p, double* xi) {
+  xi[0] = 0.0;
+  xi[p] = 1.0;
+  for (int j = 1; j < p; ++j) {
+    long double x = -cosl(3.14159265358979323846264338327950288L * j / p);
+    for (int it = 0; it < 100; ++it) {
+      long double p0 = 1, p1 = x, d0 = 0, d1 = 1;
+      for (int k = 2; k <= p; ++k) {
+        long double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
+        long double d2 = d0 + (2 * k - 1) * p1;
+        p0 = p1; p1 = p2; d0 = d1; d1 = d2;
+      }
+      long double d2P = (2 * x * d1 - p * (p + 1) * p1) / (1 - x * x);
+      long double dx = d1 / d2P;
+      x -= dx;
+      if (fabsl(dx) < 1e-22L) break;
+    }
+    xi[j] = (double)((x + 1.0L) / 2.0L);
+  }
+  for (int j = 1; j < p - j; ++j) {
+    double a = 0.5 * (xi[j] + (1.0 - xi[p - j]));
+    xi[j] = a;
+    xi[p - j] = 1.0 - a;
+  }
+  if (p % 2 == 0) xi[p / 2] = 0.5;
+}
+
+double lagrange(int p, const double* xi, int j, double x) {
+  double v = 1.0;
+  for (int k = 0; k <= p; ++k)
+    if (k != j) v *= (x - xi[k]) / (xi[j] - xi[k]);
+  return v;
+}
+
+// GL quadrature weights on [0, 1]
+void gl_weights(int p, const double* xi, double* wq) {
+  for (int j = 0; j <= p; ++j) {
+    long double x = 2.0L * xi[j] - 1.0L, p0 = 1, p1 = x;
+    for (int k = 2; k <= p; ++k) {
+      long double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    if (p == 1) p1 = x;
+    wq[j] = (double)(1.0L / ((long double)p * (p + 1) * p1 * p1));
+  }
+}
+
+// ---- tile choice -------------------------------------------------------------
+// Cells per tile per axis: divides N, tile extent <= BMAX, tile nodes <= the
+// CTA's node slots, shared memory within the opt-in limit.  Prefers the
+// largest tile (least halo re-read), then the longest x extent.
+bool choose_tiles(nat_solver* s, int prec, int smem_limit) {
+  const int D = s->D;
+  int best[3] = {1, 1, 1};
+  long long best_score = -1;
+  std::vector<int> cand[3];
+  for (int a = 0; a < 3; ++a) {
+    if (a >= D) {
+      cand[a].push_back(1);
+      continue;
+    }
+    for (int c = 1; c <= s->spec.cells[a]; ++c)
+      if (s->spec.cells[a] % c == 0 && c * s->period <= BMAX) cand[a].push_back(c);
+  }
+  const int p = s->spec.order;
+  for (int cx : cand[0])
+    for (int cy : cand[1])
+      for (int cz : cand[2]) {
+        int B[3] = {cx * s->period, D > 1 ? cy * s->period : 1, D > 2 ? cz * s->period : 1};
+        long long TB = (long long)B[0] * B[1] * B[2];
+        if (TB > STEP_THREADS * STEP_NPT) continue;
+        int Rm[3];
+        bool ok = true;
+        for (int a = 0; a < 3; ++a) {
+          Rm[a] = a < D ? B[a] + 2 * (p + 1) + 2 : 1;  // bound, refined later
+          if (Rm[a] > RMAX) ok = false;
+        }
+        if (!ok) continue;
+        if ((long long)step_smem_bytes(prec, Rm, B) > smem_limit) continue;
+        long long score = TB * 1000 + B[0];
+        if (score > best_score) {
+          best_score = score;
+          best[0] = cx; best[1] = cy; best[2] = cz;
+        }
+      }
+  if (best_score < 0) return false;
+  for (int a = 0; a < 3; ++a) s->B[a] = a < D ? best[a] * s->period : 1;
+  return true;
+}
+
+// ---- streaming tables --------------------------------------------------------
+int build_tables(nat_solver* s, const HostStencil& hs) {
+  SLTables& T = s->h_tab;
+  memset(&T, 0, sizeof(T));
+  const int p = s->spec.order, D = s->D;
+  double xi[PMAX1 + 1];
+  gl_points(p, xi);
+  T.p = p;
+  T.dim = D;
+  for (int a = 0; a < 3; ++a) {
+    AxisGeom& G = T.ax[a];
+    if (a >= D) {
+      G.n = 1; G.period = 1; G.B = 1; G.ntiles = 1; G.nd = 0;
+      T.Rmax[a] = 1;
+      continue;
+    }
+    G.n = s->n_ax[a];
+    G.period = s->period;
+    G.B = s->B[a];
+    G.ntiles = G.n / G.B;
+    // displacement classes: class 0 for e_a > 0, 1 for e_a < 0 (unit speeds)
+    G.nd = 2;
+    int Rmax = G.B;
+    for (int d = 0; d < G.nd; ++d) {
+      const double sign = d == 0 ? 1.0 : -1.0;
+      // departure x - dt * e: displacement in cell units
+      const double delta = s->dt * sign * s->spec.scaling / s->h[a];
+      int lo = 1 << 30, hi = -(1 << 30);
+      for (int c = 0; c < G.period; ++c) {
+        const double xdep = xi[c] - delta;
+        int m;
+        if (xdep >= -1e-10 && xdep <= 1.0 + 1e-10)
+          m = 0;  // found in the node's own (closed) cell
+        else
+          m = (int)floor(xdep);
+        double xl = xdep - m;
+        if (fabs(xl) < 1e-10) xl = 0;
+        if (fabs(xl - 1) < 1e-10) xl = 1;
+        for (int j = 0; j <= p; ++j) {
+          double wv = lagrange(p, xi, j, xl);
+          if (fabs(wv) < 1e-10) wv = 0.0;  // SemiLagrangian.cpp:483
+          T.w[a][d][c][j] = wv;
+          T.wf[a][d][c][j] = (float)wv;
+        }
+        int jm = 0;
+        for (int j = 1; j <= p; ++j)
+          if (fabs(T.w[a][d][c][j]) > fabs(T.w[a][d][c][jm])) jm = j;
+        T.j0[a][d][c] = jm;
+        const int off = m * G.period - c;  // window start relative to the node
+        T.off[a][d][c] = off;
+        lo = std::min(lo, c + off);
+        hi = std::max(hi, c + off);
+      }
+      G.lo[d] = lo;
+      const int hiw = (G.B - G.period) + hi + p;
+      G.R[d] = hiw - lo + 1;
+      if (G.R[d] > RMAX) return fail(s, NAT_ERR_UNSUPPORTED, "time step too large for the tile halo (axis %d)", a);
+      Rmax = std::max(Rmax, G.R[d]);
+      for (int o = 0; o < G.B; ++o) T.wst[a][d][o] = o + T.off[a][d][o % G.period] - lo;
+    }
+    T.Rmax[a] = Rmax;
+  }
+  (void)hs;
+  return NAT_OK;
+}
+
+// ---- conversion / reduction kernels ---------------------------------------
+struct Dims {
+  int nx, ny, nz;    // device lattice
+  int rx, ry, rz;    // reference lattice
+};
+
+// reference layout (double) -> device layout
+template <class Real>
+__global__ void k_upload(const double* __restrict__ src, Real* __restrict__ dst,
+                         Dims d, int Q, const double* rest_dev) {
+  const long long n = (long long)d.nx * d.ny * d.nz;
+  const long long nr = (long long)d.rx * d.ry * d.rz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n * Q;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(i / n);
+    const long long g = i - (long long)q * n;
+    const int x = (int)(g % d.nx);
+    const int y = (int)((g / d.nx) % d.ny);
+    const int z = (int)(g / ((long long)d.nx * d.ny));
+    const long long r = ((long long)z * d.ry + y) * d.rx + x;
+    const double v = src[(long long)q * nr + r];
+    if constexpr (sizeof(Real) == 4)
+      dst[i] = (Real)(v - rest_dev[q]);
+    else
+      dst[i] = (Real)v;
+  }
+}
+
+// device layout -> reference layout (periodic duplicates filled)
+template <class Real>
+__global__ void k_download(const Real* __restrict__ src, double* __restrict__ dst,
+                           Dims d, int Q, const double* rest_dev) {
+  const long long n = (long long)d.nx * d.ny * d.nz;
+  const long long nr = (long long)d.rx * d.ry * d.rz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nr * Q;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(i / nr);
+    const long long r = i - (long long)q * nr;
+    const int x = (int)(r % d.rx) % d.nx;
+    const int y = (int)((r / d.rx) % d.ry) % d.ny;
+    const int z = (int)(r / ((long long)d.rx * d.ry)) % d.nz;
+    const long long g = ((long long)z * d.ny + y) * d.nx + x;
+    const double v = (double)src[(long long)q * n + g];
+    if constexpr (sizeof(Real) == 4)
+      dst[i] = v + rest_dev[q];
+    else
+      dst[i] = v;
+  }
+}
+
+// double fields: device layout <-> reference layout (ncomp blocks)
+__global__ void k_fields_to_ref(const double* __restrict__ src, double* __restrict__ dst,
+                                Dims d, int ncomp) {
+  const long long n = (long long)d.nx * d.ny * d.nz;
+  const long long nr = (long long)d.rx * d.ry * d.rz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nr * ncomp;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(i / nr);
+    const long long r = i - (long long)q * nr;
+    const int x = (int)(r % d.rx) % d.nx;
+    const int y = (int)((r / d.rx) % d.ry) % d.ny;
+    const int z = (int)(r / ((long long)d.rx * d.ry)) % d.nz;
+    dst[i] = src[(long long)q * n + ((long long)z * d.ny + y) * d.nx + x];
+  }
+}
+
+__global__ void k_fields_from_ref(const double* __restrict__ src, double* __restrict__ dst,
+                                  Dims d, int ncomp) {
+  const long long n = (long long)d.nx * d.ny * d.nz;
+  const long long nr = (long long)d.rx * d.ry * d.rz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n * ncomp;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(i / n);
+    const long long g = i - (long long)q * n;
+    const int x = (int)(g % d.nx);
+    const int y = (int)((g / d.nx) % d.ny);
+    const int z = (int)(g / ((long long)d.nx * d.ny));
+    dst[i] = src[(long long)q * nr + ((long long)z * d.ry + y) * d.rx + x];
+  }
+}
+
+// FP64 mass / kinetic energy with Gauss-Lobatto node weights (a node on a
+// cell face of the FE_Q lattice carries the weights of both cells).
+struct QuadW {
+  double w[3][PER_MAX];
+  int period;
+};
+
+__global__ void k_mass_energy(const double* __restrict__ rho, const double* __restrict__ u,
+                              Dims d, int D, QuadW qw, double* out) {
+  const long long n = (long long)d.nx * d.ny * d.nz;
+  double m = 0, e = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % d.nx);
+    const int y = (int)((i / d.nx) % d.ny);
+    const int z = (int)(i / ((long long)d.nx * d.ny));
+    double wgt = qw.w[0][x % qw.period] * qw.w[1][y % qw.period];
+    if (D == 3) wgt *= qw.w[2][z % qw.period];
+    double uu = u[i] * u[i] + u[n + i] * u[n + i];
+    if (D == 3) uu += u[2 * n + i] * u[2 * n + i];
+    m += wgt * rho[i];
+    e += wgt * rho[i] * uu;
+  }
+  __shared__ double sm[2][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    m += __shfl_down_sync(0xffffffffu, m, o);
+    e += __shfl_down_sync(0xffffffffu, e, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    sm[0][wid] = m;
+    sm[1][wid] = e;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    m = lane < nw ? sm[0][lane] : 0.0;
+    e = lane < nw ? sm[1][lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      m += __shfl_down_sync(0xffffffffu, m, o);
+      e += __shfl_down_sync(0xffffffffu, e, o);
+    }
+    if (lane == 0) {
+      atomicAdd(out, m);
+      atomicAdd(out + 1, 0.5 * e);
+    }
+  }
+}
+
+int grid_for(long long work) {
+  long long g = (work + 255) / 256;
+  if (g > 152 * 32) g = 152 * 32;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+Dims dims_of(const nat_solver* s) {
+  Dims d;
+  d.nx = s->n_ax[0]; d.ny = s->n_ax[1]; d.nz = s->n_ax[2];
+  d.rx = s->n_ref_ax[0]; d.ry = s->n_ref_ax[1]; d.rz = s->n_ref_ax[2];
+  return d;
+}
+
+StepParams step_params(nat_solver* s, const void* fin, void* fout, int collide,
+                       int write_macro, int in_init) {
+  StepParams P;
+  P.f_in = fin;
+  P.f_out = fout;
+  P.rho = s->rho;
+  P.u = s->u;
+  P.status = s->status;
+  P.tab = s->d_tab;
+  P.n = s->n_dev;
+  P.nx = s->n_ax[0];
+  P.ny = s->n_ax[1];
+  P.nz = s->n_ax[2];
+  P.tau = s->tau;
+  P.scaling = s->spec.scaling;
+  P.write_macro = write_macro;
+  P.in_init = in_init;
+  P.collide = collide;
+  return P;
+}
+
+int launch_step(nat_solver* s, const KernelSet& ks, int collide, int write_macro) {
+  void* fin = s->f[s->cur];
+  void* fout = s->f[1 - s->cur];
+  StepParams P = step_params(s, fin, fout, collide, write_macro, 0);
+  void* args[] = {&P};
+  cudaError_t e = cudaLaunchKernel(ks.step, dim3(s->ntiles), dim3(STEP_THREADS), args,
+                                   s->smem_step, s->stream);
+  if (e != cudaSuccess) return cuda_fail(s, e, "stream-collide launch");
+  s->launches++;
+  s->cur = 1 - s->cur;
+  return NAT_OK;
+}
+
+// Decide whether the specialised kernel applies: an instantiation exists for
+// (stencil, collision, precision, order, topology), its tile divides the
+// mesh, and every departure point lies in the node's own cell or the
+// adjacent upwind cell with the dominant weight at the node's own position
+// (the compile-time window pattern of Geo<P, DG>).
+template <int P, bool DG>
+bool pattern_matches(const SLTables& T, int D) {
+  using G = Geo<P, DG>;
+  for (int a = 0; a < D; ++a) {
+    for (int d = 0; d < 2; ++d) {
+      const int s = d == 0 ? 1 : -1;
+      for (int c = 0; c < G::PER; ++c) {
+        const int cell_shift = s > 0 ? (c == 0 ? -1 : 0) : ((DG && c == P) ? 1 : 0);
+        if (T.off[a][d][c] != cell_shift * G::PER - c) return false;
+        int jm = 0;
+        for (int j = 1; j <= P; ++j)
+          if (fabs(T.w[a][d][c][j]) > fabs(T.w[a][d][c][jm])) jm = j;
+        if (jm != G::J0(s, c)) return false;
+      }
+    }
+  }
+  return true;
+}
+
+bool pattern_ok(const SLTables& T, int D, int P, bool dg) {
+  switch (P * 2 + (dg ? 1 : 0)) {
+    case 2 * 1: return pattern_matches<1, false>(T, D);
+    case 2 * 1 + 1: return pattern_matches<1, true>(T, D);
+    case 2 * 2: return pattern_matches<2, false>(T, D);
+    case 2 * 2 + 1: return pattern_matches<2, true>(T, D);
+    case 2 * 3: return pattern_matches<3, false>(T, D);
+    case 2 * 3 + 1: return pattern_matches<3, true>(T, D);
+    case 2 * 4: return pattern_matches<4, false>(T, D);
+    case 2 * 4 + 1: return pattern_matches<4, true>(T, D);
+    case 2 * 5: return pattern_matches<5, false>(T, D);
+    case 2 * 5 + 1: return pattern_matches<5, true>(T, D);
+    case 2 * 6: return pattern_matches<6, false>(T, D);
+    case 2 * 6 + 1: return pattern_matches<6, true>(T, D);
+  }
+  return false;
+}
+
+void set_v2_weights(nat_solver* s) {
+  memset(&s->w64, 0, sizeof(s->w64));
+  memset(&s->w32, 0, sizeof(s->w32));
+  for (int a = 0; a < 3; ++a)
+    for (int d = 0; d < 2; ++d)
+      for (int c = 0; c < PER_MAX; ++c)
+        for (int j = 0; j < PMAX1; ++j) {
+          s->w64.w[a][d][c][j] = s->h_tab.w[a][d][c][j];
+          s->w32.w[a][d][c][j] = (float)s->h_tab.w[a][d][c][j];
+        }
+}
+
+// Candidate specialised kernels for the current configuration.
+std::vector<V2Launch> v2_candidates(nat_solver* s, int coll_sel, int smem_optin) {
+  std::vector<V2Launch> out;
+  const bool dg = s->spec.topology == NAT_TOPO_DG;
+  if (!pattern_ok(s->h_tab, s->D, s->spec.order, dg)) return out;
+  for (const V2Launch& e :
+       find_v2(s->spec.stencil, coll_sel, s->spec.precision, s->spec.order, dg, s->spec.cells, s->D, s->n_ax[0]))
+    if ((long long)e.smem <= smem_optin) out.push_back(e);
+  return out;
+}
+
+int use_candidate(nat_solver* s, const V2Launch& e) {
+  cudaError_t ce = cudaFuncSetAttribute(e.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.smem);
+  if (ce != cudaSuccess) return cuda_fail(s, ce, "v2 smem attribute");
+  set_v2_weights(s);
+  s->v2 = e;
+  s->use_v2 = true;
+  return NAT_OK;
+}
+
+int select_v2(nat_solver* s, int coll_sel, int smem_optin) {
+  s->use_v2 = false;
+  if (s->variant == 1) return NAT_OK;
+  std::vector<V2Launch> c = v2_candidates(s, coll_sel, smem_optin);
+  if (c.empty()) {
+    if (s->variant == 2) return fail(s, NAT_ERR_UNSUPPORTED, "no specialised kernel for this configuration");
+    return NAT_OK;
+  }
+  return use_candidate(s, c.front());
+}
+
+int coll_selector(int collision) {
+  return collision == NAT_BGK_STANDARD ? L_COLL_BGK
+                                       : (collision == NAT_BGK_INCOMPRESSIBLE ? L_COLL_BGK_INC : L_COLL_KBC);
+}
+
+template <class Real>
+int launch_v2_t(nat_solver* s, const SpecWeights<Real>& W, int write_macro) {
+  StepParams2<Real> P;
+  P.f_in = static_cast<const Real*>(s->f[s->cur]);
+  P.f_out = static_cast<Real*>(s->f[1 - s->cur]);
+  P.rho = s->rho;
+  P.u = s->u;
+  P.status = s->status;
+  P.n = s->n_dev;
+  P.nx = s->n_ax[0];
+  P.ny = s->n_ax[1];
+  P.nz = s->n_ax[2];
+  P.ntx = s->n_ax[0] / s->v2.B[0];
+  P.nty = s->n_ax[1] / s->v2.B[1];
+  P.tau = s->tau;
+  P.scaling = s->spec.scaling;
+  P.write_macro = write_macro;
+  P.W = W;
+  const int grid = P.ntx * P.nty * (s->n_ax[2] / s->v2.B[2]);
+  void* args[] = {&P};
+  cudaError_t e = cudaLaunchKernel(s->v2.fn, dim3(grid), dim3(s->v2.nth), args, s->v2.smem, s->stream);
+  if (e != cudaSuccess) return cuda_fail(s, e, "specialised stream-collide launch");
+  s->launches++;
+  s->cur = 1 - s->cur;
+  return NAT_OK;
+}
+
+int launch_v2(nat_solver* s, int write_macro) {
+  return s->spec.precision == NAT_FP64 ? launch_v2_t<double>(s, s->w64, write_macro)
+                                       : launch_v2_t<float>(s, s->w32, write_macro);
+}
+
+int upload_rest(nat_solver* s) {
+  // the rest state is stored after the two doubles of the reduction buffer
+  CK(cudaMemcpyAsync(s->red + 2, s->rest, sizeof(double) * s->Q, cudaMemcpyHostToDevice,
+                     s->stream), "rest upload");
+  return NAT_OK;
+}
+
+}  // namespace
+
+size_t natgpu::step_smem_bytes(int prec, const int Rmax[3], const int B[3]) {
+  return prec == 0 ? smem_layout<double>(Rmax, B).total : smem_layout<float>(Rmax, B).total;
+}
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+const char* nat_version(void) { return "natgpu 0.1 (sm_103a)"; }
+
+int nat_destroy(nat_solver* s) {
+  if (!s) return NAT_OK;
+  cudaFree(s->f[0]);
+  cudaFree(s->f[1]);
+  cudaFree(s->rho);
+  cudaFree(s->u);
+  cudaFree(s->staging);
+  cudaFree(s->red);
+  cudaFree(s->status);
+  cudaFree(s->d_tab);
+  delete s;
+  return NAT_OK;
+}
+
+static int setup_dt(nat_solver* s, double dt) {
+  HostStencil hs;
+  get_host_stencil(s->spec.stencil, &hs);
+  s->dt = dt;
+  // tau = nu / (dt c_s^2) + 1/2 with the scaled c_s^2
+  // (collision_advanced/AuxiliaryCollisionFunctions.h:63-68, 177)
+  s->tau = s->spec.viscosity / (dt * s->cs2_scaled) + 0.5;
+  int rc = build_tables(s, hs);
+  if (rc) return rc;
+  int Rm[3] = {s->h_tab.Rmax[0], s->h_tab.Rmax[1], s->h_tab.Rmax[2]};
+  s->smem_step = step_smem_bytes(s->spec.precision, Rm, s->B);
+  for (const KernelSet* ks : {&s->ks_coll, &s->ks_stream}) {
+    if (ks->step) {
+      CK(cudaFuncSetAttribute(ks->step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)s->smem_step), "smem attribute");
+    }
+  }
+  s->ntiles = 1;
+  for (int a = 0; a < 3; ++a) s->ntiles *= s->h_tab.ax[a].ntiles;
+  CK(cudaMemcpyAsync(s->d_tab, &s->h_tab, sizeof(SLTables), cudaMemcpyHostToDevice, s->stream),
+     "table upload");
+  CK(cudaStreamSynchronize(s->stream), "table upload sync");
+  int smem_optin = 0;
+  CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device),
+     "device attribute");
+  return select_v2(s, coll_selector(s->spec.collision), smem_optin);
+}
+
+int nat_create(const nat_spec* spec, nat_solver** out) {
+  if (!spec || !out) return NAT_ERR_INVALID_ARG;
+  *out = nullptr;
+  nat_solver* s = new nat_solver();
+  s->spec = *spec;
+  HostStencil hs;
+  if (!get_host_stencil(spec->stencil, &hs)) {
+    int rc = fail(s, NAT_ERR_UNSUPPORTED, "unsupported stencil %d", spec->stencil);
+    *out = s;
+    return rc;
+  }
+  s->D = hs.D;
+  s->Q = hs.Q;
+  auto bad = [&](const char* m) {
+    fail(s, NAT_ERR_INVALID_ARG, "%s", m);
+    *out = s;
+    return NAT_ERR_INVALID_ARG;
+  };
+  if (spec->dim != hs.D) return bad("dim does not match the stencil");
+  if (spec->order < 1 || spec->order > PMAX) return bad("order must be 1..6");
+  if (spec->topology != NAT_TOPO_FEQ && spec->topology != NAT_TOPO_DG) return bad("bad topology");
+  if (spec->precision != NAT_FP64 && spec->precision != NAT_FP32_DEV) return bad("bad precision");
+  if (!(spec->scaling > 0) || !(spec->viscosity > 0)) return bad("scaling and viscosity must be > 0");
+  for (int a = 0; a < s->D; ++a) {
+    if (spec->cells[a] < 1) return bad("cells must be >= 1");
+    if (!(spec->length[a] > 0)) return bad("length must be > 0");
+    if (!spec->periodic[a]) {
+      fail(s, NAT_ERR_UNSUPPORTED, "non-periodic boundaries are not supported");
+      *out = s;
+      return NAT_ERR_UNSUPPORTED;
+    }
+  }
+  int coll;
+  switch (spec->collision) {
+    case NAT_BGK_STANDARD: coll = L_COLL_BGK; break;
+    case NAT_BGK_INCOMPRESSIBLE: coll = L_COLL_BGK_INC; break;
+    case NAT_KBC_STANDARD: coll = L_COLL_KBC; break;
+    default: return bad("bad collision model");
+  }
+  auto pick = [&](int c) -> KernelSet {
+    switch (spec->stencil) {
+      case NAT_D2Q9: return kernels_d2q9(c, spec->precision);
+      case NAT_D3Q19: return kernels_d3q19(c, spec->precision);
+      case NAT_D3Q27: return kernels_d3q27(c, spec->precision);
+    }
+    return {nullptr, nullptr};
+  };
+  s->ks_coll = pick(coll);
+  s->ks_stream = pick(L_COLL_NONE);
+  if (!s->ks_coll.step) {
+    // the reference throws for these combinations too
+    // (collision/BGKIncompressible.cpp:54-55, collision/KBCStandard.cpp:79-81)
+    fail(s, NAT_ERR_UNSUPPORTED, "collision model %d is not implemented for stencil %d",
+         spec->collision, spec->stencil);
+    *out = s;
+    return NAT_ERR_UNSUPPORTED;
+  }
+  const int p = spec->order;
+  const bool dg = spec->topology == NAT_TOPO_DG;
+  s->period = dg ? p + 1 : p;
+  s->n_dev = 1;
+  s->n_ref = 1;
+  double hmin = 1e300;
+  for (int a = 0; a < 3; ++a) {
+    if (a < s->D) {
+      s->n_ax[a] = spec->cells[a] * s->period;
+      s->n_ref_ax[a] = dg ? s->n_ax[a] : s->n_ax[a] + 1;
+      s->h[a] = spec->length[a] / spec->cells[a];
+      hmin = std::min(hmin, s->h[a]);
+    }
+    s->n_dev *= s->n_ax[a];
+    s->n_ref *= s->n_ref_ax[a];
+  }
+  s->cs2_scaled = spec->scaling * spec->scaling / 3.0;
+  for (int q = 0; q < s->Q; ++q)
+    s->rest[q] = spec->collision == NAT_BGK_INCOMPRESSIBLE ? inc_rest(q) : hs.w[q];
+  *out = s;
+  CK(cudaGetDevice(&s->device), "cudaGetDevice");
+  int smem_optin = 0;
+  CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device),
+     "device attribute");
+  if (!choose_tiles(s, spec->precision, smem_optin))
+    return fail(s, NAT_ERR_UNSUPPORTED, "no tile shape fits (cells %d %d %d, p %d)",
+                spec->cells[0], spec->cells[1], spec->cells[2], p);
+  const size_t es = spec->precision == NAT_FP64 ? 8 : 4;
+  const size_t fbytes = es * (size_t)s->Q * s->n_dev;
+#define ALLOC(ptr, bytes)                                             \
+  do {                                                                \
+    cudaError_t e_ = cudaMalloc((void**)&(ptr), (bytes));             \
+    if (e_ != cudaSuccess) {                                          \
+      cudaGetLastError();                                             \
+      return fail(s, NAT_ERR_OOM, "cudaMalloc(%zu) failed", (size_t)(bytes)); \
+    }                                                                 \
+  } while (0)
+  ALLOC(s->f[0], fbytes);
+  ALLOC(s->f[1], fbytes);
+  ALLOC(s->rho, sizeof(double) * s->n_dev);
+  ALLOC(s->u, sizeof(double) * s->D * s->n_dev);
+  ALLOC(s->staging, sizeof(double) * (size_t)std::max(s->Q, s->D + 1) * s->n_ref);
+  ALLOC(s->red, sizeof(double) * (2 + 32));
+  ALLOC(s->status, sizeof(int));
+  ALLOC(s->d_tab, sizeof(SLTables));
+#undef ALLOC
+  CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "memset");
+  CK(cudaMemsetAsync(s->rho, 0, sizeof(double) * s->n_dev, s->stream), "memset");
+  CK(cudaMemsetAsync(s->u, 0, sizeof(double) * s->D * s->n_dev, s->stream), "memset");
+  int rc = upload_rest(s);
+  if (rc) return rc;
+  double dt = spec->dt;
+  if (!(dt > 0)) {
+    // utilities/CFDSolverUtilities.cpp:92-100: |e|_max = sqrt(2) * scaling
+    dt = spec->cfl * hmin / (sqrt(2.0) * spec->scaling * p * p);
+  }
+  return setup_dt(s, dt);
+}
+
+int nat_sizes(const nat_solver* s, int64_t* n_ref, int64_t* n_dev, int* Q, int* D) {
+  if (!s) return NAT_ERR_INVALID_ARG;
+  if (n_ref) *n_ref = s->n_ref;
+  if (n_dev) *n_dev = s->n_dev;
+  if (Q) *Q = s->Q;
+  if (D) *D = s->D;
+  return NAT_OK;
+}
+
+int nat_get_dt(const nat_solver* s, double* dt, double* tau) {
+  if (!s) return NAT_ERR_INVALID_ARG;
+  if (dt) *dt = s->dt;
+  if (tau) *tau = s->tau;
+  return NAT_OK;
+}
+
+int nat_set_dt(nat_solver* s, double dt) {
+  if (!s) return NAT_ERR_INVALID_ARG;
+  if (!(dt > 0)) return fail(s, NAT_ERR_INVALID_ARG, "dt must be > 0");
+  return setup_dt(s, dt);
+}
+
+int nat_set_stream(nat_solver* s, void* stream) {
+  if (!s) return NAT_ERR_INVALID_ARG;
+  s->stream = (cudaStream_t)stream;
+  return NAT_OK;
+}
+
+int nat_upload_f(nat_solver* s, const double* f_host) {
+  if (!s || !f_host) return NAT_ERR_INVALID_ARG;
+  CK(cudaMemcpyAsync(s->staging, f_host, sizeof(double) * s->Q * s->n_ref,
+                     cudaMemcpyHostToDevice, s->stream), "upload f");
+  Dims d = dims_of(s);
+  const int g = grid_for(s->n_dev * s->Q);
+  if (s->spec.precision == NAT_FP64)
+    k_upload<double><<<g, 256, 0, s->stream>>>(s->staging, (double*)s->f[s->cur], d, s->Q, s->red + 2);
+  else
+    k_upload<float><<<g, 256, 0, s->stream>>>(s->staging, (float*)s->f[s->cur], d, s->Q, s->red + 2);
+  CK(cudaGetLastError(), "upload kernel");
+  s->launches++;
+  return NAT_OK;
+}
+
+int nat_download_f(nat_solver* s, double* f_host) {
+  if (!s || !f_host) return NAT_ERR_INVALID_ARG;
+  Dims d = dims_of(s);
+  const int g = grid_for(s->n_ref * s->Q);
+  if (s->spec.precision == NAT_FP64)
+    k_download<double><<<g, 256, 0, s->stream>>>((const double*)s->f[s->cur], s->staging, d, s->Q, s->red + 2);
+  else
+    k_download<float><<<g, 256, 0, s->stream>>>((const float*)s->f[s->cur], s->staging, d, s->Q, s->red + 2);
+  CK(cudaGetLastError(), "download kernel");
+  s->launches++;
+  CK(cudaMemcpyAsync(f_host, s->staging, sizeof(double) * s->Q * s->n_ref,
+                     cudaMemcpyDeviceToHost, s->stream), "download f");
+  CK(cudaStreamSynchronize(s->stream), "download sync");
+  return NAT_OK;
+}
+
+int nat_download_macro(nat_solver* s, double* rho_host, double* u_host) {
+  if (!s || !rho_host || !u_host) return NAT_ERR_INVALID_ARG;
+  Dims d = dims_of(s);
+  k_fields_to_ref<<<grid_for(s->n_ref), 256, 0, s->stream>>>(s->rho, s->staging, d, 1);
+  k_fields_to_ref<<<grid_for(s->n_ref * s->D), 256, 0, s->stream>>>(s->u, s->staging + s->n_ref, d, s->D);
+  CK(cudaGetLastError(), "macro kernel");
+  s->launches += 2;
+  CK(cudaMemcpyAsync(rho_host, s->staging, sizeof(double) * s->n_ref, cudaMemcpyDeviceToHost,
+                     s->stream), "download rho");
+  CK(cudaMemcpyAsync(u_host, s->staging + s->n_ref, sizeof(double) * s->D * s->n_ref,
+                     cudaMemcpyDeviceToHost, s->stream), "download u");
+  CK(cudaStreamSynchronize(s->stream), "download sync");
+  return NAT_OK;
+}
+
+int nat_upload_macro(nat_solver* s, const double* rho_host, const double* u_host) {
+  if (!s || !rho_host || !u_host) return NAT_ERR_INVALID_ARG;
+  CK(cudaMemcpyAsync(s->staging, rho_host, sizeof(double) * s->n_ref, cudaMemcpyHostToDevice,
+                     s->stream), "upload rho");
+  CK(cudaMemcpyAsync(s->staging + s->n_ref, u_host, sizeof(double) * s->D * s->n_ref,
+                     cudaMemcpyHostToDevice, s->stream), "upload u");
+  Dims d = dims_of(s);
+  k_fields_from_ref<<<grid_for(s->n_dev), 256, 0, s->stream>>>(s->staging, s->rho, d, 1);
+  k_fields_from_ref<<<grid_for(s->n_dev * s->D), 256, 0, s->stream>>>(s->staging + s->n_ref, s->u, d, s->D);
+  CK(cudaGetLastError(), "macro upload kernel");
+  s->launches += 2;
+  return NAT_OK;
+}
+
+int nat_stream(nat_solver* s, double t, double* dt_out) {
+  (void)t;
+  if (!s) return NAT_ERR_INVALID_ARG;
+  int rc = launch_step(s, s->ks_stream, 0, 0);
+  if (rc) return rc;
+  if (dt_out) *dt_out = s->dt;
+  return NAT_OK;
+}
+
+int nat_collide(nat_solver* s, int in_init) {
+  if (!s) return NAT_ERR_INVALID_ARG;
+  StepParams P = step_params(s, s->f[s->cur], s->f[s->cur], 1, 1, in_init);
+  void* args[] = {&P};
+  CK(cudaLaunchKernel(s->ks_coll.collide, dim3(grid_for(s->n_dev)), dim3(256), args, 0, s->stream),
+     "collide launch");
+  s->launches++;
+  return nat_status(s);
+}
+
+int nat_step_async(nat_solver* s, int n_steps, int write_macro) {
+  if (!s || n_steps < 0) return NAT_ERR_INVALID_ARG;
+  for (int k = 0; k < n_steps; ++k) {
+    const int wm = (write_macro && k == n_steps - 1) ? 1 : 0;
+    int rc = s->use_v2 ? launch_v2(s, wm) : launch_step(s, s->ks_coll, 1, wm);
+    if (rc) return rc;
+  }
+  return NAT_OK;
+}
+
+int nat_step(nat_solver* s, int n_steps) {
+  int rc = nat_step_async(s, n_steps, 1);
+  if (rc) return rc;
+  return nat_status(s);
+}
+
+int nat_status(nat_solver* s) {
+  if (!s) return NAT_ERR_INVALID_ARG;
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "status read");
+  CK(cudaStreamSynchronize(s->stream), "status sync");
+  if (st) {
+    CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "status clear");
+    if (st & ST_NAN) return fail(s, NAT_ERR_NAN, "NaN density in collision");
+    return fail(s, NAT_ERR_DENSITY_UNDERFLOW,
+                "Densities too small (< 1e-10) for collisions. Decrease time step size.");
+  }
+  return NAT_OK;
+}
+
+int nat_last_error(const nat_solver* s, char* buf, size_t len) {
+  if (!buf || len == 0) return NAT_ERR_INVALID_ARG;
+  const char* m = s ? s->err.c_str() : "null handle";
+  snprintf(buf, len, "%s", m);
+  return NAT_OK;
+}
+
+int nat_mass_energy(nat_solver* s, double* mass, double* ke) {
+  if (!s) return NAT_ERR_INVALID_ARG;
+  QuadW qw;
+  memset(&qw, 0, sizeof(qw));
+  const int p = s->spec.order;
+  double xi[PMAX1 + 1], wq[PMAX1 + 1];
+  gl_points(p, xi);
+  gl_weights(p, xi, wq);
+  qw.period = s->period;
+  for (int a = 0; a < 3; ++a)
+    for (int c = 0; c < s->period; ++c) {
+      double w = wq[c];
+      if (s->spec.topology == NAT_TOPO_FEQ && c == 0) w += wq[p];  // shared face node
+      qw.w[a][c] = a < s->D ? w * s->h[a] : 1.0;
+    }
+  CK(cudaMemsetAsync(s->red, 0, 2 * sizeof(double), s->stream), "memset");
+  k_mass_energy<<<grid_for(s->n_dev), 256, 0, s->stream>>>(s->rho, s->u, dims_of(s), s->D, qw, s->red);
+  CK(cudaGetLastError(), "reduction kernel");
+  s->launches++;
+  double h2[2];
+  CK(cudaMemcpyAsync(h2, s->red, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "red read");
+  CK(cudaStreamSynchronize(s->stream), "red sync");
+  if (mass) *mass = h2[0];
+  if (ke) *ke = h2[1];
+  return NAT_OK;
+}
+
+int nat_device_f(nat_solver* s, void** f_dev) {
+  if (!s || !f_dev) return NAT_ERR_INVALID_ARG;
+  *f_dev = s->f[s->cur];
+  return NAT_OK;
+}
+
+int64_t nat_launch_count(const nat_solver* s) { return s ? s->launches : -1; }
+
+int nat_set_kernel_variant(nat_solver* s, int variant) {
+  if (!s || variant < 0 || variant > 2) return NAT_ERR_INVALID_ARG;
+  s->variant = variant;
+  int smem_optin = 0;
+  CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device),
+     "device attribute");
+  return select_v2(s, coll_selector(s->spec.collision), smem_optin);
+}
+
+int nat_kernel_variant(const nat_solver* s) { return s ? (s->use_v2 ? 2 : 1) : -1; }
+
+int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
+  if (!s || steps < 1) return NAT_ERR_INVALID_ARG;
+  int smem_optin = 0;
+  CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device),
+     "device attribute");
+  const int coll_sel = coll_selector(s->spec.collision);
+  std::vector<V2Launch> cand = s->variant == 1 ? std::vector<V2Launch>() : v2_candidates(s, coll_sel, smem_optin);
+  const int ncand = (int)cand.size() + (s->variant == 2 ? 0 : 1);  // + the generic kernel
+  if (n_candidates) *n_candidates = ncand;
+  if (ncand == 0) return fail(s, NAT_ERR_UNSUPPORTED, "no kernel applies");
+  // keep the state: back it up in the staging buffer (Q * n_ref doubles >= f)
+  const size_t es = s->spec.precision == NAT_FP64 ? 8 : 4;
+  const size_t fbytes = es * (size_t)s->Q * s->n_dev;
+  const int cur0 = s->cur;
+  CK(cudaMemcpyAsync(s->staging, s->f[cur0], fbytes, cudaMemcpyDeviceToDevice, s->stream), "autotune backup");
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0), "event");
+  CK(cudaEventCreate(&e1), "event");
+  float best = 1e30f;
+  int best_i = -1;
+  for (int i = 0; i < ncand; ++i) {
+    int rc;
+    if (i < (int)cand.size()) {
+      rc = use_candidate(s, cand[i]);
+    } else {
+      s->use_v2 = false;
+      rc = NAT_OK;
+    }
+    if (rc) break;
+    rc = nat_step_async(s, 1, 0);  // warm-up
+    if (rc) break;
+    cudaEventRecord(e0, s->stream);
+    rc = nat_step_async(s, steps, 0);
+    cudaEventRecord(e1, s->stream);
+    if (rc) break;
+    CK(cudaEventSynchronize(e1), "autotune sync");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      best_i = i;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // restore the state and the status word (the trial steps may have flagged
+  // nothing of the caller's)
+  s->cur = cur0;
+  CK(cudaMemcpyAsync(s->f[cur0], s->staging, fbytes, cudaMemcpyDeviceToDevice, s->stream), "autotune restore");
+  CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "status clear");
+  CK(cudaStreamSynchronize(s->stream), "autotune restore sync");
+  if (best_i < 0) return fail(s, NAT_ERR_CUDA, "autotune: no candidate ran");
+  if (chosen) *chosen = best_i;
+  if (best_i < (int)cand.size()) return use_candidate(s, cand[best_i]);
+  s->use_v2 = false;
+  return NAT_OK;
+}
+
+int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* threads, int64_t* smem_bytes) {
+  if (!s) return NAT_ERR_INVALID_ARG;
+  if (variant) *variant = s->use_v2 ? 2 : 1;
+  for (int a = 0; a < 3; ++a)
+    if (tile_nodes) tile_nodes[a] = s->use_v2 ? s->v2.B[a] : s->B[a];
+  if (threads) *threads = s->use_v2 ? s->v2.nth : STEP_THREADS;
+  if (smem_bytes) *smem_bytes = (int64_t)(s->use_v2 ? s->v2.smem : s->smem_step);
+  return NAT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+"""Initial states of the benchmark flows (host setup, FP64 numpy).
+
+Equivalent of CFDSolver::initializeDistributions with the EQUILIBRIUM
+option (solver/CFDSolver.cpp:1103-1130): evaluate the problem's initial
+density and velocity at the support points and set f = f^eq(rho, u).
+
+Node coordinates follow the lattice layout of include/natgpu.h (reference
+layout, x fastest; FE_Q keeps the periodic duplicate nodes).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+# unit velocities and weights (stencils/D2Q9.cpp:40-61, D3Q19.cpp:37-67,
+# D3Q27.cpp:36-112 of the reference)
+_E = {
+    "D2Q9": [(0, 0, 0), (1, 0, 0), (0, 1, 0), (-1, 0, 0), (0, -1, 0), (1, 1, 0), (-1, 1, 0), (-1, -1, 0),
+             (1, -1, 0)],
+    "D3Q19": [(0, 0, 0), (1, 0, 0), (0, 0, 1), (-1, 0, 0), (0, 0, -1), (0, -1, 0), (0, 1, 0), (1, 0, 1),
+              (-1, 0, 1), (-1, 0, -1), (1, 0, -1), (1, -1, 0), (1, 1, 0), (-1, 1, 0), (-1, -1, 0),
+              (0, -1, 1), (0, 1, 1), (0, 1, -1), (0, -1, -1)],
+    "D3Q27": [(0, 0, 0), (1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1), (0, 1, 1),
+              (0, -1, -1), (0, 1, -1), (0, -1, 1), (1, 0, 1), (-1, 0, -1), (1, 0, -1), (-1, 0, 1),
+              (1, 1, 0), (-1, -1, 0), (1, -1, 0), (-1, 1, 0), (1, 1, 1), (-1, -1, -1), (1, 1, -1),
+              (-1, -1, 1), (1, -1, 1), (-1, 1, -1), (1, -1, -1), (-1, 1, 1)],
+}
+
+
+def _weights(name: str) -> np.ndarray:
+    e = np.array(_E[name])
+    nz = np.count_nonzero(e, axis=1)
+    if name == "D2Q9":
+        table = {0: 4 / 9, 1: 1 / 9, 2: 1 / 36}
+    elif name == "D3Q19":
+        table = {0: 1 / 3, 1: 1 / 18, 2: 1 / 36}
+    else:
+        table = {0: 8 / 27, 1: 2 / 27, 2: 1 / 54, 3: 1 / 216}
+    return np.array([table[int(k)] for k in nz])
+
+
+def unit_velocities(name: str) -> np.ndarray:
+    return np.array(_E[name], dtype=np.float64)
+
+
+def gl_points(p: int) -> np.ndarray:
+    """Gauss-Lobatto points on [0, 1]: end points and the roots of P_p'."""
+    if p == 1:
+        return np.array([0.0, 1.0])
+    P = np.polynomial.legendre.Legendre.basis(p)
+    r = np.sort(np.real(P.deriv().roots()))
+    xi = np.concatenate([[0.0], (r + 1) / 2, [1.0]])
+    xi = 0.5 * (xi + (1 - xi[::-1]))
+    return xi
+
+
+def node_coords(cells, order: int, lengths, topology: str = "feq") -> np.ndarray:
+    """(n_ref, 3) coordinates of the lattice nodes."""
+    dim = len(cells)
+    xi = gl_points(order)
+    axes = []
+    for a in range(3):
+        if a >= dim:
+            axes.append(np.zeros(1))
+            continue
+        N, h = cells[a], lengths[a] / cells[a]
+        if topology == "dg":
+            x = np.array([(c + xi[l]) * h for c in range(N) for l in range(order + 1)])
+        else:
+            x = np.array([(c + xi[l]) * h for c in range(N) for l in range(order)] + [N * h])
+        axes.append(x)
+    Z, Y, X = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    return np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+
+
+def equilibrium(stencil: str, scaling: float, rho: np.ndarray, u_scaled: np.ndarray) -> np.ndarray:
+    """Second-order equilibrium with scaled velocities (the legacy
+    getEquilibriumDistribution, collision/BGKStandard.cpp:23-41)."""
+    e = unit_velocities(stencil)[:, : u_scaled.shape[0]]
+    w = _weights(stencil)
+    u = u_scaled / scaling
+    ue = 3.0 * (e @ u)
+    uu = 1.5 * np.sum(u * u, axis=0)
+    return np.ascontiguousarray(w[:, None] * rho[None, :] * (1 + ue * (1 + 0.5 * ue) - uu[None, :]))
+
+
+def taylor_green_3d(X: np.ndarray, Ma: float):
+    """TaylorGreenVortex3D initial state (benchmarks/TaylorGreenVortex3D.cpp:38-58):
+    u = (sin x cos y cos z, -cos x sin y cos z, 0),
+    rho = 1 + Ma^2 (cos 2x + cos 2y)(cos 2z + 2) / 16."""
+    x, y, z = X[:, 0], X[:, 1], X[:, 2]
+    u = np.stack([np.sin(x) * np.cos(y) * np.cos(z), -np.cos(x) * np.sin(y) * np.cos(z), np.zeros_like(x)])
+    rho = 1.0 + Ma * Ma / 16.0 * (np.cos(2 * x) + np.cos(2 * y)) * (np.cos(2 * z) + 2)
+    return rho, u
+
+
+def taylor_green_2d(X: np.ndarray, Ma: float, L: float = 2 * math.pi, rho_sign: float = 1.0):
+    """TaylorGreenVortex2D at t = 0 (benchmarks/TaylorGreenVortex2D.cpp:36-59):
+    u = (sin x' cos y', -cos x' sin y'), rho = 1 + rho_sign Ma^2 (cos 2x' + cos 2y')/4,
+    x' = 2 pi x / L.  rho_sign = +1 is the reference's sign."""
+    k = 2 * math.pi / L
+    x, y = X[:, 0] * k, X[:, 1] * k
+    u = np.stack([np.sin(x) * np.cos(y), -np.cos(x) * np.sin(y)])
+    rho = 1.0 + rho_sign * Ma * Ma * 0.25 * (np.cos(2 * x) + np.cos(2 * y))
+    return rho, u
+
+
+def shear_layer_2d(X: np.ndarray, kappa: float = 80.0, delta: float = 0.05, L: float = 1.0):
+    """Double-periodic shear layer (benchmarks/ShearLayer2D.cpp:39-53 with
+    u0 = 1): u = tanh(kappa (y - L/4)) for y <= L/2, tanh(kappa (3L/4 - y))
+    above; v = delta sin(2 pi (x/L + 1/4)); rho = 1."""
+    x, y = X[:, 0] / L, X[:, 1] / L
+    ux = np.where(y <= 0.5, np.tanh(kappa * (y - 0.25)), np.tanh(kappa * (0.75 - y)))
+    uy = delta * np.sin(2 * math.pi * (x + 0.25))
+    return np.ones_like(x), np.stack([ux, uy])

@@ -1,0 +1,352 @@
+"""CPU oracle for the semi-Lagrangian stream + collide path.
+
+TEST INFRASTRUCTURE ONLY: a numpy/ctypes front-end for ``natoracle.c``, the
+plain-C FP64 restatement of NATriuM's reference algorithm (see the header of
+``natoracle.c`` for the reference file:line each function follows).  Only the
+tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may use
+it, and only as the checker.  The product package ``natrium_gb300`` never
+imports it.
+
+Parity status: pinned against the known answers and invariants of the
+reference's own tests; the reference itself cannot be built or run (deal.II,
+Trilinos, p4est, Boost and MPI are absent), so no reference-run outputs exist.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "natoracle.c")
+_LIB = os.path.join(_HERE, "_build", "liboracle.so")
+
+D2Q9, D3Q19, D3Q27, D2Q25H = 0, 1, 2, 3
+STENCIL_IDS = {"D2Q9": D2Q9, "D3Q19": D3Q19, "D3Q27": D3Q27, "D2Q25H": D2Q25H}
+
+
+def build(force: bool = False) -> str:
+    """Compile natoracle.c into oracle/_build/liboracle.so (gcc, OpenMP)."""
+    os.makedirs(os.path.dirname(_LIB), exist_ok=True)
+    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(_SRC):
+        cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c11", "-o", _LIB, _SRC, "-lm"]
+        subprocess.run(cmd, check=True)
+    return _LIB
+
+
+class _Mesh(C.Structure):
+    _fields_ = [("dim", C.c_int), ("N", C.c_int * 3), ("p", C.c_int), ("dg", C.c_int),
+                ("L", C.c_double * 3)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build()
+        L = C.CDLL(path)
+        dp = C.POINTER(C.c_double)
+        L.orc_stencil.argtypes = [C.c_int, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_int), dp, dp, dp, dp]
+        L.orc_gl_points.argtypes = [C.c_int, dp]
+        L.orc_lagrange.argtypes = [C.c_int, dp, C.c_int, C.c_double]
+        L.orc_lagrange.restype = C.c_double
+        L.orc_n_nodes.argtypes = [C.POINTER(_Mesh)]
+        L.orc_n_nodes.restype = C.c_int64
+        L.orc_node_coords.argtypes = [C.POINTER(_Mesh), dp]
+        L.orc_face_crossed_first.argtypes = [C.c_int, dp, dp, dp, dp, dp, dp]
+        L.orc_face_crossed_first.restype = C.c_int
+        L.orc_sl_assemble.argtypes = [C.POINTER(_Mesh), C.c_int, C.c_double, C.c_double]
+        L.orc_sl_assemble.restype = C.c_void_p
+        L.orc_sl_free.argtypes = [C.c_void_p]
+        L.orc_sl_nnz.argtypes = [C.c_void_p, C.c_int]
+        L.orc_sl_nnz.restype = C.c_int64
+        L.orc_sl_lifetime_hits.argtypes = [C.c_void_p]
+        L.orc_sl_csr.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int32), dp]
+        L.orc_sl_stream.argtypes = [C.c_void_p, dp, dp, C.c_int]
+        L.orc_collide_bgk.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int64, dp, dp, dp, C.c_int, C.c_int]
+        L.orc_equilibrium.argtypes = [C.c_int, C.c_double, C.c_int64, dp, dp, dp]
+        L.orc_bgk_collide_single_point.argtypes = [C.c_int, C.c_double, C.c_double, dp]
+        L.orc_collide_bgk_incompressible_d2q9.argtypes = [C.c_double, C.c_double, C.c_int64, dp, dp, dp, C.c_int]
+        L.orc_collide_kbc_d2q9.argtypes = [C.c_double, C.c_double, C.c_int64, dp, dp, dp, C.c_int, dp]
+        L.orc_collide_kbc_d3q27.argtypes = [C.c_double, C.c_double, C.c_int64, dp, dp, dp, C.c_int, dp]
+        L.orc_step_bgk.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, dp, dp, dp, dp, C.c_int, C.c_int]
+        L.orc_time_step.argtypes = [C.c_double, C.c_int, C.c_double, C.c_double]
+        L.orc_time_step.restype = C.c_double
+        L.orc_max_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+# --------------------------------------------------------------------------
+# stencils, points, basis
+# --------------------------------------------------------------------------
+
+@dataclass
+class Stencil:
+    name: str
+    id: int
+    D: int
+    Q: int
+    scaling: float
+    e: np.ndarray          # (Q, 3) scaled directions
+    w: np.ndarray          # (Q,)
+    cs2: float             # scaled c_s^2 = scaling^2 / 3
+    max_speed: float       # sqrt(2) * scaling
+
+    @property
+    def e_unit(self):
+        return self.e / self.scaling
+
+
+def stencil(name: str, scaling: float = 1.0) -> Stencil:
+    sid = STENCIL_IDS[name]
+    D, Q = C.c_int(), C.c_int()
+    e = np.zeros(3 * 32)
+    w = np.zeros(32)
+    cs2, vmax = C.c_double(), C.c_double()
+    rc = lib().orc_stencil(sid, scaling, C.byref(D), C.byref(Q), _dp(e), _dp(w), C.byref(cs2), C.byref(vmax))
+    assert rc == 0
+    q = Q.value
+    return Stencil(name, sid, D.value, q, scaling, e[: 3 * q].reshape(q, 3).copy(), w[:q].copy(), cs2.value, vmax.value)
+
+
+def gl_points(p: int) -> np.ndarray:
+    xi = np.zeros(p + 1)
+    lib().orc_gl_points(p, _dp(xi))
+    return xi
+
+
+def lagrange(p: int, xi: np.ndarray, j: int, x: float) -> float:
+    xi = np.ascontiguousarray(xi, dtype=np.float64)
+    return lib().orc_lagrange(p, _dp(xi), j, x)
+
+
+def face_crossed_first(dim, lo, h, p_in, p_out):
+    """SemiLagrangian::faceCrossedFirst for an axis-aligned cell.
+    Returns (face_id, lambda, p_boundary)."""
+    arr = lambda v: np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(-1))
+    lo, h, pi, po = arr(lo), arr(h), arr(p_in), arr(p_out)
+    pb = np.zeros(3)
+    lam = C.c_double(0)
+    fid = lib().orc_face_crossed_first(dim, _dp(lo), _dp(h), _dp(pi), _dp(po), _dp(pb), C.byref(lam))
+    return fid, lam.value, pb[:dim].copy()
+
+
+def time_step(dx_min: float, p: int, max_speed: float, cfl: float) -> float:
+    return lib().orc_time_step(dx_min, p, max_speed, cfl)
+
+
+# --------------------------------------------------------------------------
+# mesh and semi-Lagrangian operator
+# --------------------------------------------------------------------------
+
+@dataclass
+class Mesh:
+    dim: int
+    N: tuple
+    p: int
+    dg: bool = False
+    L: tuple = (2 * math.pi, 2 * math.pi, 2 * math.pi)
+
+    def c(self) -> _Mesh:
+        m = _Mesh()
+        m.dim = self.dim
+        for a in range(3):
+            m.N[a] = int(self.N[a]) if a < self.dim else 1
+            m.L[a] = float(self.L[a]) if a < self.dim else 1.0
+        m.p = self.p
+        m.dg = 1 if self.dg else 0
+        return m
+
+    def nodes_per_axis(self, a: int) -> int:
+        if a >= self.dim:
+            return 1
+        return self.N[a] * (self.p + 1) if self.dg else self.N[a] * self.p + 1
+
+    @property
+    def n_nodes(self) -> int:
+        m = self.c()
+        return int(lib().orc_n_nodes(C.byref(m)))
+
+    def coords(self) -> np.ndarray:
+        m = self.c()
+        X = np.zeros((self.n_nodes, 3))
+        lib().orc_node_coords(C.byref(m), _dp(X))
+        return X
+
+    def h_min(self) -> float:
+        return min(self.L[a] / self.N[a] for a in range(self.dim))
+
+
+class SLOperator:
+    """Per-direction CSR streaming operator assembled by the restated tracker."""
+
+    def __init__(self, mesh: Mesh, st: Stencil, dt: float):
+        self.mesh, self.st, self.dt = mesh, st, dt
+        m = mesh.c()
+        self._h = lib().orc_sl_assemble(C.byref(m), st.id, st.scaling, dt)
+        if not self._h:
+            raise RuntimeError("oracle assembly failed")
+        self.n = mesh.n_nodes
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_sl_free(self._h)
+            self._h = None
+
+    def csr(self, alpha: int):
+        nnz = lib().orc_sl_nnz(self._h, alpha)
+        rp = np.zeros(self.n + 1, dtype=np.int64)
+        col = np.zeros(max(nnz, 1), dtype=np.int32)
+        val = np.zeros(max(nnz, 1))
+        lib().orc_sl_csr(self._h, alpha, rp.ctypes.data_as(C.POINTER(C.c_int64)),
+                         col.ctypes.data_as(C.POINTER(C.c_int32)), _dp(val))
+        return rp, col[:nnz], val[:nnz]
+
+    @property
+    def lifetime_hits(self) -> int:
+        return lib().orc_sl_lifetime_hits(self._h)
+
+    def stream(self, f: np.ndarray, nthreads: int = 1) -> np.ndarray:
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        out = np.empty_like(f)
+        lib().orc_sl_stream(self._h, _dp(f), _dp(out), nthreads)
+        return out
+
+    def step_bgk(self, f, tau, nsteps=1, nthreads=1):
+        """nsteps of copy + SpMV + collide sweep, in place on f (Q, n)."""
+        assert f.dtype == np.float64 and f.flags["C_CONTIGUOUS"]
+        work = np.empty_like(f)
+        rho = np.empty(self.n)
+        u = np.empty((self.st.D, self.n))
+        rc = lib().orc_step_bgk(self._h, self.st.id, self.st.scaling, tau, _dp(f), _dp(work), _dp(rho), _dp(u),
+                                nsteps, nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle step failed rc={rc}")
+        return rho, u
+
+
+# --------------------------------------------------------------------------
+# collisions (all arrays (Q, n) / (D, n), float64, modified in place)
+# --------------------------------------------------------------------------
+
+class DensityZeroError(RuntimeError):
+    pass
+
+
+def _check(rc):
+    if rc == -2:
+        raise DensityZeroError("Densities too small (< 1e-10) for collisions.")
+    if rc != 0:
+        raise RuntimeError(f"oracle rc={rc}")
+
+
+def collide_bgk(st: Stencil, tau: float, f, rho, u, in_init=False, nthreads=1):
+    n = f.shape[1]
+    _check(lib().orc_collide_bgk(st.id, st.scaling, tau, n, _dp(f), _dp(rho), _dp(u), int(in_init), nthreads))
+
+
+def collide_bgk_incompressible_d2q9(st: Stencil, tau: float, f, rho, u, in_init=False):
+    _check(lib().orc_collide_bgk_incompressible_d2q9(st.scaling, tau, f.shape[1], _dp(f), _dp(rho), _dp(u),
+                                                     int(in_init)))
+
+
+def collide_kbc(st: Stencil, tau: float, f, rho, u, in_init=False, gamma=None):
+    g = _dp(gamma) if gamma is not None else C.POINTER(C.c_double)()
+    fn = {"D2Q9": lib().orc_collide_kbc_d2q9, "D3Q27": lib().orc_collide_kbc_d3q27}[st.name]
+    _check(fn(st.scaling, tau, f.shape[1], _dp(f), _dp(rho), _dp(u), int(in_init), g))
+
+
+def collide(st: Stencil, model: str, tau: float, f, rho, u, in_init=False):
+    if model == "BGK_STANDARD":
+        collide_bgk(st, tau, f, rho, u, in_init)
+    elif model == "BGK_INCOMPRESSIBLE":
+        collide_bgk_incompressible_d2q9(st, tau, f, rho, u, in_init)
+    elif model == "KBC_STANDARD":
+        collide_kbc(st, tau, f, rho, u, in_init)
+    else:
+        raise ValueError(model)
+
+
+def equilibrium(st: Stencil, rho: np.ndarray, u: np.ndarray) -> np.ndarray:
+    n = rho.shape[0]
+    f = np.zeros((st.Q, n))
+    lib().orc_equilibrium(st.id, st.scaling, n, _dp(np.ascontiguousarray(rho)), _dp(np.ascontiguousarray(u)), _dp(f))
+    return f
+
+
+def collide_single_point(st: Stencil, relax_param: float, fq: np.ndarray) -> np.ndarray:
+    fq = np.ascontiguousarray(fq, dtype=np.float64).copy()
+    lib().orc_bgk_collide_single_point(st.id, st.scaling, relax_param, _dp(fq))
+    return fq
+
+
+def max_threads() -> int:
+    return lib().orc_max_threads()
+
+
+# --------------------------------------------------------------------------
+# problems: Taylor-Green initial conditions, kinetic energy
+# --------------------------------------------------------------------------
+
+def tgv2d_init(X: np.ndarray, Ma: float, L: float = 2 * math.pi, rho_sign: float = 1.0):
+    """TaylorGreenVortex2D (benchmarks/TaylorGreenVortex2D.cpp:36-59) at t=0,
+    analytic density rho = 1 + rho_sign * p / c_s^2 with c_s = 1/Ma, p = 1/4
+    (cos 2x' + cos 2y'), x' = 2 pi x / L.  rho_sign=+1 is the reference's sign."""
+    k = 2 * math.pi / L
+    x, y = X[:, 0] * k, X[:, 1] * k
+    u = np.stack([np.sin(x) * np.cos(y), -np.cos(x) * np.sin(y)])
+    p = 0.25 * (np.cos(2 * x) + np.cos(2 * y))
+    rho = 1.0 + rho_sign * p * Ma * Ma
+    return rho, u
+
+
+def tgv3d_init(X: np.ndarray, Ma: float):
+    """TaylorGreenVortex3D (benchmarks/TaylorGreenVortex3D.cpp:38-58)."""
+    x, y, z = X[:, 0], X[:, 1], X[:, 2]
+    u = np.stack([np.sin(x) * np.cos(y) * np.cos(z), -np.cos(x) * np.sin(y) * np.cos(z), np.zeros_like(x)])
+    p = 1.0 / 16.0 * (np.cos(2 * x) + np.cos(2 * y)) * (np.cos(2 * z) + 2)
+    rho = 1.0 + p * Ma * Ma
+    return rho, u
+
+
+def kinetic_energy(mesh: Mesh, rho: np.ndarray, u: np.ndarray) -> float:
+    """PhysicalProperties::kineticEnergy (solver/PhysicalProperties.cpp:29-79)
+    with Gauss-Lobatto quadrature on the support points: 0.5 sum_cells sum_q
+    rho |u|^2 w_q |J|; at GL support points shape_value(i,q) = delta_iq."""
+    p, D = mesh.p, mesh.dim
+    xi = gl_points(p)
+    # GL weights on [0,1]
+    P = np.polynomial.legendre.Legendre.basis(p)
+    wq = 1.0 / (p * (p + 1)) * 2.0 / (P(2 * xi - 1) ** 2) / 2.0
+    e = rho * np.sum(u * u, axis=0)
+    n_ax = [mesh.nodes_per_axis(a) for a in range(3)]
+    E = e.reshape(n_ax[2], n_ax[1], n_ax[0])
+    total = 0.0
+    jac = 1.0
+    for a in range(D):
+        jac *= mesh.L[a] / mesh.N[a]
+    per = (lambda c: slice(c * (p + 1), c * (p + 1) + p + 1)) if mesh.dg else (lambda c: slice(c * p, c * p + p + 1))
+    if D == 2:
+        W = np.outer(wq, wq)
+        for cy in range(mesh.N[1]):
+            for cx in range(mesh.N[0]):
+                total += np.sum(E[0, per(cy), per(cx)] * W)
+    else:
+        W = np.einsum("i,j,k->ijk", wq, wq, wq)
+        for cz in range(mesh.N[2]):
+            for cy in range(mesh.N[1]):
+                for cx in range(mesh.N[0]):
+                    total += np.sum(E[per(cz), per(cy), per(cx)] * W)
+    return 0.5 * total * jac

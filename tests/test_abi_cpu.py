@@ -1,0 +1,59 @@
+"""C-ABI checks that need no GPU: the library builds/loads, exports every
+symbol include/natgpu.h declares, and rejects bad specs before touching CUDA."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+import natrium_gb300 as N
+from natrium_gb300 import build as B
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "natgpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(nat_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_library_builds_and_exports_header_symbols():
+    path = B.build()
+    assert os.path.exists(path)
+    L = N.load_library()
+    syms = header_symbols()
+    assert len(syms) >= 15
+    for s in syms:
+        assert hasattr(L, s), s
+    assert sorted(N.EXPORTS) == syms
+    assert "sm_103a" in N.version()
+
+
+@pytest.mark.parametrize("bad", [
+    dict(order=0), dict(order=9), dict(scaling=-1.0), dict(viscosity=0.0),
+    dict(cells=(0, 4)), dict(collision="BGK_STANDARD", topology="feq", length=(0.0, 1.0)),
+])
+def test_invalid_specs_are_rejected_without_gpu(bad):
+    spec = N.SolverSpec(**{**dict(stencil="D2Q9", order=2, cells=(4, 4), scaling=1.0, viscosity=0.1), **bad})
+    with pytest.raises(N.NatError) as ei:
+        N.Solver(spec)
+    assert ei.value.code == N.NAT_ERR_INVALID_ARG
+
+
+def test_unsupported_combination_is_reported():
+    # the reference throws for BGKIncompressible on anything but D2Q9
+    # (collision/BGKIncompressible.cpp:54-55) and for KBC on D3Q19 (KBCStandard.cpp:79-81)
+    for st, coll in (("D3Q19", "BGK_INCOMPRESSIBLE"), ("D3Q19", "KBC_STANDARD")):
+        spec = N.SolverSpec(stencil=st, order=2, cells=(2, 2, 2), length=(1, 1, 1), scaling=1.0,
+                            viscosity=0.1, collision=coll)
+        with pytest.raises(N.NatError) as ei:
+            N.Solver(spec)
+        assert ei.value.code == N.NAT_ERR_UNSUPPORTED
+
+
+def test_last_error_null_handle():
+    L = N.load_library()
+    buf = C.create_string_buffer(64)
+    assert L.nat_last_error(None, buf, 64) == 0
+    assert buf.value == b"null handle"
