@@ -260,7 +260,11 @@ def run_ours(args):
     sol = N.Solver(spec)
     sol.set_stream(stream.cuda_stream)
     sol.upload_f(f0)
-    ncand, chosen = sol.autotune(10)
+    if args.variant:
+        sol.set_kernel_variant(args.variant)
+        ncand, chosen = 1, 0
+    else:
+        ncand, chosen = sol.autotune(10)
     kinfo = sol.kernel_info()
     torch.cuda.synchronize()
     if ws > 1:
@@ -293,6 +297,7 @@ def run_ours(args):
 
     # --- e2e through the C ABI with host buffers -------------------------------
     f_host = torch.from_numpy(f0).pin_memory().numpy()
+    sol.upload_f(f0)
     e2e_steps = max(5, min(50, args.steps // 20))
     e2e_s = time_e2e(sol, torch, f_host, None, None, e2e_steps)
     h2d = f0.nbytes
@@ -307,7 +312,10 @@ def run_ours(args):
     sol64 = N.Solver(spec64)
     sol64.set_stream(stream.cuda_stream)
     sol64.upload_f(f0)
-    sol64.autotune(3)
+    if args.variant:
+        sol64.set_kernel_variant(args.variant)
+    else:
+        sol64.autotune(3)
     kinfo64 = sol64.kernel_info()
     steps64 = max(3, args.steps // 4)
     per64, _ = time_device(sol64, torch, stream, flush, steps64, args.warmup)
@@ -341,7 +349,7 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": alg_bytes,
-                     "kernel": ("k_sl_step_v2" if kinfo["variant"] == 2 else "k_sl_step") + "<D3Q19,float,BGK>",
+                     "kernel": {1: "k_sl_step", 2: "k_sl_step_v2", 3: "k_sl_row"}[kinfo["variant"]] + "<D3Q19,float,BGK>",
                      "tile_nodes": kinfo["tile_nodes"], "threads": kinfo["threads"],
                      "autotune": {"candidates": ncand, "chosen": chosen}},
         "cpu_baseline": cpu,
@@ -366,6 +374,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--variant", type=int, default=0,
+                    help="fused kernel: 0 autotuned, 1 generic, 3 tile, 4 row-segment")
     ap.add_argument("--profile", action="store_true",
                     help="lean run for ncu: FP32 device timing only (no e2e, FP64 leg, CPU baseline or clocks)")
     args = ap.parse_args()

@@ -164,24 +164,26 @@ int nat_mass_energy(nat_solver* s, double* mass, double* kinetic_energy);
  * values, double for NAT_FP64 and float (f - w_i) for NAT_FP32_DEV). */
 int nat_device_f(nat_solver* s, void** f_dev);
 
-/* Kernel choice for the fused step: 0 = automatic (the specialised kernel
- * when an instantiation for this order / topology / tile exists and every
- * departure point lies in the node's own or the adjacent upwind cell, the
- * generic kernel otherwise), 1 = generic kernel only, 2 = specialised kernel
- * required (NAT_ERR_UNSUPPORTED when none applies). */
+/* Kernel choice for the fused step: 0 = automatic (a specialised kernel --
+ * row-segment or tile -- when an instantiation for this stencil / model /
+ * order / topology exists and every departure point lies in the node's own
+ * or the adjacent upwind cell, the generic kernel otherwise), 1 = generic
+ * kernel only, 2 = specialised kernel required (NAT_ERR_UNSUPPORTED when
+ * none applies), 3 = tile kernel required, 4 = row-segment kernel required. */
 int nat_set_kernel_variant(nat_solver* s, int variant);
-/* The fused-step kernel in use: 1 generic, 2 specialised. */
+/* The fused-step kernel in use: 1 generic, 2 tile, 3 row-segment. */
 int nat_kernel_variant(const nat_solver* s);
 
 /* Autotuner: times `steps` fused steps with every kernel that applies to
  * this configuration (each specialised tile shape and the generic kernel),
  * keeps the fastest, and restores f and the status word afterwards.  Writes
  * the number of candidates and the index of the chosen one (the generic
- * kernel is the last) when the pointers are not NULL.  Synchronises. */
+ * kernel is the last) when the pointers are not NULL.  Synchronises.  The
+ * trial steps run on the solver's own buffers (no allocation). */
 int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen);
 
-/* The fused-step kernel in use: variant (1 generic, 2 specialised), tile
- * extent in nodes, threads per CTA, dynamic shared memory per CTA. */
+/* The fused-step kernel in use: variant (1 generic, 2 tile, 3 row-segment),
+ * nodes per CTA along each axis, threads per CTA, dynamic shared memory. */
 int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* threads,
                     int64_t* smem_bytes);
 

@@ -283,7 +283,8 @@ class Solver:
         return m.value, e.value
 
     def set_kernel_variant(self, variant: int):
-        """0 automatic, 1 generic kernel, 2 specialised kernel required."""
+        """0 automatic, 1 generic kernel, 2 specialised kernel required,
+        3 tile kernel required, 4 row-segment kernel required."""
         self._check(self._L.nat_set_kernel_variant(self._h, int(variant)))
 
     @property

@@ -44,4 +44,16 @@ struct V2Launch {
 std::vector<V2Launch> find_v2(int stencil, int coll, int prec, int P, bool dg, const int cells[3], int dim,
                               int nx);
 
+// Row-segment fused kernel (sl_row.cuh): one warp per 32 x-nodes at a fixed
+// (y, z); CTA = WY x WZ warps.
+struct RowLaunch {
+  int stencil, coll, prec, P;
+  bool dg;
+  int wy, wz;
+  const void* fn;
+};
+void row_kernels_d2q9(std::vector<RowLaunch>& v);
+void row_kernels_d3q19(std::vector<RowLaunch>& v);
+void row_kernels_d3q27(std::vector<RowLaunch>& v);
+
 }  // namespace natgpu

@@ -23,6 +23,7 @@
 #include "natgpu_common.h"
 #include "sl_step.cuh"
 #include "sl_step_v2.cuh"
+#include "sl_row.cuh"
 
 using namespace natgpu;
 
@@ -55,8 +56,10 @@ struct nat_solver {
   double rest[32];
   // specialised kernel (sl_step_v2.cuh)
   int variant = 0;  // 0 auto, 1 generic only, 2 specialised required
-  bool use_v2 = false;
+  bool use_v2 = false;  // a specialised kernel (tile or row) is in use
+  int kind = 1;         // 1 generic, 2 tile, 3 row
   V2Launch v2;
+  RowLaunch row;
   SpecWeights<double> w64;
   SpecWeights<float> w32;
 };
@@ -505,32 +508,75 @@ void set_v2_weights(nat_solver* s) {
         }
 }
 
-// Candidate specialised kernels for the current configuration.
-std::vector<V2Launch> v2_candidates(nat_solver* s, int coll_sel, int smem_optin) {
-  std::vector<V2Launch> out;
+// A specialised fused kernel: the row-segment kernel (sl_row.cuh) or the
+// tile kernel (sl_step_v2.cuh).
+struct Cand {
+  int kind;  // 2 tile, 3 row
+  V2Launch v2;
+  RowLaunch row;
+};
+
+const std::vector<RowLaunch>& row_table() {
+  static const std::vector<RowLaunch> t = [] {
+    std::vector<RowLaunch> v;
+    row_kernels_d2q9(v);
+    row_kernels_d3q19(v);
+    row_kernels_d3q27(v);
+    return v;
+  }();
+  return t;
+}
+
+// Candidate specialised kernels for the current configuration, in order of
+// preference (row kernels first).
+std::vector<Cand> v2_candidates(nat_solver* s, int coll_sel, int smem_optin) {
+  std::vector<Cand> out;
   const bool dg = s->spec.topology == NAT_TOPO_DG;
   if (!pattern_ok(s->h_tab, s->D, s->spec.order, dg)) return out;
+  for (const RowLaunch& e : row_table()) {
+    if (e.stencil != s->spec.stencil || e.coll != coll_sel || e.prec != s->spec.precision ||
+        e.P != s->spec.order || e.dg != dg)
+      continue;
+    if (s->n_ax[1] % e.wy != 0 || s->n_ax[2] % e.wz != 0) continue;
+    Cand c;
+    c.kind = 3;
+    c.row = e;
+    out.push_back(c);
+  }
   for (const V2Launch& e :
        find_v2(s->spec.stencil, coll_sel, s->spec.precision, s->spec.order, dg, s->spec.cells, s->D, s->n_ax[0]))
-    if ((long long)e.smem <= smem_optin) out.push_back(e);
+    if ((long long)e.smem <= smem_optin) {
+      Cand c;
+      c.kind = 2;
+      c.v2 = e;
+      out.push_back(c);
+    }
   return out;
 }
 
-int use_candidate(nat_solver* s, const V2Launch& e) {
-  cudaError_t ce = cudaFuncSetAttribute(e.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.smem);
-  if (ce != cudaSuccess) return cuda_fail(s, ce, "v2 smem attribute");
+int use_candidate(nat_solver* s, const Cand& c) {
+  if (c.kind == 2) {
+    cudaError_t ce = cudaFuncSetAttribute(c.v2.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.v2.smem);
+    if (ce != cudaSuccess) return cuda_fail(s, ce, "v2 smem attribute");
+    s->v2 = c.v2;
+  } else {
+    s->row = c.row;
+  }
   set_v2_weights(s);
-  s->v2 = e;
+  s->kind = c.kind;
   s->use_v2 = true;
   return NAT_OK;
 }
 
 int select_v2(nat_solver* s, int coll_sel, int smem_optin) {
   s->use_v2 = false;
+  s->kind = 1;
   if (s->variant == 1) return NAT_OK;
-  std::vector<V2Launch> c = v2_candidates(s, coll_sel, smem_optin);
+  std::vector<Cand> all = v2_candidates(s, coll_sel, smem_optin), c;
+  for (const Cand& k : all)
+    if (s->variant <= 2 || (s->variant == 3 && k.kind == 2) || (s->variant == 4 && k.kind == 3)) c.push_back(k);
   if (c.empty()) {
-    if (s->variant == 2) return fail(s, NAT_ERR_UNSUPPORTED, "no specialised kernel for this configuration");
+    if (s->variant >= 2) return fail(s, NAT_ERR_UNSUPPORTED, "no specialised kernel of the requested kind");
     return NAT_OK;
   }
   return use_candidate(s, c.front());
@@ -568,7 +614,36 @@ int launch_v2_t(nat_solver* s, const SpecWeights<Real>& W, int write_macro) {
   return NAT_OK;
 }
 
+template <class Real>
+int launch_row_t(nat_solver* s, const SpecWeights<Real>& W, int write_macro) {
+  RowParams<Real> P;
+  P.f_in = static_cast<const Real*>(s->f[s->cur]);
+  P.f_out = static_cast<Real*>(s->f[1 - s->cur]);
+  P.rho = s->rho;
+  P.u = s->u;
+  P.status = s->status;
+  P.n = (int)s->n_dev;
+  P.nx = s->n_ax[0];
+  P.ny = s->n_ax[1];
+  P.nz = s->n_ax[2];
+  P.nseg = (s->n_ax[0] + 31) / 32;
+  P.tau = s->tau;
+  P.scaling = s->spec.scaling;
+  P.write_macro = write_macro;
+  P.W = W;
+  const int grid = P.nseg * (P.ny / s->row.wy) * (P.nz / s->row.wz);
+  void* args[] = {&P};
+  cudaError_t e = cudaLaunchKernel(s->row.fn, dim3(grid), dim3(32 * s->row.wy * s->row.wz), args, 0, s->stream);
+  if (e != cudaSuccess) return cuda_fail(s, e, "row stream-collide launch");
+  s->launches++;
+  s->cur = 1 - s->cur;
+  return NAT_OK;
+}
+
 int launch_v2(nat_solver* s, int write_macro) {
+  if (s->kind == 3)
+    return s->spec.precision == NAT_FP64 ? launch_row_t<double>(s, s->w64, write_macro)
+                                         : launch_row_t<float>(s, s->w32, write_macro);
   return s->spec.precision == NAT_FP64 ? launch_v2_t<double>(s, s->w64, write_macro)
                                        : launch_v2_t<float>(s, s->w32, write_macro);
 }
@@ -931,7 +1006,7 @@ int nat_device_f(nat_solver* s, void** f_dev) {
 int64_t nat_launch_count(const nat_solver* s) { return s ? s->launches : -1; }
 
 int nat_set_kernel_variant(nat_solver* s, int variant) {
-  if (!s || variant < 0 || variant > 2) return NAT_ERR_INVALID_ARG;
+  if (!s || variant < 0 || variant > 4) return NAT_ERR_INVALID_ARG;
   s->variant = variant;
   int smem_optin = 0;
   CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device),
@@ -939,7 +1014,7 @@ int nat_set_kernel_variant(nat_solver* s, int variant) {
   return select_v2(s, coll_selector(s->spec.collision), smem_optin);
 }
 
-int nat_kernel_variant(const nat_solver* s) { return s ? (s->use_v2 ? 2 : 1) : -1; }
+int nat_kernel_variant(const nat_solver* s) { return s ? (s->use_v2 ? s->kind : 1) : -1; }
 
 int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
   if (!s || steps < 1) return NAT_ERR_INVALID_ARG;
@@ -947,8 +1022,14 @@ int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
   CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device),
      "device attribute");
   const int coll_sel = coll_selector(s->spec.collision);
-  std::vector<V2Launch> cand = s->variant == 1 ? std::vector<V2Launch>() : v2_candidates(s, coll_sel, smem_optin);
-  const int ncand = (int)cand.size() + (s->variant == 2 ? 0 : 1);  // + the generic kernel
+  std::vector<Cand> cand = s->variant == 1 ? std::vector<Cand>() : v2_candidates(s, coll_sel, smem_optin);
+  if (s->variant >= 3) {
+    std::vector<Cand> keep;
+    for (const Cand& k : cand)
+      if ((s->variant == 3 && k.kind == 2) || (s->variant == 4 && k.kind == 3)) keep.push_back(k);
+    cand.swap(keep);
+  }
+  const int ncand = (int)cand.size() + (s->variant >= 2 ? 0 : 1);  // + the generic kernel
   if (n_candidates) *n_candidates = ncand;
   if (ncand == 0) return fail(s, NAT_ERR_UNSUPPORTED, "no kernel applies");
   // keep the state: back it up in the staging buffer (Q * n_ref doubles >= f)
@@ -1001,11 +1082,15 @@ int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
 
 int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* threads, int64_t* smem_bytes) {
   if (!s) return NAT_ERR_INVALID_ARG;
-  if (variant) *variant = s->use_v2 ? 2 : 1;
-  for (int a = 0; a < 3; ++a)
-    if (tile_nodes) tile_nodes[a] = s->use_v2 ? s->v2.B[a] : s->B[a];
-  if (threads) *threads = s->use_v2 ? s->v2.nth : STEP_THREADS;
-  if (smem_bytes) *smem_bytes = (int64_t)(s->use_v2 ? s->v2.smem : s->smem_step);
+  const int k = s->use_v2 ? s->kind : 1;
+  if (variant) *variant = k;
+  for (int a = 0; a < 3; ++a) {
+    int t = k == 2 ? s->v2.B[a] : s->B[a];
+    if (k == 3) t = a == 0 ? 32 : (a == 1 ? s->row.wy : s->row.wz);
+    if (tile_nodes) tile_nodes[a] = t;
+  }
+  if (threads) *threads = k == 2 ? s->v2.nth : (k == 3 ? 32 * s->row.wy * s->row.wz : STEP_THREADS);
+  if (smem_bytes) *smem_bytes = (int64_t)(k == 2 ? s->v2.smem : (k == 3 ? 0 : s->smem_step));
   return NAT_OK;
 }
 

@@ -1,0 +1,269 @@
+// Fused semi-Lagrangian stream + collide, row-segment kernel.
+//
+// One warp owns a segment of 32 consecutive lattice nodes along x at a fixed
+// (y, z); lane l owns node x0 + l and keeps all Q streamed populations of it
+// in registers.  For a direction alpha with displacement signs (sx, sy, sz):
+//   * the y and z Lagrange factors are applied in registers: the warp loads
+//     the (p+1)^k source rows of its window (coalesced, L1/L2-cached) and sums
+//     them with the warp-uniform weights of its node classes in y and z;
+//   * if sx != 0, the yz-factored row (segment plus the window halo) goes
+//     through a warp-private shared-memory row buffer and every lane applies
+//     its own x weights (node class in x) to its window; only __syncwarp
+//     orders it, there is no CTA-wide barrier anywhere in the kernel.
+// The collision then runs on the registers and f is written once, coalesced.
+// In the FP32 deviation mode a window sum is evaluated as
+//   v_j0 + sum_{j != j0} w_j (v_j - v_j0),
+// j0 being the source node at the destination's own position (weight ~ 1):
+// a constant field is reproduced exactly and the float rounding of the small
+// off-diagonal weights only multiplies differences of neighbouring values.
+// For y and z (warp-uniform node classes) the window rows are loaded in the
+// rotated order j0, j0+1, ... so that j0 is always slot 0.
+// Same operator, tables and window pattern as the specialised tile kernel
+// (sl_step_v2.cuh, Geo<P, DG>): every departure point lies in the node's own
+// cell or the adjacent upwind cell (checked on the host).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "collision.cuh"
+#include "natgpu_common.h"
+#include "sl_step_v2.cuh"
+#include "stencils.cuh"
+
+namespace natgpu {
+
+template <class Real>
+struct RowParams {
+  const Real* f_in;
+  Real* f_out;
+  double* rho;
+  double* u;
+  int* status;
+  int n;  // nodes per block
+  int nx, ny, nz;
+  int nseg;  // 32-node segments per row
+  double tau;
+  double scaling;
+  int write_macro;
+  SpecWeights<Real> W;  // [axis][sign][class][j]
+};
+
+// window of one node along an axis: start (absolute lattice index, before
+// the periodic wrap) and the index of the dominant weight
+template <int P, bool DG, int SG>
+__device__ __forceinline__ int win_start(int node, int c) {
+  constexpr int PER = Geo<P, DG>::PER;
+  int shift = 0;
+  if constexpr (SG > 0) shift = (c == 0) ? -1 : 0;
+  if constexpr (SG < 0 && DG) shift = (c == P) ? 1 : 0;
+  return node - c + shift * PER;
+}
+template <int P, bool DG, int SG>
+__device__ __forceinline__ int win_j0(int c) {
+  if constexpr (SG > 0) return c == 0 ? P : c;
+  if constexpr (SG < 0 && DG) return c == P ? 0 : c;
+  return c;
+}
+
+__device__ __forceinline__ int wrap(int g, int n) {
+  g += g < 0 ? n : 0;
+  g -= g >= n ? n : 0;
+  return g;
+}
+
+// sum_s w_s v_s over a window whose slot 0 holds the dominant node; in the
+// deviation mode v_0 + sum_{s >= 1} w_s (v_s - v_0)
+template <bool DEV, int P, class Real>
+__device__ __forceinline__ Real wsum(const Real* w, const Real (&v)[P + 1]) {
+  if constexpr (DEV) {
+    Real acc = Real(0);
+#pragma unroll
+    for (int j = 1; j <= P; ++j) acc = fma(w[j], v[j] - v[0], acc);
+    return acc + v[0];
+  } else {
+    Real acc = w[0] * v[0];
+#pragma unroll
+    for (int j = 1; j <= P; ++j) acc = fma(w[j], v[j], acc);
+    return acc;
+  }
+}
+
+// the same over a window in natural order with the dominant slot j0 known
+// at run time (x factor, per-lane class); w_j0 is stored as 0 in the
+// deviation mode
+template <bool DEV, int P, class Real>
+__device__ __forceinline__ Real wsum_j0(const Real* w, const Real (&v)[P + 1], int j0) {
+  if constexpr (DEV) {
+    Real v0 = v[0];
+#pragma unroll
+    for (int j = 1; j <= P; ++j) v0 = (j == j0) ? v[j] : v0;
+    Real acc = Real(0);
+#pragma unroll
+    for (int j = 0; j <= P; ++j) acc = fma(w[j], v[j] - v0, acc);
+    return acc + v0;
+  } else {
+    Real acc = w[0] * v[0];
+#pragma unroll
+    for (int j = 1; j <= P; ++j) acc = fma(w[j], v[j], acc);
+    return acc;
+  }
+}
+
+// number of directions before ALPHA that have an x component
+template <class S>
+__host__ __device__ constexpr int xorder(int alpha) {
+  int k = 0;
+  for (int i = 1; i < alpha; ++i) k += S::e(i, 0) != 0;
+  return k;
+}
+
+template <class S, class Real, int COLL, int P, bool DG, int WY, int WZ>
+__global__ void __launch_bounds__(32 * WY * WZ, (sizeof(Real) == 4 ? 2 : 1))
+    k_sl_row(const __grid_constant__ RowParams<Real> prm) {
+  constexpr bool DEV = sizeof(Real) == 4;
+  constexpr int Q = S::Q;
+  constexpr int PER = Geo<P, DG>::PER;
+  constexpr int HL = PER;                  // left halo of the x window buffer
+  constexpr int BW = 32 + PER + P + 1;     // buffer width
+  constexpr int NW = WY * WZ;
+  __shared__ Real rowbuf[NW][2][BW + 1];
+
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int wyi = warp % WY, wzi = warp / WY;
+  const int bid = blockIdx.x;
+  const int seg = bid % prm.nseg;
+  const int by = (bid / prm.nseg) % (prm.ny / WY);
+  const int bz = bid / (prm.nseg * (prm.ny / WY));
+  const int nx = prm.nx, ny = prm.ny, nz = prm.nz;
+  const int x0 = seg * 32;
+  const int x = x0 + lane;
+  const bool valid = x < nx;
+  const int y = by * WY + wyi;
+  const int z = bz * WZ + wzi;
+  const int nxy = nx * ny;
+  const int node = z * nxy + y * nx + (valid ? x : 0);
+  // node classes
+  const int cx = (valid ? x : 0) % PER, cy = y % PER, cz = z % PER;
+  // x positions of this lane's two buffer slots
+  // (full modulo: a row can be shorter than the 32-lane segment)
+  const int gxa = ((x0 - HL + lane) % nx + nx) % nx;
+  const bool hasb = lane + 32 < BW;
+  const int gxb = ((x0 - HL + 32 + (hasb ? lane : 0)) % nx + nx) % nx;
+
+  // 1-D weights per CTA in shared memory, [axis][sign][class][slot]: for y
+  // and z in the rotated slot order (slot s = window index (j0 + s) mod
+  // (P+1)); for x in natural order, with the dominant weight zeroed in the
+  // deviation mode.  x weights are read per lane (class of its node), y / z
+  // weights are warp broadcasts.
+  __shared__ Real sw[3][2][PER][P + 1];
+  for (int i = threadIdx.x; i < 3 * 2 * PER * (P + 1); i += 32 * NW) {
+    const int j = i % (P + 1), c = (i / (P + 1)) % PER, sd = (i / ((P + 1) * PER)) % 2, a = i / ((P + 1) * PER * 2);
+    const int j0 = sd == 0 ? win_j0<P, DG, 1>(c) : win_j0<P, DG, -1>(c);
+    Real w;
+    if (a == 0)
+      w = (DEV && j == j0) ? Real(0) : prm.W.w[a][sd][c][j];
+    else
+      w = prm.W.w[a][sd][c][(j0 + j) % (P + 1)];
+    (&sw[0][0][0][0])[i] = w;
+  }
+  __syncthreads();
+
+  Real fs[Q];
+  fs[0] = valid ? prm.f_in[node] : Real(0);
+
+  static_for<1, Q>([&](auto I) {
+    constexpr int A = decltype(I)::value;
+    constexpr int sx = S::e(A, 0), sy = S::e(A, 1), sz = S::D == 3 ? S::e(A, 2) : 0;
+    constexpr int NJY = sy != 0 ? P + 1 : 1;
+    constexpr int NJZ = sz != 0 ? P + 1 : 1;
+    const Real* __restrict__ src = prm.f_in + (long long)A * prm.n;
+    // warp-uniform row windows
+    int ys = y, zs = z, j0y = 0, j0z = 0;
+    if constexpr (sy != 0) {
+      ys = win_start<P, DG, sy>(y, cy);
+      j0y = win_j0<P, DG, sy>(cy);
+    }
+    if constexpr (sz != 0) {
+      zs = win_start<P, DG, sz>(z, cz);
+      j0z = win_j0<P, DG, sz>(cz);
+    }
+    constexpr int dy = sy > 0 ? 0 : 1, dz = sz > 0 ? 0 : 1, dx = sx > 0 ? 0 : 1;
+    // yz-factored value at x positions gx (own) or gxa / gxb (buffer slots)
+    auto yz = [&](int gx) -> Real {
+      Real zv[P + 1];
+#pragma unroll
+      for (int jz = 0; jz < NJZ; ++jz) {
+        // rotated window order: slot 0 is the dominant row
+        const int rz = j0z + jz;
+        const int gz = wrap(zs + (rz > P ? rz - (P + 1) : rz), nz);
+        Real yv[P + 1];
+#pragma unroll
+        for (int jy = 0; jy < NJY; ++jy) {
+          const int ry = j0y + jy;
+          const int gy = wrap(ys + (ry > P ? ry - (P + 1) : ry), ny);
+          yv[jy] = __ldg(src + gz * nxy + gy * nx + gx);
+        }
+        if constexpr (sy != 0)
+          zv[jz] = wsum<DEV, P>(sw[1][dy][cy], yv);
+        else
+          zv[jz] = yv[0];
+      }
+      if constexpr (sz != 0)
+        return wsum<DEV, P>(sw[2][dz][cz], zv);
+      else
+        return zv[0];
+    };
+    Real out;
+    if constexpr (sx == 0) {
+      out = yz(valid ? x : 0);
+    } else {
+      // alternate buffers between consecutive x factors: the __syncwarp of
+      // the next one orders this one's reads before its writes
+      Real* buf = rowbuf[warp][xorder<S>(A) & 1];
+      buf[lane] = yz(gxa);
+      if (hasb) buf[lane + 32] = yz(gxb);
+      __syncwarp();
+      const int st = win_start<P, DG, sx>(x, cx) - (x0 - HL);
+      Real xv[P + 1];
+#pragma unroll
+      for (int j = 0; j <= P; ++j) xv[j] = buf[st + j];
+      out = wsum_j0<DEV, P>(sw[0][dx][cx], xv, win_j0<P, DG, sx>(cx));
+    }
+    fs[A] = out;
+  });
+
+  if (!valid) return;
+  int bad = 0;
+  Real u[3] = {0, 0, 0};
+  Real rho = Real(1);
+  Real pre[Q];
+  if constexpr (DEV) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) pre[q] = fs[q];
+  }
+  if constexpr (COLL == COLL_BGK) {
+    rho = collide_bgk<S, DEV, false>(fs, Real(1.0 / prm.tau), u, false);
+    if constexpr (DEV) conserve<S>(fs, pre);
+  } else if constexpr (COLL == COLL_BGK_INC) {
+    rho = collide_bgk_inc<DEV, false>(fs, Real(1.0 / prm.tau), u, false);
+  } else if constexpr (COLL == COLL_KBC) {
+    rho = collide_kbc<S, DEV, false>(fs, Real(prm.tau), u, false);
+    if constexpr (DEV) conserve<S>(fs, pre);
+  }
+  (void)pre;
+  if constexpr (COLL != COLL_NONE) {
+    if (!(rho >= Real(1e-10))) bad |= (rho != rho) ? ST_NAN : ST_DENSITY;
+    if (prm.write_macro) {
+      prm.rho[node] = (double)rho;
+      prm.u[node] = (double)u[0] * prm.scaling;
+      prm.u[prm.n + node] = (double)u[1] * prm.scaling;
+      if constexpr (S::D == 3) prm.u[2 * prm.n + node] = (double)u[2] * prm.scaling;
+    }
+    if (bad) atomicOr(prm.status, bad);
+  }
+#pragma unroll
+  for (int q = 0; q < Q; ++q) prm.f_out[q * prm.n + node] = fs[q];
+}
+
+}  // namespace natgpu

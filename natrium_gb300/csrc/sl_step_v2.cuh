@@ -149,15 +149,28 @@ struct Tile {
   static constexpr int mx(int a, int b) { return a > b ? a : b; }
   static constexpr int PXM = mx(mx(G::XW(BX, 1, AL), G::XW(BX, -1, AL)), G::XW(BX, 0, AL));
   static constexpr int REGION = PXM * RYM * RZM;  // one region buffer (elements)
-  static constexpr int T1 = PXM * RYM * BZ;       // after the z factor
-  static constexpr int T2 = PXM * BY * BZ;        // after the y factor
+  static constexpr int T1 = PXM * RYM * BZ;       // output of a first (non-final) stage
+  static constexpr int T2 = PXM * BY * BZ;        // output of a second (non-final) stage
+  // most factors any direction needs (3 only for the corner directions of D3Q27)
+  static constexpr int maxstages() {
+    int m = 0;
+    for (int i = 1; i < S::Q; ++i) {
+      int k = (S::e(i, 0) != 0) + (S::e(i, 1) != 0) + (D == 3 && S::e(i, 2) != 0);
+      m = k > m ? k : m;
+    }
+    return m;
+  }
+  static constexpr int NSTAGE = maxstages();
+  static constexpr int NREG = 3;  // region buffers in flight
+  static constexpr size_t ELEMS = (size_t)NREG * REGION + (NSTAGE >= 2 ? 2 * (size_t)T1 : 0) +
+                                  (NSTAGE >= 3 ? 2 * (size_t)T2 : 0) + (size_t)S::Q * TB;
   static_assert(BX % AL == 0, "tile x extent must keep 16-byte row alignment");
 };
 
 template <class S, class Real, int P, bool DG, int CX, int CY, int CZ>
 __host__ __device__ constexpr size_t v2_smem_bytes() {
   using TL = Tile<S, P, DG, CX, CY, CZ, sizeof(Real)>;
-  return 128 + sizeof(Real) * (2 * (size_t)TL::REGION + TL::T1 + TL::T2 + (size_t)S::Q * TL::TB);
+  return 128 + sizeof(Real) * TL::ELEMS;
 }
 
 // ---------------------------------------------------------------------------
@@ -267,49 +280,82 @@ __device__ __forceinline__ void load_region(const Real* __restrict__ src, Real* 
   }
 }
 
-// Stream one direction from its region buffer into the streamed buffer.
-template <class S, class Real, int P, bool DG, bool DEV, int CX, int CY, int CZ, int ALPHA, int NTH>
-__device__ __forceinline__ void stream_dir(const Real* reg, Real* t1, Real* t2, Real* sb,
-                                           const SpecWeights<Real>& W) {
-  using TL = Tile<S, P, DG, CX, CY, CZ, sizeof(Real)>;
+// Per direction: its factors in the order z, y, x (active axes only) and the
+// box extents before each of them.
+template <class S, int P, bool DG, int CX, int CY, int CZ, int ES, int ALPHA>
+struct Dir {
+  using TL = Tile<S, P, DG, CX, CY, CZ, ES>;
   using G = Geo<P, DG>;
-  constexpr int sx = S::e(ALPHA, 0), sy = S::e(ALPHA, 1), sz = TL::D == 3 ? S::e(ALPHA, 2) : 0;
-  constexpr int RX = G::R(TL::BX, sx), RY = G::R(TL::BY, sy), RZ = TL::D == 3 ? G::R(TL::BZ, sz) : 1;
-  constexpr int IP = TL::PXM;                   // row pitch of region, t1, t2
-  constexpr int XC = G::XC(TL::BX, sx, TL::AL);  // column of the region's x origin
-  constexpr int BX = TL::BX, BY = TL::BY, BZ = TL::BZ;
-  constexpr int dxs = sx > 0 ? 0 : 1, dys = sy > 0 ? 0 : 1, dzs = sz > 0 ? 0 : 1;
-  const Real* cur = reg + XC;
-  Real* t1o = t1 + XC;
-  Real* t2o = t2 + XC;
-  // z factor: (RX, RY, RZ) -> (RX, RY, BZ)
-  if constexpr (sz != 0) {
-    constexpr bool LAST = (sy == 0 && sx == 0);
-    if constexpr (LAST) {
-      factor<2, sz, Real, P, DG, DEV, CZ, RX, RY, RZ, IP, BX, NTH>(cur, sb, W.w[2][dzs]);
-      return;
-    } else {
-      factor<2, sz, Real, P, DG, DEV, CZ, RX, RY, RZ, IP, IP, NTH>(cur, t1o, W.w[2][dzs]);
-      __syncthreads();
-      cur = t1o;
+  static constexpr int sx = S::e(ALPHA, 0), sy = S::e(ALPHA, 1), sz = TL::D == 3 ? S::e(ALPHA, 2) : 0;
+  static constexpr int NS = (sz != 0) + (sy != 0) + (sx != 0);
+  static constexpr int RX = G::R(TL::BX, sx), RY = G::R(TL::BY, sy), RZ = TL::D == 3 ? G::R(TL::BZ, sz) : 1;
+  // axis of stage k
+  static constexpr int axis(int k) {
+    int a[3] = {0, 0, 0}, n = 0;
+    if (sz != 0) a[n++] = 2;
+    if (sy != 0) a[n++] = 1;
+    if (sx != 0) a[n++] = 0;
+    return a[k];
+  }
+  // extent along axis b before stage k (factors before k have reduced
+  // their axis to the tile extent)
+  static constexpr int ext(int k, int b) {
+    int e = b == 0 ? RX : (b == 1 ? RY : RZ);
+    for (int j = 0; j < k; ++j)
+      if (axis(j) == b) e = b == 0 ? TL::BX : (b == 1 ? TL::BY : TL::BZ);
+    return e;
+  }
+  static constexpr int sign(int b) { return b == 0 ? sx : (b == 1 ? sy : sz); }
+  static constexpr int cells(int b) { return b == 0 ? CX : (b == 1 ? CY : CZ); }
+  static constexpr int XC = G::XC(TL::BX, sx, TL::AL);  // column of the region x origin
+};
+
+// Stage K of direction ALPHA: reads the region (K = 0) or the previous
+// stage's buffer, writes the next stage buffer or (last stage) the streamed
+// buffer.
+template <class S, class Real, int P, bool DG, bool DEV, int CX, int CY, int CZ, int ALPHA, int K, int NTH>
+__device__ __forceinline__ void run_stage(Real* const (&reg)[3], Real* const (&st1)[2], Real* const (&st2)[2],
+                                          Real* sb, const SpecWeights<Real>& W) {
+  using TL = Tile<S, P, DG, CX, CY, CZ, sizeof(Real)>;
+  using DI = Dir<S, P, DG, CX, CY, CZ, sizeof(Real), ALPHA>;
+  constexpr int A = DI::axis(K);
+  constexpr int SG = DI::sign(A);
+  constexpr int CA = DI::cells(A);
+  constexpr int IX = DI::ext(K, 0), IY = DI::ext(K, 1), IZ = DI::ext(K, 2);
+  constexpr bool LAST = K == DI::NS - 1;
+  constexpr int IP = TL::PXM;
+  constexpr int OP = LAST ? TL::BX : TL::PXM;
+  constexpr int sidx = SG > 0 ? 0 : 1;
+  const Real* in;
+  if constexpr (K == 0)
+    in = reg[(ALPHA - 1) % 3] + DI::XC;
+  else if constexpr (K == 1)
+    in = st1[(ALPHA - 1) % 2] + DI::XC;
+  else
+    in = st2[(ALPHA - 1) % 2] + DI::XC;
+  Real* out;
+  if constexpr (LAST)
+    out = sb + ALPHA * TL::TB;
+  else if constexpr (K == 0)
+    out = st1[(ALPHA - 1) % 2] + DI::XC;
+  else
+    out = st2[(ALPHA - 1) % 2] + DI::XC;
+  factor<A, SG, Real, P, DG, DEV, CA, IX, IY, IZ, IP, OP, NTH>(in, out, W.w[A][sidx]);
+}
+
+// Phase PH of the software pipeline: stage K of direction ALPHA runs in
+// phase ALPHA - 1 + K, for every direction whose stage falls in this phase.
+template <class S, class Real, int P, bool DG, bool DEV, int CX, int CY, int CZ, int PH, int NTH>
+__device__ __forceinline__ void run_phase(Real* const (&reg)[3], Real* const (&st1)[2], Real* const (&st2)[2],
+                                          Real* sb, const SpecWeights<Real>& W) {
+  static_for<0, 3>([&](auto KK) {
+    constexpr int K = decltype(KK)::value;
+    constexpr int ALPHA = PH + 1 - K;
+    if constexpr (ALPHA >= 1 && ALPHA < S::Q) {
+      using DI = Dir<S, P, DG, CX, CY, CZ, sizeof(Real), ALPHA>;
+      if constexpr (K < DI::NS) run_stage<S, Real, P, DG, DEV, CX, CY, CZ, ALPHA, K, NTH>(reg, st1, st2, sb, W);
     }
-  }
-  // y factor: (RX, RY, BZ) -> (RX, BY, BZ)
-  if constexpr (sy != 0) {
-    constexpr bool LAST = (sx == 0);
-    if constexpr (LAST) {
-      factor<1, sy, Real, P, DG, DEV, CY, RX, RY, BZ, IP, BX, NTH>(cur, sb, W.w[1][dys]);
-      return;
-    } else {
-      factor<1, sy, Real, P, DG, DEV, CY, RX, RY, BZ, IP, IP, NTH>(cur, t2o, W.w[1][dys]);
-      __syncthreads();
-      cur = t2o;
-    }
-  }
-  // x factor: (RX, BY, BZ) -> (BX, BY, BZ), the streamed buffer
-  if constexpr (sx != 0) {
-    factor<0, sx, Real, P, DG, DEV, CX, RX, BY, BZ, IP, BX, NTH>(cur, sb, W.w[0][dxs]);
-  }
+  });
 }
 
 template <class S, class Real, int COLL, int P, bool DG, int CX, int CY, int CZ, int NTH>
@@ -319,13 +365,16 @@ __global__ void __launch_bounds__(NTH, 1) k_sl_step_v2(const __grid_constant__ S
   constexpr int Q = S::Q;
   constexpr int BX = TL::BX, BY = TL::BY, BZ = TL::BZ, TB = TL::TB;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem_raw);  // 2 mbarriers
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem_raw);  // 3 mbarriers
   __shared__ int s_abort;
-  Real* reg0 = reinterpret_cast<Real*>(smem_raw + 128);
-  Real* reg1 = reg0 + TL::REGION;
-  Real* t1 = reg1 + TL::REGION;
-  Real* t2 = t1 + TL::T1;
-  Real* sb = t2 + TL::T2;
+  Real* base = reinterpret_cast<Real*>(smem_raw + 128);
+  Real* const reg[3] = {base, base + TL::REGION, base + 2 * TL::REGION};
+  Real* stb = base + 3 * TL::REGION;
+  Real* const st1[2] = {stb, stb + (TL::NSTAGE >= 2 ? TL::T1 : 0)};
+  stb += TL::NSTAGE >= 2 ? 2 * TL::T1 : 0;
+  Real* const st2[2] = {stb, stb + (TL::NSTAGE >= 3 ? TL::T2 : 0)};
+  stb += TL::NSTAGE >= 3 ? 2 * TL::T2 : 0;
+  Real* sb = stb;
 
   const int bid = blockIdx.x;
   const int tx = bid % prm.ntx, ty = (bid / prm.ntx) % prm.nty, tz = bid / (prm.ntx * prm.nty);
@@ -337,47 +386,50 @@ __global__ void __launch_bounds__(NTH, 1) k_sl_step_v2(const __grid_constant__ S
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
+    mbar_init(&bars[2], 1);
     s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
-  // prefetch direction 1 into buffer 0
-  load_region<S, Real, P, DG, CX, CY, CZ, 1, NTH>(prm.f_in + 1 * n, reg0, &bars[0], x0, y0, z0, nx, ny, nz);
+  // prologue: regions of directions 1, 2, 3
+  static_for<1, 4>([&](auto I) {
+    constexpr int A = decltype(I)::value;
+    if constexpr (A < Q)
+      load_region<S, Real, P, DG, CX, CY, CZ, A, NTH>(prm.f_in + (long long)A * n, reg[(A - 1) % 3],
+                                                      &bars[(A - 1) % 3], x0, y0, z0, nx, ny, nz);
+  });
   // rest population: not streamed
   for (int t = threadIdx.x; t < TB; t += NTH) {
     const int x = t % BX, y = (t / BX) % BY, z = t / (BX * BY);
     sb[t] = prm.f_in[(long long)(z0 + z) * nxy + (long long)(y0 + y) * nx + (x0 + x)];
   }
   bool ok = true;
-  static_for<1, Q>([&](auto I) {
-    constexpr int A = decltype(I)::value;
-    constexpr int b = (A - 1) & 1;           // buffer of direction A
-    constexpr unsigned par = ((A - 1) >> 1) & 1;  // its use count parity
-    Real* cur = b == 0 ? reg0 : reg1;
-    Real* nxt = b == 0 ? reg1 : reg0;
+  // phases 0 .. Q: phase PH starts stage 0 of direction PH + 1
+  static_for<0, Q + 1>([&](auto I) {
+    constexpr int PH = decltype(I)::value;
+    constexpr int A = PH + 1;  // direction whose region is consumed now
     if (!ok) return;
-    if constexpr (A + 1 < Q) {
-      load_region<S, Real, P, DG, CX, CY, CZ, A + 1, NTH>(prm.f_in + (long long)(A + 1) * n, nxt,
-                                                          &bars[1 - b], x0, y0, z0, nx, ny, nz);
+    if constexpr (A < Q) {
+      if (!mbar_wait(&bars[(A - 1) % 3], ((A - 1) / 3) & 1, MBAR_MAX_POLLS)) s_abort = 1;
     }
-    if (!mbar_wait(&bars[b], par, MBAR_MAX_POLLS)) s_abort = 1;
     __syncthreads();
     if (s_abort) {
-      // wait (bounded) for the copies of the next direction, then stop
-      if constexpr (A + 1 < Q) {
-        if (threadIdx.x == 0) mbar_wait(&bars[1 - b], (A >> 1) & 1, MBAR_MAX_POLLS);
-      }
       ok = false;
       return;
     }
-    stream_dir<S, Real, P, DG, DEV, CX, CY, CZ, A, NTH>(cur, t1, t2, sb + A * TB, prm.W);
-    __syncthreads();
+    // direction A + 2 shares its region buffer with direction A - 1, whose
+    // region was last read in phase PH - 1 (before the barrier above)
+    if constexpr (A + 2 < Q && PH >= 1)
+      load_region<S, Real, P, DG, CX, CY, CZ, A + 2, NTH>(prm.f_in + (long long)(A + 2) * n, reg[(A + 1) % 3],
+                                                          &bars[(A + 1) % 3], x0, y0, z0, nx, ny, nz);
+    run_phase<S, Real, P, DG, DEV, CX, CY, CZ, PH, NTH>(reg, st1, st2, sb, prm.W);
   });
   if (!ok) {
     // a bulk copy never completed: report and stop this tile
     if (threadIdx.x == 0) atomicOr(prm.status, ST_TIMEOUT);
     return;
   }
+  __syncthreads();
 
   // collision from the streamed buffer, one write of f
   int bad = 0;

@@ -264,8 +264,8 @@ V2_CASES = [
 @pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
 @pytest.mark.parametrize("case", V2_CASES, ids=[_ids(c) for c in V2_CASES])
 def test_specialised_and_generic_kernels_agree(gpu_lib, case, precision):
-    """The compile-time specialised kernel and the generic kernel against
-    the oracle on the same input (both variants forced)."""
+    """Every fused kernel that applies (generic, tile, row-segment) against
+    the oracle on the same input, each forced in turn."""
     stencil, cells, p, dg, model = case
     st, mesh, dt, tau, spec = make_case(stencil, cells, p, dg, model, precision=precision)
     f0 = periodic_state(mesh, st, seed=9)
@@ -273,24 +273,29 @@ def test_specialised_and_generic_kernels_agree(gpu_lib, case, precision):
     f1, rho1, u1 = oracle_step(S, st, model, tau, f0, 2)
     tol = TOL64 if precision == "fp64" else 1e-6
     out = {}
-    for variant in (1, 2):
+    for variant, kind in ((1, 1), (3, 2), (4, 3)):
         with N.Solver(spec) as sol:
-            sol.set_kernel_variant(variant)
-            assert sol.kernel_variant == variant
+            try:
+                sol.set_kernel_variant(variant)
+            except N.NatError:
+                continue
+            assert sol.kernel_variant == kind
             sol.upload_f(f0)
             sol.step(2)
-            out[variant] = sol.download_f()
+            out[kind] = sol.download_f()
             rho, u = sol.download_macro()
-        assert rel_l2(out[variant], f1) <= tol, variant
-        assert rel_l2(u, u1) <= (1e-11 if precision == "fp64" else 1e-6), variant
+        assert rel_l2(out[kind], f1) <= tol, kind
+        assert rel_l2(u, u1) <= (1e-11 if precision == "fp64" else 1e-6), kind
+    assert 1 in out and len(out) >= 2
     if precision == "fp64":
-        assert rel_l2(out[1], out[2]) <= TOL64
+        for k in out:
+            assert rel_l2(out[k], out[1]) <= TOL64
 
 
 def test_automatic_variant_choice(gpu_lib):
     st, mesh, dt, tau, spec = make_case("D3Q19", (4, 2, 2), 4, True, "BGK_STANDARD", precision="fp32dev")
     with N.Solver(spec) as sol:
-        assert sol.kernel_variant == 2
+        assert sol.kernel_variant in (2, 3)
     st, mesh, dt, tau, spec = make_case("D3Q19", (3, 3, 3), 2, False, "BGK_STANDARD")
     with N.Solver(spec) as sol:
         assert sol.kernel_variant == 1
@@ -335,7 +340,35 @@ def test_autotune_keeps_state_and_parity(gpu_lib, precision):
         nc, ch = sol.autotune(3)
         assert nc >= 2 and 0 <= ch < nc
         info = sol.kernel_info()
-        assert info["variant"] in (1, 2)
+        assert info["variant"] in (1, 2, 3)
         assert rel_l2(sol.download_f(), f0) <= (TOL64 if precision == "fp64" else 1e-7)
         sol.step(1)
         assert rel_l2(sol.download_f(), f1) <= (TOL64 if precision == "fp64" else 1e-6)
+
+
+ROW_CASES = [(st, cells, p, dg, m) for (st, cells, m) in (("D2Q9", (2, 4), "BGK_STANDARD"), ("D2Q9", (4, 2), "KBC_STANDARD"),
+                                                          ("D2Q9", (2, 2), "BGK_INCOMPRESSIBLE"))
+             for p in (1, 2, 3, 4, 5, 6) for dg in (False, True)] + [
+    ("D3Q19", (2, 2, 2), p, dg, "BGK_STANDARD") for p in (2, 3, 5, 6) for dg in (False, True)] + [
+    ("D3Q27", (2, 2, 2), p, dg, m) for p in (2, 3) for dg in (False, True) for m in ("BGK_STANDARD", "KBC_STANDARD")]
+
+
+@pytest.mark.parametrize("case", ROW_CASES, ids=[_ids(c) for c in ROW_CASES])
+def test_row_kernel_all_orders(gpu_lib, case):
+    """The row-segment kernel (forced when it applies, else the automatic
+    choice) against the oracle for every FE order and both topologies."""
+    stencil, cells, p, dg, model = case
+    st, mesh, dt, tau, spec = make_case(stencil, cells, p, dg, model)
+    f0 = periodic_state(mesh, st, seed=13)
+    if model == "BGK_INCOMPRESSIBLE":
+        f0 = incompressible_equilibrium(st, f0)
+    S = O.SLOperator(mesh, st, dt)
+    f1, rho1, u1 = oracle_step(S, st, model, tau, f0, 1)
+    with N.Solver(spec) as sol:
+        try:
+            sol.set_kernel_variant(4)
+        except N.NatError:
+            sol.set_kernel_variant(0)
+        sol.upload_f(f0)
+        sol.step(1)
+        assert rel_l2(sol.download_f(), f1) <= TOL64
