@@ -329,7 +329,7 @@ def run_ours(args):
     ach64 = alg64 / (ms64 * 1e-3) / 1e9
     tr = traffic_from_profile()
     traffic = None
-    if tr and tr.get("workload") == WORKLOAD["name"]:
+    if tr and tr.get("workload") == WORKLOAD["name"] and kinfo["variant"] == 3:
         traffic = tr.get("dram_bytes_per_launch")
 
     if rank != 0:
