@@ -337,6 +337,21 @@ def run_ours(args):
             torch.distributed.destroy_process_group()
         return 0
     cpu = cpu_baseline() if ws == 1 else None
+    serving = None
+    if not args.no_serving:
+        from natrium_gb300 import serving as SV
+        arr, reqs = SV.workload(512, seed=0, rate=200.0)
+        serving = SV.run_workload(arr, reqs)
+        seq = SV.run_sequential(reqs[:32], "fp64")
+        cap = SV.run_workload(np.zeros(len(reqs)), reqs)
+        serving["capacity"] = {"solves_per_s": cap["solves_per_s"], "wall_s": cap["wall_s"],
+                               "latency_p50_s": cap["latency_p50_s"], "latency_p99_s": cap["latency_p99_s"],
+                               "node_updates_per_s": cap["node_updates_per_s"],
+                               "note": "all 512 requests submitted at t = 0 (saturated server)"}
+        serving.update({"workload": "512 D2Q9 solves (TGV / shear layer, BGK / KBC, N in {4..64}, p 2-6, "
+                                    "Ma 0.02-0.1, Re 100-5000, 50-2000 steps), Poisson 200 req/s, seed 0, "
+                                    "FP32 deviation storage",
+                        "fp64_one_at_a_time": {**seq, "sample": "first 32 requests of the same stream"}})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -360,6 +375,7 @@ def run_ours(args):
         "fp64_plain": {"value": ws * nodes / (ms64 * 1e-3), "ms_per_step": ms64, "steps": steps64,
                        "roofline_frac": ach64 / hbm, "achieved_gbs": ach64, "kernel": kinfo64},
         "speedup_vs_fp64_plain": ms64 / ms,
+        "serving": serving,
         "state_ok": ok,
     }
     print(json.dumps(line))
@@ -376,6 +392,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--variant", type=int, default=0,
                     help="fused kernel: 0 autotuned, 1 generic, 3 tile, 4 row-segment")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--profile", action="store_true",
                     help="lean run for ncu: FP32 device timing only (no e2e, FP64 leg, CPU baseline or clocks)")
     args = ap.parse_args()

@@ -190,6 +190,63 @@ int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* t
 /* Number of kernels this handle has launched (for launch accounting). */
 int64_t nat_launch_count(const nat_solver* s);
 
+/* ---- continuous-batching server (independent 2-D solves) ---------------
+ * Serving workload of the spec: many independent periodic D2Q9 solves
+ * of uneven size, order and model, admitted by their HBM footprint into a
+ * device pool and advanced together, one persistent graph-captured launch
+ * per server step.  No reference counterpart: the reference runs one solve
+ * per process (solver/CFDSolver.cpp). */
+#define NAT_INIT_TAYLOR_GREEN 0 /* benchmarks/TaylorGreenVortex2D.cpp:36-59 */
+#define NAT_INIT_SHEAR_LAYER 1  /* benchmarks/ShearLayer2D.cpp:39-53 */
+
+typedef struct nat_request {
+  int stencil;      /* NAT_D2Q9 */
+  int collision;    /* NAT_BGK_STANDARD or NAT_KBC_STANDARD */
+  int order;        /* FE_Q order 1..6 */
+  int cells[2];
+  double length[2];
+  double scaling;   /* stencil scaling (sqrt(3)/Ma for unit velocity) */
+  double viscosity;
+  double cfl;       /* dt = CFL h_min / (sqrt(2) scaling p^2) when dt <= 0 */
+  double dt;
+  int steps;        /* time steps to run */
+  int init;         /* NAT_INIT_TAYLOR_GREEN or NAT_INIT_SHEAR_LAYER */
+  double Ma;        /* density amplitude of the Taylor-Green state */
+  double u0;        /* velocity amplitude (scaled units) */
+  double kappa;     /* shear layer: tanh steepness */
+  double delta;     /* shear layer: perturbation amplitude */
+} nat_request;
+
+typedef struct nat_server_stats_t {
+  int64_t pending, live, completing, finished;
+  int64_t steps, node_updates;
+  int64_t pool_used, pool_bytes;
+  int64_t launches;
+} nat_server_stats_t;
+
+typedef struct nat_server nat_server;
+
+/* Create a server with a device pool of pool_bytes and at most max_slots
+ * live solves on the current device. */
+int nat_server_create(size_t pool_bytes, int max_slots, nat_server** out);
+int nat_server_destroy(nat_server* s);
+/* Queue a request; admitted in submission order as slots and pool memory
+ * free up. */
+int nat_server_submit(nat_server* s, const nat_request* r, int64_t* id);
+/* One server step: collect finished results, admit queued requests, advance
+ * every live solve by one time step (one graph launch). */
+int nat_server_step(nat_server* s);
+/* Ids of finished requests (up to max_ids); wait != 0 blocks until every
+ * solve that has run its last step is copied out. */
+int nat_server_poll(nat_server* s, int64_t* ids, int max_ids, int* n_done, int wait);
+/* Copy a finished request's rho (n_nodes) and scaled u (2 * n_nodes) out
+ * (device lattice order, periodic duplicates folded) and release it; status
+ * is the solve's own (NAT_OK or NAT_ERR_DENSITY_UNDERFLOW / NAT_ERR_NAN /
+ * NAT_ERR_UNSUPPORTED). rho / u may be NULL to query n_nodes. */
+int nat_server_result(nat_server* s, int64_t id, double* rho, double* u, int64_t* n_nodes, int* status);
+int nat_server_stats(const nat_server* s, nat_server_stats_t* st);
+int nat_server_last_error(const nat_server* s, char* buf, size_t len);
+
 /* Library version string. */
 const char* nat_version(void);
 

@@ -3,8 +3,10 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
 #include <vector>
 
+#include "../../include/natgpu.h"
 #include "natgpu_common.h"
 
 namespace natgpu {
@@ -40,6 +42,10 @@ struct V2Launch {
   const void* fn;
   size_t smem;
 };
+// operator tables of a solve (natgpu_api.cu), for the server's slots
+int build_solver_tables(const struct ::nat_spec* spec, double dt, SLTables* T, std::string* err);
+void gl_points_host(int p, double* xi);
+
 // every instantiation that applies, in order of preference
 std::vector<V2Launch> find_v2(int stencil, int coll, int prec, int P, bool dg, const int cells[3], int dim,
                               int nx);

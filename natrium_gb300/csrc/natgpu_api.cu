@@ -657,6 +657,41 @@ int upload_rest(nat_solver* s) {
 
 }  // namespace
 
+// Operator tables of a solve described by spec at time step dt (used by the
+// server for its slots).  Requires the compile-time window pattern of the
+// row kernel.
+int natgpu::build_solver_tables(const nat_spec* spec, double dt, SLTables* T, std::string* err) {
+  nat_solver tmp;
+  tmp.spec = *spec;
+  HostStencil hs;
+  if (!get_host_stencil(spec->stencil, &hs)) return NAT_ERR_UNSUPPORTED;
+  tmp.D = hs.D;
+  tmp.Q = hs.Q;
+  const bool dg = spec->topology == NAT_TOPO_DG;
+  tmp.period = dg ? spec->order + 1 : spec->order;
+  for (int a = 0; a < 3; ++a) {
+    if (a < tmp.D) {
+      tmp.n_ax[a] = spec->cells[a] * tmp.period;
+      tmp.h[a] = spec->length[a] / spec->cells[a];
+      tmp.B[a] = tmp.period;
+    }
+  }
+  tmp.dt = dt;
+  int rc = build_tables(&tmp, hs);
+  if (rc) {
+    if (err) *err = tmp.err;
+    return rc;
+  }
+  if (!pattern_ok(tmp.h_tab, tmp.D, spec->order, dg)) {
+    if (err) *err = "time step too large for the row kernel's window pattern";
+    return NAT_ERR_UNSUPPORTED;
+  }
+  *T = tmp.h_tab;
+  return NAT_OK;
+}
+
+void natgpu::gl_points_host(int p, double* xi) { gl_points(p, xi); }
+
 size_t natgpu::step_smem_bytes(int prec, const int Rmax[3], const int B[3]) {
   return prec == 0 ? smem_layout<double>(Rmax, B).total : smem_layout<float>(Rmax, B).total;
 }

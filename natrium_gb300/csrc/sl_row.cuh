@@ -117,57 +117,74 @@ __host__ __device__ constexpr int xorder(int alpha) {
   return k;
 }
 
-template <class S, class Real, int COLL, int P, bool DG, int WY, int WZ>
-__global__ void __launch_bounds__(32 * WY * WZ, (sizeof(Real) == 4 ? 2 : 1))
-    k_sl_row(const __grid_constant__ RowParams<Real> prm) {
+// Arguments of one row-segment work item (one solve).
+template <class Real>
+struct RowArgs {
+  const Real* f_in;
+  Real* f_out;
+  double* rho;
+  double* u;
+  int* status;
+  int n;
+  int nx, ny, nz;
+  double tau;
+  double scaling;
+  int write_macro;
+};
+
+// Element count of a weight table [3][2][PER][P+1] for order P, topology DG.
+template <int P, bool DG>
+__host__ __device__ constexpr int row_table_size() {
+  return 3 * 2 * Geo<P, DG>::PER * (P + 1);
+}
+
+// Fill a weight table from [axis][sign][class][j] weights: y and z in the
+// rotated slot order (slot s = window index (j0 + s) mod (P+1)), x in
+// natural order with the dominant weight zeroed in the deviation mode.
+// Threads t0, t0 + stride, ... of the caller cooperate.
+template <class Real, int P, bool DG>
+__device__ __forceinline__ void fill_row_table(Real* sw, const Real (&W)[3][2][PER_MAX][PMAX1], int t0,
+                                               int stride) {
   constexpr bool DEV = sizeof(Real) == 4;
-  constexpr int Q = S::Q;
   constexpr int PER = Geo<P, DG>::PER;
-  constexpr int HL = PER;                  // left halo of the x window buffer
-  constexpr int BW = 32 + PER + P + 1;     // buffer width
-  constexpr int NW = WY * WZ;
-  __shared__ Real rowbuf[NW][2][BW + 1];
-
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  const int wyi = warp % WY, wzi = warp / WY;
-  const int bid = blockIdx.x;
-  const int seg = bid % prm.nseg;
-  const int by = (bid / prm.nseg) % (prm.ny / WY);
-  const int bz = bid / (prm.nseg * (prm.ny / WY));
-  const int nx = prm.nx, ny = prm.ny, nz = prm.nz;
-  const int x0 = seg * 32;
-  const int x = x0 + lane;
-  const bool valid = x < nx;
-  const int y = by * WY + wyi;
-  const int z = bz * WZ + wzi;
-  const int nxy = nx * ny;
-  const int node = z * nxy + y * nx + (valid ? x : 0);
-  // node classes
-  const int cx = (valid ? x : 0) % PER, cy = y % PER, cz = z % PER;
-  // x positions of this lane's two buffer slots
-  // (full modulo: a row can be shorter than the 32-lane segment)
-  const int gxa = ((x0 - HL + lane) % nx + nx) % nx;
-  const bool hasb = lane + 32 < BW;
-  const int gxb = ((x0 - HL + 32 + (hasb ? lane : 0)) % nx + nx) % nx;
-
-  // 1-D weights per CTA in shared memory, [axis][sign][class][slot]: for y
-  // and z in the rotated slot order (slot s = window index (j0 + s) mod
-  // (P+1)); for x in natural order, with the dominant weight zeroed in the
-  // deviation mode.  x weights are read per lane (class of its node), y / z
-  // weights are warp broadcasts.
-  __shared__ Real sw[3][2][PER][P + 1];
-  for (int i = threadIdx.x; i < 3 * 2 * PER * (P + 1); i += 32 * NW) {
+  for (int i = t0; i < row_table_size<P, DG>(); i += stride) {
     const int j = i % (P + 1), c = (i / (P + 1)) % PER, sd = (i / ((P + 1) * PER)) % 2, a = i / ((P + 1) * PER * 2);
     const int j0 = sd == 0 ? win_j0<P, DG, 1>(c) : win_j0<P, DG, -1>(c);
     Real w;
     if (a == 0)
-      w = (DEV && j == j0) ? Real(0) : prm.W.w[a][sd][c][j];
+      w = (DEV && j == j0) ? Real(0) : W[a][sd][c][j];
     else
-      w = prm.W.w[a][sd][c][(j0 + j) % (P + 1)];
-    (&sw[0][0][0][0])[i] = w;
+      w = W[a][sd][c][(j0 + j) % (P + 1)];
+    sw[i] = w;
   }
-  __syncthreads();
+}
+
+// One warp: stream + collide the 32-node segment starting at x0 of row
+// (y, z).  swt: the weight table (fill_row_table); buf: this warp's two
+// row buffers of BW + 1 elements.
+template <class S, class Real, int COLL, int P, bool DG>
+__device__ __forceinline__ void row_body(const RowArgs<Real>& prm, const Real* swt, Real* buf2, int y, int z,
+                                         int x0, int lane) {
+  constexpr bool DEV = sizeof(Real) == 4;
+  constexpr int Q = S::Q;
+  constexpr int PER = Geo<P, DG>::PER;
+  constexpr int HL = PER;               // left halo of the x window buffer
+  constexpr int BW = 32 + PER + P + 1;  // buffer width
+  using Tab = const Real (*)[2][PER][P + 1];
+  Tab sw = reinterpret_cast<Tab>(swt);
+
+  const int nx = prm.nx, ny = prm.ny, nz = prm.nz;
+  const int x = x0 + lane;
+  const bool valid = x < nx;
+  const int nxy = nx * ny;
+  const int node = z * nxy + y * nx + (valid ? x : 0);
+  // node classes
+  const int cx = (valid ? x : 0) % PER, cy = y % PER, cz = z % PER;
+  // x positions of this lane's two buffer slots (full modulo: a row can be
+  // shorter than the 32-lane segment)
+  const int gxa = ((x0 - HL + lane) % nx + nx) % nx;
+  const bool hasb = lane + 32 < BW;
+  const int gxb = ((x0 - HL + 32 + (hasb ? lane : 0)) % nx + nx) % nx;
 
   Real fs[Q];
   fs[0] = valid ? prm.f_in[node] : Real(0);
@@ -189,7 +206,10 @@ __global__ void __launch_bounds__(32 * WY * WZ, (sizeof(Real) == 4 ? 2 : 1))
       j0z = win_j0<P, DG, sz>(cz);
     }
     constexpr int dy = sy > 0 ? 0 : 1, dz = sz > 0 ? 0 : 1, dx = sx > 0 ? 0 : 1;
-    // yz-factored value at x positions gx (own) or gxa / gxb (buffer slots)
+    (void)dz;
+    (void)dy;
+    (void)dx;
+    // yz-factored value at x position gx
     auto yz = [&](int gx) -> Real {
       Real zv[P + 1];
 #pragma unroll
@@ -220,7 +240,7 @@ __global__ void __launch_bounds__(32 * WY * WZ, (sizeof(Real) == 4 ? 2 : 1))
     } else {
       // alternate buffers between consecutive x factors: the __syncwarp of
       // the next one orders this one's reads before its writes
-      Real* buf = rowbuf[warp][xorder<S>(A) & 1];
+      Real* buf = buf2 + (xorder<S>(A) & 1) * (BW + 1);
       buf[lane] = yz(gxa);
       if (hasb) buf[lane + 32] = yz(gxb);
       __syncwarp();
@@ -264,6 +284,42 @@ __global__ void __launch_bounds__(32 * WY * WZ, (sizeof(Real) == 4 ? 2 : 1))
   }
 #pragma unroll
   for (int q = 0; q < Q; ++q) prm.f_out[q * prm.n + node] = fs[q];
+}
+
+// Single-solve kernel: CTA = WY x WZ warps over rows (y, z) and one 32-node
+// x segment.
+template <class S, class Real, int COLL, int P, bool DG, int WY, int WZ>
+__global__ void __launch_bounds__(32 * WY * WZ, (sizeof(Real) == 4 ? 2 : 1))
+    k_sl_row(const __grid_constant__ RowParams<Real> prm) {
+  constexpr int PER = Geo<P, DG>::PER;
+  constexpr int BW = 32 + PER + P + 1;
+  constexpr int NW = WY * WZ;
+  __shared__ Real rowbuf[NW][2][BW + 1];
+  __shared__ Real sw[row_table_size<P, DG>()];
+  fill_row_table<Real, P, DG>(sw, prm.W.w, threadIdx.x, 32 * NW);
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int wyi = warp % WY, wzi = warp / WY;
+  const int bid = blockIdx.x;
+  const int seg = bid % prm.nseg;
+  const int by = (bid / prm.nseg) % (prm.ny / WY);
+  const int bz = bid / (prm.nseg * (prm.ny / WY));
+  RowArgs<Real> a;
+  a.f_in = prm.f_in;
+  a.f_out = prm.f_out;
+  a.rho = prm.rho;
+  a.u = prm.u;
+  a.status = prm.status;
+  a.n = prm.n;
+  a.nx = prm.nx;
+  a.ny = prm.ny;
+  a.nz = prm.nz;
+  a.tau = prm.tau;
+  a.scaling = prm.scaling;
+  a.write_macro = prm.write_macro;
+  row_body<S, Real, COLL, P, DG>(a, sw, &rowbuf[warp][0][0], by * WY + wyi, bz * WZ + wzi, seg * 32, lane);
 }
 
 }  // namespace natgpu

@@ -364,10 +364,10 @@ __global__ void __launch_bounds__(NTH, 1) k_sl_step_v2(const __grid_constant__ S
   using TL = Tile<S, P, DG, CX, CY, CZ, sizeof(Real)>;
   constexpr int Q = S::Q;
   constexpr int BX = TL::BX, BY = TL::BY, BZ = TL::BZ, TB = TL::TB;
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem_raw);  // 3 mbarriers
+  extern __shared__ __align__(128) unsigned char smem_v2[];
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem_v2);  // 3 mbarriers
   __shared__ int s_abort;
-  Real* base = reinterpret_cast<Real*>(smem_raw + 128);
+  Real* base = reinterpret_cast<Real*>(smem_v2 + 128);
   Real* const reg[3] = {base, base + TL::REGION, base + 2 * TL::REGION};
   Real* stb = base + 3 * TL::REGION;
   Real* const st1[2] = {stb, stb + (TL::NSTAGE >= 2 ? TL::T1 : 0)};
