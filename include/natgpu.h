@@ -160,6 +160,26 @@ int nat_last_error(const nat_solver* s, char* buf, size_t len);
  * they use the macroscopic fields of the last collision. */
 int nat_mass_energy(nat_solver* s, double* mass, double* kinetic_energy);
 
+/* Allocation-free variant of nat_mass_energy.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory where they need
+ * the diagnostics: work recorded into a CUDA graph (cudaMalloc is not allowed
+ * during stream capture), hosts whose framework owns all device memory
+ * through its own pool, and loops that cannot pay for cudaMalloc's implicit
+ * synchronisation.  Inputs: rho (n) and u (dim * n) in device memory, in the
+ * device lattice order (n_axis[a] nodes per axis, periodic FE_Q duplicates
+ * folded: N_a p per axis, DG: N_a (p+1)); output: out_dev[0] = mass,
+ * out_dev[1] = kinetic energy, in device memory, written on cuda_stream.
+ * The only scratch is a 64 KiB file-scope device array that every GPU
+ * loading the library holds until exit; inputs above NAT_NOALLOC_MAX_NODES
+ * nodes are rejected (NAT_ERR_INVALID_ARG).  The first call on a device looks
+ * up the array's device address (make it before any stream capture); calls
+ * whose kernels overlap on the GPU share the array and race.  Calls no
+ * cudaMalloc / cudaFree.  Deterministic: fixed reduction order. */
+#define NAT_NOALLOC_MAX_NODES 16777216LL
+int nat_mass_energy_noalloc(const double* rho_dev, const double* u_dev, int dim, const int n_axis[3],
+                            int order, int topology, const double cell_size[3], double* out_dev,
+                            void* cuda_stream);
+
 /* Device pointers of the current distribution buffer (Q blocks of n_dev
  * values, double for NAT_FP64 and float (f - w_i) for NAT_FP32_DEV). */
 int nat_device_f(nat_solver* s, void** f_dev);

@@ -51,7 +51,7 @@ EXPORTS = [
     "nat_mass_energy", "nat_device_f", "nat_launch_count", "nat_version", "nat_set_kernel_variant",
     "nat_kernel_variant", "nat_autotune", "nat_kernel_info",
     "nat_server_create", "nat_server_destroy", "nat_server_submit", "nat_server_step", "nat_server_poll",
-    "nat_server_result", "nat_server_stats", "nat_server_last_error",
+    "nat_server_result", "nat_server_stats", "nat_server_last_error", "nat_mass_energy_noalloc",
 ]
 
 
@@ -113,6 +113,8 @@ def load_library(path: str | None = None):
     L.nat_launch_count.restype = C.c_int64
     L.nat_version.restype = C.c_char_p
     L.nat_set_kernel_variant.argtypes = [vp, C.c_int]
+    L.nat_mass_energy_noalloc.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int,
+                                          C.POINTER(C.c_double), vp, vp]
     L.nat_kernel_variant.argtypes = [vp]
     L.nat_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.nat_kernel_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), i64p]

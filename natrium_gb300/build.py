@@ -19,7 +19,8 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libnatgpu.so")
 
 SOURCES = ["natgpu_api.cu", "k_d2q9.cu", "k_d3q19.cu", "k_d3q27.cu", "k_v2.cu", "k_row_d2q9.cu",
-           "k_row_d3q19.cu", "k_row_d3q27.cu", "serve.cu"]
+           "k_row_d3q19.cu", "k_row_d3q27.cu", "serve.cu",
+           "natgpu_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
