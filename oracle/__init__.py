@@ -79,6 +79,14 @@ def lib():
         L.orc_time_step.argtypes = [C.c_double, C.c_int, C.c_double, C.c_double]
         L.orc_time_step.restype = C.c_double
         L.orc_max_threads.restype = C.c_int
+        L.orc_thermal_init.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int64, dp, dp, dp, dp, dp]
+        L.orc_thermal_feq.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int64, dp, dp, dp, dp]
+        L.orc_collide_compressible.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                               C.c_int, C.c_int, C.c_int64, dp, dp, dp, dp, dp, dp, C.c_int,
+                                               C.c_int]
+        L.orc_step_compressible.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                            C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp, dp, C.c_int,
+                                            C.c_int]
         _lib = L
     return _lib
 
@@ -237,6 +245,24 @@ class SLOperator:
         return rho, u
 
 
+    def step_compressible(self, f, g, tau, th=None, nsteps=1, nthreads=1):
+        """nsteps of stream(f), gStream(g), collide (CompressibleCFDSolver::run),
+        in place on f and g (Q, n).  Returns rho, u (scaled), T, mask."""
+        th = th or Thermal()
+        for a in (f, g):
+            assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+        work = np.empty_like(f)
+        rho = np.empty(self.n)
+        u = np.empty((self.st.D, self.n))
+        T = np.empty(self.n)
+        mask = np.empty(self.n)
+        rc = lib().orc_step_compressible(self._h, self.st.id, self.st.scaling, tau, th.gamma, th.prandtl,
+                                         int(th.prandtl_set), int(th.sutherland), int(th.quartic), _dp(f), _dp(g),
+                                         _dp(work), _dp(rho), _dp(u), _dp(T), _dp(mask), nsteps, nthreads)
+        _check(rc)
+        return rho, u, T, mask
+
+
 # --------------------------------------------------------------------------
 # collisions (all arrays (Q, n) / (D, n), float64, modified in place)
 # --------------------------------------------------------------------------
@@ -290,6 +316,49 @@ def collide_single_point(st: Stencil, relax_param: float, fq: np.ndarray) -> np.
     fq = np.ascontiguousarray(fq, dtype=np.float64).copy()
     lib().orc_bgk_collide_single_point(st.id, st.scaling, relax_param, _dp(fq))
     return fq
+
+
+@dataclass
+class Thermal:
+    """Compressible-model settings (SolverConfiguration: heat capacity ratio,
+    Prandtl number and its switch, Sutherland law switch; equilibrium scheme
+    QUARTIC_EQUILIBRIUM or BGK_EQUILIBRIUM)."""
+    gamma: float = 1.4
+    prandtl: float = 1.0
+    prandtl_set: bool = False
+    sutherland: bool = False
+    quartic: bool = True
+
+
+def thermal_init(st: Stencil, rho, u, T, gamma: float = 1.4):
+    """Equilibrium initialisation of f and g (CompressibleCFDSolver.h:849-899);
+    u scaled.  Returns (f, g), each (Q, n)."""
+    n = rho.shape[0]
+    f = np.zeros((st.Q, n))
+    g = np.zeros((st.Q, n))
+    c = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    rc = lib().orc_thermal_init(st.id, st.scaling, gamma, n, _dp(c(rho)), _dp(c(u)), _dp(c(T)), _dp(f), _dp(g))
+    _check(rc)
+    return f, g
+
+
+def thermal_feq(st: Stencil, rho, u, T, quartic: bool = True):
+    """The collision's equilibrium (quartic, Equilibria.h:130-267, or second
+    order, :66-83) at (rho, u scaled, T); (Q, n)."""
+    n = rho.shape[0]
+    feq = np.zeros((st.Q, n))
+    c = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    _check(lib().orc_thermal_feq(st.id, st.scaling, int(quartic), n, _dp(c(rho)), _dp(c(u)), _dp(c(T)), _dp(feq)))
+    return feq
+
+
+def collide_compressible(st: Stencil, tau: float, f, g, rho, u, T, mask, th: Thermal = Thermal(),
+                         in_init=False, nthreads=1):
+    """CollisionOperator::collideAll(f, g, rho, u, T, mask) with relaxWithG;
+    in place on f, g; writes rho, u (scaled, unless in_init), T, mask."""
+    _check(lib().orc_collide_compressible(st.id, st.scaling, tau, th.gamma, th.prandtl, int(th.prandtl_set),
+                                          int(th.sutherland), int(th.quartic), f.shape[1], _dp(f), _dp(g),
+                                          _dp(rho), _dp(u), _dp(T), _dp(mask), int(in_init), nthreads))
 
 
 def max_threads() -> int:

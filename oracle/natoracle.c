@@ -36,6 +36,12 @@
  *                collision/BGKStandard.cpp:23-41
  *   - BGK incompressible D2Q9: collision/BGKIncompressible.cpp:62-190
  *   - KBC D2Q9: collision/KBCStandard.cpp:88-497 (without the statistics file)
+ *   - compressible two-population BGK on D2Q25H: CollisionOperator.h:113-224,
+ *                CollisionSchemes.h:43-118 (relaxWithG), Equilibria.h:88-267
+ *                (quartic equilibrium), AuxiliaryCollisionFunctions.h:289-307,
+ *                420-566 (temperature, g^eq, Prandtl terms, Knudsen estimate,
+ *                H3/H4), CompressibleCFDSolver.h:181-314, 739-899 (stream,
+ *                gStream, collide, equilibrium initialisation)
  *   - KBC D3Q27: no reference implementation exists; the D2Q9 construction
  *                (trace kept in the shear part, product-form equilibrium of
  *                KBCStandard.cpp:26-63) is extended to D3Q27.  Parity unpinned.
@@ -1061,6 +1067,322 @@ int orc_step_bgk(const orc_sl* s, int stencil, double scaling, double tau,
     orc_sl_stream(s, f, work, nthreads);
     memcpy(f, work, sizeof(double) * (size_t)s->Q * s->n);
     rc = orc_collide_bgk(stencil, scaling, tau, s->n, f, rho, u, 0, nthreads);
+    if (rc != ORC_OK) return rc;
+  }
+  return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* compressible two-population model (D2Q25H)                                */
+/* ------------------------------------------------------------------------ */
+
+/* Per-call constants of the compressible collision: unscaled directions
+ * e = direction / scaling, weights and unscaled c_s^2 = scaled c_s^2 /
+ * scaling^2 (GeneralCollisionData, AuxiliaryCollisionFunctions.h:151-178),
+ * and the Hermite tensors computed once per collideAll call
+ * (CollisionOperator.h:151-152; calculateH3 / calculateH4,
+ * AuxiliaryCollisionFunctions.h:520-566). */
+typedef struct {
+  int D, Q;
+  double e[32][3], w[32], cs2;
+  double H3[32][2][2][2];
+  double H4[32][2][2][2][2];
+} orc_thermal_k;
+
+static int thermal_consts(int stencil, double scaling, orc_thermal_k* k) {
+  double es[3 * 32], cs2s, vmax;
+  int i, a, b, c, d;
+  if (stencil != ORC_D2Q25H) return ORC_ERR_ARG;
+  if (orc_stencil(stencil, scaling, &k->D, &k->Q, es, k->w, &cs2s, &vmax) != ORC_OK) return ORC_ERR_ARG;
+  for (i = 0; i < k->Q; i++)
+    for (a = 0; a < 3; a++) k->e[i][a] = es[3 * i + a] / scaling;
+  k->cs2 = cs2s / (scaling * scaling);
+  for (i = 0; i < k->Q; i++) {
+    const double* e = k->e[i];
+    const double cs2 = k->cs2;
+    for (a = 0; a < 2; a++)
+      for (b = 0; b < 2; b++)
+        for (c = 0; c < 2; c++) {
+          const double dbc = b == c, dac = a == c, dab = a == b;
+          k->H3[i][a][b][c] = e[a] * e[b] * e[c] - cs2 * (e[a] * dbc + e[b] * dac + e[c] * dab);
+          for (d = 0; d < 2; d++) {
+            const double dcd = c == d, dbd = b == d, dad = a == d;
+            const double power4 = e[a] * e[b] * e[c] * e[d];
+            const double power2 = e[a] * e[b] * dcd + e[a] * e[c] * dbd + e[a] * e[d] * dbc +
+                                  e[b] * e[c] * dad + e[b] * e[d] * dac + e[c] * e[d] * dab;
+            const double power0 = dab * dcd + dac * dbd + dad * dbc;
+            k->H4[i][a][b][c][d] = (power4 - cs2 * power2 + cs2 * cs2 * power0);
+          }
+        }
+  }
+  return ORC_OK;
+}
+
+/* QuarticEquilibrium::polynomial for T_D = 2 (Equilibria.h:130-267), in the
+ * reference's order of operations.  u unscaled. */
+static void quartic_feq(const orc_thermal_k* k, double rho, const double* u, double T, double* feq) {
+  const double cs2 = k->cs2;
+  double uu_term = 0.0;
+  int i, j, alp, bet;
+  for (j = 0; j < 2; j++) uu_term += -(u[j] * u[j]) / (2.0 * cs2);
+  const double T1 = cs2 * (T - 1);
+  const double a_xxx = u[0] * u[0] * u[0] + T1 * (u[0] + u[0] + u[0]);
+  const double a_xxy = u[0] * u[0] * u[1] + T1 * (u[1]);
+  const double a_xyy = u[0] * u[1] * u[1] + T1 * (u[0]);
+  const double a_yyy = u[1] * u[1] * u[1] + T1 * (u[1] + u[1] + u[1]);
+  const double a_xxxx = u[0] * u[0] * u[0] * u[0] + T1 * u[0] * u[0] * 6.0 + T1 * T1 * 3.0;
+  const double a_yyyy = u[1] * u[1] * u[1] * u[1] + T1 * u[1] * u[1] * 6.0 + T1 * T1 * 3.0;
+  const double a_xxxy = u[0] * u[0] * u[0] * u[1] + T1 * (u[0] * u[1] * 3.0);
+  const double a_xyyy = u[0] * u[1] * u[1] * u[1] + T1 * (u[0] * u[1] * 3.0);
+  const double a_xxyy = u[0] * u[0] * u[1] * u[1] + T1 * (u[0] * u[0] + u[1] * u[1]) + T1 * T1;
+  for (i = 0; i < k->Q; i++) {
+    const double* e = k->e[i];
+    const double w = k->w[i];
+    double ue_term = 0.0;
+    for (j = 0; j < 2; j++) ue_term += (u[j] * e[j]) / cs2;
+    feq[i] = w * rho * (1 + ue_term * (1 + 0.5 * (ue_term)) + uu_term);
+    for (alp = 0; alp < 2; alp++)
+      for (bet = 0; bet < 2; bet++) {
+        const double eye = alp == bet;
+        feq[i] += rho * w / (2.0 * cs2) * ((T - 1) * eye * e[alp] * e[bet] - cs2 * eye * (T - 1));
+      }
+    feq[i] += w * rho / (6. * cs2 * cs2 * cs2) *
+              (a_xxx * k->H3[i][0][0][0] + 3 * (a_xxy * k->H3[i][0][0][1] + a_xyy * k->H3[i][0][1][1]) +
+               a_yyy * k->H3[i][1][1][1]);
+    feq[i] += w * rho / (24. * cs2 * cs2 * cs2 * cs2) *
+              (k->H4[i][0][0][0][0] * a_xxxx + k->H4[i][1][1][1][1] * a_yyyy + 6.0 * k->H4[i][0][0][1][1] * a_xxyy +
+               4.0 * k->H4[i][0][1][1][1] * a_xyyy + 4.0 * k->H4[i][0][0][0][1] * a_xxxy);
+  }
+}
+
+/* BGKEquilibrium, generic form (Equilibria.h:66-83); u unscaled. */
+static void bgk_feq(const orc_thermal_k* k, double rho, const double* u, double* feq) {
+  double uu = 0.0;
+  int i, j;
+  for (j = 0; j < k->D; j++) uu += -(u[j] * u[j]) / (2.0 * k->cs2);
+  for (i = 0; i < k->Q; i++) {
+    double ue = 0.0;
+    for (j = 0; j < k->D; j++) ue += (u[j] * k->e[i][j]) / k->cs2;
+    feq[i] = k->w[i] * rho * (1 + ue * (1 + 0.5 * (ue)) + uu);
+  }
+}
+
+/* CompressibleCFDSolver::calcQuarticEquilibrium (CompressibleCFDSolver.h:790-840):
+ * the same quartic equilibrium written as full tensor contractions; the
+ * initialisation uses this form. */
+static void quartic_feq_tensor(const orc_thermal_k* k, double density, const double* velocity,
+                               double temperature, double* feq) {
+  const int dim = 2;
+  const double cs2 = k->cs2;
+  double uu_term = 0.0;
+  int i, j, alp, bet, gam, det;
+  for (j = 0; j < dim; j++) uu_term += -(velocity[j] * velocity[j]) / (2.0 * cs2);
+  for (i = 0; i < k->Q; i++) {
+    const double* e = k->e[i];
+    const double weight = k->w[i];
+    const double T1 = cs2 * (temperature - 1);
+    double ue_term = 0.0;
+    for (j = 0; j < dim; j++) ue_term += (velocity[j] * e[j]) / cs2;
+    feq[i] = weight * density * (1 + ue_term * (1 + 0.5 * (ue_term)) + uu_term);
+    for (alp = 0; alp < dim; alp++)
+      for (bet = 0; bet < dim; bet++) {
+        const double dab = alp == bet;
+        feq[i] += density * weight / (2.0 * cs2) * ((temperature - 1) * dab * e[alp] * e[bet] - cs2 * dab * (temperature - 1));
+        for (gam = 0; gam < dim; gam++) {
+          const double dbg = bet == gam, dag = alp == gam;
+          feq[i] += weight * density / (6. * cs2 * cs2 * cs2) *
+                    (velocity[alp] * velocity[bet] * velocity[gam] +
+                     T1 * (dab * velocity[gam] + dbg * velocity[alp] + dag * velocity[bet])) *
+                    (e[alp] * e[bet] * e[gam] - cs2 * (e[gam] * dab + e[bet] * dag + e[alp] * dbg));
+          for (det = 0; det < dim; det++) {
+            const double dgd = gam == det, dbd = bet == det, dad = alp == det;
+            const double power4 = e[alp] * e[bet] * e[gam] * e[det];
+            const double power2 = e[alp] * e[bet] * dgd + e[alp] * e[gam] * dbd + e[alp] * e[det] * dbg +
+                                  e[bet] * e[gam] * dad + e[bet] * e[det] * dag + e[gam] * e[det] * dab;
+            const double power0 = dab * dgd + dag * dbd + dad * dbg;
+            const double u4 = velocity[alp] * velocity[bet] * velocity[gam] * velocity[det];
+            const double u2 = velocity[alp] * velocity[bet] * dgd + velocity[alp] * velocity[gam] * dbd +
+                              velocity[alp] * velocity[det] * dbg + velocity[bet] * velocity[gam] * dad +
+                              velocity[bet] * velocity[det] * dag + velocity[gam] * velocity[det] * dab;
+            const double multieye = dab * dgd + dag * dbd + dad * dbg;
+            feq[i] += weight * density / (24. * cs2 * cs2 * cs2 * cs2) * (power4 - cs2 * power2 + cs2 * cs2 * power0) *
+                      (u4 + T1 * (u2 + T1 * multieye));
+          }
+        }
+      }
+  }
+}
+
+/* Equilibrium initialisation of both populations
+ * (CompressibleCFDSolver::initializeDistributions, CompressibleCFDSolver.h:849-899):
+ * f = f^eq(rho, u, T) (tensor form above), g = f^eq T (2 C_v - D),
+ * C_v = 1 / (gamma - 1).  u holds the scaled velocity. */
+int orc_thermal_init(int stencil, double scaling, double gamma, int64_t n, const double* rho,
+                     const double* u, const double* T, double* f, double* g) {
+  orc_thermal_k k;
+  int64_t ii;
+  if (thermal_consts(stencil, scaling, &k) != ORC_OK) return ORC_ERR_ARG;
+  const double C_v = 1. / (gamma - 1.0);
+  for (ii = 0; ii < n; ii++) {
+    double vel[2], feq[32];
+    int j;
+    for (j = 0; j < 2; j++) vel[j] = u[(int64_t)j * n + ii] / scaling;
+    quartic_feq_tensor(&k, rho[ii], vel, T[ii], feq);
+    for (j = 0; j < k.Q; j++) {
+      f[(int64_t)j * n + ii] = feq[j];
+      g[(int64_t)j * n + ii] = feq[j] * (T[ii]) * (2.0 * C_v - 2);
+    }
+  }
+  return ORC_OK;
+}
+
+/* Quartic (quartic != 0) or second-order BGK equilibrium of the collision,
+ * for tests.  u scaled; feq is Q blocks of n. */
+int orc_thermal_feq(int stencil, double scaling, int quartic, int64_t n, const double* rho,
+                    const double* u, const double* T, double* feq_out) {
+  orc_thermal_k k;
+  int64_t ii;
+  if (thermal_consts(stencil, scaling, &k) != ORC_OK) return ORC_ERR_ARG;
+  for (ii = 0; ii < n; ii++) {
+    double vel[2], feq[32];
+    int j;
+    for (j = 0; j < 2; j++) vel[j] = u[(int64_t)j * n + ii] / scaling;
+    if (quartic)
+      quartic_feq(&k, rho[ii], vel, T[ii], feq);
+    else
+      bgk_feq(&k, rho[ii], vel, feq);
+    for (j = 0; j < k.Q; j++) feq_out[(int64_t)j * n + ii] = feq[j];
+  }
+  return ORC_OK;
+}
+
+/* CollisionOperator::collideAll(f, g, ...) (CollisionOperator.h:113-224)
+ * with BGKCollision::relaxWithG (CollisionSchemes.h:43-118):
+ *   rho = sum f; u = sum e f / rho (AuxiliaryCollisionFunctions.h:232-242);
+ *   T = 0.5 / (rho C_v) sum_i (|e_i - u|^2 f_i / c_s^2 + g_i) (:289-307);
+ *   in the initialisation procedure u is then replaced by the prescribed one;
+ *   f^eq from the quartic (or second-order) equilibrium, g^eq = f^eq T (2 C_v - D)
+ *   (:420-431);
+ *   Prandtl correction (if set): f*, g* from the centred heat flux of f^neq
+ *   and the centred flux of g^neq (:445-516);
+ *   Sutherland factor (T / 0.85)^0.7 (if set);
+ *   tau_visc = (tau - 1/2) s / (T rho) + 1/2; Knudsen estimate
+ *   sum |f - f^eq| / w / Q (:474-481) written to the shock mask (the
+ *   reference's tau factor derived from it is not applied, :95-101);
+ *   f -= omega f^neq - (omega - omega_Pr) f*; g likewise.
+ * Writes rho, u (scaled, unless in_init), T and the mask.  Returns
+ * ORC_ERR_DENSITY if a density is below 1e-10. */
+int orc_collide_compressible(int stencil, double scaling, double tau, double gamma, double prandtl,
+                             int prandtl_set, int sutherland_set, int quartic, int64_t n, double* f,
+                             double* g, double* rho, double* u, double* T, double* mask, int in_init,
+                             int nthreads) {
+  orc_thermal_k k;
+  int bad = 0;
+  int64_t ii;
+  if (thermal_consts(stencil, scaling, &k) != ORC_OK) return ORC_ERR_ARG;
+  const int D = k.D, Q = k.Q;
+  const double cs2 = k.cs2;
+  const double C_v = 1. / (gamma - 1.0);
+  (void)nthreads;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(| : bad) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+  for (ii = 0; ii < n; ii++) {
+    double fl[32], gl[32], feq[32], geq[32], fNeq[32], gNeq[32], fStar[32], gStar[32];
+    double vel[2], dens = 0.0, temp;
+    int i, a, b, c;
+    for (i = 0; i < Q; i++) fl[i] = f[(int64_t)i * n + ii];
+    for (i = 0; i < Q; i++) gl[i] = g[(int64_t)i * n + ii];
+    for (i = 0; i < Q; i++) dens += fl[i];
+    if (dens < 1e-10 || dens != dens) bad = 1;
+    rho[ii] = dens;
+    for (a = 0; a < D; a++) {
+      vel[a] = 0.0;
+      for (i = 0; i < Q; i++) vel[a] += k.e[i][a] * fl[i];
+      vel[a] = vel[a] * 1.0 / dens;
+    }
+    temp = 0.0;
+    for (i = 0; i < Q; i++) {
+      double sum = 0.0;
+      for (a = 0; a < D; a++) sum += (k.e[i][a] - vel[a]) * (k.e[i][a] - vel[a]);
+      temp += sum * fl[i] / cs2 + gl[i];
+    }
+    temp = temp * 0.5 / (dens * C_v);
+    T[ii] = temp;
+    if (!in_init) {
+      for (a = 0; a < D; a++) u[(int64_t)a * n + ii] = vel[a] * scaling;
+    } else {
+      for (a = 0; a < D; a++) vel[a] = u[(int64_t)a * n + ii] / scaling;
+    }
+    if (quartic)
+      quartic_feq(&k, dens, vel, temp, feq);
+    else
+      bgk_feq(&k, dens, vel, feq);
+    for (i = 0; i < Q; i++) geq[i] = feq[i] * (temp) * (2.0 * C_v - D);
+    for (i = 0; i < Q; i++) {
+      fStar[i] = 0.0;
+      gStar[i] = 0.0;
+      fNeq[i] = fl[i] - feq[i];
+      gNeq[i] = gl[i] - geq[i];
+    }
+    if (prandtl_set) {
+      double Qn[2][2][2] = {{{0.0}}}, F[2] = {0.0, 0.0};
+      const double cs6 = 6.0 * cs2 * cs2 * cs2;
+      for (i = 0; i < Q; i++)
+        for (a = 0; a < D; a++)
+          for (b = 0; b < D; b++)
+            for (c = 0; c < D; c++)
+              Qn[a][b][c] += ((k.e[i][a] - vel[a]) * (k.e[i][b] - vel[b]) * (k.e[i][c] - vel[c])) * fNeq[i];
+      for (i = 0; i < Q; i++)
+        for (a = 0; a < D; a++) F[a] += (k.e[i][a] - vel[a]) * gNeq[i];
+      for (a = 0; a < D; a++)
+        for (b = 0; b < D; b++)
+          for (c = 0; c < D; c++)
+            for (i = 0; i < Q; i++)
+              fStar[i] += k.w[i] * (Qn[a][b][c] * (k.e[i][a] * k.e[i][b] * k.e[i][c] -
+                                                  3 * cs2 * k.e[i][c] * (double)(a == b))) / cs6;
+      for (a = 0; a < D; a++)
+        for (i = 0; i < Q; i++) gStar[i] += k.w[i] * (F[a] * k.e[i][a]) / temp;
+    }
+    double sutherland_factor = 1.0;
+    if (sutherland_set) sutherland_factor = pow(temp / 0.85, 0.7);
+    const double visc_tau = (tau - 0.5) * sutherland_factor / (temp * dens) + 0.5;
+    double knudsen = 0.0;
+    for (i = 0; i < Q; i++) knudsen += fabs(fl[i] - feq[i]) / k.w[i];
+    knudsen = knudsen / Q;
+    mask[ii] = knudsen;
+    const double prandtl_tau = (visc_tau - 0.5) / prandtl + 0.5;
+    const double visc_omega = 1. / visc_tau;
+    const double prandtl_omega = 1. / prandtl_tau;
+    const double prandtl_diff = visc_omega - prandtl_omega;
+    for (i = 0; i < Q; i++) {
+      fl[i] -= visc_omega * fNeq[i] - prandtl_diff * fStar[i];
+      gl[i] -= visc_omega * gNeq[i] - prandtl_diff * gStar[i];
+    }
+    for (i = 0; i < Q; i++) {
+      f[(int64_t)i * n + ii] = fl[i];
+      g[(int64_t)i * n + ii] = gl[i];
+    }
+  }
+  return bad ? ORC_ERR_DENSITY : ORC_OK;
+}
+
+/* One step of CompressibleCFDSolver::run (CompressibleCFDSolver.h:1013-1035):
+ * stream() and gStream() (copy + SpMV with the same operator, :181-314),
+ * then collide() (:739-788).  work is Q*n. */
+int orc_step_compressible(const orc_sl* s, int stencil, double scaling, double tau, double gamma,
+                          double prandtl, int prandtl_set, int sutherland_set, int quartic, double* f,
+                          double* g, double* work, double* rho, double* u, double* T, double* mask,
+                          int nsteps, int nthreads) {
+  int k, rc = ORC_OK;
+  const size_t bytes = sizeof(double) * (size_t)s->Q * s->n;
+  for (k = 0; k < nsteps; k++) {
+    orc_sl_stream(s, f, work, nthreads);
+    memcpy(f, work, bytes);
+    orc_sl_stream(s, g, work, nthreads);
+    memcpy(g, work, bytes);
+    rc = orc_collide_compressible(stencil, scaling, tau, gamma, prandtl, prandtl_set, sutherland_set, quartic,
+                                  s->n, f, g, rho, u, T, mask, 0, nthreads);
     if (rc != ORC_OK) return rc;
   }
   return rc;
