@@ -64,6 +64,12 @@ extern "C" {
 #define NAT_BGK_STANDARD 0      /* BGKCollision + BGKEquilibrium */
 #define NAT_BGK_INCOMPRESSIBLE 1 /* collision/BGKIncompressible.cpp (D2Q9) */
 #define NAT_KBC_STANDARD 2      /* collision/KBCStandard.cpp (D2Q9); D3Q27 extension */
+/* Compressible two-population BGK of CompressibleCFDSolver on D2Q25H: f and g
+ * streamed by the same operator (solver/CompressibleCFDSolver.h:181-314),
+ * collideAll(f, g, rho, u, T, mask) (collision_advanced/CollisionOperator.h:113-224)
+ * with BGKCollision::relaxWithG (collision_advanced/CollisionSchemes.h:43-118).
+ * Requires stencil NAT_D2Q25H (and D2Q25H requires this model), NAT_FP64. */
+#define NAT_BGK_COMPRESSIBLE 3
 
 /* ---- node topology ----------------------------------------------------- */
 #define NAT_TOPO_FEQ 0
@@ -180,6 +186,46 @@ int nat_mass_energy_noalloc(const double* rho_dev, const double* u_dev, int dim,
                             int order, int topology, const double cell_size[3], double* out_dev,
                             void* cuda_stream);
 
+/* ---- compressible two-population model (NAT_BGK_COMPRESSIBLE) ---------- */
+/* Equilibrium of the collision (SolverConfiguration equilibrium scheme). */
+#define NAT_EQ_BGK 0     /* second order, collision_advanced/Equilibria.h:66-83 */
+#define NAT_EQ_QUARTIC 1 /* quartic with temperature, Equilibria.h:88-267 (default) */
+
+/* Model settings; the defaults are the reference's SolverConfiguration
+ * defaults (solver/SolverConfiguration.cpp:21-31): gamma 1.4, Prandtl 1.0 with
+ * the Prandtl correction off, Sutherland law off; quartic equilibrium. */
+typedef struct nat_thermal {
+  double gamma;       /* heat capacity ratio; C_v = 1 / (gamma - 1) */
+  double prandtl;     /* Prandtl number, used when prandtl_set != 0 */
+  int prandtl_set;    /* apply the f*, g* correction (CollisionSchemes.h:63-79, 103-116) */
+  int sutherland_set; /* tau_visc scaled by (T / 0.85)^0.7 (CollisionSchemes.h:81-88) */
+  int equilibrium;    /* NAT_EQ_QUARTIC or NAT_EQ_BGK */
+} nat_thermal;
+
+/* Set / read the model settings of a NAT_BGK_COMPRESSIBLE handle. */
+int nat_set_thermal(nat_solver* s, const nat_thermal* t);
+int nat_get_thermal(const nat_solver* s, nat_thermal* t);
+
+/* Second population g (CompressibleCFDSolver::m_g): same layout as f. */
+int nat_upload_g(nat_solver* s, const double* g_host);
+int nat_download_g(nat_solver* s, double* g_host);
+
+/* Temperature T (n_ref) and shock-sensor mask (n_ref, the Knudsen estimate of
+ * AuxiliaryCollisionFunctions.h:474-481) written by the last collision. */
+int nat_download_thermal(nat_solver* s, double* T_host, double* mask_host);
+
+/* CompressibleCFDSolver::initializeDistributions (CompressibleCFDSolver.h:849-899),
+ * EQUILIBRIUM scheme: f = f^eq(rho, u, T) of the quartic equilibrium and
+ * g = f^eq T (2 C_v - D) at every node, computed on the device from host
+ * fields rho (n_ref), u (D * n_ref, scaled) and T (n_ref); also stores rho, u
+ * and T on the device. */
+int nat_init_thermal(nat_solver* s, const double* rho_host, const double* u_host, const double* T_host);
+
+/* nat_stream on such a handle streams f and g (stream() + gStream());
+ * nat_collide runs collideAll(f, g, rho, u, T, mask) (with in_init the
+ * velocity comes from the device copy of u, as set by nat_upload_macro);
+ * nat_step fuses stream(f), stream(g) and collide into one kernel per step. */
+
 /* Device pointers of the current distribution buffer (Q blocks of n_dev
  * values, double for NAT_FP64 and float (f - w_i) for NAT_FP32_DEV). */
 int nat_device_f(nat_solver* s, void** f_dev);
@@ -191,7 +237,8 @@ int nat_device_f(nat_solver* s, void** f_dev);
  * kernel only, 2 = specialised kernel required (NAT_ERR_UNSUPPORTED when
  * none applies), 3 = tile kernel required, 4 = row-segment kernel required. */
 int nat_set_kernel_variant(nat_solver* s, int variant);
-/* The fused-step kernel in use: 1 generic, 2 tile, 3 row-segment. */
+/* The fused-step kernel in use: 1 generic, 2 tile, 3 row-segment,
+ * 5 two-population row-segment kernel (NAT_BGK_COMPRESSIBLE). */
 int nat_kernel_variant(const nat_solver* s);
 
 /* Autotuner: times `steps` fused steps with every kernel that applies to

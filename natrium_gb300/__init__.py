@@ -12,6 +12,11 @@ on top of the C ABI of ``libnatgpu.so`` (``include/natgpu.h``):
   (collision/CollisionModel.h:74-78).
 * :class:`DistributionFunctions` -- host mirror of
   solver/DistributionFunctions.h: Q blocks of n doubles, block 0 = f_0.
+* :class:`CompressibleStep`, :class:`BGKCompressible` -- the compressible
+  two-population model on D2Q25H: ``CompressibleCFDSolver::stream()`` +
+  ``gStream()`` (solver/CompressibleCFDSolver.h:181-314) and
+  ``collideAll(f, g, rho, u, T, mask, owned, init)``
+  (collision_advanced/CollisionOperator.h:113-224).
 
 There is no CPU fallback: importing the package raises if the CUDA library is
 missing, and every call goes through the CUDA kernels.
@@ -39,7 +44,8 @@ NAT_ERR_UNSUPPORTED = 7
 
 STENCILS = {"D2Q9": 0, "D3Q19": 1, "D3Q27": 2, "D2Q25H": 3}
 STENCIL_DQ = {"D2Q9": (2, 9), "D3Q19": (3, 19), "D3Q27": (3, 27), "D2Q25H": (2, 25)}
-COLLISIONS = {"BGK_STANDARD": 0, "BGK_INCOMPRESSIBLE": 1, "KBC_STANDARD": 2}
+COLLISIONS = {"BGK_STANDARD": 0, "BGK_INCOMPRESSIBLE": 1, "KBC_STANDARD": 2, "BGK_COMPRESSIBLE": 3}
+EQUILIBRIA = {"BGK": 0, "QUARTIC": 1}
 TOPOLOGIES = {"feq": 0, "dg": 1}
 PRECISIONS = {"fp64": 0, "fp32dev": 1}
 
@@ -52,6 +58,8 @@ EXPORTS = [
     "nat_kernel_variant", "nat_autotune", "nat_kernel_info",
     "nat_server_create", "nat_server_destroy", "nat_server_submit", "nat_server_step", "nat_server_poll",
     "nat_server_result", "nat_server_stats", "nat_server_last_error", "nat_mass_energy_noalloc",
+    "nat_set_thermal", "nat_get_thermal", "nat_upload_g", "nat_download_g", "nat_download_thermal",
+    "nat_init_thermal",
 ]
 
 
@@ -75,6 +83,24 @@ class _Spec(C.Structure):
         ("scaling", C.c_double), ("viscosity", C.c_double), ("cfl", C.c_double), ("dt", C.c_double),
         ("collision", C.c_int), ("precision", C.c_int),
     ]
+
+
+class _Thermal(C.Structure):
+    _fields_ = [("gamma", C.c_double), ("prandtl", C.c_double), ("prandtl_set", C.c_int),
+                ("sutherland_set", C.c_int), ("equilibrium", C.c_int)]
+
+
+@dataclass
+class ThermalSettings:
+    """Compressible-model settings (SolverConfiguration: heat capacity ratio
+    gamma, Prandtl number and its switch, Sutherland law switch; equilibrium
+    QUARTIC or BGK).  Defaults are the reference's
+    (solver/SolverConfiguration.cpp:21-31)."""
+    gamma: float = 1.4
+    prandtl: float = 1.0
+    prandtl_set: bool = False
+    sutherland: bool = False
+    equilibrium: str = "QUARTIC"
 
 
 _lib = None
@@ -118,6 +144,12 @@ def load_library(path: str | None = None):
     L.nat_kernel_variant.argtypes = [vp]
     L.nat_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.nat_kernel_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), i64p]
+    L.nat_set_thermal.argtypes = [vp, C.POINTER(_Thermal)]
+    L.nat_get_thermal.argtypes = [vp, C.POINTER(_Thermal)]
+    L.nat_upload_g.argtypes = [vp, dp]
+    L.nat_download_g.argtypes = [vp, dp]
+    L.nat_download_thermal.argtypes = [vp, dp, dp]
+    L.nat_init_thermal.argtypes = [vp, dp, dp, dp]
     _lib = L
     return L
 
@@ -314,6 +346,41 @@ class Solver:
         self._check(self._L.nat_device_f(self._h, C.byref(p)))
         return p.value or 0
 
+    # -- compressible two-population model (collision BGK_COMPRESSIBLE) ---------
+    def set_thermal(self, t: ThermalSettings):
+        c = _Thermal(float(t.gamma), float(t.prandtl), int(t.prandtl_set), int(t.sutherland),
+                     EQUILIBRIA[t.equilibrium])
+        self._check(self._L.nat_set_thermal(self._h, C.byref(c)))
+
+    def get_thermal(self) -> ThermalSettings:
+        c = _Thermal()
+        self._check(self._L.nat_get_thermal(self._h, C.byref(c)))
+        eq = {v: k for k, v in EQUILIBRIA.items()}[c.equilibrium]
+        return ThermalSettings(c.gamma, c.prandtl, bool(c.prandtl_set), bool(c.sutherland_set), eq)
+
+    def upload_g(self, g: np.ndarray):
+        g = np.ascontiguousarray(g, dtype=np.float64)
+        if g.shape != (self.Q, self.n_ref):
+            raise ValueError(f"g must have shape {(self.Q, self.n_ref)}")
+        self._check(self._L.nat_upload_g(self._h, _dp(g)))
+
+    def download_g(self) -> np.ndarray:
+        out = np.empty((self.Q, self.n_ref))
+        self._check(self._L.nat_download_g(self._h, _dp(out)))
+        return out
+
+    def download_thermal(self):
+        """Temperature and shock-sensor mask of the last collision."""
+        T = np.empty(self.n_ref)
+        m = np.empty(self.n_ref)
+        self._check(self._L.nat_download_thermal(self._h, _dp(T), _dp(m)))
+        return T, m
+
+    def init_thermal(self, rho: np.ndarray, u: np.ndarray, T: np.ndarray):
+        """Equilibrium initialisation of f and g from rho, u (scaled), T."""
+        c = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        self._check(self._L.nat_init_thermal(self._h, _dp(c(rho)), _dp(c(u)), _dp(c(T))))
+
 
 # ---------------------------------------------------------------------------
 # mirrors of the reference interfaces
@@ -393,6 +460,54 @@ class BGKIncompressible(_CollisionModel):
 
 class KBCStandard(_CollisionModel):
     MODEL = "KBC_STANDARD"
+
+
+class CompressibleStep:
+    """CompressibleCFDSolver's streaming: stream() of f and gStream() of g with
+    the same semi-Lagrangian operator (solver/CompressibleCFDSolver.h:181-314)."""
+
+    def __init__(self, solver: Solver):
+        if solver.spec.collision != "BGK_COMPRESSIBLE":
+            raise ValueError("the solver must be created with collision BGK_COMPRESSIBLE")
+        self.solver = solver
+
+    def stream(self, f: DistributionFunctions, g: DistributionFunctions, t: float = 0.0) -> float:
+        s = self.solver
+        s.upload_f(f.f)
+        s.upload_g(g.f)
+        dt = s.stream(t)
+        f.f = s.download_f()
+        g.f = s.download_g()
+        return dt
+
+
+class BGKCompressible:
+    """CollisionOperator<2,25,QuarticEquilibrium,BGKCollision>::collideAll(f, g,
+    rho, u, T, mask, owned, inInitializationProcedure) with relaxWithG."""
+
+    def __init__(self, solver: Solver):
+        if solver.spec.collision != "BGK_COMPRESSIBLE":
+            raise ValueError("the solver must be created with collision BGK_COMPRESSIBLE")
+        self.solver = solver
+
+    def collideAll(self, f: DistributionFunctions, g: DistributionFunctions, densities: np.ndarray,
+                   velocities: np.ndarray, temperature: np.ndarray, maskShockSensor: np.ndarray,
+                   locally_owned_dofs=None, inInitializationProcedure: bool = False):
+        s = self.solver
+        s.upload_f(f.f)
+        s.upload_g(g.f)
+        if inInitializationProcedure:
+            s.upload_macro(np.ascontiguousarray(densities), np.ascontiguousarray(velocities))
+        s.collide(inInitializationProcedure)
+        f.f[...] = s.download_f()
+        g.f[...] = s.download_g()
+        rho, u = s.download_macro()
+        T, m = s.download_thermal()
+        densities[...] = rho
+        if not inInitializationProcedure:
+            velocities[...] = u
+        temperature[...] = T
+        maskShockSensor[...] = m
 
 
 def version() -> str:

@@ -62,4 +62,10 @@ void row_kernels_d2q9(std::vector<RowLaunch>& v);
 void row_kernels_d3q19(std::vector<RowLaunch>& v);
 void row_kernels_d3q27(std::vector<RowLaunch>& v);
 
+// Compressible two-population model on D2Q25H (k_thermal.cu): fused
+// stream(f, g) (+ relaxWithG), collision only, equilibrium initialisation.
+cudaError_t launch_thermal_step(const ThermalStep& P, bool collide, cudaStream_t st);
+cudaError_t launch_thermal_collide(const ThermalPoint& P, int grid, cudaStream_t st);
+cudaError_t launch_thermal_init(const ThermalPoint& P, int grid, cudaStream_t st);
+
 }  // namespace natgpu

@@ -62,6 +62,14 @@ struct nat_solver {
   RowLaunch row;
   SpecWeights<double> w64;
   SpecWeights<float> w32;
+  // compressible two-population model (D2Q25H)
+  bool thermal = false;
+  nat_thermal th;
+  double* g[2] = {nullptr, nullptr};  // second population, same layout as f
+  double* T = nullptr;                // temperature
+  double* mask = nullptr;             // shock sensor (Knudsen estimate)
+  ThermalModel tm;
+  ThermalTables tt;
 };
 
 namespace {
@@ -91,12 +99,16 @@ int cuda_fail(nat_solver* s, cudaError_t e, const char* what) {
 // ---- stencil metadata (host) ---------------------------------------------
 struct HostStencil {
   int D, Q;
-  double e[32][3];  // unit velocities
+  double e[32][3];  // unscaled velocities
   double w[32];
+  // per-axis displacement classes: count and scaled speed of each (the
+  // departure point is x - dt * cls along the axis)
+  int nd;
+  double cls[ND_MAX];
 };
 
 template <class S>
-HostStencil host_stencil() {
+HostStencil host_stencil(double scaling) {
   HostStencil h;
   h.D = S::D;
   h.Q = S::Q;
@@ -104,14 +116,59 @@ HostStencil host_stencil() {
     for (int a = 0; a < 3; ++a) h.e[i][a] = S::e(i, a);
     h.w[i] = S::w(i);
   }
+  h.nd = 2;
+  h.cls[0] = scaling;  // e_a = +1
+  h.cls[1] = -scaling;
   return h;
 }
 
-bool get_host_stencil(int id, HostStencil* out) {
+// D2Q25H speeds and weights exactly as the reference forms them
+// (stencils/D2Q25H.cpp:37-84); e unscaled = direction / scaling, as
+// GeneralCollisionData does (AuxiliaryCollisionFunctions.h:161-165).
+void d2q25h_speeds(double scaling, double* cm_s, double* cn_s) {
+  *cm_s = scaling * sqrt(5. - sqrt(10.)) / sqrt(3.);
+  *cn_s = sqrt(5. + sqrt(10.)) * scaling / sqrt(3.);
+}
+
+void d2q25h_weights(double* w0, double* wm, double* wn) {
+  const double r = (sqrt(5.) - sqrt(2.)) / sqrt(3.);
+  *w0 = (-3 - 3 * r * r * r * r + 54 * r * r) / (75 * r * r);
+  *wm = (9 * r * r * r * r - 6 - 27 * r * r) / (300 * r * r * (r * r - 1));
+  *wn = (9 - 6 * r * r * r * r - 27 * r * r) / (300 * (1 - r * r));
+}
+
+HostStencil host_stencil_d2q25h(double scaling) {
+  HostStencil h;
+  memset(&h, 0, sizeof(h));
+  h.D = 2;
+  h.Q = 25;
+  double cm_s, cn_s, w0, wm, wn;
+  d2q25h_speeds(scaling, &cm_s, &cn_s);
+  d2q25h_weights(&w0, &wm, &wn);
+  const double sp[3] = {0.0, cm_s / scaling, cn_s / scaling};
+  const double w1[3] = {w0, wm, wn};
+  for (int i = 0; i < 25; ++i) {
+    for (int a = 0; a < 2; ++a) {
+      const int c = SD2Q25H::code(i, a);
+      h.e[i][a] = c < 0 ? -sp[-c] : sp[c];
+    }
+    const int cx = SD2Q25H::code(i, 0), cy = SD2Q25H::code(i, 1);
+    h.w[i] = w1[cx < 0 ? -cx : cx] * w1[cy < 0 ? -cy : cy];
+  }
+  h.nd = 4;
+  h.cls[0] = cm_s;  // dcls order: +c_m, -c_m, +c_n, -c_n
+  h.cls[1] = -cm_s;
+  h.cls[2] = cn_s;
+  h.cls[3] = -cn_s;
+  return h;
+}
+
+bool get_host_stencil(int id, HostStencil* out, double scaling) {
   switch (id) {
-    case NAT_D2Q9: *out = host_stencil<SD2Q9>(); return true;
-    case NAT_D3Q19: *out = host_stencil<SD3Q19>(); return true;
-    case NAT_D3Q27: *out = host_stencil<SD3Q27>(); return true;
+    case NAT_D2Q9: *out = host_stencil<SD2Q9>(scaling); return true;
+    case NAT_D3Q19: *out = host_stencil<SD3Q19>(scaling); return true;
+    case NAT_D3Q27: *out = host_stencil<SD3Q27>(scaling); return true;
+    case NAT_D2Q25H: *out = host_stencil_d2q25h(scaling); return true;
     default: return false;
   }
 }
@@ -230,13 +287,13 @@ int build_tables(nat_solver* s, const HostStencil& hs) {
     G.period = s->period;
     G.B = s->B[a];
     G.ntiles = G.n / G.B;
-    // displacement classes: class 0 for e_a > 0, 1 for e_a < 0 (unit speeds)
-    G.nd = 2;
+    // displacement classes of the stencil (unit stencils: 0 for e_a > 0,
+    // 1 for e_a < 0; D2Q25H: +c_m, -c_m, +c_n, -c_n)
+    G.nd = hs.nd;
     int Rmax = G.B;
     for (int d = 0; d < G.nd; ++d) {
-      const double sign = d == 0 ? 1.0 : -1.0;
       // departure x - dt * e: displacement in cell units
-      const double delta = s->dt * sign * s->spec.scaling / s->h[a];
+      const double delta = s->dt * hs.cls[d] / s->h[a];
       int lo = 1 << 30, hi = -(1 << 30);
       for (int c = 0; c < G.period; ++c) {
         const double xdep = xi[c] - delta;
@@ -272,7 +329,6 @@ int build_tables(nat_solver* s, const HostStencil& hs) {
     }
     T.Rmax[a] = Rmax;
   }
-  (void)hs;
   return NAT_OK;
 }
 
@@ -648,6 +704,120 @@ int launch_v2(nat_solver* s, int write_macro) {
                                        : launch_v2_t<float>(s, s->w32, write_macro);
 }
 
+// ---- compressible two-population model ------------------------------------
+// Per-solve constants of the collision, from the reference's stencil formulas.
+void fill_thermal_model(nat_solver* s) {
+  ThermalModel& m = s->tm;
+  memset(&m, 0, sizeof(m));
+  const double sc = s->spec.scaling;
+  double cm_s, cn_s, w0, wm, wn;
+  d2q25h_speeds(sc, &cm_s, &cn_s);
+  d2q25h_weights(&w0, &wm, &wn);
+  const double sp[3] = {0.0, cm_s / sc, cn_s / sc};
+  const double w1[3] = {w0, wm, wn};
+  // unscaled c_s^2 = scaled c_s^2 / scaling^2 (AuxiliaryCollisionFunctions.h:171-172)
+  const double c = s->cs2_scaled / (sc * sc);
+  m.cs2 = c;
+  for (int g = 0; g < TH_NG; ++g) {
+    const double X = sp[SD2Q25H::gx(g)], Y = sp[SD2Q25H::gy(g)];
+    m.X[g] = X;
+    m.Y[g] = Y;
+    m.e2[g] = X * X + Y * Y;
+    m.w[g] = w1[SD2Q25H::gx(g)] * w1[SD2Q25H::gy(g)];
+    m.winv[g] = 1.0 / m.w[g];
+    // Hermite tensors at (+X, +Y) (AuxiliaryCollisionFunctions.h:520-566)
+    m.h3[g][0] = X * X * X - 3.0 * c * X;
+    m.h3[g][1] = X * X * Y - c * Y;
+    m.h3[g][2] = X * Y * Y - c * X;
+    m.h3[g][3] = Y * Y * Y - 3.0 * c * Y;
+    m.h4[g][0] = X * X * X * X - 6.0 * c * X * X + 3.0 * c * c;
+    m.h4[g][1] = X * X * X * Y - 3.0 * c * X * Y;
+    m.h4[g][2] = X * X * Y * Y - c * (X * X + Y * Y) + c * c;
+    m.h4[g][3] = X * Y * Y * Y - 3.0 * c * X * Y;
+    m.h4[g][4] = Y * Y * Y * Y - 6.0 * c * Y * Y + 3.0 * c * c;
+  }
+  m.tau = s->tau;
+  m.scaling = sc;
+  m.C_v = 1.0 / (s->th.gamma - 1.0);
+  m.gfac = 2.0 * m.C_v - s->D;
+  m.prandtl = s->th.prandtl;
+  m.prandtl_set = s->th.prandtl_set ? 1 : 0;
+  m.sutherland_set = s->th.sutherland_set ? 1 : 0;
+  m.quartic = s->th.equilibrium == NAT_EQ_QUARTIC ? 1 : 0;
+}
+
+// Window tables of the two-population row kernel from the operator tables.
+int setup_thermal_tables(nat_solver* s) {
+  ThermalTables& t = s->tt;
+  memset(&t, 0, sizeof(t));
+  const SLTables& T = s->h_tab;
+  t.p = T.p;
+  t.per = s->period;
+  int lo = 1 << 30, hi = -(1 << 30);
+  for (int a = 0; a < 2; ++a)
+    for (int d = 0; d < T.ax[a].nd; ++d)
+      for (int c = 0; c < s->period; ++c) {
+        t.off[a][d][c] = T.off[a][d][c];
+        for (int j = 0; j <= T.p; ++j) t.w[a][d][c][j] = T.w[a][d][c][j];
+        if (a == 0) {
+          lo = std::min(lo, T.off[0][d][c]);
+          hi = std::max(hi, T.off[0][d][c] + T.p);
+        }
+      }
+  t.xl = lo;
+  t.bw = 32 + hi - lo;
+  if (t.bw > TH_BWMAX)
+    return fail(s, NAT_ERR_UNSUPPORTED, "time step too large for the x window of the two-population kernel");
+  fill_thermal_model(s);
+  return NAT_OK;
+}
+
+ThermalStep thermal_step_params(nat_solver* s, int write_macro) {
+  ThermalStep P;
+  P.f_in = static_cast<const double*>(s->f[s->cur]);
+  P.g_in = s->g[s->cur];
+  P.f_out = static_cast<double*>(s->f[1 - s->cur]);
+  P.g_out = s->g[1 - s->cur];
+  P.rho = s->rho;
+  P.u = s->u;
+  P.T = s->T;
+  P.mask = s->mask;
+  P.status = s->status;
+  P.n = (int)s->n_dev;
+  P.nx = s->n_ax[0];
+  P.ny = s->n_ax[1];
+  P.nseg = (s->n_ax[0] + 31) / 32;
+  P.write_macro = write_macro;
+  P.tb = s->tt;
+  P.M = s->tm;
+  return P;
+}
+
+ThermalPoint thermal_point_params(nat_solver* s, int in_init) {
+  ThermalPoint P;
+  P.f_in = nullptr;
+  P.f = static_cast<double*>(s->f[s->cur]);
+  P.g = s->g[s->cur];
+  P.rho = s->rho;
+  P.u = s->u;
+  P.T = s->T;
+  P.mask = s->mask;
+  P.status = s->status;
+  P.n = s->n_dev;
+  P.in_init = in_init;
+  P.M = s->tm;
+  return P;
+}
+
+int launch_thermal(nat_solver* s, bool collide, int write_macro) {
+  ThermalStep P = thermal_step_params(s, write_macro);
+  cudaError_t e = launch_thermal_step(P, collide, s->stream);
+  if (e != cudaSuccess) return cuda_fail(s, e, "two-population stream-collide launch");
+  s->launches++;
+  s->cur = 1 - s->cur;
+  return NAT_OK;
+}
+
 int upload_rest(nat_solver* s) {
   // the rest state is stored after the two doubles of the reduction buffer
   CK(cudaMemcpyAsync(s->red + 2, s->rest, sizeof(double) * s->Q, cudaMemcpyHostToDevice,
@@ -664,7 +834,7 @@ int natgpu::build_solver_tables(const nat_spec* spec, double dt, SLTables* T, st
   nat_solver tmp;
   tmp.spec = *spec;
   HostStencil hs;
-  if (!get_host_stencil(spec->stencil, &hs)) return NAT_ERR_UNSUPPORTED;
+  if (!get_host_stencil(spec->stencil, &hs, spec->scaling)) return NAT_ERR_UNSUPPORTED;
   tmp.D = hs.D;
   tmp.Q = hs.Q;
   const bool dg = spec->topology == NAT_TOPO_DG;
@@ -713,19 +883,24 @@ int nat_destroy(nat_solver* s) {
   cudaFree(s->red);
   cudaFree(s->status);
   cudaFree(s->d_tab);
+  cudaFree(s->g[0]);
+  cudaFree(s->g[1]);
+  cudaFree(s->T);
+  cudaFree(s->mask);
   delete s;
   return NAT_OK;
 }
 
 static int setup_dt(nat_solver* s, double dt) {
   HostStencil hs;
-  get_host_stencil(s->spec.stencil, &hs);
+  get_host_stencil(s->spec.stencil, &hs, s->spec.scaling);
   s->dt = dt;
   // tau = nu / (dt c_s^2) + 1/2 with the scaled c_s^2
   // (collision_advanced/AuxiliaryCollisionFunctions.h:63-68, 177)
   s->tau = s->spec.viscosity / (dt * s->cs2_scaled) + 0.5;
   int rc = build_tables(s, hs);
   if (rc) return rc;
+  if (s->thermal) return setup_thermal_tables(s);
   int Rm[3] = {s->h_tab.Rmax[0], s->h_tab.Rmax[1], s->h_tab.Rmax[2]};
   s->smem_step = step_smem_bytes(s->spec.precision, Rm, s->B);
   for (const KernelSet* ks : {&s->ks_coll, &s->ks_stream}) {
@@ -745,13 +920,57 @@ static int setup_dt(nat_solver* s, double dt) {
   return select_v2(s, coll_selector(s->spec.collision), smem_optin);
 }
 
+// Device state of a NAT_BGK_COMPRESSIBLE handle: f and g double-buffered,
+// rho, u, T, mask; the window tables live in the launch parameters.
+static int create_thermal(nat_solver* s, double hmin) {
+  const int p = s->spec.order;
+  for (int a = 0; a < 3; ++a) s->B[a] = a < s->D ? s->period : 1;
+  const size_t fbytes = sizeof(double) * (size_t)s->Q * s->n_dev;
+#define ALLOC(ptr, bytes)                                             \
+  do {                                                                \
+    cudaError_t e_ = cudaMalloc((void**)&(ptr), (bytes));             \
+    if (e_ != cudaSuccess) {                                          \
+      cudaGetLastError();                                             \
+      return fail(s, NAT_ERR_OOM, "cudaMalloc(%zu) failed", (size_t)(bytes)); \
+    }                                                                 \
+  } while (0)
+  ALLOC(s->f[0], fbytes);
+  ALLOC(s->f[1], fbytes);
+  ALLOC(s->g[0], fbytes);
+  ALLOC(s->g[1], fbytes);
+  ALLOC(s->rho, sizeof(double) * s->n_dev);
+  ALLOC(s->u, sizeof(double) * s->D * s->n_dev);
+  ALLOC(s->T, sizeof(double) * s->n_dev);
+  ALLOC(s->mask, sizeof(double) * s->n_dev);
+  ALLOC(s->staging, sizeof(double) * (size_t)s->Q * s->n_ref);
+  ALLOC(s->red, sizeof(double) * (2 + 32));
+  ALLOC(s->status, sizeof(int));
+  ALLOC(s->d_tab, sizeof(SLTables));
+#undef ALLOC
+  CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "memset");
+  CK(cudaMemsetAsync(s->rho, 0, sizeof(double) * s->n_dev, s->stream), "memset");
+  CK(cudaMemsetAsync(s->u, 0, sizeof(double) * s->D * s->n_dev, s->stream), "memset");
+  CK(cudaMemsetAsync(s->T, 0, sizeof(double) * s->n_dev, s->stream), "memset");
+  CK(cudaMemsetAsync(s->mask, 0, sizeof(double) * s->n_dev, s->stream), "memset");
+  // SolverConfiguration defaults (solver/SolverConfiguration.cpp:21-31)
+  s->th.gamma = 1.4;
+  s->th.prandtl = 1.0;
+  s->th.prandtl_set = 0;
+  s->th.sutherland_set = 0;
+  s->th.equilibrium = NAT_EQ_QUARTIC;
+  s->kind = 5;
+  double dt = s->spec.dt;
+  if (!(dt > 0)) dt = s->spec.cfl * hmin / (sqrt(2.0) * s->spec.scaling * p * p);
+  return setup_dt(s, dt);
+}
+
 int nat_create(const nat_spec* spec, nat_solver** out) {
   if (!spec || !out) return NAT_ERR_INVALID_ARG;
   *out = nullptr;
   nat_solver* s = new nat_solver();
   s->spec = *spec;
   HostStencil hs;
-  if (!get_host_stencil(spec->stencil, &hs)) {
+  if (!get_host_stencil(spec->stencil, &hs, spec->scaling)) {
     int rc = fail(s, NAT_ERR_UNSUPPORTED, "unsupported stencil %d", spec->stencil);
     *out = s;
     return rc;
@@ -782,7 +1001,15 @@ int nat_create(const nat_spec* spec, nat_solver** out) {
     case NAT_BGK_STANDARD: coll = L_COLL_BGK; break;
     case NAT_BGK_INCOMPRESSIBLE: coll = L_COLL_BGK_INC; break;
     case NAT_KBC_STANDARD: coll = L_COLL_KBC; break;
+    case NAT_BGK_COMPRESSIBLE: coll = L_COLL_NONE; break;
     default: return bad("bad collision model");
+  }
+  s->thermal = spec->collision == NAT_BGK_COMPRESSIBLE;
+  if (s->thermal != (spec->stencil == NAT_D2Q25H) || (s->thermal && spec->precision != NAT_FP64)) {
+    fail(s, NAT_ERR_UNSUPPORTED,
+         "the compressible two-population model runs on D2Q25H in FP64, and D2Q25H runs only that model");
+    *out = s;
+    return NAT_ERR_UNSUPPORTED;
   }
   auto pick = [&](int c) -> KernelSet {
     switch (spec->stencil) {
@@ -792,9 +1019,11 @@ int nat_create(const nat_spec* spec, nat_solver** out) {
     }
     return {nullptr, nullptr};
   };
-  s->ks_coll = pick(coll);
-  s->ks_stream = pick(L_COLL_NONE);
-  if (!s->ks_coll.step) {
+  if (!s->thermal) {
+    s->ks_coll = pick(coll);
+    s->ks_stream = pick(L_COLL_NONE);
+  }
+  if (!s->thermal && !s->ks_coll.step) {
     // the reference throws for these combinations too
     // (collision/BGKIncompressible.cpp:54-55, collision/KBCStandard.cpp:79-81)
     fail(s, NAT_ERR_UNSUPPORTED, "collision model %d is not implemented for stencil %d",
@@ -823,6 +1052,7 @@ int nat_create(const nat_spec* spec, nat_solver** out) {
     s->rest[q] = spec->collision == NAT_BGK_INCOMPRESSIBLE ? inc_rest(q) : hs.w[q];
   *out = s;
   CK(cudaGetDevice(&s->device), "cudaGetDevice");
+  if (s->thermal) return create_thermal(s, hmin);
   int smem_optin = 0;
   CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device),
      "device attribute");
@@ -952,7 +1182,7 @@ int nat_upload_macro(nat_solver* s, const double* rho_host, const double* u_host
 int nat_stream(nat_solver* s, double t, double* dt_out) {
   (void)t;
   if (!s) return NAT_ERR_INVALID_ARG;
-  int rc = launch_step(s, s->ks_stream, 0, 0);
+  int rc = s->thermal ? launch_thermal(s, false, 0) : launch_step(s, s->ks_stream, 0, 0);
   if (rc) return rc;
   if (dt_out) *dt_out = s->dt;
   return NAT_OK;
@@ -960,6 +1190,12 @@ int nat_stream(nat_solver* s, double t, double* dt_out) {
 
 int nat_collide(nat_solver* s, int in_init) {
   if (!s) return NAT_ERR_INVALID_ARG;
+  if (s->thermal) {
+    ThermalPoint TP = thermal_point_params(s, in_init);
+    CK(launch_thermal_collide(TP, grid_for(s->n_dev), s->stream), "two-population collide launch");
+    s->launches++;
+    return nat_status(s);
+  }
   StepParams P = step_params(s, s->f[s->cur], s->f[s->cur], 1, 1, in_init);
   void* args[] = {&P};
   CK(cudaLaunchKernel(s->ks_coll.collide, dim3(grid_for(s->n_dev)), dim3(256), args, 0, s->stream),
@@ -972,7 +1208,8 @@ int nat_step_async(nat_solver* s, int n_steps, int write_macro) {
   if (!s || n_steps < 0) return NAT_ERR_INVALID_ARG;
   for (int k = 0; k < n_steps; ++k) {
     const int wm = (write_macro && k == n_steps - 1) ? 1 : 0;
-    int rc = s->use_v2 ? launch_v2(s, wm) : launch_step(s, s->ks_coll, 1, wm);
+    int rc = s->thermal ? launch_thermal(s, true, wm)
+                        : (s->use_v2 ? launch_v2(s, wm) : launch_step(s, s->ks_coll, 1, wm));
     if (rc) return rc;
   }
   return NAT_OK;
@@ -1042,6 +1279,11 @@ int64_t nat_launch_count(const nat_solver* s) { return s ? s->launches : -1; }
 
 int nat_set_kernel_variant(nat_solver* s, int variant) {
   if (!s || variant < 0 || variant > 4) return NAT_ERR_INVALID_ARG;
+  if (s->thermal) {
+    // one kernel serves the two-population model
+    if (variant == 0) return NAT_OK;
+    return fail(s, NAT_ERR_UNSUPPORTED, "the two-population model has a single fused kernel");
+  }
   s->variant = variant;
   int smem_optin = 0;
   CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device),
@@ -1049,10 +1291,15 @@ int nat_set_kernel_variant(nat_solver* s, int variant) {
   return select_v2(s, coll_selector(s->spec.collision), smem_optin);
 }
 
-int nat_kernel_variant(const nat_solver* s) { return s ? (s->use_v2 ? s->kind : 1) : -1; }
+int nat_kernel_variant(const nat_solver* s) { return s ? (s->thermal ? 5 : (s->use_v2 ? s->kind : 1)) : -1; }
 
 int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
   if (!s || steps < 1) return NAT_ERR_INVALID_ARG;
+  if (s->thermal) {
+    if (n_candidates) *n_candidates = 1;
+    if (chosen) *chosen = 0;
+    return NAT_OK;
+  }
   int smem_optin = 0;
   CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device),
      "device attribute");
@@ -1117,6 +1364,17 @@ int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
 
 int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* threads, int64_t* smem_bytes) {
   if (!s) return NAT_ERR_INVALID_ARG;
+  if (s->thermal) {
+    if (variant) *variant = 5;
+    if (tile_nodes) {
+      tile_nodes[0] = 32;
+      tile_nodes[1] = 1;
+      tile_nodes[2] = 1;
+    }
+    if (threads) *threads = 32 * TH_WARPS;
+    if (smem_bytes) *smem_bytes = 0;
+    return NAT_OK;
+  }
   const int k = s->use_v2 ? s->kind : 1;
   if (variant) *variant = k;
   for (int a = 0; a < 3; ++a) {
@@ -1126,6 +1384,84 @@ int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* t
   }
   if (threads) *threads = k == 2 ? s->v2.nth : (k == 3 ? 32 * s->row.wy * s->row.wz : STEP_THREADS);
   if (smem_bytes) *smem_bytes = (int64_t)(k == 2 ? s->v2.smem : (k == 3 ? 0 : s->smem_step));
+  return NAT_OK;
+}
+
+int nat_set_thermal(nat_solver* s, const nat_thermal* t) {
+  if (!s || !t) return NAT_ERR_INVALID_ARG;
+  if (!s->thermal) return fail(s, NAT_ERR_UNSUPPORTED, "not a NAT_BGK_COMPRESSIBLE handle");
+  if (!(t->gamma > 1.0) || !(t->prandtl > 0.0) ||
+      (t->equilibrium != NAT_EQ_QUARTIC && t->equilibrium != NAT_EQ_BGK))
+    return fail(s, NAT_ERR_INVALID_ARG, "gamma must be > 1, prandtl > 0, equilibrium NAT_EQ_QUARTIC or NAT_EQ_BGK");
+  s->th = *t;
+  fill_thermal_model(s);
+  return NAT_OK;
+}
+
+int nat_get_thermal(const nat_solver* s, nat_thermal* t) {
+  if (!s || !t) return NAT_ERR_INVALID_ARG;
+  if (!s->thermal) return NAT_ERR_UNSUPPORTED;
+  *t = s->th;
+  return NAT_OK;
+}
+
+int nat_upload_g(nat_solver* s, const double* g_host) {
+  if (!s || !g_host) return NAT_ERR_INVALID_ARG;
+  if (!s->thermal) return fail(s, NAT_ERR_UNSUPPORTED, "not a NAT_BGK_COMPRESSIBLE handle");
+  CK(cudaMemcpyAsync(s->staging, g_host, sizeof(double) * s->Q * s->n_ref, cudaMemcpyHostToDevice, s->stream),
+     "upload g");
+  k_upload<double><<<grid_for(s->n_dev * s->Q), 256, 0, s->stream>>>(s->staging, s->g[s->cur], dims_of(s), s->Q,
+                                                                      s->red + 2);
+  CK(cudaGetLastError(), "upload kernel");
+  s->launches++;
+  return NAT_OK;
+}
+
+int nat_download_g(nat_solver* s, double* g_host) {
+  if (!s || !g_host) return NAT_ERR_INVALID_ARG;
+  if (!s->thermal) return fail(s, NAT_ERR_UNSUPPORTED, "not a NAT_BGK_COMPRESSIBLE handle");
+  k_download<double><<<grid_for(s->n_ref * s->Q), 256, 0, s->stream>>>(s->g[s->cur], s->staging, dims_of(s), s->Q,
+                                                                        s->red + 2);
+  CK(cudaGetLastError(), "download kernel");
+  s->launches++;
+  CK(cudaMemcpyAsync(g_host, s->staging, sizeof(double) * s->Q * s->n_ref, cudaMemcpyDeviceToHost, s->stream),
+     "download g");
+  CK(cudaStreamSynchronize(s->stream), "download sync");
+  return NAT_OK;
+}
+
+int nat_download_thermal(nat_solver* s, double* T_host, double* mask_host) {
+  if (!s || !T_host || !mask_host) return NAT_ERR_INVALID_ARG;
+  if (!s->thermal) return fail(s, NAT_ERR_UNSUPPORTED, "not a NAT_BGK_COMPRESSIBLE handle");
+  Dims d = dims_of(s);
+  k_fields_to_ref<<<grid_for(s->n_ref), 256, 0, s->stream>>>(s->T, s->staging, d, 1);
+  k_fields_to_ref<<<grid_for(s->n_ref), 256, 0, s->stream>>>(s->mask, s->staging + s->n_ref, d, 1);
+  CK(cudaGetLastError(), "thermal fields kernel");
+  s->launches += 2;
+  CK(cudaMemcpyAsync(T_host, s->staging, sizeof(double) * s->n_ref, cudaMemcpyDeviceToHost, s->stream),
+     "download T");
+  CK(cudaMemcpyAsync(mask_host, s->staging + s->n_ref, sizeof(double) * s->n_ref, cudaMemcpyDeviceToHost,
+                     s->stream), "download mask");
+  CK(cudaStreamSynchronize(s->stream), "download sync");
+  return NAT_OK;
+}
+
+int nat_init_thermal(nat_solver* s, const double* rho_host, const double* u_host, const double* T_host) {
+  if (!s || !rho_host || !u_host || !T_host) return NAT_ERR_INVALID_ARG;
+  if (!s->thermal) return fail(s, NAT_ERR_UNSUPPORTED, "not a NAT_BGK_COMPRESSIBLE handle");
+  int rc = nat_upload_macro(s, rho_host, u_host);
+  if (rc) return rc;
+  // the staging buffer is reused once the copies above are done (same stream)
+  CK(cudaMemcpyAsync(s->staging + (1 + s->D) * s->n_ref, T_host, sizeof(double) * s->n_ref,
+                     cudaMemcpyHostToDevice, s->stream), "upload T");
+  k_fields_from_ref<<<grid_for(s->n_dev), 256, 0, s->stream>>>(s->staging + (1 + s->D) * s->n_ref, s->T,
+                                                               dims_of(s), 1);
+  CK(cudaGetLastError(), "T upload kernel");
+  s->launches++;
+  ThermalPoint P = thermal_point_params(s, 0);
+  CK(launch_thermal_init(P, grid_for(s->n_dev), s->stream), "two-population init launch");
+  s->launches++;
+  CK(cudaStreamSynchronize(s->stream), "init sync");
   return NAT_OK;
 }
 

@@ -69,6 +69,44 @@ struct SD3Q27 {
   }
 };
 
+// D2Q25H (stencils/D2Q25H.cpp:37-84): the velocities are the products of the
+// 1-D set {0, +-c_m, +-c_n}, c_m = sqrt(5 - sqrt 10) / sqrt 3 and
+// c_n = sqrt(5 + sqrt 10) / sqrt 3 (unscaled); the weights are products of
+// the 1-D weights.  The speeds themselves are not integers, so code(i, a)
+// gives the component as a code (0 none, +-1 +-c_m, +-2 +-c_n); the values
+// come from the host.  dcls(i, a): 0 +c_m, 1 -c_m, 2 +c_n, 3 -c_n, -1 none.
+// group(i): the symmetry group (|code_x|, |code_y|) of the direction --
+// (0,0) 0, (1,0) 1, (0,1) 2, (2,0) 3, (0,2) 4, (1,1) 5, (2,2) 6, (1,2) 7,
+// (2,1) 8 -- whose members share |e_x|, |e_y| and the weight.
+struct SD2Q25H {
+  static constexpr int ID = 3, D = 2, Q = 25, NG = 9;
+  __host__ __device__ static constexpr int code(int i, int a) {
+    constexpr int C[25][2] = {{0, 0},  {1, 0},   {0, 1},   {-1, 0}, {0, -1}, {1, 1},   {-1, 1},
+                              {-1, -1}, {1, -1}, {2, 0},   {0, 2},  {-2, 0}, {0, -2},  {2, 2},
+                              {-2, 2}, {-2, -2}, {2, -2},  {1, 2},  {1, -2}, {-1, -2}, {-1, 2},
+                              {2, 1},  {2, -1},  {-2, -1}, {-2, 1}};
+    return C[i][a];
+  }
+  __host__ __device__ static constexpr int dcls(int i, int a) {
+    return code(i, a) == 1 ? 0 : (code(i, a) == -1 ? 1 : (code(i, a) == 2 ? 2 : (code(i, a) == -2 ? 3 : -1)));
+  }
+  // sign of the component (+1 for none)
+  __host__ __device__ static constexpr int sgn(int i, int a) { return code(i, a) < 0 ? -1 : 1; }
+  __host__ __device__ static constexpr int group(int i) {
+    constexpr int G[3][3] = {{0, 2, 4}, {1, 5, 7}, {3, 8, 6}};  // [|code_x|][|code_y|]
+    return G[code(i, 0) < 0 ? -code(i, 0) : code(i, 0)][code(i, 1) < 0 ? -code(i, 1) : code(i, 1)];
+  }
+  // |code| per axis of a group
+  __host__ __device__ static constexpr int gx(int g) {
+    constexpr int X[9] = {0, 1, 0, 2, 0, 1, 2, 1, 2};
+    return X[g];
+  }
+  __host__ __device__ static constexpr int gy(int g) {
+    constexpr int Y[9] = {0, 0, 1, 0, 2, 1, 2, 2, 1};
+    return Y[g];
+  }
+};
+
 // compile-time loop helper
 template <int I>
 struct IC {

@@ -42,3 +42,43 @@ def oracle_step(S, st, model, tau, f, nsteps=1):
         f = S.stream(f)
         O.collide(st, model, tau, f, rho, u)
     return f, rho, u
+
+
+# ---------------------------------------------------------------------------
+# compressible two-population model (D2Q25H)
+# ---------------------------------------------------------------------------
+
+def thermal_case(N_cells, p, dg=True, scaling=1.0, nu=1e-3, L=1.0, cfl=0.4):
+    st = O.stencil("D2Q25H", scaling)
+    mesh = O.Mesh(2, tuple(N_cells), p, dg, (L, L, L))
+    dt = O.time_step(mesh.h_min(), p, st.max_speed, cfl)
+    tau = nu / (dt * st.cs2) + 0.5
+    spec = N.SolverSpec(stencil="D2Q25H", order=p, cells=tuple(N_cells), length=(L, L), scaling=scaling,
+                        viscosity=nu, dt=dt, collision="BGK_COMPRESSIBLE", precision="fp64",
+                        topology="dg" if dg else "feq")
+    return st, mesh, dt, tau, spec
+
+
+def thermal_state(mesh, st, seed=0, gamma=1.4, amp=1e-3):
+    """Smooth periodic rho, u (scaled), T on the support points, the
+    equilibrium f, g of the oracle, and a seeded non-equilibrium perturbation."""
+    X = mesh.coords()
+    k = 2 * math.pi / mesh.L[0]
+    x, y = X[:, 0] * k, X[:, 1] * k
+    rho = 1.0 + 0.1 * np.sin(x) * np.cos(y)
+    u = np.stack([0.1 * np.sin(x + 0.3) * np.cos(y), -0.08 * np.cos(x) * np.sin(2 * y)]) * st.scaling
+    T = 1.0 + 0.1 * np.cos(x - 0.2) * np.sin(y + 0.1)
+    f, g = O.thermal_init(st, rho, u, T, gamma)
+    rng = np.random.default_rng(seed)
+    # perturb consistently on periodic duplicates of the FE_Q lattice
+    pf = rng.standard_normal(f.shape)
+    pg = rng.standard_normal(g.shape)
+    if not mesh.dg:
+        nx, ny = mesh.nodes_per_axis(0), mesh.nodes_per_axis(1)
+        for a in (pf, pg):
+            v = a.reshape(a.shape[0], ny, nx)
+            v[:, :, nx - 1] = v[:, :, 0]
+            v[:, ny - 1, :] = v[:, 0, :]
+    f = f * (1.0 + amp * pf)
+    g = g * (1.0 + amp * pg)
+    return rho, u, T, np.ascontiguousarray(f), np.ascontiguousarray(g)

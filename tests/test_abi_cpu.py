@@ -52,6 +52,18 @@ def test_unsupported_combination_is_reported():
         assert ei.value.code == N.NAT_ERR_UNSUPPORTED
 
 
+def test_compressible_model_combinations_are_checked():
+    # the compressible two-population model runs on D2Q25H in FP64 only, and
+    # D2Q25H only runs that model
+    for st, coll, prec in (("D2Q9", "BGK_COMPRESSIBLE", "fp64"), ("D2Q25H", "BGK_STANDARD", "fp64"),
+                           ("D2Q25H", "BGK_COMPRESSIBLE", "fp32dev")):
+        spec = N.SolverSpec(stencil=st, order=2, cells=(2, 2), length=(1, 1), scaling=1.0,
+                            viscosity=0.1, collision=coll, precision=prec)
+        with pytest.raises(N.NatError) as ei:
+            N.Solver(spec)
+        assert ei.value.code == N.NAT_ERR_UNSUPPORTED
+
+
 def test_last_error_null_handle():
     L = N.load_library()
     buf = C.create_string_buffer(64)

@@ -1,0 +1,172 @@
+"""Parity of the compressible two-population path (D2Q25H, quartic
+equilibrium, relaxWithG) on the GPU with the CPU oracle.
+
+Plain FP64: relative L2 <= 1e-12 per step for f, g, rho, u and T against the
+oracle's restatement (copy + CSR SpMV of f and of g with the same operator,
+then CollisionOperator::collideAll(f, g, ...)); the shock-sensor mask (a sum
+of |f - f^eq|, i.e. of small differences) within 1e-9.
+"""
+import numpy as np
+import pytest
+
+import natrium_gb300 as N
+import oracle as O
+from tests.gpu_cases import rel_l2, thermal_case, thermal_state
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+
+CASES = [((4, 4), p, dg) for p in (1, 2, 3, 4, 5, 6) for dg in (False, True)]
+
+
+def _th(settings: N.ThermalSettings) -> O.Thermal:
+    return O.Thermal(settings.gamma, settings.prandtl, settings.prandtl_set, settings.sutherland,
+                     settings.equilibrium == "QUARTIC")
+
+
+def _run(spec, f0, g0, settings=None, nsteps=1):
+    with N.Solver(spec) as sol:
+        if settings is not None:
+            sol.set_thermal(settings)
+        sol.upload_f(f0)
+        sol.upload_g(g0)
+        sol.step(nsteps)
+        f, g = sol.download_f(), sol.download_g()
+        rho, u = sol.download_macro()
+        T, m = sol.download_thermal()
+        assert sol.kernel_variant == 5
+    return f, g, rho, u, T, m
+
+
+@pytest.mark.parametrize("case", CASES, ids=[f"p{c[1]}-{'dg' if c[2] else 'feq'}" for c in CASES])
+def test_fp64_step_matches_oracle(gpu_lib, case):
+    cells, p, dg = case
+    st, mesh, dt, tau, spec = thermal_case(cells, p, dg)
+    rho0, u0, T0, f0, g0 = thermal_state(mesh, st, seed=p)
+    S = O.SLOperator(mesh, st, dt)
+    f1, g1 = f0.copy(), g0.copy()
+    r1, u1, T1, m1 = S.step_compressible(f1, g1, tau)
+    f, g, rho, u, T, m = _run(spec, f0, g0)
+    assert rel_l2(f, f1) <= TOL64
+    assert rel_l2(g, g1) <= TOL64
+    assert rel_l2(rho, r1) <= TOL64
+    assert rel_l2(u, u1) <= 1e-11
+    assert rel_l2(T, T1) <= TOL64
+    assert rel_l2(m, m1) <= 1e-9
+
+
+SETTINGS = [
+    N.ThermalSettings(prandtl=0.71, prandtl_set=True),
+    N.ThermalSettings(sutherland=True),
+    N.ThermalSettings(equilibrium="BGK"),
+    N.ThermalSettings(gamma=1.67, prandtl=2.0, prandtl_set=True, sutherland=True),
+]
+
+
+@pytest.mark.parametrize("settings", SETTINGS, ids=["prandtl", "sutherland", "bgk-eq", "all"])
+def test_fp64_settings_match_oracle(gpu_lib, settings):
+    st, mesh, dt, tau, spec = thermal_case((4, 3), 2, True, scaling=1.3, nu=2e-3)
+    rho0, u0, T0, f0, g0 = thermal_state(mesh, st, seed=7, gamma=settings.gamma)
+    S = O.SLOperator(mesh, st, dt)
+    f1, g1 = f0.copy(), g0.copy()
+    r1, u1, T1, m1 = S.step_compressible(f1, g1, tau, _th(settings))
+    f, g, rho, u, T, m = _run(spec, f0, g0, settings)
+    assert rel_l2(f, f1) <= TOL64
+    assert rel_l2(g, g1) <= TOL64
+    assert rel_l2(T, T1) <= TOL64
+    assert rel_l2(m, m1) <= 1e-9
+
+
+def test_fp64_ten_steps(gpu_lib):
+    st, mesh, dt, tau, spec = thermal_case((6, 5), 2, True)
+    rho0, u0, T0, f0, g0 = thermal_state(mesh, st, seed=11)
+    S = O.SLOperator(mesh, st, dt)
+    f1, g1 = f0.copy(), g0.copy()
+    r1, u1, T1, m1 = S.step_compressible(f1, g1, tau, nsteps=10)
+    f, g, rho, u, T, m = _run(spec, f0, g0, nsteps=10)
+    assert rel_l2(f, f1) <= TOL64
+    assert rel_l2(g, g1) <= TOL64
+    assert rel_l2(T, T1) <= TOL64
+    assert rel_l2(u, u1) <= 1e-10
+
+
+@pytest.mark.parametrize("dg", [False, True])
+def test_stream_only_streams_both_populations(gpu_lib, dg):
+    st, mesh, dt, tau, spec = thermal_case((4, 4), 3, dg)
+    rho0, u0, T0, f0, g0 = thermal_state(mesh, st, seed=2)
+    S = O.SLOperator(mesh, st, dt)
+    fo, go = S.stream(f0), S.stream(g0)
+    f, g = N.DistributionFunctions(f0.copy()), N.DistributionFunctions(g0.copy())
+    with N.Solver(spec) as sol:
+        dt_out = N.CompressibleStep(sol).stream(f, g)
+    assert dt_out == pytest.approx(dt, rel=1e-15)
+    assert rel_l2(f.f, fo) <= TOL64
+    assert rel_l2(g.f, go) <= TOL64
+
+
+@pytest.mark.parametrize("in_init", [False, True])
+def test_collide_all_matches_oracle(gpu_lib, in_init):
+    st, mesh, dt, tau, spec = thermal_case((3, 4), 2, True, scaling=1.2)
+    rho0, u0, T0, f0, g0 = thermal_state(mesh, st, seed=4, amp=5e-3)
+    n = mesh.n_nodes
+    fo, go = f0.copy(), g0.copy()
+    ro, To, mo = np.zeros(n), np.zeros(n), np.zeros(n)
+    uo = (u0 * 1.1).copy() if in_init else np.zeros((2, n))
+    O.collide_compressible(st, tau, fo, go, ro, uo, To, mo, in_init=in_init)
+    f, g = N.DistributionFunctions(f0.copy()), N.DistributionFunctions(g0.copy())
+    rho, T, m = np.zeros(n), np.zeros(n), np.zeros(n)
+    u = (u0 * 1.1).copy() if in_init else np.zeros((2, n))
+    with N.Solver(spec) as sol:
+        N.BGKCompressible(sol).collideAll(f, g, rho, u, T, m, None, in_init)
+    assert rel_l2(f.f, fo) <= TOL64
+    assert rel_l2(g.f, go) <= TOL64
+    assert rel_l2(rho, ro) <= TOL64
+    assert rel_l2(u, uo) <= 1e-11
+    assert rel_l2(T, To) <= TOL64
+    assert rel_l2(m, mo) <= 1e-9
+
+
+@pytest.mark.parametrize("dg", [False, True])
+def test_equilibrium_initialisation_matches_oracle(gpu_lib, dg):
+    st, mesh, dt, tau, spec = thermal_case((4, 4), 4, dg, scaling=1.5)
+    rho0, u0, T0, f0, g0 = thermal_state(mesh, st, seed=1, gamma=1.3)
+    fo, go = O.thermal_init(st, rho0, u0, T0, gamma=1.3)
+    with N.Solver(spec) as sol:
+        sol.set_thermal(N.ThermalSettings(gamma=1.3))
+        sol.init_thermal(rho0, u0, T0)
+        f, g = sol.download_f(), sol.download_g()
+        rho, u = sol.download_macro()
+    assert rel_l2(f, fo) <= 1e-14
+    assert rel_l2(g, go) <= 1e-14
+    assert rel_l2(rho, rho0) == 0.0
+
+
+def test_uniform_state_is_stationary_on_device(gpu_lib):
+    st, mesh, dt, tau, spec = thermal_case((5, 4), 3, False, scaling=1.1)
+    n = mesh.n_nodes
+    rho = np.full(n, 0.9)
+    u = np.stack([np.full(n, 0.07), np.full(n, -0.02)]) * st.scaling
+    T = np.full(n, 1.05)
+    with N.Solver(spec) as sol:
+        sol.init_thermal(rho, u, T)
+        f0 = sol.download_f()
+        sol.step(5)
+        f = sol.download_f()
+        T1, m = sol.download_thermal()
+    assert np.abs(f - f0).max() < 1e-13
+    assert np.allclose(T1, 1.05, rtol=1e-13)
+    assert np.abs(m).max() < 1e-12
+
+
+def test_density_underflow_is_reported(gpu_lib):
+    st, mesh, dt, tau, spec = thermal_case((2, 2), 2, True)
+    n = mesh.n_nodes
+    f = np.zeros((25, n))
+    f[0] = 1.0
+    f[0, 3] = 0.0
+    with N.Solver(spec) as sol:
+        sol.upload_f(f)
+        sol.upload_g(np.zeros((25, n)))
+        with pytest.raises(N.CollisionException):
+            sol.collide()
