@@ -201,6 +201,65 @@ def cpu_baseline(sample_cells=(8, 8, 8), steps=5):
                       f"{threads} OpenMP threads"}
 
 
+COMPRESSIBLE = dict(
+    name="riemann2d_d2q25h_quartic_sl_dg_p2_128x128",
+    cells=(128, 128), order=2, topology="dg", scaling=1.0, viscosity=1e-3, cfl=0.4, velocity_unit=1.58,
+    t_end=0.3,
+)
+
+
+def compressible_spec():
+    import natrium_gb300 as N
+    c = COMPRESSIBLE
+    return N.SolverSpec(stencil="D2Q25H", order=c["order"], cells=c["cells"], length=(1.0, 1.0),
+                        scaling=c["scaling"], viscosity=c["viscosity"], cfl=c["cfl"], collision="BGK_COMPRESSIBLE",
+                        precision="fp64", topology=c["topology"])
+
+
+def bench_compressible(torch, stream, flush, steps: int = 200, warmup: int = 5, full_run: bool = True):
+    """The compressible two-population path (D2Q25H, quartic BGK with g) on
+    the four-quadrant Riemann problem: 128^2 cells, FE_DGQ p = 2 (147,456
+    nodes x 25 x 2 populations), FP64, periodic box.  Device-timed steps plus
+    (full_run) the whole run to t = 0.3 with a mass-conservation check."""
+    import natrium_gb300 as N
+    from natrium_gb300 import problems as P
+    c = COMPRESSIBLE
+    spec = compressible_spec()
+    X = P.node_coords(spec.cells, spec.order, spec.length, spec.topology)
+    rho, u, T = P.riemann_2d(X, c["velocity_unit"], spec.scaling)
+    sol = N.Solver(spec)
+    sol.set_stream(stream.cuda_stream)
+    sol.init_thermal(rho, u, T)
+    per, launches = time_device(sol, torch, stream, flush, steps, warmup)
+    ms = sum(per) / steps
+    n = sol.n_dev
+    out = {"workload": c["name"], "nodes": n, "dtype": "f64", "steps": steps, "ms_per_step": ms,
+           "value": n / (ms * 1e-3), "unit": UNIT, "kernel": "k_thermal_step<true>", "gpu_launches": launches,
+           "algorithmic_bytes_per_launch": 2 * 2 * sol.Q * 8 * n,
+           "achieved_gbs": 2 * 2 * sol.Q * 8 * n / (ms * 1e-3) / 1e9,
+           "boundaries": "periodic (walls / extrapolation not built)",
+           "state": "lattice units: u / 1.58, T = 3 (p / rho) / 1.58^2, nu = 1e-3, scaling 1, CFL 0.4"}
+    if full_run:
+        sol.init_thermal(rho, u, T)
+        sol.step(1)
+        m0, _ = sol.mass_energy()
+        dt = sol.dt
+        nsteps = int(round(c["t_end"] * c["velocity_unit"] / dt))
+        t0 = time.perf_counter()
+        sol.step(nsteps - 1)
+        wall = time.perf_counter() - t0
+        m1, _ = sol.mass_energy()
+        r, _ = sol.download_macro()
+        Tn, _ = sol.download_thermal()
+        out["full_run"] = {"steps": nsteps, "t_end_lattice": nsteps * dt, "wall_s": wall,
+                           "mass_rel_change": abs(m1 - m0) / abs(m0),
+                           "rho_range": [float(r.min()), float(r.max())],
+                           "T_range": [float(Tn.min()), float(Tn.max())],
+                           "finite": bool(np.isfinite(r).all() and np.isfinite(Tn).all())}
+    sol.close()
+    return out
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -253,6 +312,10 @@ def run_ours(args):
         dist.init_process_group("nccl")
     stream = torch.cuda.Stream()
     flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+    if args.compressible_only:
+        print(json.dumps(bench_compressible(torch, stream, flush, steps=args.steps, warmup=args.warmup,
+                                            full_run=not args.profile)))
+        return 0
 
     # --- FP32-deviation path (headline) -------------------------------------
     spec = spec_for("fp32dev")
@@ -337,6 +400,7 @@ def run_ours(args):
             torch.distributed.destroy_process_group()
         return 0
     cpu = cpu_baseline() if ws == 1 else None
+    compressible = bench_compressible(torch, stream, flush)
     serving = None
     if not args.no_serving:
         from natrium_gb300 import serving as SV
@@ -376,6 +440,7 @@ def run_ours(args):
                        "roofline_frac": ach64 / hbm, "achieved_gbs": ach64, "kernel": kinfo64},
         "speedup_vs_fp64_plain": ms64 / ms,
         "serving": serving,
+        "compressible": compressible,
         "state_ok": ok,
     }
     print(json.dumps(line))
@@ -395,6 +460,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--profile", action="store_true",
                     help="lean run for ncu: FP32 device timing only (no e2e, FP64 leg, CPU baseline or clocks)")
+    ap.add_argument("--compressible-only", action="store_true",
+                    help="time only the compressible D2Q25H leg (prints its JSON object)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -114,3 +114,37 @@ def shear_layer_2d(X: np.ndarray, kappa: float = 80.0, delta: float = 0.05, L: f
     ux = np.where(y <= 0.5, np.tanh(kappa * (y - 0.25)), np.tanh(kappa * (0.75 - y)))
     uy = delta * np.sin(2 * math.pi * (x + 0.25))
     return np.ones_like(x), np.stack([ux, uy])
+
+
+# Four-quadrant 2-D Riemann problem on [0, 1]^2 (discontinuities at x = 1/2
+# and y = 1/2); states (rho, u, v, p) per quadrant.
+RIEMANN2D_QUADRANTS = {
+    "upper_right": (1.5, 0.0, 0.0, 1.5),
+    "upper_left": (0.5323, 1.206, 0.0, 0.3),
+    "lower_left": (0.138, 1.206, 1.206, 0.029),
+    "lower_right": (0.5323, 0.0, 1.206, 0.3),
+}
+
+
+def riemann_2d(X: np.ndarray, velocity_unit: float = 1.58, scaling: float = 1.0):
+    """Initial rho, scaled u and lattice temperature of the four-quadrant
+    Riemann problem at the points X.  A physical velocity u maps to the
+    lattice velocity u / velocity_unit, and p / rho to the lattice temperature
+    T = (p / rho) / (c_s^2 velocity_unit^2) with c_s^2 = 1/3 (T = 1 is the
+    lattice reference temperature of the quartic equilibrium).  The
+    compressible solver of the reference states its Riemann problem directly
+    in these lattice units (benchmarks/Riemann2D.cpp:41-106)."""
+    x, y = X[:, 0], X[:, 1]
+    n = X.shape[0]
+    rho = np.empty(n)
+    u = np.empty((2, n))
+    T = np.empty(n)
+    right, up = x > 0.5, y > 0.5
+    for mask, key in ((right & up, "upper_right"), (~right & up, "upper_left"), (~right & ~up, "lower_left"),
+                      (right & ~up, "lower_right")):
+        r, ux, uy, p = RIEMANN2D_QUADRANTS[key]
+        rho[mask] = r
+        u[0, mask] = ux / velocity_unit
+        u[1, mask] = uy / velocity_unit
+        T[mask] = 3.0 * (p / r) / velocity_unit ** 2
+    return rho, u * scaling, T
