@@ -208,23 +208,19 @@ COMPRESSIBLE = dict(
 )
 
 
-def compressible_spec():
+def compressible_spec(precision: str = "fp64"):
     import natrium_gb300 as N
     c = COMPRESSIBLE
     return N.SolverSpec(stencil="D2Q25H", order=c["order"], cells=c["cells"], length=(1.0, 1.0),
                         scaling=c["scaling"], viscosity=c["viscosity"], cfl=c["cfl"], collision="BGK_COMPRESSIBLE",
-                        precision="fp64", topology=c["topology"])
+                        precision=precision, topology=c["topology"])
 
 
-def bench_compressible(torch, stream, flush, steps: int = 200, warmup: int = 5, full_run: bool = True):
-    """The compressible two-population path (D2Q25H, quartic BGK with g) on
-    the four-quadrant Riemann problem: 128^2 cells, FE_DGQ p = 2 (147,456
-    nodes x 25 x 2 populations), FP64, periodic box.  Device-timed steps plus
-    (full_run) the whole run to t = 0.3 with a mass-conservation check."""
+def _compressible_leg(torch, stream, flush, precision, steps, warmup, full_run):
     import natrium_gb300 as N
     from natrium_gb300 import problems as P
     c = COMPRESSIBLE
-    spec = compressible_spec()
+    spec = compressible_spec(precision)
     X = P.node_coords(spec.cells, spec.order, spec.length, spec.topology)
     rho, u, T = P.riemann_2d(X, c["velocity_unit"], spec.scaling)
     sol = N.Solver(spec)
@@ -233,30 +229,54 @@ def bench_compressible(torch, stream, flush, steps: int = 200, warmup: int = 5, 
     per, launches = time_device(sol, torch, stream, flush, steps, warmup)
     ms = sum(per) / steps
     n = sol.n_dev
-    out = {"workload": c["name"], "nodes": n, "dtype": "f64", "steps": steps, "ms_per_step": ms,
-           "value": n / (ms * 1e-3), "unit": UNIT, "kernel": "k_thermal_step<true>", "gpu_launches": launches,
-           "algorithmic_bytes_per_launch": 2 * 2 * sol.Q * 8 * n,
-           "achieved_gbs": 2 * 2 * sol.Q * 8 * n / (ms * 1e-3) / 1e9,
-           "boundaries": "periodic (walls / extrapolation not built)",
-           "state": "lattice units: u / 1.58, T = 3 (p / rho) / 1.58^2, nu = 1e-3, scaling 1, CFL 0.4"}
+    es = 8 if precision == "fp64" else 4
+    out = {"precision": precision, "ms_per_step": ms, "value": n / (ms * 1e-3), "gpu_launches": launches,
+           "algorithmic_bytes_per_launch": 2 * 2 * sol.Q * es * n,
+           "achieved_gbs": 2 * 2 * sol.Q * es * n / (ms * 1e-3) / 1e9,
+           "kernel": f"k_thermal_step<{'double' if es == 8 else 'float'},true>"}
+    fields = None
     if full_run:
         sol.init_thermal(rho, u, T)
         sol.step(1)
         m0, _ = sol.mass_energy()
         dt = sol.dt
         nsteps = int(round(c["t_end"] * c["velocity_unit"] / dt))
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         sol.step(nsteps - 1)
         wall = time.perf_counter() - t0
         m1, _ = sol.mass_energy()
-        r, _ = sol.download_macro()
+        r, uu = sol.download_macro()
         Tn, _ = sol.download_thermal()
+        fields = (r, uu, Tn)
         out["full_run"] = {"steps": nsteps, "t_end_lattice": nsteps * dt, "wall_s": wall,
                            "mass_rel_change": abs(m1 - m0) / abs(m0),
                            "rho_range": [float(r.min()), float(r.max())],
                            "T_range": [float(Tn.min()), float(Tn.max())],
                            "finite": bool(np.isfinite(r).all() and np.isfinite(Tn).all())}
     sol.close()
+    return out, n, fields
+
+
+def bench_compressible(torch, stream, flush, steps: int = 200, warmup: int = 5, full_run: bool = True):
+    """The compressible two-population path (D2Q25H, quartic BGK with g) on
+    the four-quadrant Riemann problem: 128^2 cells, FE_DGQ p = 2 (147,456
+    nodes x 25 x 2 populations), periodic box.  FP32 deviation storage (the
+    configuration's storage) and plain FP64, each device-timed; with full_run
+    both also run to t = 0.3 and the FP32 fields are compared with the FP64
+    ones (the FP64 path matches the oracle to 1e-12 per step)."""
+    c = COMPRESSIBLE
+    o32, n, F32 = _compressible_leg(torch, stream, flush, "fp32dev", steps, warmup, full_run)
+    o64, _, F64 = _compressible_leg(torch, stream, flush, "fp64", max(20, steps // 4), warmup, full_run)
+    out = {"workload": c["name"], "nodes": n, "dtype": "f32", "unit": UNIT, "value": o32["value"],
+           "ms_per_step": o32["ms_per_step"], "fp32dev": o32, "fp64": o64,
+           "speedup_fp32dev_vs_fp64": o64["ms_per_step"] / o32["ms_per_step"],
+           "boundaries": "periodic (walls / extrapolation not built)",
+           "state": "lattice units: u / 1.58, T = 3 (p / rho) / 1.58^2, nu = 1e-3, scaling 1, CFL 0.4"}
+    if full_run:
+        rl2 = lambda a, b: float(np.sqrt(np.sum((a - b) ** 2) / np.sum(b ** 2)))
+        out["fp32dev_vs_fp64_at_t_end"] = {"rel_l2_rho": rl2(F32[0], F64[0]), "rel_l2_u": rl2(F32[1], F64[1]),
+                                           "rel_l2_T": rl2(F32[2], F64[2])}
     return out
 
 

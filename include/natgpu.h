@@ -68,7 +68,9 @@ extern "C" {
  * streamed by the same operator (solver/CompressibleCFDSolver.h:181-314),
  * collideAll(f, g, rho, u, T, mask) (collision_advanced/CollisionOperator.h:113-224)
  * with BGKCollision::relaxWithG (collision_advanced/CollisionSchemes.h:43-118).
- * Requires stencil NAT_D2Q25H (and D2Q25H requires this model), NAT_FP64. */
+ * Requires stencil NAT_D2Q25H (and D2Q25H requires this model).  Precision
+ * NAT_FP64, or NAT_FP32_DEV: f - w_i and g - w_i g_ref (g_ref = 3, the
+ * rest-state g^eq / f^eq for gamma = 1.4) stored and computed in float. */
 #define NAT_BGK_COMPRESSIBLE 3
 
 /* ---- node topology ----------------------------------------------------- */

@@ -1,5 +1,5 @@
 // Kernels of the compressible two-population model (sl_thermal.cuh) and
-// their host launchers.
+// their host launchers: FP64 and FP32-deviation instantiations.
 #include <cuda_runtime.h>
 
 #include "launch.h"
@@ -7,22 +7,44 @@
 
 namespace natgpu {
 
-cudaError_t launch_thermal_step(const ThermalStep& P, bool collide, cudaStream_t st) {
+template <class Real>
+static cudaError_t step_t(const ThermalStepT<Real>& P, bool collide, cudaStream_t st) {
   const int warps = P.nseg * P.ny;
   const int grid = (warps + TH_WARPS - 1) / TH_WARPS;
-  void* args[] = {const_cast<ThermalStep*>(&P)};
-  const void* fn = collide ? (const void*)k_thermal_step<true> : (const void*)k_thermal_step<false>;
+  void* args[] = {const_cast<ThermalStepT<Real>*>(&P)};
+  const void* fn =
+      collide ? (const void*)k_thermal_step<Real, true> : (const void*)k_thermal_step<Real, false>;
   return cudaLaunchKernel(fn, dim3(grid), dim3(32 * TH_WARPS), args, 0, st);
 }
 
-cudaError_t launch_thermal_collide(const ThermalPoint& P, int grid, cudaStream_t st) {
-  void* args[] = {const_cast<ThermalPoint*>(&P)};
-  return cudaLaunchKernel((const void*)k_thermal_collide, dim3(grid), dim3(256), args, 0, st);
+cudaError_t launch_thermal_step(const ThermalStepT<double>& P, bool collide, cudaStream_t st) {
+  return step_t(P, collide, st);
+}
+cudaError_t launch_thermal_step(const ThermalStepT<float>& P, bool collide, cudaStream_t st) {
+  return step_t(P, collide, st);
 }
 
-cudaError_t launch_thermal_init(const ThermalPoint& P, int grid, cudaStream_t st) {
-  void* args[] = {const_cast<ThermalPoint*>(&P)};
-  return cudaLaunchKernel((const void*)k_thermal_init, dim3(grid), dim3(256), args, 0, st);
+template <class Real>
+static cudaError_t collide_t(const ThermalPointT<Real>& P, int grid, cudaStream_t st) {
+  void* args[] = {const_cast<ThermalPointT<Real>*>(&P)};
+  return cudaLaunchKernel((const void*)k_thermal_collide<Real>, dim3(grid), dim3(256), args, 0, st);
+}
+
+cudaError_t launch_thermal_collide(const ThermalPointT<double>& P, int grid, cudaStream_t st) {
+  return collide_t(P, grid, st);
+}
+cudaError_t launch_thermal_collide(const ThermalPointT<float>& P, int grid, cudaStream_t st) {
+  return collide_t(P, grid, st);
+}
+
+cudaError_t launch_thermal_init(const ThermalPointT<double>& P, void* f, void* g, bool fp32, int grid,
+                                cudaStream_t st) {
+  if (fp32) {
+    k_thermal_init<float><<<grid, 256, 0, st>>>(P, static_cast<float*>(f), static_cast<float*>(g));
+  } else {
+    k_thermal_init<double><<<grid, 256, 0, st>>>(P, static_cast<double*>(f), static_cast<double*>(g));
+  }
+  return cudaGetLastError();
 }
 
 }  // namespace natgpu

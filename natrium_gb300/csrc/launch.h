@@ -63,9 +63,13 @@ void row_kernels_d3q19(std::vector<RowLaunch>& v);
 void row_kernels_d3q27(std::vector<RowLaunch>& v);
 
 // Compressible two-population model on D2Q25H (k_thermal.cu): fused
-// stream(f, g) (+ relaxWithG), collision only, equilibrium initialisation.
-cudaError_t launch_thermal_step(const ThermalStep& P, bool collide, cudaStream_t st);
-cudaError_t launch_thermal_collide(const ThermalPoint& P, int grid, cudaStream_t st);
-cudaError_t launch_thermal_init(const ThermalPoint& P, int grid, cudaStream_t st);
+// stream(f, g) (+ relaxWithG), collision only, equilibrium initialisation;
+// FP64 and FP32-deviation forms.
+cudaError_t launch_thermal_step(const ThermalStepT<double>& P, bool collide, cudaStream_t st);
+cudaError_t launch_thermal_step(const ThermalStepT<float>& P, bool collide, cudaStream_t st);
+cudaError_t launch_thermal_collide(const ThermalPointT<double>& P, int grid, cudaStream_t st);
+cudaError_t launch_thermal_collide(const ThermalPointT<float>& P, int grid, cudaStream_t st);
+cudaError_t launch_thermal_init(const ThermalPointT<double>& P, void* f, void* g, bool fp32, int grid,
+                                cudaStream_t st);
 
 }  // namespace natgpu

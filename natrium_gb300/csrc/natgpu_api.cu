@@ -65,11 +65,14 @@ struct nat_solver {
   // compressible two-population model (D2Q25H)
   bool thermal = false;
   nat_thermal th;
-  double* g[2] = {nullptr, nullptr};  // second population, same layout as f
-  double* T = nullptr;                // temperature
-  double* mask = nullptr;             // shock sensor (Knudsen estimate)
-  ThermalModel tm;
-  ThermalTables tt;
+  void* g[2] = {nullptr, nullptr};  // second population, same layout and type as f
+  double* T = nullptr;              // temperature
+  double* mask = nullptr;           // shock sensor (Knudsen estimate)
+  double gref = 3.0;                // FP32 deviation storage of g: g - w_i gref
+  ThermalModelT<double> tm;
+  ThermalModelT<float> tmf;
+  ThermalTablesT<double> tt;
+  ThermalTablesT<float> ttf;
 };
 
 namespace {
@@ -707,7 +710,7 @@ int launch_v2(nat_solver* s, int write_macro) {
 // ---- compressible two-population model ------------------------------------
 // Per-solve constants of the collision, from the reference's stencil formulas.
 void fill_thermal_model(nat_solver* s) {
-  ThermalModel& m = s->tm;
+  ThermalModelT<double>& m = s->tm;
   memset(&m, 0, sizeof(m));
   const double sc = s->spec.scaling;
   double cm_s, cn_s, w0, wm, wn;
@@ -744,11 +747,33 @@ void fill_thermal_model(nat_solver* s) {
   m.prandtl_set = s->th.prandtl_set ? 1 : 0;
   m.sutherland_set = s->th.sutherland_set ? 1 : 0;
   m.quartic = s->th.equilibrium == NAT_EQ_QUARTIC ? 1 : 0;
+  m.gref = s->gref;
+  // float copy for the FP32 deviation form
+  ThermalModelT<float>& mf = s->tmf;
+  for (int g = 0; g < TH_NG; ++g) {
+    mf.X[g] = (float)m.X[g];
+    mf.Y[g] = (float)m.Y[g];
+    mf.e2[g] = (float)m.e2[g];
+    mf.w[g] = (float)m.w[g];
+    mf.winv[g] = (float)m.winv[g];
+    for (int k = 0; k < 4; ++k) mf.h3[g][k] = (float)m.h3[g][k];
+    for (int k = 0; k < 5; ++k) mf.h4[g][k] = (float)m.h4[g][k];
+  }
+  mf.cs2 = (float)m.cs2;
+  mf.tau = (float)m.tau;
+  mf.C_v = (float)m.C_v;
+  mf.gfac = (float)m.gfac;
+  mf.gref = (float)m.gref;
+  mf.prandtl = (float)m.prandtl;
+  mf.scaling = m.scaling;
+  mf.prandtl_set = m.prandtl_set;
+  mf.sutherland_set = m.sutherland_set;
+  mf.quartic = m.quartic;
 }
 
 // Window tables of the two-population row kernel from the operator tables.
 int setup_thermal_tables(nat_solver* s) {
-  ThermalTables& t = s->tt;
+  ThermalTablesT<double>& t = s->tt;
   memset(&t, 0, sizeof(t));
   const SLTables& T = s->h_tab;
   t.p = T.p;
@@ -758,6 +783,7 @@ int setup_thermal_tables(nat_solver* s) {
     for (int d = 0; d < T.ax[a].nd; ++d)
       for (int c = 0; c < s->period; ++c) {
         t.off[a][d][c] = T.off[a][d][c];
+        t.j0[a][d][c] = T.j0[a][d][c];
         for (int j = 0; j <= T.p; ++j) t.w[a][d][c][j] = T.w[a][d][c][j];
         if (a == 0) {
           lo = std::min(lo, T.off[0][d][c]);
@@ -768,16 +794,31 @@ int setup_thermal_tables(nat_solver* s) {
   t.bw = 32 + hi - lo;
   if (t.bw > TH_BWMAX)
     return fail(s, NAT_ERR_UNSUPPORTED, "time step too large for the x window of the two-population kernel");
+  ThermalTablesT<float>& tf = s->ttf;
+  memset(&tf, 0, sizeof(tf));
+  for (int a = 0; a < 2; ++a)
+    for (int d = 0; d < ND_MAX; ++d)
+      for (int c = 0; c < PER_MAX; ++c) {
+        tf.off[a][d][c] = t.off[a][d][c];
+        tf.j0[a][d][c] = t.j0[a][d][c];
+        for (int j = 0; j < PMAX1; ++j) tf.w[a][d][c][j] = (float)t.w[a][d][c][j];
+      }
+  tf.p = t.p;
+  tf.per = t.per;
+  tf.xl = t.xl;
+  tf.bw = t.bw;
   fill_thermal_model(s);
   return NAT_OK;
 }
 
-ThermalStep thermal_step_params(nat_solver* s, int write_macro) {
-  ThermalStep P;
-  P.f_in = static_cast<const double*>(s->f[s->cur]);
-  P.g_in = s->g[s->cur];
-  P.f_out = static_cast<double*>(s->f[1 - s->cur]);
-  P.g_out = s->g[1 - s->cur];
+template <class Real>
+ThermalStepT<Real> thermal_step_params(nat_solver* s, int write_macro, const ThermalTablesT<Real>& tb,
+                                       const ThermalModelT<Real>& M) {
+  ThermalStepT<Real> P;
+  P.f_in = static_cast<const Real*>(s->f[s->cur]);
+  P.g_in = static_cast<const Real*>(s->g[s->cur]);
+  P.f_out = static_cast<Real*>(s->f[1 - s->cur]);
+  P.g_out = static_cast<Real*>(s->g[1 - s->cur]);
   P.rho = s->rho;
   P.u = s->u;
   P.T = s->T;
@@ -788,16 +829,16 @@ ThermalStep thermal_step_params(nat_solver* s, int write_macro) {
   P.ny = s->n_ax[1];
   P.nseg = (s->n_ax[0] + 31) / 32;
   P.write_macro = write_macro;
-  P.tb = s->tt;
-  P.M = s->tm;
+  P.tb = tb;
+  P.M = M;
   return P;
 }
 
-ThermalPoint thermal_point_params(nat_solver* s, int in_init) {
-  ThermalPoint P;
-  P.f_in = nullptr;
-  P.f = static_cast<double*>(s->f[s->cur]);
-  P.g = s->g[s->cur];
+template <class Real>
+ThermalPointT<Real> thermal_point_params(nat_solver* s, int in_init, const ThermalModelT<Real>& M) {
+  ThermalPointT<Real> P;
+  P.f = static_cast<Real*>(s->f[s->cur]);
+  P.g = static_cast<Real*>(s->g[s->cur]);
   P.rho = s->rho;
   P.u = s->u;
   P.T = s->T;
@@ -805,13 +846,16 @@ ThermalPoint thermal_point_params(nat_solver* s, int in_init) {
   P.status = s->status;
   P.n = s->n_dev;
   P.in_init = in_init;
-  P.M = s->tm;
+  P.M = M;
   return P;
 }
 
 int launch_thermal(nat_solver* s, bool collide, int write_macro) {
-  ThermalStep P = thermal_step_params(s, write_macro);
-  cudaError_t e = launch_thermal_step(P, collide, s->stream);
+  cudaError_t e;
+  if (s->spec.precision == NAT_FP64)
+    e = launch_thermal_step(thermal_step_params<double>(s, write_macro, s->tt, s->tm), collide, s->stream);
+  else
+    e = launch_thermal_step(thermal_step_params<float>(s, write_macro, s->ttf, s->tmf), collide, s->stream);
   if (e != cudaSuccess) return cuda_fail(s, e, "two-population stream-collide launch");
   s->launches++;
   s->cur = 1 - s->cur;
@@ -925,7 +969,8 @@ static int setup_dt(nat_solver* s, double dt) {
 static int create_thermal(nat_solver* s, double hmin) {
   const int p = s->spec.order;
   for (int a = 0; a < 3; ++a) s->B[a] = a < s->D ? s->period : 1;
-  const size_t fbytes = sizeof(double) * (size_t)s->Q * s->n_dev;
+  const size_t es = s->spec.precision == NAT_FP64 ? sizeof(double) : sizeof(float);
+  const size_t fbytes = es * (size_t)s->Q * s->n_dev;
 #define ALLOC(ptr, bytes)                                             \
   do {                                                                \
     cudaError_t e_ = cudaMalloc((void**)&(ptr), (bytes));             \
@@ -943,7 +988,7 @@ static int create_thermal(nat_solver* s, double hmin) {
   ALLOC(s->T, sizeof(double) * s->n_dev);
   ALLOC(s->mask, sizeof(double) * s->n_dev);
   ALLOC(s->staging, sizeof(double) * (size_t)s->Q * s->n_ref);
-  ALLOC(s->red, sizeof(double) * (2 + 32));
+  ALLOC(s->red, sizeof(double) * (2 + 32 + 32));
   ALLOC(s->status, sizeof(int));
   ALLOC(s->d_tab, sizeof(SLTables));
 #undef ALLOC
@@ -951,6 +996,16 @@ static int create_thermal(nat_solver* s, double hmin) {
   CK(cudaMemsetAsync(s->rho, 0, sizeof(double) * s->n_dev, s->stream), "memset");
   CK(cudaMemsetAsync(s->u, 0, sizeof(double) * s->D * s->n_dev, s->stream), "memset");
   CK(cudaMemsetAsync(s->T, 0, sizeof(double) * s->n_dev, s->stream), "memset");
+  // deviation reference states of the FP32 form: f - w_i, g - w_i gref
+  // (gref: g^eq / f^eq at T = 1 for the default gamma 1.4; fixed per solve)
+  s->gref = 2.0 / (1.4 - 1.0) - s->D;
+  double grest[32];
+  for (int q = 0; q < s->Q; ++q) grest[q] = s->rest[q] * s->gref;
+  int rc0 = upload_rest(s);
+  if (rc0) return rc0;
+  CK(cudaMemcpyAsync(s->red + 2 + 32, grest, sizeof(double) * s->Q, cudaMemcpyHostToDevice, s->stream),
+     "g rest upload");
+  CK(cudaStreamSynchronize(s->stream), "rest upload sync");
   CK(cudaMemsetAsync(s->mask, 0, sizeof(double) * s->n_dev, s->stream), "memset");
   // SolverConfiguration defaults (solver/SolverConfiguration.cpp:21-31)
   s->th.gamma = 1.4;
@@ -1005,9 +1060,9 @@ int nat_create(const nat_spec* spec, nat_solver** out) {
     default: return bad("bad collision model");
   }
   s->thermal = spec->collision == NAT_BGK_COMPRESSIBLE;
-  if (s->thermal != (spec->stencil == NAT_D2Q25H) || (s->thermal && spec->precision != NAT_FP64)) {
+  if (s->thermal != (spec->stencil == NAT_D2Q25H)) {
     fail(s, NAT_ERR_UNSUPPORTED,
-         "the compressible two-population model runs on D2Q25H in FP64, and D2Q25H runs only that model");
+         "the compressible two-population model runs on D2Q25H, and D2Q25H runs only that model");
     *out = s;
     return NAT_ERR_UNSUPPORTED;
   }
@@ -1191,8 +1246,12 @@ int nat_stream(nat_solver* s, double t, double* dt_out) {
 int nat_collide(nat_solver* s, int in_init) {
   if (!s) return NAT_ERR_INVALID_ARG;
   if (s->thermal) {
-    ThermalPoint TP = thermal_point_params(s, in_init);
-    CK(launch_thermal_collide(TP, grid_for(s->n_dev), s->stream), "two-population collide launch");
+    if (s->spec.precision == NAT_FP64)
+      CK(launch_thermal_collide(thermal_point_params<double>(s, in_init, s->tm), grid_for(s->n_dev), s->stream),
+         "two-population collide launch");
+    else
+      CK(launch_thermal_collide(thermal_point_params<float>(s, in_init, s->tmf), grid_for(s->n_dev), s->stream),
+         "two-population collide launch");
     s->launches++;
     return nat_status(s);
   }
@@ -1410,8 +1469,11 @@ int nat_upload_g(nat_solver* s, const double* g_host) {
   if (!s->thermal) return fail(s, NAT_ERR_UNSUPPORTED, "not a NAT_BGK_COMPRESSIBLE handle");
   CK(cudaMemcpyAsync(s->staging, g_host, sizeof(double) * s->Q * s->n_ref, cudaMemcpyHostToDevice, s->stream),
      "upload g");
-  k_upload<double><<<grid_for(s->n_dev * s->Q), 256, 0, s->stream>>>(s->staging, s->g[s->cur], dims_of(s), s->Q,
-                                                                      s->red + 2);
+  const int gr = grid_for(s->n_dev * s->Q);
+  if (s->spec.precision == NAT_FP64)
+    k_upload<double><<<gr, 256, 0, s->stream>>>(s->staging, (double*)s->g[s->cur], dims_of(s), s->Q, s->red + 2 + 32);
+  else
+    k_upload<float><<<gr, 256, 0, s->stream>>>(s->staging, (float*)s->g[s->cur], dims_of(s), s->Q, s->red + 2 + 32);
   CK(cudaGetLastError(), "upload kernel");
   s->launches++;
   return NAT_OK;
@@ -1420,8 +1482,13 @@ int nat_upload_g(nat_solver* s, const double* g_host) {
 int nat_download_g(nat_solver* s, double* g_host) {
   if (!s || !g_host) return NAT_ERR_INVALID_ARG;
   if (!s->thermal) return fail(s, NAT_ERR_UNSUPPORTED, "not a NAT_BGK_COMPRESSIBLE handle");
-  k_download<double><<<grid_for(s->n_ref * s->Q), 256, 0, s->stream>>>(s->g[s->cur], s->staging, dims_of(s), s->Q,
-                                                                        s->red + 2);
+  const int gr = grid_for(s->n_ref * s->Q);
+  if (s->spec.precision == NAT_FP64)
+    k_download<double><<<gr, 256, 0, s->stream>>>((const double*)s->g[s->cur], s->staging, dims_of(s), s->Q,
+                                                  s->red + 2 + 32);
+  else
+    k_download<float><<<gr, 256, 0, s->stream>>>((const float*)s->g[s->cur], s->staging, dims_of(s), s->Q,
+                                                 s->red + 2 + 32);
   CK(cudaGetLastError(), "download kernel");
   s->launches++;
   CK(cudaMemcpyAsync(g_host, s->staging, sizeof(double) * s->Q * s->n_ref, cudaMemcpyDeviceToHost, s->stream),
@@ -1458,8 +1525,9 @@ int nat_init_thermal(nat_solver* s, const double* rho_host, const double* u_host
                                                                dims_of(s), 1);
   CK(cudaGetLastError(), "T upload kernel");
   s->launches++;
-  ThermalPoint P = thermal_point_params(s, 0);
-  CK(launch_thermal_init(P, grid_for(s->n_dev), s->stream), "two-population init launch");
+  CK(launch_thermal_init(thermal_point_params<double>(s, 0, s->tm), s->f[s->cur], s->g[s->cur],
+                         s->spec.precision != NAT_FP64, grid_for(s->n_dev), s->stream),
+     "two-population init launch");
   s->launches++;
   CK(cudaStreamSynchronize(s->stream), "init sync");
   return NAT_OK;

@@ -90,40 +90,47 @@ constexpr int TH_NG = 9;
 
 // Compressible two-population model (D2Q25H, sl_thermal.cuh).
 // Per-solve constants of the collision (built on the host from the
-// reference's stencil formulas).  Group values are for the member with
-// e_x >= 0, e_y >= 0.
-struct ThermalModel {
-  double X[TH_NG], Y[TH_NG];  // |e_x|, |e_y| (unscaled)
-  double e2[TH_NG];           // |e|^2
-  double w[TH_NG];            // weight of every member
-  double winv[TH_NG];         // 1 / weight (Knudsen estimate)
-  double h3[TH_NG][4];        // H_xxx, H_xxy, H_xyy, H_yyy
-  double h4[TH_NG][5];        // H_xxxx, H_xxxy, H_xxyy, H_xyyy, H_yyyy
-  double cs2;                 // unscaled c_s^2 (scaled c_s^2 / scaling^2)
-  double tau;                 // nu / (dt c_s^2 scaled) + 1/2
+// reference's stencil formulas) in the arithmetic type Real.  Group values
+// are for the member with e_x >= 0, e_y >= 0.
+template <class Real>
+struct ThermalModelT {
+  Real X[TH_NG], Y[TH_NG];  // |e_x|, |e_y| (unscaled)
+  Real e2[TH_NG];           // |e|^2
+  Real w[TH_NG];            // weight of every member
+  Real winv[TH_NG];         // 1 / weight (Knudsen estimate)
+  Real h3[TH_NG][4];        // H_xxx, H_xxy, H_xyy, H_yyy
+  Real h4[TH_NG][5];        // H_xxxx, H_xxxy, H_xxyy, H_xyyy, H_yyyy
+  Real cs2;                 // unscaled c_s^2 (scaled c_s^2 / scaling^2)
+  Real tau;                 // nu / (dt c_s^2 scaled) + 1/2
+  Real C_v;                 // 1 / (gamma - 1)
+  Real gfac;                // 2 C_v - D
+  Real gref;                // deviation storage of g: g - w_i gref (fixed per solve)
+  Real prandtl;
   double scaling;
-  double C_v;                 // 1 / (gamma - 1)
-  double gfac;                // 2 C_v - D
-  double prandtl;
   int prandtl_set;
   int sutherland_set;
-  int quartic;                // 1: quartic equilibrium, 0: second-order BGK equilibrium
+  int quartic;              // 1: quartic equilibrium, 0: second-order BGK equilibrium
 };
 
 // Streaming tables of the two axes: [axis][displacement class][node class].
-struct ThermalTables {
-  double w[2][ND_MAX][PER_MAX][PMAX1];
+template <class Real>
+struct ThermalTablesT {
+  Real w[2][ND_MAX][PER_MAX][PMAX1];
   int off[2][ND_MAX][PER_MAX];
+  int j0[2][ND_MAX][PER_MAX];  // window index of the dominant weight
   int p, per;
   int xl;  // first buffer position relative to the segment start
   int bw;  // buffer width (<= TH_BWMAX)
 };
 
-struct ThermalStep {
-  const double* f_in;
-  const double* g_in;
-  double* f_out;
-  double* g_out;
+// Real = double: plain FP64 state.  Real = float: deviations f - w_i and
+// g - w_i gref stored and computed in float.
+template <class Real>
+struct ThermalStepT {
+  const Real* f_in;
+  const Real* g_in;
+  Real* f_out;
+  Real* g_out;
   double* rho;
   double* u;
   double* T;
@@ -131,14 +138,14 @@ struct ThermalStep {
   int* status;
   int n, nx, ny, nseg;
   int write_macro;
-  ThermalTables tb;
-  ThermalModel M;
+  ThermalTablesT<Real> tb;
+  ThermalModelT<Real> M;
 };
 
-struct ThermalPoint {
-  const double* f_in;  // collide / init: in place on f_out, g_out
-  double* f;
-  double* g;
+template <class Real>
+struct ThermalPointT {
+  Real* f;  // collide / init: in place
+  Real* g;
   double* rho;
   double* u;
   double* T;
@@ -146,7 +153,7 @@ struct ThermalPoint {
   int* status;
   long long n;
   int in_init;
-  ThermalModel M;
+  ThermalModelT<Real> M;
 };
 
 }  // namespace natgpu

@@ -53,10 +53,10 @@ def test_unsupported_combination_is_reported():
 
 
 def test_compressible_model_combinations_are_checked():
-    # the compressible two-population model runs on D2Q25H in FP64 only, and
-    # D2Q25H only runs that model
+    # the compressible two-population model runs on D2Q25H only, and D2Q25H
+    # only runs that model
     for st, coll, prec in (("D2Q9", "BGK_COMPRESSIBLE", "fp64"), ("D2Q25H", "BGK_STANDARD", "fp64"),
-                           ("D2Q25H", "BGK_COMPRESSIBLE", "fp32dev")):
+                           ("D2Q25H", "KBC_STANDARD", "fp32dev")):
         spec = N.SolverSpec(stencil=st, order=2, cells=(2, 2), length=(1, 1), scaling=1.0,
                             viscosity=0.1, collision=coll, precision=prec)
         with pytest.raises(N.NatError) as ei:

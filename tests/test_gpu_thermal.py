@@ -170,3 +170,63 @@ def test_density_underflow_is_reported(gpu_lib):
         sol.upload_g(np.zeros((25, n)))
         with pytest.raises(N.CollisionException):
             sol.collide()
+
+
+# ---------------------------------------------------------------------------
+# FP32 deviation storage (f - w_i, g - w_i g_ref in float) against the FP64
+# oracle.  Tolerances: one step, relative L2 <= 2e-7 for f, g, rho and T and
+# <= 2e-6 for u; 200 steps of the smooth state, <= 1e-5 for rho and T and
+# <= 1e-4 for u (float rounding accumulates over the steps).
+# ---------------------------------------------------------------------------
+
+def _spec32(spec):
+    spec.precision = "fp32dev"
+    return spec
+
+
+@pytest.mark.parametrize("dg", [False, True])
+def test_fp32_step_close_to_oracle(gpu_lib, dg):
+    st, mesh, dt, tau, spec = thermal_case((6, 6), 3, dg, scaling=1.2)
+    rho0, u0, T0, f0, g0 = thermal_state(mesh, st, seed=9)
+    S = O.SLOperator(mesh, st, dt)
+    f1, g1 = f0.copy(), g0.copy()
+    r1, u1, T1, m1 = S.step_compressible(f1, g1, tau)
+    f, g, rho, u, T, m = _run(_spec32(spec), f0, g0)
+    assert rel_l2(f, f1) <= 2e-7
+    assert rel_l2(g, g1) <= 2e-7
+    assert rel_l2(rho, r1) <= 2e-7
+    assert rel_l2(T, T1) <= 2e-7
+    assert rel_l2(u, u1) <= 2e-6
+
+
+@pytest.mark.parametrize("settings", [N.ThermalSettings(), N.ThermalSettings(prandtl=0.71, prandtl_set=True,
+                                                                             sutherland=True, gamma=1.67)],
+                         ids=["default", "prandtl-sutherland-gamma"])
+def test_fp32_200_steps_close_to_oracle(gpu_lib, settings):
+    st, mesh, dt, tau, spec = thermal_case((8, 8), 2, True)
+    rho0, u0, T0, f0, g0 = thermal_state(mesh, st, seed=12, gamma=settings.gamma, amp=0.0)
+    S = O.SLOperator(mesh, st, dt)
+    f1, g1 = f0.copy(), g0.copy()
+    r1, u1, T1, m1 = S.step_compressible(f1, g1, tau, _th(settings), nsteps=200, nthreads=O.max_threads())
+    f, g, rho, u, T, m = _run(_spec32(spec), f0, g0, settings, nsteps=200)
+    assert rel_l2(rho, r1) <= 1e-5
+    assert rel_l2(T, T1) <= 1e-5
+    assert rel_l2(u, u1) <= 1e-4
+
+
+def test_fp32_initialisation_and_uniform_state(gpu_lib):
+    st, mesh, dt, tau, spec = thermal_case((4, 4), 2, False, scaling=1.1)
+    n = mesh.n_nodes
+    rho = np.full(n, 1.2)
+    u = np.stack([np.full(n, 0.05), np.full(n, 0.02)]) * st.scaling
+    T = np.full(n, 0.9)
+    fo, go = O.thermal_init(st, rho, u, T)
+    with N.Solver(_spec32(spec)) as sol:
+        sol.init_thermal(rho, u, T)
+        f, g = sol.download_f(), sol.download_g()
+        sol.step(10)
+        f10 = sol.download_f()
+        T10, _ = sol.download_thermal()
+    assert rel_l2(f, fo) <= 1e-7 and rel_l2(g, go) <= 1e-7
+    assert rel_l2(f10, fo) <= 1e-6
+    assert np.allclose(T10, 0.9, rtol=1e-6)
