@@ -448,7 +448,8 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": alg_bytes,
-                     "kernel": {1: "k_sl_step", 2: "k_sl_step_v2", 3: "k_sl_row"}[kinfo["variant"]] + "<D3Q19,float,BGK>",
+                     "kernel": {1: "k_sl_step", 2: "k_sl_step_v2", 3: "k_sl_row", 6: "k_sl_rowt"}[kinfo["variant"]]
+                               + "<D3Q19,float,BGK>",
                      "tile_nodes": kinfo["tile_nodes"], "threads": kinfo["threads"],
                      "autotune": {"candidates": ncand, "chosen": chosen}},
         "cpu_baseline": cpu,
@@ -476,7 +477,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--variant", type=int, default=0,
-                    help="fused kernel: 0 autotuned, 1 generic, 3 tile, 4 row-segment")
+                    help="fused kernel: 0 autotuned, 1 generic, 3 tile, 4 row-segment, 6 bulk-copy row-segment")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--profile", action="store_true",
                     help="lean run for ncu: FP32 device timing only (no e2e, FP64 leg, CPU baseline or clocks)")

@@ -1,0 +1,38 @@
+// Row-segment kernel (sl_row.cuh) with the streamed values in shared memory
+// and 64 registers per thread (more resident warps): D3Q27, FP32 deviation.
+#include "launch.h"
+#include "sl_row.cuh"
+
+namespace natgpu {
+
+namespace {
+
+template <class S, int COLL, int P, bool DG, int WY, int MINB>
+RowLaunch sentry(int coll) {
+  RowLaunch e;
+  e.stencil = S::ID;
+  e.coll = coll;
+  e.prec = 1;
+  e.P = P;
+  e.dg = DG;
+  e.wy = WY;
+  e.wz = 1;
+  e.fn = (const void*)&k_sl_row<S, float, COLL, P, DG, WY, 1, true, MINB>;
+  return e;
+}
+
+template <class S, int COLL, int P>
+void add_orders(std::vector<RowLaunch>& t, int coll) {
+  t.push_back(sentry<S, COLL, P, true, 4, 8>(coll));
+  t.push_back(sentry<S, COLL, P, false, 4, 8>(coll));
+  if constexpr (P < PMAX) add_orders<S, COLL, P + 1>(t, coll);
+}
+
+}  // namespace
+
+void row_ss_kernels_d3q27(std::vector<RowLaunch>& v) {
+  add_orders<SD3Q27, COLL_BGK, 1>(v, L_COLL_BGK);
+  add_orders<SD3Q27, COLL_KBC, 1>(v, L_COLL_KBC);
+}
+
+}  // namespace natgpu

@@ -57,10 +57,19 @@ struct RowLaunch {
   bool dg;
   int wy, wz;
   const void* fn;
+  int kind = 3;      // 3: row kernel (sl_row.cuh), 6: bulk-copy row kernel (sl_rowt.cuh)
+  size_t smem = 0;   // dynamic shared memory (kind 6)
+  int align = 1;     // nx must be a multiple of this (kind 6: aligned row copies)
+  int min_nx = 0;    // and at least this (kind 6: at most two pieces per row)
 };
 void row_kernels_d2q9(std::vector<RowLaunch>& v);
 void row_kernels_d3q19(std::vector<RowLaunch>& v);
 void row_kernels_d3q27(std::vector<RowLaunch>& v);
+void row_ss_kernels_d3q19(std::vector<RowLaunch>& v);
+void row_ss_kernels_d3q27(std::vector<RowLaunch>& v);
+void rowt_kernels_d3q19(std::vector<RowLaunch>& v);
+void rowt_kernels_d3q27_bgk(std::vector<RowLaunch>& v);
+void rowt_kernels_d3q27_kbc(std::vector<RowLaunch>& v);
 
 // Compressible two-population model on D2Q25H (k_thermal.cu): fused
 // stream(f, g) (+ relaxWithG), collision only, equilibrium initialisation;

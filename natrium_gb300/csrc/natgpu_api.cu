@@ -24,6 +24,7 @@
 #include "sl_step.cuh"
 #include "sl_step_v2.cuh"
 #include "sl_row.cuh"
+#include "sl_rowt.cuh"
 
 using namespace natgpu;
 
@@ -579,8 +580,14 @@ const std::vector<RowLaunch>& row_table() {
   static const std::vector<RowLaunch> t = [] {
     std::vector<RowLaunch> v;
     row_kernels_d2q9(v);
+    // the shared-state float variants first: preferred when they apply
+    row_ss_kernels_d3q19(v);
+    row_ss_kernels_d3q27(v);
     row_kernels_d3q19(v);
     row_kernels_d3q27(v);
+    rowt_kernels_d3q19(v);
+    rowt_kernels_d3q27_bgk(v);
+    rowt_kernels_d3q27_kbc(v);
     return v;
   }();
   return t;
@@ -597,8 +604,10 @@ std::vector<Cand> v2_candidates(nat_solver* s, int coll_sel, int smem_optin) {
         e.P != s->spec.order || e.dg != dg)
       continue;
     if (s->n_ax[1] % e.wy != 0 || s->n_ax[2] % e.wz != 0) continue;
+    if (e.kind == 6 && (s->n_ax[0] % e.align != 0 || s->n_ax[0] < e.min_nx || (long long)e.smem > smem_optin))
+      continue;
     Cand c;
-    c.kind = 3;
+    c.kind = e.kind;
     c.row = e;
     out.push_back(c);
   }
@@ -619,6 +628,11 @@ int use_candidate(nat_solver* s, const Cand& c) {
     if (ce != cudaSuccess) return cuda_fail(s, ce, "v2 smem attribute");
     s->v2 = c.v2;
   } else {
+    if (c.row.smem > 0) {
+      cudaError_t ce =
+          cudaFuncSetAttribute(c.row.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.row.smem);
+      if (ce != cudaSuccess) return cuda_fail(s, ce, "row smem attribute");
+    }
     s->row = c.row;
   }
   set_v2_weights(s);
@@ -627,13 +641,16 @@ int use_candidate(nat_solver* s, const Cand& c) {
   return NAT_OK;
 }
 
+// kernel kind required by a nat_set_kernel_variant value >= 3
+int variant_kind(int variant) { return variant == 3 ? 2 : (variant == 4 ? 3 : variant); }
+
 int select_v2(nat_solver* s, int coll_sel, int smem_optin) {
   s->use_v2 = false;
   s->kind = 1;
   if (s->variant == 1) return NAT_OK;
   std::vector<Cand> all = v2_candidates(s, coll_sel, smem_optin), c;
   for (const Cand& k : all)
-    if (s->variant <= 2 || (s->variant == 3 && k.kind == 2) || (s->variant == 4 && k.kind == 3)) c.push_back(k);
+    if (s->variant <= 2 || variant_kind(s->variant) == k.kind) c.push_back(k);
   if (c.empty()) {
     if (s->variant >= 2) return fail(s, NAT_ERR_UNSUPPORTED, "no specialised kernel of the requested kind");
     return NAT_OK;
@@ -692,7 +709,8 @@ int launch_row_t(nat_solver* s, const SpecWeights<Real>& W, int write_macro) {
   P.W = W;
   const int grid = P.nseg * (P.ny / s->row.wy) * (P.nz / s->row.wz);
   void* args[] = {&P};
-  cudaError_t e = cudaLaunchKernel(s->row.fn, dim3(grid), dim3(32 * s->row.wy * s->row.wz), args, 0, s->stream);
+  cudaError_t e =
+      cudaLaunchKernel(s->row.fn, dim3(grid), dim3(32 * s->row.wy * s->row.wz), args, s->row.smem, s->stream);
   if (e != cudaSuccess) return cuda_fail(s, e, "row stream-collide launch");
   s->launches++;
   s->cur = 1 - s->cur;
@@ -700,7 +718,7 @@ int launch_row_t(nat_solver* s, const SpecWeights<Real>& W, int write_macro) {
 }
 
 int launch_v2(nat_solver* s, int write_macro) {
-  if (s->kind == 3)
+  if (s->kind == 3 || s->kind == 6)
     return s->spec.precision == NAT_FP64 ? launch_row_t<double>(s, s->w64, write_macro)
                                          : launch_row_t<float>(s, s->w32, write_macro);
   return s->spec.precision == NAT_FP64 ? launch_v2_t<double>(s, s->w64, write_macro)
@@ -792,6 +810,9 @@ int setup_thermal_tables(nat_solver* s) {
       }
   t.xl = lo;
   t.bw = 32 + hi - lo;
+  const int ny = s->n_ax[1];
+  for (int d = 0; d < ND_MAX; ++d)
+    for (int c = 0; c < PER_MAX; ++c) t.offy[d][c] = ((t.off[1][d][c] % ny) + ny) % ny;
   if (t.bw > TH_BWMAX)
     return fail(s, NAT_ERR_UNSUPPORTED, "time step too large for the x window of the two-population kernel");
   ThermalTablesT<float>& tf = s->ttf;
@@ -801,6 +822,7 @@ int setup_thermal_tables(nat_solver* s) {
       for (int c = 0; c < PER_MAX; ++c) {
         tf.off[a][d][c] = t.off[a][d][c];
         tf.j0[a][d][c] = t.j0[a][d][c];
+        if (a == 0) tf.offy[d][c] = t.offy[d][c];
         for (int j = 0; j < PMAX1; ++j) tf.w[a][d][c][j] = (float)t.w[a][d][c][j];
       }
   tf.p = t.p;
@@ -1337,7 +1359,7 @@ int nat_device_f(nat_solver* s, void** f_dev) {
 int64_t nat_launch_count(const nat_solver* s) { return s ? s->launches : -1; }
 
 int nat_set_kernel_variant(nat_solver* s, int variant) {
-  if (!s || variant < 0 || variant > 4) return NAT_ERR_INVALID_ARG;
+  if (!s || variant < 0 || variant > 6 || variant == 5) return NAT_ERR_INVALID_ARG;
   if (s->thermal) {
     // one kernel serves the two-population model
     if (variant == 0) return NAT_OK;
@@ -1367,7 +1389,7 @@ int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
   if (s->variant >= 3) {
     std::vector<Cand> keep;
     for (const Cand& k : cand)
-      if ((s->variant == 3 && k.kind == 2) || (s->variant == 4 && k.kind == 3)) keep.push_back(k);
+      if (variant_kind(s->variant) == k.kind) keep.push_back(k);
     cand.swap(keep);
   }
   const int ncand = (int)cand.size() + (s->variant >= 2 ? 0 : 1);  // + the generic kernel
@@ -1438,11 +1460,12 @@ int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* t
   if (variant) *variant = k;
   for (int a = 0; a < 3; ++a) {
     int t = k == 2 ? s->v2.B[a] : s->B[a];
-    if (k == 3) t = a == 0 ? 32 : (a == 1 ? s->row.wy : s->row.wz);
+    if (k == 3 || k == 6) t = a == 0 ? 32 : (a == 1 ? s->row.wy : s->row.wz);
     if (tile_nodes) tile_nodes[a] = t;
   }
-  if (threads) *threads = k == 2 ? s->v2.nth : (k == 3 ? 32 * s->row.wy * s->row.wz : STEP_THREADS);
-  if (smem_bytes) *smem_bytes = (int64_t)(k == 2 ? s->v2.smem : (k == 3 ? 0 : s->smem_step));
+  const bool row = k == 3 || k == 6;
+  if (threads) *threads = k == 2 ? s->v2.nth : (row ? 32 * s->row.wy * s->row.wz : STEP_THREADS);
+  if (smem_bytes) *smem_bytes = (int64_t)(k == 2 ? s->v2.smem : (row ? s->row.smem : s->smem_step));
   return NAT_OK;
 }
 

@@ -118,6 +118,7 @@ struct ThermalTablesT {
   Real w[2][ND_MAX][PER_MAX][PMAX1];
   int off[2][ND_MAX][PER_MAX];
   int j0[2][ND_MAX][PER_MAX];  // window index of the dominant weight
+  int offy[ND_MAX][PER_MAX];   // y window offset reduced to [0, ny): rows wrap by subtraction only
   int p, per;
   int xl;  // first buffer position relative to the segment start
   int bw;  // buffer width (<= TH_BWMAX)

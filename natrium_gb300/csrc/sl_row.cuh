@@ -159,12 +159,55 @@ __device__ __forceinline__ void fill_row_table(Real* sw, const Real (&W)[3][2][P
   }
 }
 
+// Collision of one node whose streamed values are in fs_s[q * 32 + lane]
+// (shared memory written by the same lane), and the single write of f.
+template <class S, class Real, int COLL>
+__device__ __forceinline__ void row_collide(const RowArgs<Real>& prm, const Real* fs_s, int node, int lane) {
+  constexpr bool DEV = sizeof(Real) == 4;
+  constexpr int Q = S::Q;
+  Real fs[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) fs[q] = fs_s[q * 32 + lane];
+  Real u[3] = {0, 0, 0};
+  Real rho = Real(1);
+  if constexpr (COLL == COLL_BGK) {
+    rho = collide_bgk<S, DEV, false>(fs, Real(1.0 / prm.tau), u, false);
+  } else if constexpr (COLL == COLL_BGK_INC) {
+    rho = collide_bgk_inc<DEV, false>(fs, Real(1.0 / prm.tau), u, false);
+  } else if constexpr (COLL == COLL_KBC) {
+    rho = collide_kbc<S, DEV, false>(fs, Real(prm.tau), u, false);
+  }
+  if constexpr (DEV && (COLL == COLL_BGK || COLL == COLL_KBC)) {
+    Real pre[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) pre[q] = fs_s[q * 32 + lane];
+    conserve<S>(fs, pre);
+  }
+  if constexpr (COLL != COLL_NONE) {
+    int bad = 0;
+    if (!(rho >= Real(1e-10))) bad |= (rho != rho) ? ST_NAN : ST_DENSITY;
+    if (prm.write_macro) {
+      prm.rho[node] = (double)rho;
+      prm.u[node] = (double)u[0] * prm.scaling;
+      prm.u[prm.n + node] = (double)u[1] * prm.scaling;
+      if constexpr (S::D == 3) prm.u[2 * prm.n + node] = (double)u[2] * prm.scaling;
+    }
+    if (bad) atomicOr(prm.status, bad);
+  }
+#pragma unroll
+  for (int q = 0; q < Q; ++q) prm.f_out[q * prm.n + node] = fs[q];
+}
+
 // One warp: stream + collide the 32-node segment starting at x0 of row
 // (y, z).  swt: the weight table (fill_row_table); buf: this warp's two
-// row buffers of BW + 1 elements.
-template <class S, class Real, int COLL, int P, bool DG>
+// row buffers of BW + 1 elements.  With fs_s != nullptr (SS) the streamed
+// values go to this warp's shared array fs_s[Q][32] instead of registers:
+// far fewer live registers while streaming (more resident warps to hide the
+// load latency); the collision reads them back, and its mass/momentum
+// projection takes the pre-collision values from there as well.
+template <class S, class Real, int COLL, int P, bool DG, bool SS = false>
 __device__ __forceinline__ void row_body(const RowArgs<Real>& prm, const Real* swt, Real* buf2, int y, int z,
-                                         int x0, int lane) {
+                                         int x0, int lane, Real* fs_s = nullptr) {
   constexpr bool DEV = sizeof(Real) == 4;
   constexpr int Q = S::Q;
   constexpr int PER = Geo<P, DG>::PER;
@@ -186,8 +229,11 @@ __device__ __forceinline__ void row_body(const RowArgs<Real>& prm, const Real* s
   const bool hasb = lane + 32 < BW;
   const int gxb = ((x0 - HL + 32 + (hasb ? lane : 0)) % nx + nx) % nx;
 
-  Real fs[Q];
-  fs[0] = valid ? prm.f_in[node] : Real(0);
+  Real fs[SS ? 1 : Q];
+  if constexpr (SS)
+    fs_s[lane] = valid ? prm.f_in[node] : Real(0);
+  else
+    fs[0] = valid ? prm.f_in[node] : Real(0);
 
   static_for<1, Q>([&](auto I) {
     constexpr int A = decltype(I)::value;
@@ -250,51 +296,62 @@ __device__ __forceinline__ void row_body(const RowArgs<Real>& prm, const Real* s
       for (int j = 0; j <= P; ++j) xv[j] = buf[st + j];
       out = wsum_j0<DEV, P>(sw[0][dx][cx], xv, win_j0<P, DG, sx>(cx));
     }
-    fs[A] = out;
+    if constexpr (SS)
+      fs_s[A * 32 + lane] = out;
+    else
+      fs[A] = out;
   });
 
   if (!valid) return;
-  int bad = 0;
-  Real u[3] = {0, 0, 0};
-  Real rho = Real(1);
-  Real pre[Q];
-  if constexpr (DEV) {
+  if constexpr (SS) {
+    row_collide<S, Real, COLL>(prm, fs_s, node, lane);
+    return;
+  } else {
+    int bad = 0;
+    Real u[3] = {0, 0, 0};
+    Real rho = Real(1);
+    Real pre[Q];
+    if constexpr (DEV) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) pre[q] = fs[q];
-  }
-  if constexpr (COLL == COLL_BGK) {
-    rho = collide_bgk<S, DEV, false>(fs, Real(1.0 / prm.tau), u, false);
-    if constexpr (DEV) conserve<S>(fs, pre);
-  } else if constexpr (COLL == COLL_BGK_INC) {
-    rho = collide_bgk_inc<DEV, false>(fs, Real(1.0 / prm.tau), u, false);
-  } else if constexpr (COLL == COLL_KBC) {
-    rho = collide_kbc<S, DEV, false>(fs, Real(prm.tau), u, false);
-    if constexpr (DEV) conserve<S>(fs, pre);
-  }
-  (void)pre;
-  if constexpr (COLL != COLL_NONE) {
-    if (!(rho >= Real(1e-10))) bad |= (rho != rho) ? ST_NAN : ST_DENSITY;
-    if (prm.write_macro) {
-      prm.rho[node] = (double)rho;
-      prm.u[node] = (double)u[0] * prm.scaling;
-      prm.u[prm.n + node] = (double)u[1] * prm.scaling;
-      if constexpr (S::D == 3) prm.u[2 * prm.n + node] = (double)u[2] * prm.scaling;
+      for (int q = 0; q < Q; ++q) pre[q] = fs[q];
     }
-    if (bad) atomicOr(prm.status, bad);
-  }
+    if constexpr (COLL == COLL_BGK) {
+      rho = collide_bgk<S, DEV, false>(fs, Real(1.0 / prm.tau), u, false);
+      if constexpr (DEV) conserve<S>(fs, pre);
+    } else if constexpr (COLL == COLL_BGK_INC) {
+      rho = collide_bgk_inc<DEV, false>(fs, Real(1.0 / prm.tau), u, false);
+    } else if constexpr (COLL == COLL_KBC) {
+      rho = collide_kbc<S, DEV, false>(fs, Real(prm.tau), u, false);
+      if constexpr (DEV) conserve<S>(fs, pre);
+    }
+    (void)pre;
+    if constexpr (COLL != COLL_NONE) {
+      if (!(rho >= Real(1e-10))) bad |= (rho != rho) ? ST_NAN : ST_DENSITY;
+      if (prm.write_macro) {
+        prm.rho[node] = (double)rho;
+        prm.u[node] = (double)u[0] * prm.scaling;
+        prm.u[prm.n + node] = (double)u[1] * prm.scaling;
+        if constexpr (S::D == 3) prm.u[2 * prm.n + node] = (double)u[2] * prm.scaling;
+      }
+      if (bad) atomicOr(prm.status, bad);
+    }
 #pragma unroll
-  for (int q = 0; q < Q; ++q) prm.f_out[q * prm.n + node] = fs[q];
+    for (int q = 0; q < Q; ++q) prm.f_out[q * prm.n + node] = fs[q];
+  }
 }
 
 // Single-solve kernel: CTA = WY x WZ warps over rows (y, z) and one 32-node
 // x segment.
-template <class S, class Real, int COLL, int P, bool DG, int WY, int WZ>
-__global__ void __launch_bounds__(32 * WY * WZ, (sizeof(Real) == 4 ? 2 : 1))
-    k_sl_row(const __grid_constant__ RowParams<Real> prm) {
+// SS: streamed values in shared memory (row_body), MINB: resident CTAs per
+// SM the register allocation is sized for.
+template <class S, class Real, int COLL, int P, bool DG, int WY, int WZ, bool SS = false,
+          int MINB = (sizeof(Real) == 4 ? 2 : 1)>
+__global__ void __launch_bounds__(32 * WY * WZ, MINB) k_sl_row(const __grid_constant__ RowParams<Real> prm) {
   constexpr int PER = Geo<P, DG>::PER;
   constexpr int BW = 32 + PER + P + 1;
   constexpr int NW = WY * WZ;
   __shared__ Real rowbuf[NW][2][BW + 1];
+  __shared__ Real fs_sh[SS ? NW : 1][SS ? S::Q * 32 : 1];
   __shared__ Real sw[row_table_size<P, DG>()];
   fill_row_table<Real, P, DG>(sw, prm.W.w, threadIdx.x, 32 * NW);
   __syncthreads();
@@ -319,7 +376,8 @@ __global__ void __launch_bounds__(32 * WY * WZ, (sizeof(Real) == 4 ? 2 : 1))
   a.tau = prm.tau;
   a.scaling = prm.scaling;
   a.write_macro = prm.write_macro;
-  row_body<S, Real, COLL, P, DG>(a, sw, &rowbuf[warp][0][0], by * WY + wyi, bz * WZ + wzi, seg * 32, lane);
+  row_body<S, Real, COLL, P, DG, SS>(a, sw, &rowbuf[warp][0][0], by * WY + wyi, bz * WZ + wzi, seg * 32, lane,
+                                     SS ? fs_sh[SS ? warp : 0] : nullptr);
 }
 
 }  // namespace natgpu

@@ -344,6 +344,9 @@ __global__ void __launch_bounds__(32 * TH_WARPS, (sizeof(Real) == 4 ? 2 : 1))
   const int xs = valid ? x : x0;
   const int node = y * nx + xs;
   const int cx = xs % per, cy = y % per;
+  // x position of this lane's first buffer slot (the buffer spans at most 64)
+  const int gxa = ((x0 + P.tb.xl + lane) % nx + nx) % nx;
+  const bool hasb = lane + 32 < P.tb.bw;
 
   Real fs[TH_Q], gs[TH_Q];
   fs[0] = P.f_in[node];
@@ -354,23 +357,9 @@ __global__ void __launch_bounds__(32 * TH_WARPS, (sizeof(Real) == 4 ? 2 : 1))
     constexpr int dx = SD2Q25H::dcls(A, 0), dy = SD2Q25H::dcls(A, 1);
     const Real* __restrict__ fsrc = P.f_in + (long long)A * n;
     const Real* __restrict__ gsrc = P.g_in + (long long)A * n;
-    // warp-uniform y window: rows, weights, dominant slot
-    int rowoff[PMAX1];
-    const Real* wy = nullptr;
-    int j0y = 0;
-    if constexpr (dy >= 0) {
-      const int ys = y + P.tb.off[1][dy][cy];
-#pragma unroll
-      for (int j = 0; j < PMAX1; ++j) {
-        int rr = ys + j;
-        rr = ((rr % ny) + ny) % ny;
-        rowoff[j] = rr * nx;
-      }
-      wy = P.tb.w[1][dy][cy];
-      j0y = P.tb.j0[1][dy][cy];
-    } else {
-      rowoff[0] = y * nx;
-    }
+    // warp-uniform y window start (y + offy + j < 2 ny + p < 3 ny: two
+    // conditional subtractions wrap a row index)
+    const int ys = dy >= 0 ? y + P.tb.offy[dy < 0 ? 0 : dy][cy] : y;
     auto ysum = [&](int gx, Real& vf, Real& vg) {
       if constexpr (dy >= 0) {
         Real af[PMAX1], ag[PMAX1];
@@ -379,15 +368,19 @@ __global__ void __launch_bounds__(32 * TH_WARPS, (sizeof(Real) == 4 ? 2 : 1))
           af[j] = Real(0);
           ag[j] = Real(0);
           if (j <= p) {
-            af[j] = __ldg(fsrc + rowoff[j] + gx);
-            ag[j] = __ldg(gsrc + rowoff[j] + gx);
+            int rr = ys + j;
+            rr -= rr >= ny ? ny : 0;
+            rr -= rr >= ny ? ny : 0;
+            const int o = rr * nx + gx;
+            af[j] = __ldg(fsrc + o);
+            ag[j] = __ldg(gsrc + o);
           }
         }
-        vf = th_wsum<Real>(wy, af, p, j0y);
-        vg = th_wsum<Real>(wy, ag, p, j0y);
+        vf = th_wsum<Real>(P.tb.w[1][dy][cy], af, p, P.tb.j0[1][dy][cy]);
+        vg = th_wsum<Real>(P.tb.w[1][dy][cy], ag, p, P.tb.j0[1][dy][cy]);
       } else {
-        vf = __ldg(fsrc + rowoff[0] + gx);
-        vg = __ldg(gsrc + rowoff[0] + gx);
+        vf = __ldg(fsrc + ys * nx + gx);
+        vg = __ldg(gsrc + ys * nx + gx);
       }
     };
     if constexpr (dx < 0) {
@@ -395,13 +388,18 @@ __global__ void __launch_bounds__(32 * TH_WARPS, (sizeof(Real) == 4 ? 2 : 1))
     } else {
       Real* bf = &bufs[warp][(th_xorder(A) & 1) * 2][0];
       Real* bg = &bufs[warp][(th_xorder(A) & 1) * 2 + 1][0];
-      for (int kk = lane; kk < P.tb.bw; kk += 32) {
-        int gx = x0 + P.tb.xl + kk;
-        gx = ((gx % nx) + nx) % nx;
+      {
         Real vf, vg;
-        ysum(gx, vf, vg);
-        bf[kk] = vf;
-        bg[kk] = vg;
+        ysum(gxa, vf, vg);
+        bf[lane] = vf;
+        bg[lane] = vg;
+        if (hasb) {
+          int gxb = gxa + 32;
+          while (gxb >= nx) gxb -= nx;
+          ysum(gxb, vf, vg);
+          bf[lane + 32] = vf;
+          bg[lane + 32] = vg;
+        }
       }
       __syncwarp();
       const int st = lane * (valid ? 1 : 0) + soffx[dx][cx] - P.tb.xl;

@@ -372,3 +372,75 @@ def test_row_kernel_all_orders(gpu_lib, case):
         sol.upload_f(f0)
         sol.step(1)
         assert rel_l2(sol.download_f(), f1) <= TOL64
+
+
+# The bulk-copy row kernel (sl_rowt.cuh, kernel kind 6) needs x rows of at
+# least one copy width and 16-byte aligned row starts, so these meshes are
+# longer in x than the cases above.
+ROWT_CASES = [
+    ("D3Q19", (12, 4, 2), 4, True, "BGK_STANDARD"),
+    ("D3Q19", (32, 2, 2), 2, False, "BGK_STANDARD"),
+    ("D3Q19", (16, 4, 2), 3, False, "BGK_STANDARD"),
+    ("D3Q27", (12, 2, 2), 3, True, "BGK_STANDARD"),
+    ("D3Q27", (16, 4, 2), 2, True, "KBC_STANDARD"),
+]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
+@pytest.mark.parametrize("case", ROWT_CASES, ids=[_ids(c) for c in ROWT_CASES])
+def test_bulk_copy_row_kernel_matches_oracle(gpu_lib, case, precision):
+    stencil, cells, p, dg, model = case
+    st, mesh, dt, tau, spec = make_case(stencil, cells, p, dg, model, precision=precision)
+    f0 = periodic_state(mesh, st, seed=21)
+    S = O.SLOperator(mesh, st, dt)
+    f1, rho1, u1 = oracle_step(S, st, model, tau, f0, 2)
+    with N.Solver(spec) as sol:
+        sol.set_kernel_variant(6)
+        assert sol.kernel_variant == 6
+        assert sol.kernel_info()["smem_bytes"] > 0
+        sol.upload_f(f0)
+        sol.step(2)
+        f = sol.download_f()
+        rho, u = sol.download_macro()
+        sol.set_kernel_variant(1)
+        sol.upload_f(f0)
+        sol.step(2)
+        fg = sol.download_f()
+    tol = TOL64 if precision == "fp64" else 1e-6
+    assert rel_l2(f, f1) <= tol
+    assert rel_l2(rho, rho1) <= tol
+    assert rel_l2(u, u1) <= (1e-11 if precision == "fp64" else 1e-6)
+    if precision == "fp64":
+        assert rel_l2(f, fg) <= TOL64
+
+
+# The row kernel with its streamed values in shared memory (FP32, 3-D, one
+# z row per CTA of 4 or 8 warps) is the first row candidate when ny is a
+# multiple of 4.
+SS_CASES = [
+    ("D3Q19", (4, 4, 2), 4, True, "BGK_STANDARD"),
+    ("D3Q19", (3, 4, 3), 2, False, "BGK_STANDARD"),
+    ("D3Q19", (2, 8, 2), 1, True, "BGK_STANDARD"),
+    ("D3Q27", (3, 4, 2), 3, True, "BGK_STANDARD"),
+    ("D3Q27", (4, 4, 2), 3, False, "KBC_STANDARD"),
+]
+
+
+@pytest.mark.parametrize("case", SS_CASES, ids=[_ids(c) for c in SS_CASES])
+def test_shared_state_row_kernel_matches_oracle(gpu_lib, case):
+    stencil, cells, p, dg, model = case
+    st, mesh, dt, tau, spec = make_case(stencil, cells, p, dg, model, precision="fp32dev")
+    f0 = periodic_state(mesh, st, seed=23)
+    S = O.SLOperator(mesh, st, dt)
+    f1, rho1, u1 = oracle_step(S, st, model, tau, f0, 3)
+    with N.Solver(spec) as sol:
+        sol.set_kernel_variant(4)
+        info = sol.kernel_info()
+        assert info["variant"] == 3 and info["tile_nodes"][2] == 1, info
+        sol.upload_f(f0)
+        sol.step(3)
+        f = sol.download_f()
+        rho, u = sol.download_macro()
+    assert rel_l2(f, f1) <= 1e-6
+    assert rel_l2(rho, rho1) <= 1e-6
+    assert rel_l2(u, u1) <= 1e-6
