@@ -420,7 +420,7 @@ def run_ours(args):
             torch.distributed.destroy_process_group()
         return 0
     cpu = cpu_baseline() if ws == 1 else None
-    compressible = bench_compressible(torch, stream, flush)
+    compressible = None if args.no_compressible else bench_compressible(torch, stream, flush)
     serving = None
     if not args.no_serving:
         from natrium_gb300 import serving as SV
@@ -448,7 +448,7 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": alg_bytes,
-                     "kernel": {1: "k_sl_step", 2: "k_sl_step_v2", 3: "k_sl_row", 6: "k_sl_rowt"}[kinfo["variant"]]
+                     "kernel": {1: "k_sl_step", 2: "k_sl_step_v2", 3: "k_sl_row", 6: "k_sl_rowt", 7: "k_sl_rowg"}[kinfo["variant"]]
                                + "<D3Q19,float,BGK>",
                      "tile_nodes": kinfo["tile_nodes"], "threads": kinfo["threads"],
                      "autotune": {"candidates": ncand, "chosen": chosen}},
@@ -477,10 +477,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--variant", type=int, default=0,
-                    help="fused kernel: 0 autotuned, 1 generic, 3 tile, 4 row-segment, 6 bulk-copy row-segment")
+                    help="fused kernel: 0 autotuned, 1 generic, 3 tile, 4 row-segment, 6 bulk-copy row-segment, "
+                         "7 row-group")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--profile", action="store_true",
                     help="lean run for ncu: FP32 device timing only (no e2e, FP64 leg, CPU baseline or clocks)")
+    ap.add_argument("--no-compressible", action="store_true", help="skip the compressible D2Q25H leg")
     ap.add_argument("--compressible-only", action="store_true",
                     help="time only the compressible D2Q25H leg (prints its JSON object)")
     args = ap.parse_args()

@@ -239,11 +239,12 @@ int nat_device_f(nat_solver* s, void** f_dev);
  * kernel only, 2 = specialised kernel required (NAT_ERR_UNSUPPORTED when
  * none applies), 3 = tile kernel required, 4 = row-segment kernel required,
  * 6 = bulk-copy row-segment kernel required (3-D stencils; per-warp
- * cp.async.bulk pipeline of the source rows). */
+ * cp.async.bulk pipeline of the source rows), 7 = row-group kernel required
+ * (3-D, FP32: 2-4 warps own a whole x row, no halo recomputation). */
 int nat_set_kernel_variant(nat_solver* s, int variant);
 /* The fused-step kernel in use: 1 generic, 2 tile, 3 row-segment,
  * 5 two-population row-segment kernel (NAT_BGK_COMPRESSIBLE),
- * 6 bulk-copy row-segment kernel. */
+ * 6 bulk-copy row-segment kernel, 7 row-group kernel. */
 int nat_kernel_variant(const nat_solver* s);
 
 /* Autotuner: times `steps` fused steps with every kernel that applies to

@@ -321,7 +321,7 @@ class Solver:
     def set_kernel_variant(self, variant: int):
         """0 automatic, 1 generic kernel, 2 specialised kernel required,
         3 tile kernel required, 4 row-segment kernel required, 6 bulk-copy
-        row-segment kernel required."""
+        row-segment kernel required, 7 row-group kernel required."""
         self._check(self._L.nat_set_kernel_variant(self._h, int(variant)))
 
     @property

@@ -21,7 +21,8 @@ LIB = os.path.join(OUT_DIR, "libnatgpu.so")
 SOURCES = ["natgpu_api.cu", "k_d2q9.cu", "k_d3q19.cu", "k_d3q27.cu", "k_v2.cu", "k_row_d2q9.cu",
            "k_row_d3q19.cu", "k_row_d3q27.cu", "serve.cu",
            "natgpu_noalloc.cu", "k_thermal.cu", "k_rowt_d3q19.cu", "k_rowt_d3q27_bgk.cu",
-           "k_rowt_d3q27_kbc.cu", "k_row_ss_d3q19.cu", "k_row_ss_d3q27.cu"]
+           "k_rowt_d3q27_kbc.cu", "k_row_ss_d3q19.cu", "k_row_ss_d3q27.cu",
+           "k_rowg_d3q19.cu", "k_rowg_d3q27.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -67,6 +68,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    for o in objs:  # every build recompiles all sources; the objects are not kept
+        try:
+            os.remove(o)
+        except OSError:
+            pass
     return LIB
 
 

@@ -57,7 +57,9 @@ struct RowLaunch {
   bool dg;
   int wy, wz;
   const void* fn;
-  int kind = 3;      // 3: row kernel (sl_row.cuh), 6: bulk-copy row kernel (sl_rowt.cuh)
+  int kind = 3;      // 3: row kernel (sl_row.cuh), 6: bulk-copy row kernel (sl_rowt.cuh),
+                     // 7: row-group kernel (sl_rowg.cuh; wy = rows per CTA)
+  int g = 0;         // kind 7: warps per x row (32 (g - 1) < nx <= 32 g)
   size_t smem = 0;   // dynamic shared memory (kind 6)
   int align = 1;     // nx must be a multiple of this (kind 6: aligned row copies)
   int min_nx = 0;    // and at least this (kind 6: at most two pieces per row)
@@ -66,6 +68,8 @@ void row_kernels_d2q9(std::vector<RowLaunch>& v);
 void row_kernels_d3q19(std::vector<RowLaunch>& v);
 void row_kernels_d3q27(std::vector<RowLaunch>& v);
 void row_ss_kernels_d3q19(std::vector<RowLaunch>& v);
+void rowg_kernels_d3q19(std::vector<RowLaunch>& v);
+void rowg_kernels_d3q27(std::vector<RowLaunch>& v);
 void row_ss_kernels_d3q27(std::vector<RowLaunch>& v);
 void rowt_kernels_d3q19(std::vector<RowLaunch>& v);
 void rowt_kernels_d3q27_bgk(std::vector<RowLaunch>& v);

@@ -580,7 +580,10 @@ const std::vector<RowLaunch>& row_table() {
   static const std::vector<RowLaunch> t = [] {
     std::vector<RowLaunch> v;
     row_kernels_d2q9(v);
-    // the shared-state float variants first: preferred when they apply
+    // the row-group and shared-state float variants first: preferred when
+    // they apply
+    rowg_kernels_d3q19(v);
+    rowg_kernels_d3q27(v);
     row_ss_kernels_d3q19(v);
     row_ss_kernels_d3q27(v);
     row_kernels_d3q19(v);
@@ -605,6 +608,8 @@ std::vector<Cand> v2_candidates(nat_solver* s, int coll_sel, int smem_optin) {
       continue;
     if (s->n_ax[1] % e.wy != 0 || s->n_ax[2] % e.wz != 0) continue;
     if (e.kind == 6 && (s->n_ax[0] % e.align != 0 || s->n_ax[0] < e.min_nx || (long long)e.smem > smem_optin))
+      continue;
+    if (e.kind == 7 && (s->n_ax[0] > 32 * e.g || s->n_ax[0] <= 32 * (e.g - 1) || s->n_ax[0] < e.min_nx))
       continue;
     Cand c;
     c.kind = e.kind;
@@ -707,10 +712,14 @@ int launch_row_t(nat_solver* s, const SpecWeights<Real>& W, int write_macro) {
   P.scaling = s->spec.scaling;
   P.write_macro = write_macro;
   P.W = W;
-  const int grid = P.nseg * (P.ny / s->row.wy) * (P.nz / s->row.wz);
+  int grid = P.nseg * (P.ny / s->row.wy) * (P.nz / s->row.wz);
+  int nth = 32 * s->row.wy * s->row.wz;
+  if (s->row.kind == 7) {  // row group: g warps per row, wy rows per CTA
+    grid = (P.ny / s->row.wy) * P.nz;
+    nth = 32 * s->row.g * s->row.wy;
+  }
   void* args[] = {&P};
-  cudaError_t e =
-      cudaLaunchKernel(s->row.fn, dim3(grid), dim3(32 * s->row.wy * s->row.wz), args, s->row.smem, s->stream);
+  cudaError_t e = cudaLaunchKernel(s->row.fn, dim3(grid), dim3(nth), args, s->row.smem, s->stream);
   if (e != cudaSuccess) return cuda_fail(s, e, "row stream-collide launch");
   s->launches++;
   s->cur = 1 - s->cur;
@@ -718,7 +727,7 @@ int launch_row_t(nat_solver* s, const SpecWeights<Real>& W, int write_macro) {
 }
 
 int launch_v2(nat_solver* s, int write_macro) {
-  if (s->kind == 3 || s->kind == 6)
+  if (s->kind == 3 || s->kind == 6 || s->kind == 7)
     return s->spec.precision == NAT_FP64 ? launch_row_t<double>(s, s->w64, write_macro)
                                          : launch_row_t<float>(s, s->w32, write_macro);
   return s->spec.precision == NAT_FP64 ? launch_v2_t<double>(s, s->w64, write_macro)
@@ -1359,7 +1368,7 @@ int nat_device_f(nat_solver* s, void** f_dev) {
 int64_t nat_launch_count(const nat_solver* s) { return s ? s->launches : -1; }
 
 int nat_set_kernel_variant(nat_solver* s, int variant) {
-  if (!s || variant < 0 || variant > 6 || variant == 5) return NAT_ERR_INVALID_ARG;
+  if (!s || variant < 0 || variant > 7 || variant == 5) return NAT_ERR_INVALID_ARG;
   if (s->thermal) {
     // one kernel serves the two-population model
     if (variant == 0) return NAT_OK;
@@ -1461,10 +1470,12 @@ int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* t
   for (int a = 0; a < 3; ++a) {
     int t = k == 2 ? s->v2.B[a] : s->B[a];
     if (k == 3 || k == 6) t = a == 0 ? 32 : (a == 1 ? s->row.wy : s->row.wz);
+    if (k == 7) t = a == 0 ? 32 * s->row.g : (a == 1 ? s->row.wy : 1);
     if (tile_nodes) tile_nodes[a] = t;
   }
-  const bool row = k == 3 || k == 6;
-  if (threads) *threads = k == 2 ? s->v2.nth : (row ? 32 * s->row.wy * s->row.wz : STEP_THREADS);
+  const bool row = k == 3 || k == 6 || k == 7;
+  if (threads)
+    *threads = k == 2 ? s->v2.nth : (k == 7 ? 32 * s->row.g * s->row.wy : (row ? 32 * s->row.wy * s->row.wz : STEP_THREADS));
   if (smem_bytes) *smem_bytes = (int64_t)(k == 2 ? s->v2.smem : (row ? s->row.smem : s->smem_step));
   return NAT_OK;
 }

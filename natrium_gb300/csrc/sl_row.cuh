@@ -171,9 +171,9 @@ __device__ __forceinline__ void row_collide(const RowArgs<Real>& prm, const Real
   Real u[3] = {0, 0, 0};
   Real rho = Real(1);
   if constexpr (COLL == COLL_BGK) {
-    rho = collide_bgk<S, DEV, false>(fs, Real(1.0 / prm.tau), u, false);
+    rho = collide_bgk<S, DEV, false>(fs, Real(1) / Real(prm.tau), u, false);
   } else if constexpr (COLL == COLL_BGK_INC) {
-    rho = collide_bgk_inc<DEV, false>(fs, Real(1.0 / prm.tau), u, false);
+    rho = collide_bgk_inc<DEV, false>(fs, Real(1) / Real(prm.tau), u, false);
   } else if constexpr (COLL == COLL_KBC) {
     rho = collide_kbc<S, DEV, false>(fs, Real(prm.tau), u, false);
   }
@@ -316,10 +316,10 @@ __device__ __forceinline__ void row_body(const RowArgs<Real>& prm, const Real* s
       for (int q = 0; q < Q; ++q) pre[q] = fs[q];
     }
     if constexpr (COLL == COLL_BGK) {
-      rho = collide_bgk<S, DEV, false>(fs, Real(1.0 / prm.tau), u, false);
+      rho = collide_bgk<S, DEV, false>(fs, Real(1) / Real(prm.tau), u, false);
       if constexpr (DEV) conserve<S>(fs, pre);
     } else if constexpr (COLL == COLL_BGK_INC) {
-      rho = collide_bgk_inc<DEV, false>(fs, Real(1.0 / prm.tau), u, false);
+      rho = collide_bgk_inc<DEV, false>(fs, Real(1) / Real(prm.tau), u, false);
     } else if constexpr (COLL == COLL_KBC) {
       rho = collide_kbc<S, DEV, false>(fs, Real(prm.tau), u, false);
       if constexpr (DEV) conserve<S>(fs, pre);

@@ -254,10 +254,10 @@ __global__ void __launch_bounds__(32 * WY * WZ, (sizeof(Real) == 4 ? 2 : 1))
     for (int q = 0; q < Q; ++q) pre[q] = fs[q];
   }
   if constexpr (COLL == COLL_BGK) {
-    rho = collide_bgk<S, DEV, false>(fs, Real(1.0 / prm.tau), u, false);
+    rho = collide_bgk<S, DEV, false>(fs, Real(1) / Real(prm.tau), u, false);
     if constexpr (DEV) conserve<S>(fs, pre);
   } else if constexpr (COLL == COLL_BGK_INC) {
-    rho = collide_bgk_inc<DEV, false>(fs, Real(1.0 / prm.tau), u, false);
+    rho = collide_bgk_inc<DEV, false>(fs, Real(1) / Real(prm.tau), u, false);
   } else if constexpr (COLL == COLL_KBC) {
     rho = collide_kbc<S, DEV, false>(fs, Real(prm.tau), u, false);
     if constexpr (DEV) conserve<S>(fs, pre);

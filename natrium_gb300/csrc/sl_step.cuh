@@ -288,10 +288,10 @@ __global__ void __launch_bounds__(NT) k_sl_step(const StepParams P) {
       for (int q = 0; q < Q; ++q) pre[q] = fs[k][q];
     }
     if constexpr (COLL == COLL_BGK) {
-      rho = collide_bgk<S, DEV, DEV>(fs[k], Real(1.0 / P.tau), u, false);
+      rho = collide_bgk<S, DEV, DEV>(fs[k], Real(1) / Real(P.tau), u, false);
       if constexpr (DEV) conserve<S>(fs[k], pre);
     } else if constexpr (COLL == COLL_BGK_INC) {
-      rho = collide_bgk_inc<DEV, DEV>(fs[k], Real(1.0 / P.tau), u, false);
+      rho = collide_bgk_inc<DEV, DEV>(fs[k], Real(1) / Real(P.tau), u, false);
     } else if constexpr (COLL == COLL_KBC) {
       rho = collide_kbc<S, DEV, DEV>(fs[k], Real(P.tau), u, false);
       if constexpr (DEV) conserve<S>(fs[k], pre);
@@ -340,14 +340,14 @@ __global__ void __launch_bounds__(256) k_collide(const StepParams P) {
 #pragma unroll
     for (int q = 0; q < Q; ++q) pre[q] = v[q];
     if constexpr (COLL == COLL_BGK_INC) {
-      rho = collide_bgk_inc<DEV, DEV>(v, Real(1.0 / P.tau), u, given);
+      rho = collide_bgk_inc<DEV, DEV>(v, Real(1) / Real(P.tau), u, given);
     } else if constexpr (COLL == COLL_KBC) {
       rho = collide_kbc<S, DEV, DEV>(v, Real(P.tau), u, given);
       if constexpr (DEV) {
         if (!given) conserve<S>(v, pre);
       }
     } else {
-      rho = collide_bgk<S, DEV, DEV>(v, Real(1.0 / P.tau), u, given);
+      rho = collide_bgk<S, DEV, DEV>(v, Real(1) / Real(P.tau), u, given);
       // with a prescribed velocity the momentum is not a collision invariant
       if constexpr (DEV) {
         if (!given) conserve<S>(v, pre);

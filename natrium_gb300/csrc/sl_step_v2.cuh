@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(NTH, 1) k_sl_step_v2(const __grid_constant__ S
 
   // collision from the streamed buffer, one write of f
   int bad = 0;
-  const Real inv_tau = Real(1.0 / prm.tau);
+  const Real inv_tau = Real(1) / Real(prm.tau);
   for (int t = threadIdx.x; t < TB; t += NTH) {
     Real v[Q], pre[Q];
 #pragma unroll

@@ -444,3 +444,33 @@ def test_shared_state_row_kernel_matches_oracle(gpu_lib, case):
     assert rel_l2(f, f1) <= 1e-6
     assert rel_l2(rho, rho1) <= 1e-6
     assert rel_l2(u, u1) <= 1e-6
+
+
+# Row-group kernel (sl_rowg.cuh, kernel kind 7): G warps own a whole x row
+# (32 (G - 1) < nx <= 32 G, G = 2..4).
+ROWG_CASES = [
+    ("D3Q19", (16, 4, 2), 4, True, "BGK_STANDARD"),
+    ("D3Q19", (20, 4, 2), 2, False, "BGK_STANDARD"),
+    ("D3Q19", (32, 2, 2), 3, False, "BGK_STANDARD"),
+    ("D3Q27", (12, 2, 2), 3, True, "BGK_STANDARD"),
+    ("D3Q27", (16, 4, 2), 2, True, "KBC_STANDARD"),
+]
+
+
+@pytest.mark.parametrize("case", ROWG_CASES, ids=[_ids(c) for c in ROWG_CASES])
+def test_row_group_kernel_matches_oracle(gpu_lib, case):
+    stencil, cells, p, dg, model = case
+    st, mesh, dt, tau, spec = make_case(stencil, cells, p, dg, model, precision="fp32dev")
+    f0 = periodic_state(mesh, st, seed=29)
+    S = O.SLOperator(mesh, st, dt)
+    f1, rho1, u1 = oracle_step(S, st, model, tau, f0, 3)
+    with N.Solver(spec) as sol:
+        sol.set_kernel_variant(7)
+        assert sol.kernel_variant == 7
+        sol.upload_f(f0)
+        sol.step(3)
+        f = sol.download_f()
+        rho, u = sol.download_macro()
+    assert rel_l2(f, f1) <= 1e-6
+    assert rel_l2(rho, rho1) <= 1e-6
+    assert rel_l2(u, u1) <= 1e-6
