@@ -91,7 +91,8 @@ typedef struct nat_spec {
   int topology;     /* NAT_TOPO_FEQ or NAT_TOPO_DG */
   int cells[3];     /* uniform Cartesian cells per axis (unused axes: 1) */
   double length[3]; /* box edge lengths; the box is [0, L_a) */
-  int periodic[3];  /* must be 1 on every used axis */
+  int periodic[3];  /* 1: periodic axis; 0: two wall faces (DG topology only),
+                       bounce-back at rest until nat_set_boundary changes them */
   double scaling;   /* stencil scaling (e = scaling * unit vectors) */
   double viscosity; /* kinematic viscosity nu */
   double cfl;       /* used when dt <= 0: dt = CFL h_min / (sqrt(2) scaling p^2)
@@ -187,6 +188,22 @@ int nat_mass_energy(nat_solver* s, double* mass, double* kinetic_energy);
 int nat_mass_energy_noalloc(const double* rho_dev, const double* u_dev, int dim, const int n_axis[3],
                             int order, int topology, const double cell_size[3], double* out_dev,
                             void* cuda_stream);
+
+/* ---- wall boundaries ----------------------------------------------------
+ * Faces of a non-periodic axis: 0 x-, 1 x+, 2 y-, 3 y+, 4 z-, 5 z+.  A
+ * departure path that meets a wall is handled as SemiLagrangian::
+ * fillSparseObject does (advection/SemiLagrangian.cpp:354-399):
+ *   NAT_BC_VELOCITY_BOUNCE_BACK (boundaries/VelocityNeqBounceBack.h): the path
+ *     reverses at the wall and takes the opposite population; the wall adds
+ *     2 w_alpha rho_w (e_alpha . u_wall) / c_s^2 with rho_w = 1, scaled units
+ *     (VelocityNeqBounceBack.cpp:137-194);
+ *   NAT_BC_DO_NOTHING (boundaries/DoNothingBoundary.h): the population is taken
+ *     from x + dt e_alpha instead.
+ * The two-population model streams g through the same rows, without the
+ * wall term.  Those rows are evaluated after the interior streaming. */
+#define NAT_BC_VELOCITY_BOUNCE_BACK 1
+#define NAT_BC_DO_NOTHING 2
+int nat_set_boundary(nat_solver* s, int face, int kind, const double u_wall[3]);
 
 /* ---- compressible two-population model (NAT_BGK_COMPRESSIBLE) ---------- */
 /* Equilibrium of the collision (SolverConfiguration equilibrium scheme). */

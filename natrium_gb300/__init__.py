@@ -59,7 +59,7 @@ EXPORTS = [
     "nat_server_create", "nat_server_destroy", "nat_server_submit", "nat_server_step", "nat_server_poll",
     "nat_server_result", "nat_server_stats", "nat_server_last_error", "nat_mass_energy_noalloc",
     "nat_set_thermal", "nat_get_thermal", "nat_upload_g", "nat_download_g", "nat_download_thermal",
-    "nat_init_thermal",
+    "nat_init_thermal", "nat_set_boundary",
 ]
 
 
@@ -150,6 +150,7 @@ def load_library(path: str | None = None):
     L.nat_download_g.argtypes = [vp, dp]
     L.nat_download_thermal.argtypes = [vp, dp, dp]
     L.nat_init_thermal.argtypes = [vp, dp, dp, dp]
+    L.nat_set_boundary.argtypes = [vp, C.c_int, C.c_int, dp]
     _lib = L
     return L
 
@@ -175,6 +176,7 @@ class SolverSpec:
     collision: str = "BGK_STANDARD"
     precision: str = "fp64"
     topology: str = "feq"
+    periodic: tuple = (True, True, True)  # False: two wall faces on that axis (DG only)
 
     @property
     def dim(self) -> int:
@@ -189,7 +191,7 @@ class SolverSpec:
         for a in range(3):
             s.cells[a] = int(self.cells[a]) if a < self.dim else 1
             s.length[a] = float(self.length[a]) if a < self.dim else 1.0
-            s.periodic[a] = 1
+            s.periodic[a] = 1 if (a >= self.dim or self.periodic[a]) else 0
         s.scaling = float(self.scaling)
         s.viscosity = float(self.viscosity)
         s.cfl = float(self.cfl)
@@ -346,6 +348,15 @@ class Solver:
         p = C.c_void_p()
         self._check(self._L.nat_device_f(self._h, C.byref(p)))
         return p.value or 0
+
+    # -- wall boundaries -------------------------------------------------------------
+    def set_boundary(self, face: int, kind: str = "VELOCITY_BOUNCE_BACK", u_wall=(0.0, 0.0, 0.0)):
+        """Kind of wall face `face` (0 x-, 1 x+, 2 y-, 3 y+, 4 z-, 5 z+) of a
+        non-periodic axis: VELOCITY_BOUNCE_BACK (wall velocity u_wall, scaled)
+        or DO_NOTHING."""
+        k = {"VELOCITY_BOUNCE_BACK": 1, "DO_NOTHING": 2}[kind]
+        uw = np.ascontiguousarray(np.asarray(u_wall, dtype=np.float64).reshape(3))
+        self._check(self._L.nat_set_boundary(self._h, int(face), k, _dp(uw)))
 
     # -- compressible two-population model (collision BGK_COMPRESSIBLE) ---------
     def set_thermal(self, t: ThermalSettings):

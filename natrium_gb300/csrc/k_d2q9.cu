@@ -9,18 +9,18 @@ static KernelSet pick_d2q9(int coll) {
   using S = SD2Q9;
   switch (coll) {
     case L_COLL_NONE:
-      return {(const void*)&k_sl_step<S, Real, COLL_NONE, STEP_NPT>, nullptr};
+      return {(const void*)&k_sl_step<S, Real, COLL_NONE, STEP_NPT>, nullptr, nullptr};
     case L_COLL_BGK:
       return {(const void*)&k_sl_step<S, Real, COLL_BGK, STEP_NPT>,
-              (const void*)&k_collide<S, Real, COLL_BGK>};
+              (const void*)&k_collide<S, Real, COLL_BGK>, (const void*)&k_wall_nodes<S, Real, COLL_BGK>};
     case L_COLL_BGK_INC:
       return {(const void*)&k_sl_step<S, Real, COLL_BGK_INC, STEP_NPT>,
-              (const void*)&k_collide<S, Real, COLL_BGK_INC>};
+              (const void*)&k_collide<S, Real, COLL_BGK_INC>, (const void*)&k_wall_nodes<S, Real, COLL_BGK_INC>};
     case L_COLL_KBC:
       return {(const void*)&k_sl_step<S, Real, COLL_KBC, STEP_NPT>,
-              (const void*)&k_collide<S, Real, COLL_KBC>};
+              (const void*)&k_collide<S, Real, COLL_KBC>, (const void*)&k_wall_nodes<S, Real, COLL_KBC>};
     default:
-      return {nullptr, nullptr};
+      return {nullptr, nullptr, nullptr};
   }
 }
 

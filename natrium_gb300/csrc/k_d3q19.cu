@@ -9,12 +9,12 @@ static KernelSet pick_d3q19(int coll) {
   using S = SD3Q19;
   switch (coll) {
     case L_COLL_NONE:
-      return {(const void*)&k_sl_step<S, Real, COLL_NONE, STEP_NPT>, nullptr};
+      return {(const void*)&k_sl_step<S, Real, COLL_NONE, STEP_NPT>, nullptr, nullptr};
     case L_COLL_BGK:
       return {(const void*)&k_sl_step<S, Real, COLL_BGK, STEP_NPT>,
-              (const void*)&k_collide<S, Real, COLL_BGK>};
+              (const void*)&k_collide<S, Real, COLL_BGK>, (const void*)&k_wall_nodes<S, Real, COLL_BGK>};
     default:
-      return {nullptr, nullptr};
+      return {nullptr, nullptr, nullptr};
   }
 }
 

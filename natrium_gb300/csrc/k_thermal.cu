@@ -47,4 +47,21 @@ cudaError_t launch_thermal_init(const ThermalPointT<double>& P, void* f, void* g
   return cudaGetLastError();
 }
 
+template <class Real>
+static cudaError_t wall_nodes_t(const ThermalStepT<Real>& P, int nbn, const int* node, const int* ptr,
+                                const int* col, const Real* w, const double* cst, cudaStream_t st) {
+  const int grid = (nbn + 127) / 128;
+  k_thermal_wall_nodes<Real><<<grid, 128, 0, st>>>(P, nbn, node, ptr, col, w, cst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_thermal_wall_nodes(const ThermalStepT<double>& P, int nbn, const int* node, const int* ptr,
+                                      const int* col, const double* w, const double* cst, cudaStream_t st) {
+  return wall_nodes_t(P, nbn, node, ptr, col, w, cst, st);
+}
+cudaError_t launch_thermal_wall_nodes(const ThermalStepT<float>& P, int nbn, const int* node, const int* ptr,
+                                      const int* col, const float* w, const double* cst, cudaStream_t st) {
+  return wall_nodes_t(P, nbn, node, ptr, col, w, cst, st);
+}
+
 }  // namespace natgpu

@@ -15,8 +15,9 @@ namespace natgpu {
 enum { L_COLL_NONE = 0, L_COLL_BGK = 1, L_COLL_BGK_INC = 2, L_COLL_KBC = 3 };
 
 struct KernelSet {
-  const void* step;     // fused stream(+collide) kernel, NULL if unsupported
-  const void* collide;  // collide-only kernel, NULL for COLL_NONE
+  const void* step;      // fused stream(+collide) kernel, NULL if unsupported
+  const void* collide;   // collide-only kernel, NULL for COLL_NONE
+  const void* wallnode;  // fused step of the wall nodes (k_wall_nodes), NULL for COLL_NONE
 };
 
 // prec: 0 = FP64, 1 = FP32 deviation
@@ -84,5 +85,11 @@ cudaError_t launch_thermal_collide(const ThermalPointT<double>& P, int grid, cud
 cudaError_t launch_thermal_collide(const ThermalPointT<float>& P, int grid, cudaStream_t st);
 cudaError_t launch_thermal_init(const ThermalPointT<double>& P, void* f, void* g, bool fp32, int grid,
                                 cudaStream_t st);
+// fused step of the wall nodes of the two-population model: rows as
+// k_wall_nodes, f and g through the same rows (constant slots f, g)
+cudaError_t launch_thermal_wall_nodes(const ThermalStepT<double>& P, int nbn, const int* node, const int* ptr,
+                                      const int* col, const double* w, const double* cst, cudaStream_t st);
+cudaError_t launch_thermal_wall_nodes(const ThermalStepT<float>& P, int nbn, const int* node, const int* ptr,
+                                      const int* col, const float* w, const double* cst, cudaStream_t st);
 
 }  // namespace natgpu

@@ -74,6 +74,20 @@ struct nat_solver {
   ThermalModelT<float> tmf;
   ThermalTablesT<double> tt;
   ThermalTablesT<float> ttf;
+  // wall boundaries (non-periodic axes): per face kind and wall velocity, and
+  // the rows of the streaming operator whose departure path meets a wall
+  bool walls = false;
+  int bc[6] = {0, 0, 0, 0, 0, 0};
+  double uw[6][3] = {{0}};
+  int nbr = 0;                   // boundary rows
+  int* d_br_dst = nullptr;       // destination index dir * n_dev + node
+  int* d_br_ptr = nullptr;       // nbr + 1 offsets into col / w
+  int* d_br_col = nullptr;       // source index dir * n_dev + node
+  double* d_br_w = nullptr;      // Lagrange weights (FP64)
+  float* d_br_wf = nullptr;      // the same in float
+  double* d_br_c = nullptr;      // per row: f const, f const (deviation form), g const, g const (deviation)
+  int nbn = 0;                   // wall nodes: nodes with a row that meets a wall; their
+  int* d_bn_node = nullptr;      // Q - 1 rows are rows k (Q-1) .. k (Q-1) + Q - 2 above
 };
 
 namespace {
@@ -893,6 +907,289 @@ int launch_thermal(nat_solver* s, bool collide, int write_macro) {
   return NAT_OK;
 }
 
+// ---- wall boundaries ----------------------------------------------------------
+// Rows of the streaming operator whose departure path meets a wall face,
+// evaluated as sparse rows after the interior streaming (the interior kernel
+// computes those rows with the periodic window; this overwrites them):
+//   f_out[dst] = sum_k w_k f_in[col_k] + c
+// (SemiLagrangian.cpp:354-399 for the rows, SemiLagrangianBoundaryHandler::apply
+// and VelocityNeqBounceBack.cpp:137-194 for the wall-velocity term c).
+template <class Real>
+__global__ void k_wall_rows(int nbr, const int* __restrict__ dst, const int* __restrict__ ptr,
+                            const int* __restrict__ col, const Real* __restrict__ w, const double* __restrict__ cst,
+                            int cst_slot, const Real* __restrict__ f_in, Real* __restrict__ f_out) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nbr; r += gridDim.x * blockDim.x) {
+    Real acc = Real(cst[4 * r + cst_slot]);
+    for (int k = ptr[r]; k < ptr[r + 1]; ++k) acc = fma(w[k], f_in[col[k]], acc);
+    f_out[dst[r]] = acc;
+  }
+}
+
+// First face of the axis-aligned cell [lo, lo + h] crossed by the segment
+// p_in -> p_out (unit coordinates snapped at 1e-10; the x face is taken
+// first, later faces only when strictly earlier); -1 if p_out lies in the
+// closed cell.  Writes the crossing point.  Restates
+// SemiLagrangian::faceCrossedFirst for MappingCartesian (SemiLagrangian.cpp:525-699).
+int face_crossed_first(int D, const double* lo, const double* h, const double* p_in, const double* p_out,
+                       double* p_b) {
+  double pi[3], po[3], lambda = 100.0;
+  int face = -1;
+  auto snap = [](double v) { return fabs(v) < 1e-10 ? 0.0 : (fabs(v - 1.0) < 1e-10 ? 1.0 : v); };
+  for (int a = 0; a < D; ++a) {
+    pi[a] = snap((p_in[a] - lo[a]) / h[a]);
+    po[a] = snap((p_out[a] - lo[a]) / h[a]);
+  }
+  for (int a = 0; a < D; ++a) {
+    double lam;
+    int f;
+    if (po[a] < 0) {
+      lam = (0 - pi[a]) / (po[a] - pi[a]);
+      f = 2 * a;
+    } else if (po[a] > 1) {
+      lam = (1 - pi[a]) / (po[a] - pi[a]);
+      f = 2 * a + 1;
+    } else {
+      continue;
+    }
+    if (a == 0 || lam < lambda) {
+      lambda = lam;
+      face = f;
+    }
+  }
+  if (face < 0) return -1;
+  for (int a = 0; a < D; ++a) p_b[a] = lo[a] + snap(pi[a] + (po[a] - pi[a]) * lambda) * h[a];
+  return face;
+}
+
+int build_wall_rows(nat_solver* s) {
+  cudaFree(s->d_br_dst);
+  cudaFree(s->d_br_ptr);
+  cudaFree(s->d_br_col);
+  cudaFree(s->d_br_w);
+  cudaFree(s->d_br_wf);
+  cudaFree(s->d_br_c);
+  cudaFree(s->d_bn_node);
+  s->d_br_dst = s->d_br_ptr = s->d_br_col = s->d_bn_node = nullptr;
+  s->d_br_w = s->d_br_c = nullptr;
+  s->d_br_wf = nullptr;
+  s->nbr = 0;
+  s->nbn = 0;
+  if (!s->walls) return NAT_OK;
+  HostStencil hs;
+  get_host_stencil(s->spec.stencil, &hs, s->spec.scaling);
+  const int D = s->D, Q = s->Q, p = s->spec.order, PER = s->period;
+  double xi[PMAX1 + 1];
+  gl_points(p, xi);
+  double es[32][3];
+  int opp[32];
+  for (int i = 0; i < Q; ++i)
+    for (int a = 0; a < 3; ++a) es[i][a] = a < D ? hs.e[i][a] * s->spec.scaling : 0.0;
+  for (int i = 0; i < Q; ++i) {
+    opp[i] = 0;
+    for (int j = 0; j < Q; ++j)
+      if (es[j][0] == -es[i][0] && es[j][1] == -es[i][1] && es[j][2] == -es[i][2]) opp[i] = j;
+  }
+  double grest[32];
+  for (int q = 0; q < Q; ++q) grest[q] = s->rest[q] * s->gref;
+  std::vector<int> dst, ptr(1, 0), col, bnodes;
+  std::vector<double> w, cst;
+  const long long n = s->n_dev;
+  const int* N = s->spec.cells;
+  // the departure path of one (node, direction): source direction, cell and
+  // point where it ends, wall term; returns the number of wall hits (-1: the
+  // lifetime cap was reached, identity row)
+  struct Path {
+    int sdir, cell[3];
+    double dep[3], c;
+  };
+  auto trace = [&](const double* x, const int* own, int alpha, Path& P) -> int {
+    // defaults (also what an identity row of the lifetime cap uses)
+    P.sdir = alpha;
+    P.c = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      P.cell[a] = own[a];
+      P.dep[a] = x[a];
+    }
+    int cdir = alpha, hit_dn = 0, hits = 0, life = 0;
+    int cell[3] = {own[0], own[1], own[2]};
+    double cur[3] = {x[0], x[1], x[2]}, dep[3] = {0, 0, 0};
+    for (int a = 0; a < D; ++a) dep[a] = x[a] - s->dt * es[alpha][a];
+    double c = 0.0;
+    for (;;) {
+      if (++life > 50) {  // lifetime cap (SemiLagrangian.cpp:252-271): identity row; the
+        P.c = c;          // wall terms of the hits before it stay registered
+        return -1;
+      }
+      double lo[3], pb[3];
+      for (int a = 0; a < D; ++a) lo[a] = cell[a] * s->h[a];
+      const int face = face_crossed_first(D, lo, s->h, cur, dep, pb);
+      if (face < 0) break;
+      const int ax = face / 2, upper = face % 2;
+      const bool at_boundary = upper ? (cell[ax] == N[ax] - 1) : (cell[ax] == 0);
+      if (at_boundary && !s->spec.periodic[ax] && s->bc[face] == NAT_BC_VELOCITY_BOUNCE_BACK) {
+        double dist = 0.0, ve = 0.0, exu = 0.0;
+        cdir = opp[cdir];
+        for (int a = 0; a < D; ++a) {
+          dist += (dep[a] - pb[a]) * (dep[a] - pb[a]);
+          ve += es[cdir][a] * es[cdir][a];
+        }
+        dist = sqrt(dist);
+        ve = sqrt(ve);
+        for (int a = 0; a < D; ++a) {
+          cur[a] = pb[a];
+          dep[a] = cur[a] - es[cdir][a] * dist / ve;
+        }
+        for (int a = 0; a < D; ++a) exu += s->uw[face][a] * es[alpha][a];
+        c += 2.0 * hs.w[alpha] * 1.0 * exu / s->cs2_scaled;
+        ++hits;
+        continue;
+      }
+      if (at_boundary && !s->spec.periodic[ax]) {  // do-nothing
+        for (int a = 0; a < D; ++a) {
+          cur[a] = dep[a] + s->dt * es[cdir][a];
+          dep[a] = cur[a] + s->dt * es[cdir][a];
+        }
+        cdir = opp[cdir];
+        hit_dn = 1;
+        ++hits;
+        continue;
+      }
+      for (int a = 0; a < D; ++a) cur[a] = pb[a];
+      if (at_boundary) {  // periodic: translate by the box length
+        const double shift = upper ? -s->spec.length[ax] : s->spec.length[ax];
+        cur[ax] += shift;
+        dep[ax] += shift;
+        cell[ax] = upper ? 0 : N[ax] - 1;
+      } else {
+        cell[ax] += upper ? 1 : -1;
+      }
+    }
+    if (hit_dn) cdir = opp[cdir];  // SemiLagrangian.cpp:312-316
+    P.sdir = cdir;
+    P.c = c;
+    for (int a = 0; a < 3; ++a) {
+      P.cell[a] = cell[a];
+      P.dep[a] = dep[a];
+    }
+    return hits;
+  };
+  for (long long node = 0; node < n; ++node) {
+    int idx[3] = {(int)(node % s->n_ax[0]), (int)((node / s->n_ax[0]) % s->n_ax[1]),
+                  (int)(node / ((long long)s->n_ax[0] * s->n_ax[1]))};
+    double x[3] = {0, 0, 0};
+    int own[3] = {0, 0, 0};
+    for (int a = 0; a < D; ++a) {
+      own[a] = idx[a] / PER;
+      x[a] = own[a] * s->h[a] + xi[idx[a] % PER] * s->h[a];
+    }
+    // a node is a wall node when one of its paths meets a wall; all its rows
+    // are then evaluated as sparse rows
+    Path paths[32];
+    int hits[32];
+    bool wall_node = false;
+    for (int alpha = 1; alpha < Q; ++alpha) {
+      hits[alpha] = trace(x, own, alpha, paths[alpha]);
+      if (hits[alpha] != 0) wall_node = true;
+    }
+    if (!wall_node) continue;
+    bnodes.push_back((int)node);
+    for (int alpha = 1; alpha < Q; ++alpha) {
+      const Path& P = paths[alpha];
+      const bool identity = hits[alpha] < 0;
+      const int sdir = identity ? alpha : P.sdir;
+      int cell[3] = {own[0], own[1], own[2]};
+      if (!identity)
+        for (int a = 0; a < D; ++a) cell[a] = P.cell[a];
+      double l1[3][PMAX1];
+      for (int a = 0; a < 3; ++a)
+        for (int j = 0; j < PMAX1; ++j) l1[a][j] = (a >= D && j == 0) ? 1.0 : 0.0;
+      for (int a = 0; a < D; ++a) {
+        if (identity) {
+          cell[a] = own[a];
+          for (int j = 0; j <= p; ++j) l1[a][j] = (j == idx[a] % PER) ? 1.0 : 0.0;
+          continue;
+        }
+        double ul = (P.dep[a] - cell[a] * s->h[a]) / s->h[a];
+        if (fabs(ul) < 1e-10) ul = 0.0;
+        if (fabs(ul - 1.0) < 1e-10) ul = 1.0;
+        for (int j = 0; j <= p; ++j) l1[a][j] = lagrange(p, xi, j, ul);
+      }
+      const double c = P.c;
+      const int np1 = p + 1;
+      const int nloc = D == 3 ? np1 * np1 * np1 : np1 * np1;
+      double wrest = 0.0, wgrest = 0.0;
+      for (int li = 0; li < nloc; ++li) {
+        const int lx = li % np1, ly = (li / np1) % np1, lz = D == 3 ? li / (np1 * np1) : 0;
+        const double v = l1[0][lx] * l1[1][ly] * (D == 3 ? l1[2][lz] : 1.0);
+        if (fabs(v) < 1e-10) continue;  // SemiLagrangian.cpp:483
+        const long long src = ((long long)(cell[2] * PER + lz) * s->n_ax[1] + (cell[1] * PER + ly)) * s->n_ax[0] +
+                              (cell[0] * PER + lx);
+        col.push_back((int)(sdir * n + src));
+        w.push_back(v);
+        wrest += v * s->rest[sdir];
+        wgrest += v * grest[sdir];
+      }
+      dst.push_back((int)(alpha * n + node));
+      ptr.push_back((int)col.size());
+      cst.push_back(c);                           // plain f
+      cst.push_back(c + wrest - s->rest[alpha]);  // f - w_i storage
+      cst.push_back(0.0);                         // plain g: no wall term
+      cst.push_back(wgrest - grest[alpha]);       // g - w_i g_ref storage
+    }
+  }
+  s->nbn = (int)bnodes.size();
+  s->nbr = (int)dst.size();
+  if (s->nbr == 0) return NAT_OK;
+  // every index must address the Q x n_dev state (checked before any launch)
+  const long long qn = (long long)Q * n;
+  for (int v : col)
+    if (v < 0 || v >= qn) return fail(s, NAT_ERR_CUDA, "internal error: wall row column %d out of range", v);
+  for (int v : dst)
+    if (v < 0 || v >= qn) return fail(s, NAT_ERR_CUDA, "internal error: wall row destination %d out of range", v);
+  std::vector<float> wf(w.begin(), w.end());
+#define WALLOC(ptr_, bytes_)                                                  \
+  do {                                                                        \
+    if (cudaMalloc((void**)&(ptr_), (bytes_)) != cudaSuccess) {               \
+      cudaGetLastError();                                                     \
+      return fail(s, NAT_ERR_OOM, "cudaMalloc(%zu) failed", (size_t)(bytes_)); \
+    }                                                                         \
+  } while (0)
+  WALLOC(s->d_br_dst, sizeof(int) * dst.size());
+  WALLOC(s->d_br_ptr, sizeof(int) * ptr.size());
+  WALLOC(s->d_br_col, sizeof(int) * std::max<size_t>(col.size(), 1));
+  WALLOC(s->d_br_w, sizeof(double) * std::max<size_t>(w.size(), 1));
+  WALLOC(s->d_br_wf, sizeof(float) * std::max<size_t>(w.size(), 1));
+  WALLOC(s->d_br_c, sizeof(double) * cst.size());
+  WALLOC(s->d_bn_node, sizeof(int) * bnodes.size());
+#undef WALLOC
+  CK(cudaMemcpy(s->d_br_dst, dst.data(), sizeof(int) * dst.size(), cudaMemcpyHostToDevice), "wall rows");
+  CK(cudaMemcpy(s->d_br_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice), "wall rows");
+  if (!col.empty()) {
+    CK(cudaMemcpy(s->d_br_col, col.data(), sizeof(int) * col.size(), cudaMemcpyHostToDevice), "wall rows");
+    CK(cudaMemcpy(s->d_br_w, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice), "wall rows");
+    CK(cudaMemcpy(s->d_br_wf, wf.data(), sizeof(float) * wf.size(), cudaMemcpyHostToDevice), "wall rows");
+  }
+  CK(cudaMemcpy(s->d_br_c, cst.data(), sizeof(double) * cst.size(), cudaMemcpyHostToDevice), "wall rows");
+  CK(cudaMemcpy(s->d_bn_node, bnodes.data(), sizeof(int) * bnodes.size(), cudaMemcpyHostToDevice), "wall nodes");
+  return NAT_OK;
+}
+
+// Overwrite the wall rows of a streamed buffer (f: slot 0/1, g: slot 2 or none).
+int launch_wall_rows(nat_solver* s, const void* in, void* out, bool g_pop) {
+  if (!s->walls || s->nbr == 0) return NAT_OK;
+  const int grid = std::min((s->nbr + 255) / 256, 152 * 8);
+  if (s->spec.precision == NAT_FP64) {
+    k_wall_rows<double><<<grid, 256, 0, s->stream>>>(s->nbr, s->d_br_dst, s->d_br_ptr, s->d_br_col, s->d_br_w,
+                                                     s->d_br_c, g_pop ? 2 : 0, (const double*)in, (double*)out);
+  } else {
+    k_wall_rows<float><<<grid, 256, 0, s->stream>>>(s->nbr, s->d_br_dst, s->d_br_ptr, s->d_br_col, s->d_br_wf,
+                                                    s->d_br_c, g_pop ? 3 : 1, (const float*)in, (float*)out);
+  }
+  CK(cudaGetLastError(), "wall rows kernel");
+  s->launches++;
+  return NAT_OK;
+}
+
 int upload_rest(nat_solver* s) {
   // the rest state is stored after the two doubles of the reduction buffer
   CK(cudaMemcpyAsync(s->red + 2, s->rest, sizeof(double) * s->Q, cudaMemcpyHostToDevice,
@@ -948,6 +1245,10 @@ extern "C" {
 
 const char* nat_version(void) { return "natgpu 0.1 (sm_103a)"; }
 
+static int launch_collide(nat_solver* s, int in_init);
+static int launch_walls(nat_solver* s);
+static int launch_wall_nodes(nat_solver* s, int write_macro);
+
 int nat_destroy(nat_solver* s) {
   if (!s) return NAT_OK;
   cudaFree(s->f[0]);
@@ -962,6 +1263,13 @@ int nat_destroy(nat_solver* s) {
   cudaFree(s->g[1]);
   cudaFree(s->T);
   cudaFree(s->mask);
+  cudaFree(s->d_br_dst);
+  cudaFree(s->d_br_ptr);
+  cudaFree(s->d_br_col);
+  cudaFree(s->d_br_w);
+  cudaFree(s->d_br_wf);
+  cudaFree(s->d_br_c);
+  cudaFree(s->d_bn_node);
   delete s;
   return NAT_OK;
 }
@@ -975,6 +1283,10 @@ static int setup_dt(nat_solver* s, double dt) {
   s->tau = s->spec.viscosity / (dt * s->cs2_scaled) + 0.5;
   int rc = build_tables(s, hs);
   if (rc) return rc;
+  if (s->walls) {
+    rc = build_wall_rows(s);
+    if (rc) return rc;
+  }
   if (s->thermal) return setup_thermal_tables(s);
   int Rm[3] = {s->h_tab.Rmax[0], s->h_tab.Rmax[1], s->h_tab.Rmax[2]};
   s->smem_step = step_smem_bytes(s->spec.precision, Rm, s->B);
@@ -1077,9 +1389,14 @@ int nat_create(const nat_spec* spec, nat_solver** out) {
     if (spec->cells[a] < 1) return bad("cells must be >= 1");
     if (!(spec->length[a] > 0)) return bad("length must be > 0");
     if (!spec->periodic[a]) {
-      fail(s, NAT_ERR_UNSUPPORTED, "non-periodic boundaries are not supported");
-      *out = s;
-      return NAT_ERR_UNSUPPORTED;
+      if (spec->topology != NAT_TOPO_DG) {
+        fail(s, NAT_ERR_UNSUPPORTED, "wall boundaries need the DG node topology");
+        *out = s;
+        return NAT_ERR_UNSUPPORTED;
+      }
+      // walls default to bounce-back at rest (VelocityNeqBounceBack, u = 0)
+      s->walls = true;
+      s->bc[2 * a] = s->bc[2 * a + 1] = NAT_BC_VELOCITY_BOUNCE_BACK;
     }
   }
   int coll;
@@ -1270,12 +1587,20 @@ int nat_stream(nat_solver* s, double t, double* dt_out) {
   if (!s) return NAT_ERR_INVALID_ARG;
   int rc = s->thermal ? launch_thermal(s, false, 0) : launch_step(s, s->ks_stream, 0, 0);
   if (rc) return rc;
+  rc = launch_walls(s);
+  if (rc) return rc;
   if (dt_out) *dt_out = s->dt;
   return NAT_OK;
 }
 
 int nat_collide(nat_solver* s, int in_init) {
   if (!s) return NAT_ERR_INVALID_ARG;
+  int rc = launch_collide(s, in_init);
+  if (rc) return rc;
+  return nat_status(s);
+}
+
+static int launch_collide(nat_solver* s, int in_init) {
   if (s->thermal) {
     if (s->spec.precision == NAT_FP64)
       CK(launch_thermal_collide(thermal_point_params<double>(s, in_init, s->tm), grid_for(s->n_dev), s->stream),
@@ -1284,14 +1609,69 @@ int nat_collide(nat_solver* s, int in_init) {
       CK(launch_thermal_collide(thermal_point_params<float>(s, in_init, s->tmf), grid_for(s->n_dev), s->stream),
          "two-population collide launch");
     s->launches++;
-    return nat_status(s);
+    return NAT_OK;
   }
   StepParams P = step_params(s, s->f[s->cur], s->f[s->cur], 1, 1, in_init);
   void* args[] = {&P};
   CK(cudaLaunchKernel(s->ks_coll.collide, dim3(grid_for(s->n_dev)), dim3(256), args, 0, s->stream),
      "collide launch");
   s->launches++;
-  return nat_status(s);
+  return NAT_OK;
+}
+
+// Fused step of the wall nodes, after the lattice-wide fused kernel of the
+// same step (reads the pre-step buffer, overwrites the wall nodes).
+static int launch_wall_nodes(nat_solver* s, int write_macro) {
+  if (!s->walls || s->nbn == 0) return NAT_OK;
+  if (s->thermal) {
+    // the step's buffers: launch_thermal toggled cur, so swap in and out
+    cudaError_t e;
+    if (s->spec.precision == NAT_FP64) {
+      ThermalStepT<double> P = thermal_step_params<double>(s, write_macro, s->tt, s->tm);
+      P.f_in = static_cast<const double*>(s->f[1 - s->cur]);
+      P.g_in = static_cast<const double*>(s->g[1 - s->cur]);
+      P.f_out = static_cast<double*>(s->f[s->cur]);
+      P.g_out = static_cast<double*>(s->g[s->cur]);
+      e = launch_thermal_wall_nodes(P, s->nbn, s->d_bn_node, s->d_br_ptr, s->d_br_col, s->d_br_w, s->d_br_c,
+                                    s->stream);
+    } else {
+      ThermalStepT<float> P = thermal_step_params<float>(s, write_macro, s->ttf, s->tmf);
+      P.f_in = static_cast<const float*>(s->f[1 - s->cur]);
+      P.g_in = static_cast<const float*>(s->g[1 - s->cur]);
+      P.f_out = static_cast<float*>(s->f[s->cur]);
+      P.g_out = static_cast<float*>(s->g[s->cur]);
+      e = launch_thermal_wall_nodes(P, s->nbn, s->d_bn_node, s->d_br_ptr, s->d_br_col, s->d_br_wf, s->d_br_c,
+                                    s->stream);
+    }
+    if (e != cudaSuccess) return cuda_fail(s, e, "two-population wall nodes");
+    s->launches++;
+    return NAT_OK;
+  }
+  // the step's buffers: launch_* toggled cur, so the input is the other one
+  StepParams P = step_params(s, s->f[1 - s->cur], s->f[s->cur], 1, write_macro, 0);
+  void* args[2];
+  WallNodes<double> W64;
+  WallNodes<float> W32;
+  args[0] = &P;
+  if (s->spec.precision == NAT_FP64) {
+    W64 = {s->nbn, s->d_bn_node, s->d_br_ptr, s->d_br_col, s->d_br_w, s->d_br_c, 0};
+    args[1] = &W64;
+  } else {
+    W32 = {s->nbn, s->d_bn_node, s->d_br_ptr, s->d_br_col, s->d_br_wf, s->d_br_c, 1};
+    args[1] = &W32;
+  }
+  CK(cudaLaunchKernel(s->ks_coll.wallnode, dim3((s->nbn + 127) / 128), dim3(128), args, 0, s->stream),
+     "wall nodes launch");
+  s->launches++;
+  return NAT_OK;
+}
+
+// The wall rows of the buffers just streamed (f, and g for the two-population model).
+static int launch_walls(nat_solver* s) {
+  if (!s->walls) return NAT_OK;
+  int rc = launch_wall_rows(s, s->f[1 - s->cur], s->f[s->cur], false);
+  if (!rc && s->thermal) rc = launch_wall_rows(s, s->g[1 - s->cur], s->g[s->cur], true);
+  return rc;
 }
 
 int nat_step_async(nat_solver* s, int n_steps, int write_macro) {
@@ -1300,6 +1680,8 @@ int nat_step_async(nat_solver* s, int n_steps, int write_macro) {
     const int wm = (write_macro && k == n_steps - 1) ? 1 : 0;
     int rc = s->thermal ? launch_thermal(s, true, wm)
                         : (s->use_v2 ? launch_v2(s, wm) : launch_step(s, s->ks_coll, 1, wm));
+    // wall nodes: redone from their sparse rows (fused stream + collide)
+    if (!rc && s->walls) rc = launch_wall_nodes(s, wm);
     if (rc) return rc;
   }
   return NAT_OK;
@@ -1478,6 +1860,17 @@ int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* t
     *threads = k == 2 ? s->v2.nth : (k == 7 ? 32 * s->row.g * s->row.wy : (row ? 32 * s->row.wy * s->row.wz : STEP_THREADS));
   if (smem_bytes) *smem_bytes = (int64_t)(k == 2 ? s->v2.smem : (row ? s->row.smem : s->smem_step));
   return NAT_OK;
+}
+
+int nat_set_boundary(nat_solver* s, int face, int kind, const double u_wall[3]) {
+  if (!s || face < 0 || face >= 2 * s->D) return NAT_ERR_INVALID_ARG;
+  if (s->spec.periodic[face / 2])
+    return fail(s, NAT_ERR_INVALID_ARG, "face %d belongs to a periodic axis", face);
+  if (kind != NAT_BC_VELOCITY_BOUNCE_BACK && kind != NAT_BC_DO_NOTHING)
+    return fail(s, NAT_ERR_INVALID_ARG, "unknown boundary kind %d", kind);
+  s->bc[face] = kind;
+  for (int a = 0; a < 3; ++a) s->uw[face][a] = (u_wall && kind == NAT_BC_VELOCITY_BOUNCE_BACK) ? u_wall[a] : 0.0;
+  return build_wall_rows(s);
 }
 
 int nat_set_thermal(nat_solver* s, const nat_thermal* t) {

@@ -315,6 +315,71 @@ __global__ void __launch_bounds__(NT) k_sl_step(const StepParams P) {
   }
 }
 
+// Rows of the streaming operator of the wall nodes (nodes with a departure
+// path that meets a wall face), built on the host: Q - 1 rows per node,
+// row k (Q - 1) + alpha - 1 holding sum_j w_j f_in[col_j] + cst[4 row + slot].
+template <class Real>
+struct WallNodes {
+  int nbn;
+  const int* node;
+  const int* ptr;
+  const int* col;
+  const Real* w;
+  const double* cst;
+  int slot;
+};
+
+// Fused step of the wall nodes: gather their streamed values through the
+// sparse rows, collide, write f (and rho/u on output steps).  Runs after the
+// fused kernel of the whole lattice and overwrites the wall nodes, whose
+// periodic-window values there are not the wall's.
+template <class S, class Real, int COLL>
+__global__ void __launch_bounds__(128) k_wall_nodes(const StepParams P, const WallNodes<Real> W) {
+  constexpr bool DEV = sizeof(Real) == 4;
+  constexpr int Q = S::Q;
+  const long long n = P.n;
+  const Real* __restrict__ fin = static_cast<const Real*>(P.f_in);
+  Real* __restrict__ fout = static_cast<Real*>(P.f_out);
+  int bad = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < W.nbn; k += gridDim.x * blockDim.x) {
+    const int node = W.node[k];
+    Real v[Q];
+    v[0] = fin[node];
+#pragma unroll
+    for (int a = 1; a < Q; ++a) {
+      const int r = k * (Q - 1) + a - 1;
+      Real acc = Real(W.cst[4 * r + W.slot]);
+      for (int j = W.ptr[r]; j < W.ptr[r + 1]; ++j) acc = fma(W.w[j], fin[W.col[j]], acc);
+      v[a] = acc;
+    }
+    Real u[3] = {0, 0, 0};
+    Real rho = Real(1);
+    Real pre[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) pre[q] = v[q];
+    if constexpr (COLL == COLL_BGK) {
+      rho = collide_bgk<S, DEV, DEV>(v, Real(1) / Real(P.tau), u, false);
+      if constexpr (DEV) conserve<S>(v, pre);
+    } else if constexpr (COLL == COLL_BGK_INC) {
+      rho = collide_bgk_inc<DEV, DEV>(v, Real(1) / Real(P.tau), u, false);
+    } else if constexpr (COLL == COLL_KBC) {
+      rho = collide_kbc<S, DEV, DEV>(v, Real(P.tau), u, false);
+      if constexpr (DEV) conserve<S>(v, pre);
+    }
+    (void)pre;
+    if (!(rho >= Real(1e-10))) bad |= (rho != rho) ? ST_NAN : ST_DENSITY;
+    if (P.write_macro) {
+      P.rho[node] = (double)rho;
+      P.u[node] = (double)u[0] * P.scaling;
+      P.u[n + node] = (double)u[1] * P.scaling;
+      if constexpr (S::D == 3) P.u[2 * n + node] = (double)u[2] * P.scaling;
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) fout[(long long)q * n + node] = v[q];
+  }
+  if (bad) atomicOr(P.status, bad);
+}
+
 // Collision only (CollisionModel::collideAll on the device state), in place.
 template <class S, class Real, int COLL>
 __global__ void __launch_bounds__(256) k_collide(const StepParams P) {

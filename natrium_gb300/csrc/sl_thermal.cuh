@@ -439,6 +439,55 @@ __global__ void __launch_bounds__(32 * TH_WARPS, (sizeof(Real) == 4 ? 2 : 1))
   }
 }
 
+// Fused step of the wall nodes (nodes with a departure path that meets a
+// wall face): f and g gathered through the host-built rows of the node
+// (row k (Q - 1) + alpha - 1; constants: slot 0 / 1 for f in FP64 / FP32
+// deviation storage, 2 / 3 for g), relaxWithG, one write.  Runs after the
+// fused kernel of the whole lattice and overwrites the wall nodes.
+template <class Real>
+__global__ void __launch_bounds__(128) k_thermal_wall_nodes(const __grid_constant__ ThermalStepT<Real> P, int nbn,
+                                                            const int* __restrict__ bnode,
+                                                            const int* __restrict__ ptr,
+                                                            const int* __restrict__ col, const Real* __restrict__ w,
+                                                            const double* __restrict__ cst) {
+  constexpr bool DEV = sizeof(Real) == 4;
+  const int n = P.n;
+  int bad = 0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nbn; k += gridDim.x * blockDim.x) {
+    const int node = bnode[k];
+    Real f[TH_Q], g[TH_Q];
+    f[0] = P.f_in[node];
+    g[0] = P.g_in[node];
+#pragma unroll
+    for (int a = 1; a < TH_Q; ++a) {
+      const int r = k * (TH_Q - 1) + a - 1;
+      Real af = Real(cst[4 * r + (DEV ? 1 : 0)]), ag = Real(cst[4 * r + (DEV ? 3 : 2)]);
+      for (int j = ptr[r]; j < ptr[r + 1]; ++j) {
+        af = fma(w[j], P.f_in[col[j]], af);
+        ag = fma(w[j], P.g_in[col[j]], ag);
+      }
+      f[a] = af;
+      g[a] = ag;
+    }
+    Real ux = Real(0), uy = Real(0);
+    double rho, T, kn;
+    bad |= thermal_relax<Real>(P.M, f, g, false, ux, uy, rho, T, kn);
+    if (P.write_macro) {
+      P.rho[node] = rho;
+      P.u[node] = (double)ux * P.M.scaling;
+      P.u[n + node] = (double)uy * P.M.scaling;
+      P.T[node] = T;
+      P.mask[node] = kn;
+    }
+#pragma unroll
+    for (int q = 0; q < TH_Q; ++q) {
+      P.f_out[(long long)q * n + node] = f[q];
+      P.g_out[(long long)q * n + node] = g[q];
+    }
+  }
+  if (bad) atomicOr(P.status, bad);
+}
+
 // Collision only (CollisionOperator::collideAll(f, g, ...)), in place.
 template <class Real>
 __global__ void __launch_bounds__(256) k_thermal_collide(const __grid_constant__ ThermalPointT<Real> P) {

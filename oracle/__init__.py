@@ -40,7 +40,11 @@ def build(force: bool = False) -> str:
 
 class _Mesh(C.Structure):
     _fields_ = [("dim", C.c_int), ("N", C.c_int * 3), ("p", C.c_int), ("dg", C.c_int),
-                ("L", C.c_double * 3)]
+                ("L", C.c_double * 3), ("bc", C.c_int * 6), ("uw", (C.c_double * 3) * 6)]
+
+
+# boundary kinds of the six faces x-, x+, y-, y+, z-, z+
+BC_PERIODIC, BC_VELOCITY_BOUNCE_BACK, BC_DO_NOTHING = 0, 1, 2
 
 
 _lib = None
@@ -69,6 +73,9 @@ def lib():
         L.orc_sl_lifetime_hits.argtypes = [C.c_void_p]
         L.orc_sl_csr.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int32), dp]
         L.orc_sl_stream.argtypes = [C.c_void_p, dp, dp, C.c_int]
+        L.orc_sl_csr_dirs.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int32)]
+        L.orc_sl_bconst.argtypes = [C.c_void_p, C.c_int, dp]
+        L.orc_sl_wall_hits.argtypes = [C.c_void_p]
         L.orc_collide_bgk.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int64, dp, dp, dp, C.c_int, C.c_int]
         L.orc_equilibrium.argtypes = [C.c_int, C.c_double, C.c_int64, dp, dp, dp]
         L.orc_bgk_collide_single_point.argtypes = [C.c_int, C.c_double, C.c_double, dp]
@@ -166,6 +173,8 @@ class Mesh:
     p: int
     dg: bool = False
     L: tuple = (2 * math.pi, 2 * math.pi, 2 * math.pi)
+    bc: tuple = (0, 0, 0, 0, 0, 0)          # per face x-, x+, y-, y+, z-, z+: BC_*
+    uw: tuple = ((0.0, 0.0, 0.0),) * 6      # wall velocity of bounce-back faces (scaled)
 
     def c(self) -> _Mesh:
         m = _Mesh()
@@ -175,6 +184,10 @@ class Mesh:
             m.L[a] = float(self.L[a]) if a < self.dim else 1.0
         m.p = self.p
         m.dg = 1 if self.dg else 0
+        for f in range(6):
+            m.bc[f] = int(self.bc[f])
+            for a in range(3):
+                m.uw[f][a] = float(self.uw[f][a])
         return m
 
     def nodes_per_axis(self, a: int) -> int:
@@ -225,6 +238,21 @@ class SLOperator:
     @property
     def lifetime_hits(self) -> int:
         return lib().orc_sl_lifetime_hits(self._h)
+
+    @property
+    def wall_hits(self) -> int:
+        return lib().orc_sl_wall_hits(self._h)
+
+    def csr_dirs(self, alpha: int) -> np.ndarray:
+        nnz = lib().orc_sl_nnz(self._h, alpha)
+        d = np.zeros(max(nnz, 1), dtype=np.int32)
+        lib().orc_sl_csr_dirs(self._h, alpha, d.ctypes.data_as(C.POINTER(C.c_int32)))
+        return d[:nnz]
+
+    def bconst(self, alpha: int) -> np.ndarray:
+        b = np.zeros(self.n)
+        lib().orc_sl_bconst(self._h, alpha, _dp(b))
+        return b
 
     def stream(self, f: np.ndarray, nthreads: int = 1) -> np.ndarray:
         f = np.ascontiguousarray(f, dtype=np.float64)

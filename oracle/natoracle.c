@@ -227,12 +227,19 @@ double orc_lagrange(int p, const double* xi, int j, double x) {
 /* Cartesian mesh, reference node numbering                                 */
 /* ------------------------------------------------------------------------ */
 
+/* Boundary kinds of the six box faces (x-, x+, y-, y+, z-, z+). */
+#define ORC_BC_PERIODIC 0
+#define ORC_BC_VELOCITY_BOUNCE_BACK 1 /* boundaries/VelocityNeqBounceBack */
+#define ORC_BC_DO_NOTHING 2           /* boundaries/DoNothingBoundary */
+
 typedef struct {
   int dim;
   int N[3];
   int p;
   int dg; /* 0: FE_Q (the reference's semi-Lagrangian element), 1: FE_DGQ */
   double L[3];
+  int bc[6];       /* per face: ORC_BC_*; both faces of an axis periodic or neither */
+  double uw[6][3]; /* wall velocity of a bounce-back face (scaled units) */
 } orc_mesh;
 
 static int nodes_per_axis(const orc_mesh* m, int a) {
@@ -361,15 +368,22 @@ typedef struct {
   int Q, D;
   int64_t n;
   int64_t* rowptr[32]; /* per streamed direction alpha = 1..Q-1 */
-  int32_t* col[32];
+  int32_t* col[32];    /* source node */
+  int32_t* sdir[32];   /* source direction (alpha itself unless a wall reversed the path) */
   double* val[32];
+  double* bconst[32];  /* per row: wall-velocity term of bounce-back hits (NULL: none) */
   int64_t nnz[32];
   int n_lifetime_hits;
+  int n_wall_hits;
 } orc_sl;
 
+/* LagrangianPathTracker: destination (dest, alpha), the direction whose
+ * population is currently followed (cdir), and the do-nothing flag. */
 typedef struct {
   int64_t dest;
   int alpha;
+  int cdir;
+  int hit_dn;
   int cell[3];
   double cur[3], dep[3];
   int life;
@@ -379,11 +393,12 @@ typedef struct {
 typedef struct {
   int64_t* row;
   int32_t* col;
+  int32_t* sdir;
   double* val;
   int64_t size, cap;
 } coo;
 
-static int coo_push(coo* c, int64_t r, int32_t col, double v) {
+static int coo_push(coo* c, int64_t r, int32_t col, int32_t sdir, double v) {
   if (c->size == c->cap) {
     int64_t nc = c->cap ? 2 * c->cap : 1024;
     int64_t* nr = (int64_t*)realloc(c->row, nc * sizeof(int64_t));
@@ -392,6 +407,9 @@ static int coo_push(coo* c, int64_t r, int32_t col, double v) {
     int32_t* ncol = (int32_t*)realloc(c->col, nc * sizeof(int32_t));
     if (!ncol) return ORC_ERR_OOM;
     c->col = ncol;
+    int32_t* nsd = (int32_t*)realloc(c->sdir, nc * sizeof(int32_t));
+    if (!nsd) return ORC_ERR_OOM;
+    c->sdir = nsd;
     double* nv = (double*)realloc(c->val, nc * sizeof(double));
     if (!nv) return ORC_ERR_OOM;
     c->val = nv;
@@ -399,6 +417,7 @@ static int coo_push(coo* c, int64_t r, int32_t col, double v) {
   }
   c->row[c->size] = r;
   c->col[c->size] = col;
+  c->sdir[c->size] = sdir;
   c->val[c->size] = v;
   c->size++;
   return ORC_OK;
@@ -410,7 +429,9 @@ void orc_sl_free(orc_sl* s) {
   for (a = 0; a < 32; a++) {
     free(s->rowptr[a]);
     free(s->col[a]);
+    free(s->sdir[a]);
     free(s->val[a]);
+    free(s->bconst[a]);
   }
   free(s);
 }
@@ -421,7 +442,13 @@ void orc_sl_free(orc_sl* s) {
  * cell order that holds it), its departure points x - dt e_alpha are followed
  * across faces (periodic faces shift the points by the box length), and the
  * FE shape values of the cell that holds the departure point become the row.
- * Only periodic boxes are supported here (the configurations' boundaries). */
+ * Non-periodic faces (SemiLagrangian.cpp:354-399):
+ *   VelocityNeqBounceBack: the followed direction is reversed, the path
+ *     continues from the wall point for the remaining length, and the hit adds
+ *     2 w_alpha rho_w (e_alpha . u_w) / c_s^2 (rho_w = 1) to the destination
+ *     (boundaries/VelocityNeqBounceBack.cpp:137-194);
+ *   DoNothingBoundary: the path restarts at the destination and runs the
+ *     other way (x + dt e_alpha); the population stays alpha. */
 orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
                         double dt) {
   int D, Q, a, alpha;
@@ -435,6 +462,7 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
   int c_iter;
   double* vals = NULL;
   double h[3] = {1, 1, 1};
+  int opp[32];
 
   if (orc_stencil(stencil, scaling, &D, &Q, e, w, &cs2, &vmax) != ORC_OK)
     return NULL;
@@ -445,6 +473,16 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
     h[a] = m->L[a] / m->N[a];
   }
   orc_gl_points(p, xi);
+  for (alpha = 0; alpha < Q; alpha++) {
+    int j, k;
+    opp[alpha] = 0;
+    for (j = 0; j < Q; j++) {
+      int same = 1;
+      for (k = 0; k < 3; k++)
+        if (e[3 * j + k] != -e[3 * alpha + k]) same = 0;
+      if (same) opp[alpha] = j;
+    }
+  }
   s = (orc_sl*)calloc(1, sizeof(orc_sl));
   if (!s) return NULL;
   s->Q = Q;
@@ -485,6 +523,8 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
         tracker el;
         el.dest = g;
         el.alpha = alpha;
+        el.cdir = alpha;
+        el.hit_dn = 0;
         el.life = 0;
         for (a = 0; a < 3; a++) {
           el.cell[a] = cc[a];
@@ -495,7 +535,7 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
           el.life++;
           if (el.life > 50) {
             /* SemiLagrangian.cpp:252-271: identity entry */
-            if (coo_push(&buf[alpha], g, (int32_t)g, 1.0)) goto fail;
+            if (coo_push(&buf[alpha], g, (int32_t)g, alpha, 1.0)) goto fail;
             s->n_lifetime_hits++;
             break;
           }
@@ -503,6 +543,7 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
           for (a = 0; a < D; a++) lo[a] = el.cell[a] * h[a];
           int face = orc_face_crossed_first(D, lo, h, el.cur, el.dep, pb, &lam);
           if (face == -1) {
+            if (el.hit_dn) el.cdir = opp[el.cdir]; /* SemiLagrangian.cpp:312-316 */
             /* found: shape values of the cell at the departure point
              * (SemiLagrangianTools.cpp:15-64, snap to [0,1] at 1e-10) */
             double l1[3][16];
@@ -531,7 +572,7 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
                 tt /= (p + 1);
               }
               int64_t src = cell_node_index(m, el.cell, ll);
-              if (coo_push(&buf[alpha], g, (int32_t)src, vals[lj])) goto fail;
+              if (coo_push(&buf[alpha], g, (int32_t)src, el.cdir, vals[lj])) goto fail;
             }
             break;
           }
@@ -539,6 +580,43 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
           int upper = face % 2;
           int at_boundary =
               upper ? (el.cell[ax] == m->N[ax] - 1) : (el.cell[ax] == 0);
+          if (at_boundary && m->bc[face] == ORC_BC_VELOCITY_BOUNCE_BACK) {
+            /* SemiLagrangian.cpp:357-386: reverse the followed direction,
+             * continue from the wall point for the remaining length */
+            double dist = 0.0, ve = 0.0, exu = 0.0;
+            el.cdir = opp[el.cdir];
+            for (a = 0; a < D; a++) {
+              dist += (el.dep[a] - pb[a]) * (el.dep[a] - pb[a]);
+              ve += e[3 * el.cdir + a] * e[3 * el.cdir + a];
+            }
+            dist = sqrt(dist);
+            ve = sqrt(ve);
+            for (a = 0; a < D; a++) {
+              el.cur[a] = pb[a];
+              el.dep[a] = el.cur[a] - e[3 * el.cdir + a] * dist / ve;
+            }
+            /* VelocityNeqBounceBack.cpp:168-192, rho = 1, scaled e and c_s^2 */
+            for (a = 0; a < D; a++) exu += m->uw[face][a] * e[3 * alpha + a];
+            if (!s->bconst[alpha]) {
+              s->bconst[alpha] = (double*)calloc((size_t)n, sizeof(double));
+              if (!s->bconst[alpha]) goto fail;
+            }
+            s->bconst[alpha][g] += 2 * w[alpha] * 1.0 * exu / cs2;
+            s->n_wall_hits++;
+            continue;
+          }
+          if (at_boundary && m->bc[face] == ORC_BC_DO_NOTHING) {
+            /* SemiLagrangian.cpp:388-399: restart at the destination and
+             * follow the opposite direction */
+            for (a = 0; a < D; a++) {
+              el.cur[a] = el.dep[a] + dt * e[3 * el.cdir + a];
+              el.dep[a] = el.cur[a] + dt * e[3 * el.cdir + a];
+            }
+            el.cdir = opp[el.cdir];
+            el.hit_dn = 1;
+            s->n_wall_hits++;
+            continue;
+          }
           for (a = 0; a < D; a++) el.cur[a] = pb[a];
           if (at_boundary) {
             /* periodic face (SemiLagrangian.cpp:336-353): translate the
@@ -566,9 +644,10 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
     for (k = 0; k < n; k++) cnt[k + 1] += cnt[k];
     s->rowptr[alpha] = cnt;
     s->col[alpha] = (int32_t*)malloc(sizeof(int32_t) * (c->size + 1));
+    s->sdir[alpha] = (int32_t*)malloc(sizeof(int32_t) * (c->size + 1));
     s->val[alpha] = (double*)malloc(sizeof(double) * (c->size + 1));
     int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (n + 1));
-    if (!s->col[alpha] || !s->val[alpha] || !fill) {
+    if (!s->col[alpha] || !s->sdir[alpha] || !s->val[alpha] || !fill) {
       free(fill);
       goto fail;
     }
@@ -577,12 +656,14 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
       int64_t r = c->row[k];
       int64_t pos = fill[r]++;
       s->col[alpha][pos] = c->col[k];
+      s->sdir[alpha][pos] = c->sdir[k];
       s->val[alpha][pos] = c->val[k];
     }
     free(fill);
     s->nnz[alpha] = c->size;
     free(c->row);
     free(c->col);
+    free(c->sdir);
     free(c->val);
     memset(c, 0, sizeof(coo));
   }
@@ -593,6 +674,7 @@ fail:
   for (a = 0; a < 32; a++) {
     free(buf[a].row);
     free(buf[a].col);
+    free(buf[a].sdir);
     free(buf[a].val);
   }
   free(vals);
@@ -620,8 +702,22 @@ int orc_sl_csr(const orc_sl* s, int alpha, int64_t* rowptr, int32_t* col,
 /* SemiLagrangian::stream (SemiLagrangian.h:150-161): f_old = f, then
  * fStream <- A * f_old.fStream (block diagonal for periodic boxes); f_0 is
  * not streamed.  f_old / f_new: Q blocks of n doubles. */
+static int sl_stream(const orc_sl* s, const double* f_old, double* f_new, int nthreads, int wall_terms);
+
 int orc_sl_stream(const orc_sl* s, const double* f_old, double* f_new,
                   int nthreads) {
+  return sl_stream(s, f_old, f_new, nthreads, 1);
+}
+
+/* The second population of the compressible model goes through the same
+ * matrix (CompressibleCFDSolver::gStream, CompressibleCFDSolver.h:279-314)
+ * without the wall-velocity terms: SemiLagrangianBoundaryHandler::apply only
+ * changes f (SemiLagrangianBoundaryHandler.cpp:27-32, VelocityNeqBounceBack.cpp:190-193). */
+int orc_sl_stream_g(const orc_sl* s, const double* g_old, double* g_new, int nthreads) {
+  return sl_stream(s, g_old, g_new, nthreads, 0);
+}
+
+static int sl_stream(const orc_sl* s, const double* f_old, double* f_new, int nthreads, int wall_terms) {
   int alpha;
   int64_t n = s->n;
   (void)nthreads;
@@ -629,8 +725,9 @@ int orc_sl_stream(const orc_sl* s, const double* f_old, double* f_new,
   for (alpha = 1; alpha < s->Q; alpha++) {
     const int64_t* rp = s->rowptr[alpha];
     const int32_t* cl = s->col[alpha];
+    const int32_t* sd = s->sdir[alpha];
     const double* vl = s->val[alpha];
-    const double* x = f_old + (int64_t)alpha * n;
+    const double* bc = wall_terms ? s->bconst[alpha] : NULL;
     double* y = f_new + (int64_t)alpha * n;
     int64_t r;
 #ifdef _OPENMP
@@ -639,12 +736,32 @@ int orc_sl_stream(const orc_sl* s, const double* f_old, double* f_new,
     for (r = 0; r < n; r++) {
       double acc = 0.0;
       int64_t k;
-      for (k = rp[r]; k < rp[r + 1]; k++) acc += vl[k] * x[cl[k]];
-      y[r] = acc;
+      for (k = rp[r]; k < rp[r + 1]; k++) acc += vl[k] * f_old[(int64_t)sd[k] * n + cl[k]];
+      /* SemiLagrangianBoundaryHandler::apply after the vmult: wall terms */
+      y[r] = bc ? acc + bc[r] : acc;
     }
   }
   return ORC_OK;
 }
+
+/* Source directions of the entries of direction alpha (CSR order). */
+int orc_sl_csr_dirs(const orc_sl* s, int alpha, int32_t* sdir) {
+  if (!s || alpha < 1 || alpha >= s->Q) return ORC_ERR_ARG;
+  memcpy(sdir, s->sdir[alpha], sizeof(int32_t) * s->nnz[alpha]);
+  return ORC_OK;
+}
+
+/* Wall-velocity terms of direction alpha (n values; zeros when none). */
+int orc_sl_bconst(const orc_sl* s, int alpha, double* b) {
+  if (!s || alpha < 1 || alpha >= s->Q) return ORC_ERR_ARG;
+  if (s->bconst[alpha])
+    memcpy(b, s->bconst[alpha], sizeof(double) * s->n);
+  else
+    memset(b, 0, sizeof(double) * s->n);
+  return ORC_OK;
+}
+
+int orc_sl_wall_hits(const orc_sl* s) { return s ? s->n_wall_hits : -1; }
 
 /* ------------------------------------------------------------------------ */
 /* collisions                                                                */
@@ -1379,7 +1496,7 @@ int orc_step_compressible(const orc_sl* s, int stencil, double scaling, double t
   for (k = 0; k < nsteps; k++) {
     orc_sl_stream(s, f, work, nthreads);
     memcpy(f, work, bytes);
-    orc_sl_stream(s, g, work, nthreads);
+    orc_sl_stream_g(s, g, work, nthreads);
     memcpy(g, work, bytes);
     rc = orc_collide_compressible(stencil, scaling, tau, gamma, prandtl, prandtl_set, sutherland_set, quartic,
                                   s->n, f, g, rho, u, T, mask, 0, nthreads);
