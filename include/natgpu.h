@@ -245,6 +245,22 @@ int nat_init_thermal(nat_solver* s, const double* rho_host, const double* u_host
  * velocity comes from the device copy of u, as set by nat_upload_macro);
  * nat_step fuses stream(f), stream(g) and collide into one kernel per step. */
 
+/* ---- checkpoint and output ----------------------------------------------
+ * Checkpoint (solver/Checkpoint.cpp:74-112 writes a status file with
+ * iteration, time, stencil scaling and FE order, and the f vectors): one
+ * binary file with a header (those fields plus the lattice) and f (and g for
+ * NAT_BGK_COMPRESSIBLE) in the reference layout, FP64.  Loading checks that
+ * lattice, stencil, order and scaling are the handle's. */
+int nat_checkpoint_save(nat_solver* s, const char* path, int64_t iteration, double time);
+int nat_checkpoint_load(nat_solver* s, const char* path, int64_t* iteration, double* time);
+
+/* Solution output (CFDSolver.cpp:1001-1069 writes rho, ux, uy[, uz] with
+ * deal.II's DataOut): an ASCII VTK unstructured-grid file whose points are
+ * the lattice nodes (reference layout) and whose cells are the p^D sub-cells
+ * between neighbouring nodes of every element; point data rho, ux, uy[, uz]
+ * and, for NAT_BGK_COMPRESSIBLE, T and shock_sensor, from the last collision. */
+int nat_write_vtu(nat_solver* s, const char* path);
+
 /* Device pointers of the current distribution buffer (Q blocks of n_dev
  * values, double for NAT_FP64 and float (f - w_i) for NAT_FP32_DEV). */
 int nat_device_f(nat_solver* s, void** f_dev);

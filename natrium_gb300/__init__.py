@@ -59,7 +59,7 @@ EXPORTS = [
     "nat_server_create", "nat_server_destroy", "nat_server_submit", "nat_server_step", "nat_server_poll",
     "nat_server_result", "nat_server_stats", "nat_server_last_error", "nat_mass_energy_noalloc",
     "nat_set_thermal", "nat_get_thermal", "nat_upload_g", "nat_download_g", "nat_download_thermal",
-    "nat_init_thermal", "nat_set_boundary",
+    "nat_init_thermal", "nat_set_boundary", "nat_checkpoint_save", "nat_checkpoint_load", "nat_write_vtu",
 ]
 
 
@@ -151,6 +151,9 @@ def load_library(path: str | None = None):
     L.nat_download_thermal.argtypes = [vp, dp, dp]
     L.nat_init_thermal.argtypes = [vp, dp, dp, dp]
     L.nat_set_boundary.argtypes = [vp, C.c_int, C.c_int, dp]
+    L.nat_checkpoint_save.argtypes = [vp, C.c_char_p, C.c_int64, C.c_double]
+    L.nat_checkpoint_load.argtypes = [vp, C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_double)]
+    L.nat_write_vtu.argtypes = [vp, C.c_char_p]
     _lib = L
     return L
 
@@ -348,6 +351,19 @@ class Solver:
         p = C.c_void_p()
         self._check(self._L.nat_device_f(self._h, C.byref(p)))
         return p.value or 0
+
+    # -- checkpoint and output ---------------------------------------------------------
+    def save_checkpoint(self, path: str, iteration: int = 0, time: float = 0.0):
+        self._check(self._L.nat_checkpoint_save(self._h, os.fsencode(path), int(iteration), float(time)))
+
+    def load_checkpoint(self, path: str):
+        """Restore f (and g); returns (iteration, time) of the checkpoint."""
+        it, t = C.c_int64(), C.c_double()
+        self._check(self._L.nat_checkpoint_load(self._h, os.fsencode(path), C.byref(it), C.byref(t)))
+        return it.value, t.value
+
+    def write_vtu(self, path: str):
+        self._check(self._L.nat_write_vtu(self._h, os.fsencode(path)))
 
     # -- wall boundaries -------------------------------------------------------------
     def set_boundary(self, face: int, kind: str = "VELOCITY_BOUNCE_BACK", u_wall=(0.0, 0.0, 0.0)):
