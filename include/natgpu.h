@@ -100,6 +100,16 @@ typedef struct nat_spec {
   double dt;        /* time step; <= 0 selects the CFL rule */
   int collision;    /* NAT_BGK_STANDARD ... */
   int precision;    /* NAT_FP64 or NAT_FP32_DEV */
+  /* MappingQ1 cells (advection/AdvectionOperator.cpp:59-63 picks MappingQ1
+   * when the problem is not Cartesian): NULL = the Cartesian box of `length`;
+   * else the vertices of the structured grid of cells[] cells, x fastest,
+   * (cells[0]+1)(cells[1]+1)[(cells[2]+1)] points of 3 doubles each (z
+   * ignored in 2-D), copied at creation.  Every cell is the multilinear
+   * image of the unit cell; a periodic axis needs one translation vector
+   * between the vertices of its two faces (PeriodicBoundary.cpp:184-270).
+   * The CFL time step then uses the smallest distance between two vertices
+   * of a cell (utilities/CFDSolverUtilities.cpp:69-84). */
+  const double* vertices;
 } nat_spec;
 
 typedef struct nat_solver nat_solver;
@@ -277,7 +287,8 @@ int nat_device_f(nat_solver* s, void** f_dev);
 int nat_set_kernel_variant(nat_solver* s, int variant);
 /* The fused-step kernel in use: 1 generic, 2 tile, 3 row-segment,
  * 5 two-population row-segment kernel (NAT_BGK_COMPRESSIBLE),
- * 6 bulk-copy row-segment kernel, 7 row-group kernel. */
+ * 6 bulk-copy row-segment kernel, 7 row-group kernel, 8 departure-point
+ * kernel of mapped (MappingQ1) meshes. */
 int nat_kernel_variant(const nat_solver* s);
 
 /* Autotuner: times `steps` fused steps with every kernel that applies to

@@ -81,7 +81,7 @@ class _Spec(C.Structure):
         ("dim", C.c_int), ("stencil", C.c_int), ("order", C.c_int), ("topology", C.c_int),
         ("cells", C.c_int * 3), ("length", C.c_double * 3), ("periodic", C.c_int * 3),
         ("scaling", C.c_double), ("viscosity", C.c_double), ("cfl", C.c_double), ("dt", C.c_double),
-        ("collision", C.c_int), ("precision", C.c_int),
+        ("collision", C.c_int), ("precision", C.c_int), ("vertices", C.POINTER(C.c_double)),
     ]
 
 
@@ -180,6 +180,9 @@ class SolverSpec:
     precision: str = "fp64"
     topology: str = "feq"
     periodic: tuple = (True, True, True)  # False: two wall faces on that axis (DG only)
+    # MappingQ1 cells: grid vertices of shape (N0+1, N1+1[, N2+1], dim) indexed
+    # [i, j(, k)]; None = the Cartesian box of `length`
+    vertices: object = None
 
     @property
     def dim(self) -> int:
@@ -201,7 +204,24 @@ class SolverSpec:
         s.dt = float(self.dt)
         s.collision = COLLISIONS[self.collision]
         s.precision = PRECISIONS[self.precision]
+        v = self.vertex_array()
+        if v is not None:
+            s._keep = v  # alive until nat_create has copied it
+            s.vertices = v.ctypes.data_as(C.POINTER(C.c_double))
         return s
+
+    def vertex_array(self):
+        """The vertices in the C layout: x fastest, 3 doubles per vertex."""
+        if self.vertices is None:
+            return None
+        D = self.dim
+        v = np.asarray(self.vertices, dtype=np.float64)
+        shape = tuple(int(self.cells[a]) + 1 for a in range(D))
+        if v.shape != shape + (D,):
+            raise ValueError(f"vertices must have shape {shape + (D,)}, got {v.shape}")
+        out = np.zeros(shape[::-1] + (3,))
+        out[..., :D] = np.transpose(v, tuple(range(D))[::-1] + (D,))
+        return np.ascontiguousarray(out.reshape(-1, 3))
 
 
 class Solver:

@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -88,6 +89,12 @@ struct nat_solver {
   double* d_br_c = nullptr;      // per row: f const, f const (deviation form), g const, g const (deviation)
   int nbn = 0;                   // wall nodes: nodes with a row that meets a wall; their
   int* d_bn_node = nullptr;      // Q - 1 rows are rows k (Q-1) .. k (Q-1) + Q - 2 above
+  // MappingQ1 cells: every node is a "wall node" (all rows sparse), the
+  // Cartesian fused kernels are not used
+  bool mapped = false;
+  std::vector<double> vtx;       // grid vertices, x fastest, 3 doubles each
+  double pv[3][3] = {{0}};       // periodic translation of each axis
+  double* d_mw = nullptr;        // per-node quadrature weight (mass / energy)
 };
 
 namespace {
@@ -439,7 +446,7 @@ struct QuadW {
 };
 
 __global__ void k_mass_energy(const double* __restrict__ rho, const double* __restrict__ u,
-                              Dims d, int D, QuadW qw, double* out) {
+                              Dims d, int D, QuadW qw, const double* __restrict__ node_w, double* out) {
   const long long n = (long long)d.nx * d.ny * d.nz;
   double m = 0, e = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -449,6 +456,7 @@ __global__ void k_mass_energy(const double* __restrict__ rho, const double* __re
     const int z = (int)(i / ((long long)d.nx * d.ny));
     double wgt = qw.w[0][x % qw.period] * qw.w[1][y % qw.period];
     if (D == 3) wgt *= qw.w[2][z % qw.period];
+    if (node_w) wgt = node_w[i];  // mapped cells: per-node weights
     double uu = u[i] * u[i] + u[n + i] * u[n + i];
     if (D == 3) uu += u[2 * n + i] * u[2 * n + i];
     m += wgt * rho[i];
@@ -961,6 +969,184 @@ int face_crossed_first(int D, const double* lo, const double* h, const double* p
   return face;
 }
 
+// ---- MappingQ1: multilinear image of the unit cell from its 2^D vertices ----
+const double* grid_vertex(const nat_solver* s, int i, int j, int k) {
+  const int n0 = s->spec.cells[0] + 1, n1 = s->D > 1 ? s->spec.cells[1] + 1 : 1;
+  return s->vtx.data() + 3 * (((long long)k * n1 + j) * n0 + i);
+}
+
+// x(u) of cell c, and the Jacobian dx_r/du_a when J is not null
+void q1_map(const nat_solver* s, const int* c, const double* u, double* x, double (*J)[3]) {
+  const int D = s->D;
+  for (int r = 0; r < 3; ++r) {
+    x[r] = 0.0;
+    if (J)
+      for (int a = 0; a < 3; ++a) J[r][a] = 0.0;
+  }
+  for (int k = 0; k < (1 << D); ++k) {
+    const int b[3] = {k & 1, (k >> 1) & 1, (k >> 2) & 1};
+    double phi = 1.0, dphi[3];
+    for (int a = 0; a < D; ++a) phi *= b[a] ? u[a] : 1.0 - u[a];
+    for (int a = 0; a < D; ++a) {
+      dphi[a] = b[a] ? 1.0 : -1.0;
+      for (int q = 0; q < D; ++q)
+        if (q != a) dphi[a] *= b[q] ? u[q] : 1.0 - u[q];
+    }
+    const double* v = grid_vertex(s, c[0] + b[0], D > 1 ? c[1] + b[1] : 0, D > 2 ? c[2] + b[2] : 0);
+    for (int r = 0; r < D; ++r) {
+      x[r] += phi * v[r];
+      if (J)
+        for (int a = 0; a < D; ++a) J[r][a] += dphi[a] * v[r];
+    }
+  }
+}
+
+double det3(const double (*M)[3]) {
+  return M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) - M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+         M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+}
+
+double q1_det(int D, const double (*J)[3]) { return D == 2 ? J[0][0] * J[1][1] - J[0][1] * J[1][0] : det3(J); }
+
+// J du = r (Cramer's rule); false for a singular J
+bool q1_solve(int D, const double (*J)[3], const double* r, double* du) {
+  const double det = q1_det(D, J);
+  if (det == 0.0) return false;
+  if (D == 2) {
+    du[0] = (J[1][1] * r[0] - J[0][1] * r[1]) / det;
+    du[1] = (-J[1][0] * r[0] + J[0][0] * r[1]) / det;
+    return true;
+  }
+  for (int col = 0; col < 3; ++col) {
+    double M[3][3];
+    for (int row = 0; row < 3; ++row)
+      for (int a = 0; a < 3; ++a) M[row][a] = a == col ? r[row] : J[row][a];
+    du[col] = det3(M) / det;
+  }
+  return true;
+}
+
+// Unit coordinates of x in cell c (the reference calls
+// MappingQ1::transform_real_to_unit_cell): Newton's method from the cell
+// centre, each step halved (up to 12 times) until the residual decreases;
+// converged once a step is below 1e-14.  False when it cannot converge (the
+// reference's ExcTransformationFailed).
+bool q1_inverse(const nat_solver* s, const int* c, const double* x, double* u) {
+  const int D = s->D;
+  double y[3], J[3][3], r[3] = {0, 0, 0}, res = 0.0;
+  for (int a = 0; a < 3; ++a) u[a] = a < D ? 0.5 : 0.0;
+  q1_map(s, c, u, y, J);
+  for (int a = 0; a < D; ++a) {
+    r[a] = y[a] - x[a];
+    res += r[a] * r[a];
+  }
+  for (int it = 0; it < 100; ++it) {
+    double du[3] = {0, 0, 0}, step = 1.0, stp = 0.0;
+    bool ok = false;
+    if (!q1_solve(D, J, r, du)) return false;
+    for (int a = 0; a < D; ++a) stp += du[a] * du[a];
+    for (int k = 0; k <= 12; ++k, step *= 0.5) {
+      double un[3] = {u[0], u[1], u[2]}, yn[3], Jn[3][3], rn[3] = {0, 0, 0}, rs = 0.0;
+      for (int a = 0; a < D; ++a) un[a] = u[a] - step * du[a];
+      q1_map(s, c, un, yn, Jn);
+      for (int a = 0; a < D; ++a) {
+        rn[a] = yn[a] - x[a];
+        rs += rn[a] * rn[a];
+      }
+      if (rs < res || rs == 0.0) {
+        for (int a = 0; a < D; ++a) {
+          u[a] = un[a];
+          r[a] = rn[a];
+        }
+        memcpy(J, Jn, sizeof(Jn));
+        res = rs;
+        ok = true;
+        break;
+      }
+    }
+    if (!ok) return stp < 1e-24;  // stuck at round-off
+    if (stp * step * step < 1e-28 || res == 0.0) return true;
+  }
+  return false;
+}
+
+// faceCrossedFirstWithoutMapping (SemiLagrangian.cpp:702-757), used when an
+// inverse map fails: each face is the plane through its first vertex with
+// the normal of its first two edges (SemiLagrangianTools.cpp:151-168); the
+// smallest lambda in [0, 1) wins.  Face vertices in the cell numbering
+// bx + 2 by + 4 bz.
+int face_crossed_first_planar(const nat_solver* s, const int* c, const double* p_in, const double* p_out,
+                              double* p_b) {
+  static const int FV2[4][2] = {{0, 2}, {1, 3}, {0, 1}, {2, 3}};
+  static const int FV3[6][3] = {{0, 2, 4}, {1, 3, 5}, {0, 4, 1}, {2, 6, 3}, {0, 1, 2}, {4, 5, 6}};
+  const int D = s->D;
+  double lambda_min = 1.0;
+  int index_min = 0;
+  for (int i = 0; i < 2 * D; ++i) {
+    const double* v[3];
+    for (int k = 0; k < D; ++k) {
+      const int cv = D == 2 ? FV2[i][k] : FV3[i][k];
+      v[k] = grid_vertex(s, c[0] + (cv & 1), c[1] + ((cv >> 1) & 1), D > 2 ? c[2] + ((cv >> 2) & 1) : 0);
+    }
+    double n[3];
+    if (D == 2) {
+      n[0] = v[1][1] - v[0][1];
+      n[1] = -(v[1][0] - v[0][0]);
+    } else {
+      double d1[3], d2[3];
+      for (int a = 0; a < 3; ++a) {
+        d1[a] = v[1][a] - v[0][a];
+        d2[a] = v[2][a] - v[0][a];
+      }
+      n[0] = d1[1] * d2[2] - d1[2] * d2[1];
+      n[1] = d1[2] * d2[0] - d1[0] * d2[2];
+      n[2] = d1[0] * d2[1] - d1[1] * d2[0];
+    }
+    double num = 0.0, den = 0.0;
+    for (int a = 0; a < D; ++a) {
+      num += (p_in[a] - v[0][a]) * n[a];
+      den += (p_in[a] - p_out[a]) * n[a];
+    }
+    const double lam = num / den;
+    if (lam < 0) continue;
+    if (lam < lambda_min) {
+      lambda_min = lam;
+      index_min = i;
+    }
+  }
+  if (lambda_min == 1) return -1;
+  for (int a = 0; a < D; ++a) p_b[a] = p_in[a] + (p_out[a] - p_in[a]) * lambda_min;
+  return index_min;
+}
+
+// faceCrossedFirst with the mapping (SemiLagrangian.cpp:525-699): the face
+// search of the unit cell on the inverse-mapped points, the crossing point
+// mapped back; the planar search when an inverse map fails
+// (SemiLagrangian.cpp:280-288).
+int face_crossed_first_q1(const nat_solver* s, const int* c, const double* p_in, const double* p_out,
+                          double* p_b) {
+  double pi[3] = {0, 0, 0}, po[3] = {0, 0, 0};
+  if (!q1_inverse(s, c, p_in, pi) || !q1_inverse(s, c, p_out, po))
+    return face_crossed_first_planar(s, c, p_in, p_out, p_b);
+  static const double lo[3] = {0, 0, 0}, one[3] = {1, 1, 1};
+  double hu[3] = {0, 0, 0};
+  const int face = face_crossed_first(s->D, lo, one, pi, po, hu);
+  if (face >= 0) q1_map(s, c, hu, p_b, nullptr);
+  return face;
+}
+
+// Position of the node at Gauss-Lobatto point (xi[l0], xi[l1], xi[l2]) of cell c.
+void node_point(const nat_solver* s, const int* c, const int* l, const double* xi, double* x) {
+  x[0] = x[1] = x[2] = 0.0;
+  if (s->mapped) {
+    double u[3] = {0, 0, 0};
+    for (int a = 0; a < s->D; ++a) u[a] = xi[l[a]];
+    q1_map(s, c, u, x, nullptr);
+    return;
+  }
+  for (int a = 0; a < s->D; ++a) x[a] = c[a] * s->h[a] + xi[l[a]] * s->h[a];
+}
+
 int build_wall_rows(nat_solver* s) {
   cudaFree(s->d_br_dst);
   cudaFree(s->d_br_ptr);
@@ -974,7 +1160,7 @@ int build_wall_rows(nat_solver* s) {
   s->d_br_wf = nullptr;
   s->nbr = 0;
   s->nbn = 0;
-  if (!s->walls) return NAT_OK;
+  if (!s->walls && !s->mapped) return NAT_OK;
   HostStencil hs;
   get_host_stencil(s->spec.stencil, &hs, s->spec.scaling);
   const int D = s->D, Q = s->Q, p = s->spec.order, PER = s->period;
@@ -1022,7 +1208,8 @@ int build_wall_rows(nat_solver* s) {
       }
       double lo[3], pb[3];
       for (int a = 0; a < D; ++a) lo[a] = cell[a] * s->h[a];
-      const int face = face_crossed_first(D, lo, s->h, cur, dep, pb);
+      const int face = s->mapped ? face_crossed_first_q1(s, cell, cur, dep, pb)
+                                 : face_crossed_first(D, lo, s->h, cur, dep, pb);
       if (face < 0) break;
       const int ax = face / 2, upper = face % 2;
       const bool at_boundary = upper ? (cell[ax] == N[ax] - 1) : (cell[ax] == 0);
@@ -1055,10 +1242,12 @@ int build_wall_rows(nat_solver* s) {
         continue;
       }
       for (int a = 0; a < D; ++a) cur[a] = pb[a];
-      if (at_boundary) {  // periodic: translate by the box length
-        const double shift = upper ? -s->spec.length[ax] : s->spec.length[ax];
-        cur[ax] += shift;
-        dep[ax] += shift;
+      if (at_boundary) {  // periodic: translate by the axis' period vector
+        for (int a = 0; a < D; ++a) {
+          const double shift = upper ? -s->pv[ax][a] : s->pv[ax][a];
+          cur[a] += shift;
+          dep[a] += shift;
+        }
         cell[ax] = upper ? 0 : N[ax] - 1;
       } else {
         cell[ax] += upper ? 1 : -1;
@@ -1077,11 +1266,12 @@ int build_wall_rows(nat_solver* s) {
     int idx[3] = {(int)(node % s->n_ax[0]), (int)((node / s->n_ax[0]) % s->n_ax[1]),
                   (int)(node / ((long long)s->n_ax[0] * s->n_ax[1]))};
     double x[3] = {0, 0, 0};
-    int own[3] = {0, 0, 0};
+    int own[3] = {0, 0, 0}, loc[3] = {0, 0, 0};
     for (int a = 0; a < D; ++a) {
       own[a] = idx[a] / PER;
-      x[a] = own[a] * s->h[a] + xi[idx[a] % PER] * s->h[a];
+      loc[a] = idx[a] % PER;
     }
+    node_point(s, own, loc, xi, x);
     // a node is a wall node when one of its paths meets a wall; all its rows
     // are then evaluated as sparse rows
     Path paths[32];
@@ -1091,7 +1281,7 @@ int build_wall_rows(nat_solver* s) {
       hits[alpha] = trace(x, own, alpha, paths[alpha]);
       if (hits[alpha] != 0) wall_node = true;
     }
-    if (!wall_node) continue;
+    if (!wall_node && !s->mapped) continue;
     bnodes.push_back((int)node);
     for (int alpha = 1; alpha < Q; ++alpha) {
       const Path& P = paths[alpha];
@@ -1103,13 +1293,19 @@ int build_wall_rows(nat_solver* s) {
       double l1[3][PMAX1];
       for (int a = 0; a < 3; ++a)
         for (int j = 0; j < PMAX1; ++j) l1[a][j] = (a >= D && j == 0) ? 1.0 : 0.0;
+      double ud[3] = {0, 0, 0};
+      if (!identity && s->mapped && !q1_inverse(s, cell, P.dep, ud))
+        return fail(s, NAT_ERR_UNSUPPORTED,
+                    "the inverse map of cell (%d %d %d) failed at a departure point; the mesh is too distorted "
+                    "for this time step",
+                    cell[0], cell[1], cell[2]);
       for (int a = 0; a < D; ++a) {
         if (identity) {
           cell[a] = own[a];
           for (int j = 0; j <= p; ++j) l1[a][j] = (j == idx[a] % PER) ? 1.0 : 0.0;
           continue;
         }
-        double ul = (P.dep[a] - cell[a] * s->h[a]) / s->h[a];
+        double ul = s->mapped ? ud[a] : (P.dep[a] - cell[a] * s->h[a]) / s->h[a];
         if (fabs(ul) < 1e-10) ul = 0.0;
         if (fabs(ul - 1.0) < 1e-10) ul = 1.0;
         for (int j = 0; j <= p; ++j) l1[a][j] = lagrange(p, xi, j, ul);
@@ -1122,8 +1318,10 @@ int build_wall_rows(nat_solver* s) {
         const int lx = li % np1, ly = (li / np1) % np1, lz = D == 3 ? li / (np1 * np1) : 0;
         const double v = l1[0][lx] * l1[1][ly] * (D == 3 ? l1[2][lz] : 1.0);
         if (fabs(v) < 1e-10) continue;  // SemiLagrangian.cpp:483
-        const long long src = ((long long)(cell[2] * PER + lz) * s->n_ax[1] + (cell[1] * PER + ly)) * s->n_ax[0] +
-                              (cell[0] * PER + lx);
+        // the FE_Q node p of the last cell of a periodic axis is node 0
+        const int ix = (cell[0] * PER + lx) % s->n_ax[0], iy = (cell[1] * PER + ly) % s->n_ax[1],
+                  iz = (cell[2] * PER + lz) % s->n_ax[2];
+        const long long src = ((long long)iz * s->n_ax[1] + iy) * s->n_ax[0] + ix;
         col.push_back((int)(sdir * n + src));
         w.push_back(v);
         wrest += v * s->rest[sdir];
@@ -1176,7 +1374,7 @@ int build_wall_rows(nat_solver* s) {
 
 // Overwrite the wall rows of a streamed buffer (f: slot 0/1, g: slot 2 or none).
 int launch_wall_rows(nat_solver* s, const void* in, void* out, bool g_pop) {
-  if (!s->walls || s->nbr == 0) return NAT_OK;
+  if ((!s->walls && !s->mapped) || s->nbr == 0) return NAT_OK;
   const int grid = std::min((s->nbr + 255) / 256, 152 * 8);
   if (s->spec.precision == NAT_FP64) {
     k_wall_rows<double><<<grid, 256, 0, s->stream>>>(s->nbr, s->d_br_dst, s->d_br_ptr, s->d_br_col, s->d_br_w,
@@ -1270,7 +1468,99 @@ int nat_destroy(nat_solver* s) {
   cudaFree(s->d_br_wf);
   cudaFree(s->d_br_c);
   cudaFree(s->d_bn_node);
+  cudaFree(s->d_mw);
   delete s;
+  return NAT_OK;
+}
+
+// MappingQ1 mesh of nat_spec::vertices: copy, check, period vectors, the
+// smallest vertex distance of a cell (utilities/CFDSolverUtilities.cpp:69-84)
+// and the per-node quadrature weights (Gauss-Lobatto weight times det J of
+// every cell holding the node).  The box lengths become the grid's extents.
+static int setup_mapping(nat_solver* s, const double* vertices, double* hmin) {
+  const int D = s->D;
+  const int* N = s->spec.cells;
+  const long long nv = (long long)(N[0] + 1) * (N[1] + 1) * (D == 3 ? N[2] + 1 : 1);
+  s->vtx.assign(vertices, vertices + 3 * nv);
+  for (double v : s->vtx)
+    if (!std::isfinite(v)) return fail(s, NAT_ERR_INVALID_ARG, "vertices must be finite");
+  s->mapped = true;
+  // period vectors: the offset between the vertices of the two faces of an
+  // axis, one vector for all of them on a periodic axis
+  for (int a = 0; a < D; ++a) {
+    const int nb = a == 0 ? 1 : 0, nc = a == 2 ? 1 : 2;
+    const int mb = N[nb] + 1, mc = D > 2 ? N[nc] + 1 : 1;
+    double lo = 1e300, hi = -1e300;
+    for (int ic = 0; ic < mc; ++ic)
+      for (int ib = 0; ib < mb; ++ib) {
+        int i0[3] = {0, 0, 0}, i1[3] = {0, 0, 0};
+        i0[nb] = i1[nb] = ib;
+        if (D > 2) i0[nc] = i1[nc] = ic;
+        i1[a] = N[a];
+        const double* v0 = grid_vertex(s, i0[0], i0[1], i0[2]);
+        const double* v1 = grid_vertex(s, i1[0], i1[1], i1[2]);
+        for (int b = 0; b < D; ++b) {
+          const double d = v1[b] - v0[b];
+          if (ib == 0 && ic == 0)
+            s->pv[a][b] = d;
+          else if (s->spec.periodic[a] && fabs(d - s->pv[a][b]) > 1e-12 * (fabs(d) + 1.0))
+            return fail(s, NAT_ERR_INVALID_ARG, "periodic axis %d: the two faces' vertices differ by more than one "
+                        "translation", a);
+        }
+      }
+    for (long long k = 0; k < nv; ++k) {
+      lo = std::min(lo, s->vtx[3 * k + a]);
+      hi = std::max(hi, s->vtx[3 * k + a]);
+    }
+    s->spec.length[a] = s->spec.periodic[a] ? fabs(s->pv[a][a]) : hi - lo;
+    if (!(s->spec.length[a] > 0)) return fail(s, NAT_ERR_INVALID_ARG, "degenerate vertex grid along axis %d", a);
+    s->h[a] = s->spec.length[a] / N[a];
+  }
+  // cells: positive det J at the corners, smallest vertex distance
+  const int p = s->spec.order, PER = s->period, np1 = p + 1;
+  double xi[PMAX1 + 1], wq[PMAX1 + 1];
+  gl_points(p, xi);
+  gl_weights(p, xi, wq);
+  std::vector<double> mw((size_t)s->n_dev, 0.0);
+  *hmin = 1e300;
+  const int ncz = D == 3 ? N[2] : 1;
+  for (int cz = 0; cz < ncz; ++cz)
+    for (int cy = 0; cy < N[1]; ++cy)
+      for (int cx = 0; cx < N[0]; ++cx) {
+        const int c[3] = {cx, cy, cz};
+        const double* cv[8];
+        for (int k = 0; k < (1 << D); ++k)
+          cv[k] = grid_vertex(s, cx + (k & 1), cy + ((k >> 1) & 1), D > 2 ? cz + ((k >> 2) & 1) : 0);
+        for (int i = 0; i < (1 << D); ++i) {
+          for (int j = i + 1; j < (1 << D); ++j) {
+            double d2 = 0.0;
+            for (int a = 0; a < D; ++a) d2 += (cv[i][a] - cv[j][a]) * (cv[i][a] - cv[j][a]);
+            *hmin = std::min(*hmin, sqrt(d2));
+          }
+          const double u[3] = {(double)(i & 1), (double)((i >> 1) & 1), (double)((i >> 2) & 1)};
+          double x[3], J[3][3];
+          q1_map(s, c, u, x, J);
+          if (!(q1_det(D, J) > 0))
+            return fail(s, NAT_ERR_INVALID_ARG, "cell (%d %d %d) is inverted or degenerate", cx, cy, cz);
+        }
+        const int nloc = D == 3 ? np1 * np1 * np1 : np1 * np1;
+        for (int li = 0; li < nloc; ++li) {
+          const int l[3] = {li % np1, (li / np1) % np1, D == 3 ? li / (np1 * np1) : 0};
+          const double u[3] = {xi[l[0]], xi[l[1]], D == 3 ? xi[l[2]] : 0.0};
+          double x[3], J[3][3];
+          q1_map(s, c, u, x, J);
+          double w = q1_det(D, J);
+          for (int a = 0; a < D; ++a) w *= wq[l[a]];
+          const int ix = (cx * PER + l[0]) % s->n_ax[0], iy = (cy * PER + l[1]) % s->n_ax[1],
+                    iz = (cz * PER + l[2]) % s->n_ax[2];
+          mw[((size_t)iz * s->n_ax[1] + iy) * s->n_ax[0] + ix] += w;
+        }
+      }
+  if (cudaMalloc((void**)&s->d_mw, sizeof(double) * mw.size()) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(s, NAT_ERR_OOM, "cudaMalloc(%zu) failed", sizeof(double) * mw.size());
+  }
+  CK(cudaMemcpy(s->d_mw, mw.data(), sizeof(double) * mw.size(), cudaMemcpyHostToDevice), "node weights");
   return NAT_OK;
 }
 
@@ -1283,7 +1573,7 @@ static int setup_dt(nat_solver* s, double dt) {
   s->tau = s->spec.viscosity / (dt * s->cs2_scaled) + 0.5;
   int rc = build_tables(s, hs);
   if (rc) return rc;
-  if (s->walls) {
+  if (s->walls || s->mapped) {
     rc = build_wall_rows(s);
     if (rc) return rc;
   }
@@ -1445,6 +1735,7 @@ int nat_create(const nat_spec* spec, nat_solver** out) {
       s->n_ax[a] = spec->cells[a] * s->period;
       s->n_ref_ax[a] = dg ? s->n_ax[a] : s->n_ax[a] + 1;
       s->h[a] = spec->length[a] / spec->cells[a];
+      s->pv[a][a] = spec->length[a];
       hmin = std::min(hmin, s->h[a]);
     }
     s->n_dev *= s->n_ax[a];
@@ -1454,7 +1745,12 @@ int nat_create(const nat_spec* spec, nat_solver** out) {
   for (int q = 0; q < s->Q; ++q)
     s->rest[q] = spec->collision == NAT_BGK_INCOMPRESSIBLE ? inc_rest(q) : hs.w[q];
   *out = s;
+  s->spec.vertices = nullptr;  // not retained: the grid is copied
   CK(cudaGetDevice(&s->device), "cudaGetDevice");
+  if (spec->vertices) {
+    int rc = setup_mapping(s, spec->vertices, &hmin);
+    if (rc) return rc;
+  }
   if (s->thermal) return create_thermal(s, hmin);
   int smem_optin = 0;
   CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device),
@@ -1585,7 +1881,18 @@ int nat_upload_macro(nat_solver* s, const double* rho_host, const double* u_host
 int nat_stream(nat_solver* s, double t, double* dt_out) {
   (void)t;
   if (!s) return NAT_ERR_INVALID_ARG;
-  int rc = s->thermal ? launch_thermal(s, false, 0) : launch_step(s, s->ks_stream, 0, 0);
+  int rc = NAT_OK;
+  if (s->mapped) {
+    // every row is a sparse row; the rest population stays
+    s->cur = 1 - s->cur;
+    const size_t es = s->spec.precision == NAT_FP64 ? 8 : 4;
+    CK(cudaMemcpyAsync(s->f[s->cur], s->f[1 - s->cur], es * s->n_dev, cudaMemcpyDeviceToDevice, s->stream),
+       "rest population");
+    if (s->thermal)
+      CK(cudaMemcpyAsync(s->g[s->cur], s->g[1 - s->cur], es * s->n_dev, cudaMemcpyDeviceToDevice, s->stream),
+         "rest population");
+  } else
+    rc = s->thermal ? launch_thermal(s, false, 0) : launch_step(s, s->ks_stream, 0, 0);
   if (rc) return rc;
   rc = launch_walls(s);
   if (rc) return rc;
@@ -1622,7 +1929,7 @@ static int launch_collide(nat_solver* s, int in_init) {
 // Fused step of the wall nodes, after the lattice-wide fused kernel of the
 // same step (reads the pre-step buffer, overwrites the wall nodes).
 static int launch_wall_nodes(nat_solver* s, int write_macro) {
-  if (!s->walls || s->nbn == 0) return NAT_OK;
+  if ((!s->walls && !s->mapped) || s->nbn == 0) return NAT_OK;
   if (s->thermal) {
     // the step's buffers: launch_thermal toggled cur, so swap in and out
     cudaError_t e;
@@ -1668,7 +1975,7 @@ static int launch_wall_nodes(nat_solver* s, int write_macro) {
 
 // The wall rows of the buffers just streamed (f, and g for the two-population model).
 static int launch_walls(nat_solver* s) {
-  if (!s->walls) return NAT_OK;
+  if (!s->walls && !s->mapped) return NAT_OK;
   int rc = launch_wall_rows(s, s->f[1 - s->cur], s->f[s->cur], false);
   if (!rc && s->thermal) rc = launch_wall_rows(s, s->g[1 - s->cur], s->g[s->cur], true);
   return rc;
@@ -1678,10 +1985,14 @@ int nat_step_async(nat_solver* s, int n_steps, int write_macro) {
   if (!s || n_steps < 0) return NAT_ERR_INVALID_ARG;
   for (int k = 0; k < n_steps; ++k) {
     const int wm = (write_macro && k == n_steps - 1) ? 1 : 0;
-    int rc = s->thermal ? launch_thermal(s, true, wm)
-                        : (s->use_v2 ? launch_v2(s, wm) : launch_step(s, s->ks_coll, 1, wm));
+    int rc = NAT_OK;
+    if (s->mapped)
+      s->cur = 1 - s->cur;  // every node is stepped from its sparse rows
+    else
+      rc = s->thermal ? launch_thermal(s, true, wm)
+                      : (s->use_v2 ? launch_v2(s, wm) : launch_step(s, s->ks_coll, 1, wm));
     // wall nodes: redone from their sparse rows (fused stream + collide)
-    if (!rc && s->walls) rc = launch_wall_nodes(s, wm);
+    if (!rc && (s->walls || s->mapped)) rc = launch_wall_nodes(s, wm);
     if (rc) return rc;
   }
   return NAT_OK;
@@ -1730,7 +2041,7 @@ int nat_mass_energy(nat_solver* s, double* mass, double* ke) {
       qw.w[a][c] = a < s->D ? w * s->h[a] : 1.0;
     }
   CK(cudaMemsetAsync(s->red, 0, 2 * sizeof(double), s->stream), "memset");
-  k_mass_energy<<<grid_for(s->n_dev), 256, 0, s->stream>>>(s->rho, s->u, dims_of(s), s->D, qw, s->red);
+  k_mass_energy<<<grid_for(s->n_dev), 256, 0, s->stream>>>(s->rho, s->u, dims_of(s), s->D, qw, s->d_mw, s->red);
   CK(cudaGetLastError(), "reduction kernel");
   s->launches++;
   double h2[2];
@@ -1751,6 +2062,10 @@ int64_t nat_launch_count(const nat_solver* s) { return s ? s->launches : -1; }
 
 int nat_set_kernel_variant(nat_solver* s, int variant) {
   if (!s || variant < 0 || variant > 7 || variant == 5) return NAT_ERR_INVALID_ARG;
+  if (s->mapped) {
+    if (variant == 0) return NAT_OK;
+    return fail(s, NAT_ERR_UNSUPPORTED, "mapped meshes run the departure-point kernel only");
+  }
   if (s->thermal) {
     // one kernel serves the two-population model
     if (variant == 0) return NAT_OK;
@@ -1763,11 +2078,15 @@ int nat_set_kernel_variant(nat_solver* s, int variant) {
   return select_v2(s, coll_selector(s->spec.collision), smem_optin);
 }
 
-int nat_kernel_variant(const nat_solver* s) { return s ? (s->thermal ? 5 : (s->use_v2 ? s->kind : 1)) : -1; }
+int nat_kernel_variant(const nat_solver* s) {
+  if (!s) return -1;
+  if (s->mapped) return 8;
+  return s->thermal ? 5 : (s->use_v2 ? s->kind : 1);
+}
 
 int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
   if (!s || steps < 1) return NAT_ERR_INVALID_ARG;
-  if (s->thermal) {
+  if (s->thermal || s->mapped) {
     if (n_candidates) *n_candidates = 1;
     if (chosen) *chosen = 0;
     return NAT_OK;
@@ -1836,6 +2155,13 @@ int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
 
 int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* threads, int64_t* smem_bytes) {
   if (!s) return NAT_ERR_INVALID_ARG;
+  if (s->mapped) {
+    if (variant) *variant = 8;
+    if (tile_nodes) tile_nodes[0] = tile_nodes[1] = tile_nodes[2] = 1;
+    if (threads) *threads = 128;
+    if (smem_bytes) *smem_bytes = 0;
+    return NAT_OK;
+  }
   if (s->thermal) {
     if (variant) *variant = 5;
     if (tile_nodes) {
@@ -2078,7 +2404,7 @@ int nat_write_vtu(nat_solver* s, const char* path) {
   }
   double xi[PMAX1 + 1];
   gl_points(p, xi);
-  // node coordinates per axis, reference layout
+  // node coordinates per axis, reference layout (Cartesian box)
   std::vector<double> ax[3];
   for (int a = 0; a < 3; ++a) {
     if (a >= D) {
@@ -2123,7 +2449,27 @@ int nat_write_vtu(nat_solver* s, const char* path) {
   fprintf(fp, "<Points>\n<DataArray type=\"Float64\" NumberOfComponents=\"3\" format=\"ascii\">\n");
   for (int k = 0; k < nr[2]; ++k)
     for (int j = 0; j < nr[1]; ++j)
-      for (int i = 0; i < nr[0]; ++i) fprintf(fp, "%.17g %.17g %.17g\n", ax[0][i], ax[1][j], ax[2][k]);
+      for (int i = 0; i < nr[0]; ++i) {
+        if (!s->mapped) {
+          fprintf(fp, "%.17g %.17g %.17g\n", ax[0][i], ax[1][j], ax[2][k]);
+          continue;
+        }
+        // mapped cell: the cell map at the node's Gauss-Lobatto point
+        const int ii[3] = {i, j, k};
+        int c[3] = {0, 0, 0}, l[3] = {0, 0, 0};
+        for (int a = 0; a < D; ++a) {
+          if (dg) {
+            c[a] = ii[a] / (p + 1);
+            l[a] = ii[a] % (p + 1);
+          } else {
+            c[a] = std::min(ii[a] / p, s->spec.cells[a] - 1);
+            l[a] = ii[a] - c[a] * p;
+          }
+        }
+        double x[3];
+        node_point(s, c, l, xi, x);
+        fprintf(fp, "%.17g %.17g %.17g\n", x[0], x[1], x[2]);
+      }
   fprintf(fp, "</DataArray>\n</Points>\n<Cells>\n<DataArray type=\"Int64\" Name=\"connectivity\" format=\"ascii\">\n");
   for (size_t q = 0; q < conn.size(); ++q) fprintf(fp, "%lld%c", conn[q], (q % nv == (size_t)nv - 1) ? '\n' : ' ');
   fprintf(fp, "</DataArray>\n<DataArray type=\"Int64\" Name=\"offsets\" format=\"ascii\">\n");

@@ -74,6 +74,89 @@ def node_coords(cells, order: int, lengths, topology: str = "feq") -> np.ndarray
     return np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
 
 
+def mapped_node_coords(vertices, order: int, topology: str = "feq") -> np.ndarray:
+    """(n_ref, 3) coordinates of the lattice nodes of a MappingQ1 grid: the
+    multilinear map of each cell (vertices of shape (N0+1, N1+1[, N2+1], dim))
+    at its Gauss-Lobatto points; FE_Q nodes on a cell face come from the
+    lower cell except at the last face of an axis."""
+    v = np.asarray(vertices, dtype=np.float64)
+    dim = v.shape[-1]
+    cells = tuple(s - 1 for s in v.shape[:dim])
+    xi = gl_points(order)
+    per = order + 1 if topology == "dg" else order
+    idx = []
+    for a in range(3):
+        if a >= dim:
+            idx.append((np.zeros(1, int), np.zeros(1)))
+            continue
+        n = cells[a] * per + (0 if topology == "dg" else 1)
+        i = np.arange(n)
+        c = np.minimum(i // per, cells[a] - 1)
+        u = xi[i - c * per]
+        idx.append((c, u))
+    out = np.zeros((len(idx[2][0]), len(idx[1][0]), len(idx[0][0]), 3))
+    for k in range(1 << dim):
+        b = [(k >> a) & 1 for a in range(dim)]
+        phi = [(u if b[a] else 1.0 - u) for a, (c, u) in enumerate(idx[:dim])]
+        cidx = [c + b[a] for a, (c, u) in enumerate(idx[:dim])]
+        if dim == 2:
+            w = phi[1][:, None] * phi[0][None, :]
+            vv = v[cidx[0][None, :], cidx[1][:, None]]
+            out[0, :, :, :2] += w[..., None] * vv
+        else:
+            w = phi[2][:, None, None] * phi[1][None, :, None] * phi[0][None, None, :]
+            vv = v[cidx[0][None, None, :], cidx[1][None, :, None], cidx[2][:, None, None]]
+            out[..., :3] += w[..., None] * vv
+    return out.reshape(-1, 3)
+
+
+def wavy_grid(cells, lengths, amplitude: float) -> np.ndarray:
+    """A smoothly deformed periodic grid: the box vertices moved by
+    amplitude * h_a * (1 + 0.3 a) * prod_b sin(2 pi x_b / L_b) along each
+    axis a (zero on every face, so each axis keeps the translation L_a e_a)."""
+    dim = len(cells)
+    axes = [np.linspace(0.0, lengths[a], cells[a] + 1) for a in range(dim)]
+    X = np.stack(np.meshgrid(*axes, indexing="ij"), -1)
+    ph = np.ones(X.shape[:-1])
+    for a in range(dim):
+        ph = ph * np.sin(2 * math.pi * X[..., a] / lengths[a])
+    V = X.copy()
+    for a in range(dim):
+        V[..., a] += amplitude * lengths[a] / cells[a] * (1 + 0.3 * a) * ph
+    return V
+
+
+def lubrication_sine_grid(length: float = 1.0, average_height: float = 0.25, amplitude: float = 0.05,
+                          cell_aspect_ratio: float = 1.0, refinement: int = 2, roughness_height: float = 0.0,
+                          roughness_length_ratio: int = 1) -> np.ndarray:
+    """Vertices of the LubricationSine channel (benchmarks/LubricationSine.cpp:33-54,
+    95-104, LubricationSine.h:80-105): a box [0, L] x [0, H] of
+    L / H / aspect x 1 cells refined `refinement` times, mapped by
+    x -> x + lambda A / (2 pi H) sin(2 pi x / lambda) and
+    y -> y_r(y) / H * (H + A cos(2 pi x' / lambda) + R cos(2 pi x' ratio / lambda)),
+    y_r(y) = H (1/2 + tanh(pi (y / H - 1/2)) / (2 tanh(pi / 2))), lambda = L.
+    x is periodic; the bottom (y = 0) and the wavy top are the walls."""
+    H, A, lam = average_height, amplitude, length
+    nx = int(length / average_height / cell_aspect_ratio) * 2 ** refinement
+    ny = 2 ** refinement
+    x = np.linspace(0.0, length, nx + 1)
+    y = np.linspace(0.0, H, ny + 1)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    xr = X + lam * A / H / (2 * math.pi) * np.sin(2 * math.pi * X / lam)
+    yr = H * (0.5 + 0.5 * np.tanh((Y / H - 0.5) * math.pi) / math.tanh(0.5 * math.pi))
+    upper = H + A * np.cos(2 * math.pi * xr / lam) + roughness_height * np.cos(
+        2 * math.pi * xr / (lam / roughness_length_ratio))
+    return np.stack([xr, yr / H * upper], -1)
+
+
+def lubrication_sine_velocity(X: np.ndarray, bottom_velocity: float, average_height: float, amplitude: float):
+    """Initial velocity (LubricationSine.cpp:78-87): u = U (1 - y / (H - A))^2, v = 0."""
+    upper = average_height - amplitude
+    u = np.zeros((2, X.shape[0]))
+    u[0] = bottom_velocity * (1.0 - X[:, 1] / upper) ** 2
+    return u
+
+
 def equilibrium(stencil: str, scaling: float, rho: np.ndarray, u_scaled: np.ndarray) -> np.ndarray:
     """Second-order equilibrium with scaled velocities (the legacy
     getEquilibriumDistribution, collision/BGKStandard.cpp:23-41)."""

@@ -40,7 +40,8 @@ def build(force: bool = False) -> str:
 
 class _Mesh(C.Structure):
     _fields_ = [("dim", C.c_int), ("N", C.c_int * 3), ("p", C.c_int), ("dg", C.c_int),
-                ("L", C.c_double * 3), ("bc", C.c_int * 6), ("uw", (C.c_double * 3) * 6)]
+                ("L", C.c_double * 3), ("bc", C.c_int * 6), ("uw", (C.c_double * 3) * 6),
+                ("vtx", C.POINTER(C.c_double))]
 
 
 # boundary kinds of the six faces x-, x+, y-, y+, z-, z+
@@ -175,6 +176,21 @@ class Mesh:
     L: tuple = (2 * math.pi, 2 * math.pi, 2 * math.pi)
     bc: tuple = (0, 0, 0, 0, 0, 0)          # per face x-, x+, y-, y+, z-, z+: BC_*
     uw: tuple = ((0.0, 0.0, 0.0),) * 6      # wall velocity of bounce-back faces (scaled)
+    # MappingQ1 cells: grid vertices, array of shape (N0+1, N1+1[, N2+1], D)
+    # indexed [i, j(, k)]; None = the Cartesian box of lengths L
+    vertices: object = None
+
+    def vertex_array(self):
+        """The vertices as the C layout wants them: x fastest, 3 doubles each."""
+        if self.vertices is None:
+            return None
+        v = np.asarray(self.vertices, dtype=np.float64)
+        shape = tuple(self.N[a] + 1 for a in range(self.dim))
+        if v.shape != shape + (self.dim,):
+            raise ValueError(f"vertices must have shape {shape + (self.dim,)}")
+        out = np.zeros(shape[::-1] + (3,))
+        out[..., :self.dim] = np.transpose(v, tuple(range(self.dim))[::-1] + (self.dim,))
+        return np.ascontiguousarray(out.reshape(-1, 3))
 
     def c(self) -> _Mesh:
         m = _Mesh()
@@ -188,6 +204,10 @@ class Mesh:
             m.bc[f] = int(self.bc[f])
             for a in range(3):
                 m.uw[f][a] = float(self.uw[f][a])
+        v = self.vertex_array()
+        if v is not None:
+            m._keep = v
+            m.vtx = _dp(v)
         return m
 
     def nodes_per_axis(self, a: int) -> int:
@@ -207,6 +227,18 @@ class Mesh:
         return X
 
     def h_min(self) -> float:
+        if self.vertices is not None:
+            # minimum over cells of the smallest distance between two of the
+            # cell's vertices (CFDSolverUtilities.cpp:69-84)
+            v = np.asarray(self.vertices, dtype=np.float64)
+            D = self.dim
+            corners = [tuple((k >> a) & 1 for a in range(D)) for k in range(1 << D)]
+
+            def corner(b):
+                return v[tuple(slice(b[a], v.shape[a] - 1 + b[a]) for a in range(D))]
+            d = min(np.linalg.norm(corner(b1) - corner(b2), axis=-1).min()
+                    for i, b1 in enumerate(corners) for b2 in corners[i + 1:])
+            return float(d)
         return min(self.L[a] / self.N[a] for a in range(self.dim))
 
 

@@ -240,6 +240,10 @@ typedef struct {
   double L[3];
   int bc[6];       /* per face: ORC_BC_*; both faces of an axis periodic or neither */
   double uw[6][3]; /* wall velocity of a bounce-back face (scaled units) */
+  /* MappingQ1 cells (NULL: the Cartesian box, MappingCartesian): the grid
+   * vertices, x fastest, (N0+1)(N1+1)(N2+1) points of 3 doubles; a periodic
+   * axis needs vertex N_a = vertex 0 + L_a e_a */
+  const double* vtx;
 } orc_mesh;
 
 static int nodes_per_axis(const orc_mesh* m, int a) {
@@ -288,6 +292,112 @@ static int64_t cell_node_index(const orc_mesh* m, const int* c, const int* l) {
   return idx;
 }
 
+/* ---- MappingQ1 (multilinear map of a cell from its 2^D vertices) -------- */
+static const double* grid_vertex(const orc_mesh* m, int i, int j, int k) {
+  const int n0 = m->N[0] + 1, n1 = m->dim > 1 ? m->N[1] + 1 : 1;
+  return m->vtx + 3 * (((int64_t)k * n1 + j) * n0 + i);
+}
+
+/* x = sum over corners of prod_a (b_a ? u_a : 1 - u_a) V_corner; also the
+ * Jacobian J[r][a] = dx_r / du_a when J != NULL */
+static void q1_map(const orc_mesh* m, const int* c, const double* u, double* x, double J[3][3]) {
+  const int D = m->dim, nc = 1 << D;
+  int k, a, r;
+  for (r = 0; r < 3; r++) {
+    x[r] = 0.0;
+    if (J)
+      for (a = 0; a < 3; a++) J[r][a] = 0.0;
+  }
+  for (k = 0; k < nc; k++) {
+    int b[3] = {k & 1, (k >> 1) & 1, (k >> 2) & 1};
+    double phi = 1.0, dphi[3];
+    for (a = 0; a < D; a++) phi *= b[a] ? u[a] : 1.0 - u[a];
+    for (a = 0; a < D; a++) {
+      dphi[a] = b[a] ? 1.0 : -1.0;
+      int q;
+      for (q = 0; q < D; q++)
+        if (q != a) dphi[a] *= b[q] ? u[q] : 1.0 - u[q];
+    }
+    const double* v = grid_vertex(m, c[0] + b[0], D > 1 ? c[1] + b[1] : 0, D > 2 ? c[2] + b[2] : 0);
+    for (r = 0; r < D; r++) {
+      x[r] += phi * v[r];
+      if (J)
+        for (a = 0; a < D; a++) J[r][a] += dphi[a] * v[r];
+    }
+  }
+}
+
+/* J du = r for D = 2 or 3 (Cramer's rule); -1 for a singular J */
+static int q1_solve(int D, double J[3][3], const double* r, double* du) {
+  if (D == 2) {
+    const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    if (det == 0.0) return -1;
+    du[0] = (J[1][1] * r[0] - J[0][1] * r[1]) / det;
+    du[1] = (-J[1][0] * r[0] + J[0][0] * r[1]) / det;
+    return 0;
+  }
+  const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                     J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                     J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  if (det == 0.0) return -1;
+  int col, row, a;
+  for (col = 0; col < 3; col++) {
+    double M[3][3];
+    for (row = 0; row < 3; row++)
+      for (a = 0; a < 3; a++) M[row][a] = a == col ? r[row] : J[row][a];
+    du[col] = (M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) -
+               M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+               M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0])) / det;
+  }
+  return 0;
+}
+
+/* Inverse of the cell map (the reference calls
+ * MappingQ1::transform_real_to_unit_cell): Newton's method from the cell
+ * centre, each step halved (up to 12 times) until the residual decreases.
+ * Converged when a step is below 1e-14 in unit coordinates; -1 when the
+ * residual cannot be decreased before that (the reference's
+ * ExcTransformationFailed), or after 100 steps. */
+static int q1_inverse(const orc_mesh* m, const int* c, const double* x, double* u) {
+  const int D = m->dim;
+  int it, a;
+  double y[3], J[3][3], r[3], res = 0.0;
+  for (a = 0; a < 3; a++) u[a] = a < D ? 0.5 : 0.0;
+  q1_map(m, c, u, y, J);
+  for (a = 0; a < D; a++) {
+    r[a] = y[a] - x[a];
+    res += r[a] * r[a];
+  }
+  for (it = 0; it < 100; it++) {
+    double du[3] = {0, 0, 0}, step = 1.0, stp = 0.0;
+    int k, ok = 0;
+    if (q1_solve(D, J, r, du)) return -1;
+    for (a = 0; a < D; a++) stp += du[a] * du[a];
+    for (k = 0; k <= 12; k++, step *= 0.5) {
+      double un[3] = {u[0], u[1], u[2]}, yn[3], Jn[3][3], rn[3], rs = 0.0;
+      for (a = 0; a < D; a++) un[a] = u[a] - step * du[a];
+      q1_map(m, c, un, yn, Jn);
+      for (a = 0; a < D; a++) {
+        rn[a] = yn[a] - x[a];
+        rs += rn[a] * rn[a];
+      }
+      if (rs < res || rs == 0.0) {
+        for (a = 0; a < D; a++) {
+          u[a] = un[a];
+          r[a] = rn[a];
+        }
+        memcpy(J, Jn, sizeof(Jn));
+        res = rs;
+        ok = 1;
+        break;
+      }
+    }
+    if (!ok) return stp < 1e-24 ? 0 : -1; /* stuck at round-off */
+    if (stp * step * step < 1e-28 || res == 0.0) return 0;
+  }
+  return -1;
+}
+
 void orc_node_coords(const orc_mesh* m, double* X) {
   double xi[16];
   int64_t n = orc_n_nodes(m), g;
@@ -305,6 +415,17 @@ void orc_node_coords(const orc_mesh* m, double* X) {
       double h = m->L[a] / m->N[a];
       axis_cell_local(m, a, ii[a], &c, &l);
       X[3 * g + a] = c * h + xi[l] * h;
+    }
+    if (m->vtx) {
+      /* mapped node: the cell's map at the Gauss-Lobatto unit point */
+      int c[3] = {0, 0, 0}, l[3] = {0, 0, 0};
+      double u[3] = {0, 0, 0}, x[3];
+      for (a = 0; a < m->dim; a++) {
+        axis_cell_local(m, a, ii[a], &c[a], &l[a]);
+        u[a] = xi[l[a]];
+      }
+      q1_map(m, c, u, x, NULL);
+      for (a = 0; a < 3; a++) X[3 * g + a] = a < m->dim ? x[a] : 0.0;
     }
   }
 }
@@ -357,6 +478,70 @@ int orc_face_crossed_first(int dim, const double* lo, const double* h,
     if (fabs(hh[a] - 1) < 1e-10) hh[a] = 1;
     p_boundary[a] = lo[a] + hh[a] * h[a];
   }
+  return face;
+}
+
+/* faceCrossedFirst with the mapping (SemiLagrangian.cpp:525-699): both points
+ * to unit coordinates of the cell, the face with the smallest lambda in unit
+ * space, the crossing point mapped back to real space. */
+/* faceCrossedFirstWithoutMapping (SemiLagrangian.cpp:702-757), taken when
+ * an inverse map fails: every face is treated as the plane through its first
+ * vertex with the normal of its first edges (SemiLagrangianTools.cpp:151-168);
+ * the smallest non-negative lambda below 1 wins, faces in order 0..2D-1.
+ * Face vertices in the cell numbering bx + 2 by + 4 bz. */
+static int face_crossed_first_planar(const orc_mesh* m, const int* c, const double* p_in, const double* p_out,
+                                     double* p_boundary) {
+  static const int FV2[4][2] = {{0, 2}, {1, 3}, {0, 1}, {2, 3}};
+  static const int FV3[6][3] = {{0, 2, 4}, {1, 3, 5}, {0, 4, 1}, {2, 6, 3}, {0, 1, 2}, {4, 5, 6}};
+  const int D = m->dim;
+  double lambda_min = 1.0;
+  int i, a, index_min = 0;
+  for (i = 0; i < 2 * D; i++) {
+    const double* v[3];
+    int k;
+    for (k = 0; k < D; k++) {
+      const int cv = D == 2 ? FV2[i][k] : FV3[i][k];
+      v[k] = grid_vertex(m, c[0] + (cv & 1), c[1] + ((cv >> 1) & 1), D > 2 ? c[2] + ((cv >> 2) & 1) : 0);
+    }
+    double n[3];
+    if (D == 2) {
+      n[0] = v[1][1] - v[0][1]; /* cross_product_2d(d) = (d_y, -d_x) */
+      n[1] = -(v[1][0] - v[0][0]);
+    } else {
+      double d1[3], d2[3];
+      for (a = 0; a < 3; a++) {
+        d1[a] = v[1][a] - v[0][a];
+        d2[a] = v[2][a] - v[0][a];
+      }
+      n[0] = d1[1] * d2[2] - d1[2] * d2[1];
+      n[1] = d1[2] * d2[0] - d1[0] * d2[2];
+      n[2] = d1[0] * d2[1] - d1[1] * d2[0];
+    }
+    double num = 0.0, den = 0.0;
+    for (a = 0; a < D; a++) {
+      num += (p_in[a] - v[0][a]) * n[a];
+      den += (p_in[a] - p_out[a]) * n[a];
+    }
+    const double lam = num / den;
+    if (lam < 0) continue;
+    if (lam < lambda_min) {
+      lambda_min = lam;
+      index_min = i;
+    }
+  }
+  if (lambda_min == 1) return -1;
+  for (a = 0; a < D; a++) p_boundary[a] = p_in[a] + (p_out[a] - p_in[a]) * lambda_min;
+  return index_min;
+}
+
+static int face_crossed_first_q1(const orc_mesh* m, const int* c, const double* p_in, const double* p_out,
+                                 double* p_boundary) {
+  const int D = m->dim;
+  double pi[3] = {0, 0, 0}, po[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, one[3] = {1, 1, 1}, hu[3] = {0, 0, 0}, lam;
+  if (q1_inverse(m, c, p_in, pi) || q1_inverse(m, c, p_out, po))
+    return face_crossed_first_planar(m, c, p_in, p_out, p_boundary); /* SemiLagrangian.cpp:283-287 */
+  const int face = orc_face_crossed_first(D, lo, one, pi, po, hu, &lam);
+  if (face >= 0) q1_map(m, c, hu, p_boundary, NULL);
   return face;
 }
 
@@ -436,6 +621,40 @@ void orc_sl_free(orc_sl* s) {
   free(s);
 }
 
+/* Periodic translation per axis: L_a e_a on the box; with mapped cells the
+ * offset between the two faces' vertices, which must be the same vector for
+ * all of them on a periodic axis (PeriodicBoundary.cpp:184-270, the offset of
+ * face 1 to face 0).  -1 when a periodic axis has no common offset. */
+static int periodic_offsets(const orc_mesh* m, double pv[3][3]) {
+  const int D = m->dim;
+  int a, b;
+  for (a = 0; a < D; a++) {
+    for (b = 0; b < 3; b++) pv[a][b] = a == b ? m->L[a] : 0.0;
+    if (!m->vtx) continue;
+    /* the vertex lattice of face a-, walked over the other axes */
+    const int nb = a == 0 ? 1 : 0, nc = a == 2 ? 1 : 2;
+    const int mb = m->N[nb] + 1, mc = D > 2 ? m->N[nc] + 1 : 1;
+    int ib, ic;
+    for (ic = 0; ic < mc; ic++)
+      for (ib = 0; ib < mb; ib++) {
+        int lo_i[3] = {0, 0, 0}, hi_i[3] = {0, 0, 0};
+        lo_i[nb] = hi_i[nb] = ib;
+        if (D > 2) lo_i[nc] = hi_i[nc] = ic;
+        hi_i[a] = m->N[a];
+        const double* v0 = grid_vertex(m, lo_i[0], lo_i[1], lo_i[2]);
+        const double* v1 = grid_vertex(m, hi_i[0], hi_i[1], hi_i[2]);
+        for (b = 0; b < D; b++) {
+          const double d = v1[b] - v0[b];
+          if (ib == 0 && ic == 0)
+            pv[a][b] = d;
+          else if (m->bc[2 * a] == ORC_BC_PERIODIC && fabs(d - pv[a][b]) > 1e-12 * (fabs(d) + 1.0))
+            return -1;
+        }
+      }
+  }
+  return 0;
+}
+
 /* Assemble the streaming operator for all streamed directions.
  * Restates SemiLagrangian::fillSparseObject (SemiLagrangian.cpp:145-522) for
  * an axis-aligned periodic box: every node is traced once (the first cell in
@@ -462,6 +681,7 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
   int c_iter;
   double* vals = NULL;
   double h[3] = {1, 1, 1};
+  double pv[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   int opp[32];
 
   if (orc_stencil(stencil, scaling, &D, &Q, e, w, &cs2, &vmax) != ORC_OK)
@@ -473,6 +693,7 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
     h[a] = m->L[a] / m->N[a];
   }
   orc_gl_points(p, xi);
+  if (periodic_offsets(m, pv)) return NULL;
   for (alpha = 0; alpha < Q; alpha++) {
     int j, k;
     opp[alpha] = 0;
@@ -519,6 +740,11 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
       tracked[g] = 1;
       double x[3] = {0, 0, 0};
       for (a = 0; a < D; a++) x[a] = cc[a] * h[a] + xi[l[a]] * h[a];
+      if (m->vtx) {
+        double ul[3] = {0, 0, 0};
+        for (a = 0; a < D; a++) ul[a] = xi[l[a]];
+        q1_map(m, cc, ul, x, NULL);
+      }
       for (alpha = 1; alpha < Q; alpha++) {
         tracker el;
         el.dest = g;
@@ -539,17 +765,19 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
             s->n_lifetime_hits++;
             break;
           }
-          double lo[3], pb[3], lam;
+          double lo[3], pb[3], lam, ud[3] = {0, 0, 0};
           for (a = 0; a < D; a++) lo[a] = el.cell[a] * h[a];
-          int face = orc_face_crossed_first(D, lo, h, el.cur, el.dep, pb, &lam);
+          int face = m->vtx ? face_crossed_first_q1(m, el.cell, el.cur, el.dep, pb)
+                            : orc_face_crossed_first(D, lo, h, el.cur, el.dep, pb, &lam);
           if (face == -1) {
             if (el.hit_dn) el.cdir = opp[el.cdir]; /* SemiLagrangian.cpp:312-316 */
             /* found: shape values of the cell at the departure point
              * (SemiLagrangianTools.cpp:15-64, snap to [0,1] at 1e-10) */
             double l1[3][16];
             int k, lj;
+            if (m->vtx && q1_inverse(m, el.cell, el.dep, ud)) goto fail;
             for (a = 0; a < D; a++) {
-              double uu = (el.dep[a] - lo[a]) / h[a];
+              double uu = m->vtx ? ud[a] : (el.dep[a] - lo[a]) / h[a];
               if (fabs(uu) < 1e-10) uu = 0;
               if (fabs(uu - 1) < 1e-10) uu = 1;
               for (k = 0; k <= p; k++) l1[a][k] = orc_lagrange(p, xi, k, uu);
@@ -621,9 +849,11 @@ orc_sl* orc_sl_assemble(const orc_mesh* m, int stencil, double scaling,
           if (at_boundary) {
             /* periodic face (SemiLagrangian.cpp:336-353): translate the
              * boundary point and the departure point by the box length */
-            double shift = upper ? -m->L[ax] : m->L[ax];
-            el.cur[ax] += shift;
-            el.dep[ax] += shift;
+            for (a = 0; a < D; a++) {
+              const double shift = upper ? -pv[ax][a] : pv[ax][a];
+              el.cur[a] += shift;
+              el.dep[a] += shift;
+            }
             el.cell[ax] = upper ? 0 : m->N[ax] - 1;
           } else {
             el.cell[ax] += upper ? 1 : -1;
