@@ -1,0 +1,21 @@
+// Departure-point kernels of mapped (MappingQ1) meshes for D2Q9, orders 1-6
+// (compiled as its own translation unit).
+#include "launch.h"
+#include "sl_mapped.cuh"
+
+namespace natgpu {
+
+template <class Real>
+static const void* pick(int coll, int p) {
+  switch (coll) {
+    case L_COLL_NONE: return mapped_for_order<SD2Q9, Real, COLL_NONE>(p);
+    case L_COLL_BGK: return mapped_for_order<SD2Q9, Real, COLL_BGK>(p);
+    case L_COLL_BGK_INC: return mapped_for_order<SD2Q9, Real, COLL_BGK_INC>(p);
+    case L_COLL_KBC: return mapped_for_order<SD2Q9, Real, COLL_KBC>(p);
+  }
+  return nullptr;
+}
+
+const void* mapped_kernel_d2q9(int coll, int prec, int p) { return prec == 0 ? pick<double>(coll, p) : pick<float>(coll, p); }
+
+}  // namespace natgpu

@@ -25,6 +25,12 @@ KernelSet kernels_d2q9(int coll, int prec);
 KernelSet kernels_d3q19(int coll, int prec);
 KernelSet kernels_d3q27(int coll, int prec);
 
+// departure-point kernels of mapped meshes (sl_mapped.cuh) for order p;
+// NULL when the combination is not instantiated
+const void* mapped_kernel_d2q9(int coll, int prec, int p);
+const void* mapped_kernel_d3q19(int coll, int prec, int p);
+const void* mapped_kernel_d3q27(int coll, int prec, int p);
+
 // threads per CTA of the fused kernel and nodes per thread
 constexpr int STEP_THREADS = 256;
 constexpr int STEP_NPT = 2;

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/natgpu.h"
@@ -25,6 +26,7 @@
 #include "sl_step.cuh"
 #include "sl_step_v2.cuh"
 #include "sl_row.cuh"
+#include "sl_mapped.cuh"
 #include "sl_rowt.cuh"
 
 using namespace natgpu;
@@ -95,6 +97,13 @@ struct nat_solver {
   std::vector<double> vtx;       // grid vertices, x fastest, 3 doubles each
   double pv[3][3] = {{0}};       // periodic translation of each axis
   double* d_mw = nullptr;        // per-node quadrature weight (mass / energy)
+  // departure-point rows (sl_mapped.cuh), one population only
+  int* d_mp_base = nullptr;
+  void* d_mp_u = nullptr;        // Real
+  void* d_mp_c = nullptr;        // Real
+  unsigned char* d_mp_flags = nullptr;
+  const void* mp_step = nullptr;    // kernels for this stencil / model / order / precision
+  const void* mp_stream = nullptr;
 };
 
 namespace {
@@ -534,6 +543,45 @@ int launch_step(nat_solver* s, const KernelSet& ks, int collide, int write_macro
   s->launches++;
   s->cur = 1 - s->cur;
   return NAT_OK;
+}
+
+// Departure-point kernel of a mapped mesh (sl_mapped.cuh): stream (+ collide)
+// every node from its rows.
+template <class Real>
+int launch_mapped_t(nat_solver* s, const void* kern, int collide, int write_macro) {
+  StepParams P = step_params(s, s->f[s->cur], s->f[1 - s->cur], collide, write_macro, 0);
+  MappedRows<Real> R;
+  R.base = s->d_mp_base;
+  R.u = static_cast<const Real*>(s->d_mp_u);
+  R.cst = static_cast<const Real*>(s->d_mp_c);
+  R.flags = s->d_mp_flags;
+  for (int a = 0; a < 3; ++a) R.nax[a] = s->n_ax[a];
+  LagrangeTab<Real> L;
+  memset(&L, 0, sizeof(L));
+  double xi[PMAX1 + 1];
+  const int p = s->spec.order;
+  gl_points(p, xi);
+  for (int j = 0; j <= p; ++j) {
+    double R = 1.0;
+    for (int m = 0; m <= p; ++m)
+      if (m != j) R /= xi[j] - xi[m];
+    L.xi[j] = (Real)xi[j];
+    L.R[j] = (Real)R;
+  }
+  void* args[] = {&P, &R, &L};
+  const long long blocks = (s->n_dev + MAP_THREADS - 1) / MAP_THREADS;
+  cudaError_t e = cudaLaunchKernel(kern, dim3((unsigned)blocks), dim3(MAP_THREADS), args, 0, s->stream);
+  if (e != cudaSuccess) return cuda_fail(s, e, "departure-point kernel launch");
+  s->launches++;
+  s->cur = 1 - s->cur;
+  return NAT_OK;
+}
+
+int launch_mapped(nat_solver* s, bool collide, int write_macro) {
+  const void* k = collide ? s->mp_step : s->mp_stream;
+  if (!k) return fail(s, NAT_ERR_UNSUPPORTED, "no departure-point kernel for this configuration");
+  return s->spec.precision == NAT_FP64 ? launch_mapped_t<double>(s, k, collide, write_macro)
+                                       : launch_mapped_t<float>(s, k, collide, write_macro);
 }
 
 // Decide whether the specialised kernel applies: an instantiation exists for
@@ -1147,6 +1195,73 @@ void node_point(const nat_solver* s, const int* c, const int* l, const double* x
   for (int a = 0; a < s->D; ++a) x[a] = c[a] * s->h[a] + xi[l[a]] * s->h[a];
 }
 
+void free_mapped_rows(nat_solver* s) {
+  cudaFree(s->d_mp_base);
+  cudaFree(s->d_mp_u);
+  cudaFree(s->d_mp_c);
+  cudaFree(s->d_mp_flags);
+  s->d_mp_base = nullptr;
+  s->d_mp_u = s->d_mp_c = nullptr;
+  s->d_mp_flags = nullptr;
+}
+
+// Departure-point rows to the device in the solve's arithmetic type.
+int upload_mapped_rows(nat_solver* s, const std::vector<int>& base, const std::vector<double>& u,
+                       const std::vector<double>& c2, const std::vector<unsigned char>& flags) {
+  const bool f64 = s->spec.precision == NAT_FP64;
+  const size_t es = f64 ? 8 : 4, nr = base.size();
+  // every gathered index must address the Q x n_dev state
+  const int P = s->spec.order;
+  const long long qn = (long long)s->Q * s->n_dev;
+  const long long st[3] = {1, s->n_ax[0], (long long)s->n_ax[0] * s->n_ax[1]};
+  for (size_t r = 0; r < nr; ++r) {
+    long long lo = base[r], hi = base[r];
+    for (int a = 0; a < s->D; ++a) {
+      if (flags[r] & (1u << a)) {
+        lo += (long long)(P - s->n_ax[a]) * st[a];
+        hi += (long long)(P - 1) * st[a];
+      } else {
+        hi += (long long)P * st[a];
+      }
+    }
+    if (lo < 0 || hi >= qn)
+      return fail(s, NAT_ERR_CUDA, "internal error: departure-point row %zu addresses %lld..%lld", r, lo, hi);
+  }
+  std::vector<unsigned char> ub(u.size() * es), cb(nr * es);
+  for (size_t i = 0; i < u.size(); ++i) {
+    if (f64)
+      memcpy(&ub[i * 8], &u[i], 8);
+    else {
+      const float v = (float)u[i];
+      memcpy(&ub[i * 4], &v, 4);
+    }
+  }
+  for (size_t r = 0; r < nr; ++r) {
+    const double c = c2[2 * r + (f64 ? 0 : 1)];
+    if (f64)
+      memcpy(&cb[r * 8], &c, 8);
+    else {
+      const float v = (float)c;
+      memcpy(&cb[r * 4], &v, 4);
+    }
+  }
+  auto alloc = [&](void** p, size_t bytes) -> bool {
+    if (cudaMalloc(p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return true;
+  };
+  if (!alloc((void**)&s->d_mp_base, sizeof(int) * nr) || !alloc(&s->d_mp_u, ub.size()) ||
+      !alloc(&s->d_mp_c, cb.size()) || !alloc((void**)&s->d_mp_flags, nr))
+    return fail(s, NAT_ERR_OOM, "cudaMalloc of the departure-point rows failed");
+  CK(cudaMemcpy(s->d_mp_base, base.data(), sizeof(int) * nr, cudaMemcpyHostToDevice), "mapped rows");
+  CK(cudaMemcpy(s->d_mp_u, ub.data(), ub.size(), cudaMemcpyHostToDevice), "mapped rows");
+  CK(cudaMemcpy(s->d_mp_c, cb.data(), cb.size(), cudaMemcpyHostToDevice), "mapped rows");
+  CK(cudaMemcpy(s->d_mp_flags, flags.data(), nr, cudaMemcpyHostToDevice), "mapped rows");
+  return NAT_OK;
+}
+
 int build_wall_rows(nat_solver* s) {
   cudaFree(s->d_br_dst);
   cudaFree(s->d_br_ptr);
@@ -1160,6 +1275,7 @@ int build_wall_rows(nat_solver* s) {
   s->d_br_wf = nullptr;
   s->nbr = 0;
   s->nbn = 0;
+  free_mapped_rows(s);
   if (!s->walls && !s->mapped) return NAT_OK;
   HostStencil hs;
   get_host_stencil(s->spec.stencil, &hs, s->spec.scaling);
@@ -1177,8 +1293,6 @@ int build_wall_rows(nat_solver* s) {
   }
   double grest[32];
   for (int q = 0; q < Q; ++q) grest[q] = s->rest[q] * s->gref;
-  std::vector<int> dst, ptr(1, 0), col, bnodes;
-  std::vector<double> w, cst;
   const long long n = s->n_dev;
   const int* N = s->spec.cells;
   // the departure path of one (node, direction): source direction, cell and
@@ -1262,7 +1376,35 @@ int build_wall_rows(nat_solver* s) {
     }
     return hits;
   };
-  for (long long node = 0; node < n; ++node) {
+  // mapped meshes (one population): departure-point rows of every node
+  // (sl_mapped.cuh) instead of sparse matrix rows
+  const bool dp = s->mapped && !s->thermal;
+  std::vector<int> mp_base;
+  std::vector<double> mp_u, mp_c;
+  std::vector<unsigned char> mp_flags;
+  if (dp) {
+    if ((long long)Q * n > INT32_MAX) return fail(s, NAT_ERR_UNSUPPORTED, "Q x nodes exceeds 2^31");
+    mp_base.assign((size_t)(Q - 1) * n, 0);
+    mp_u.assign((size_t)(Q - 1) * D * n, 0.0);
+    mp_c.assign((size_t)2 * (Q - 1) * n, 0.0);
+    mp_flags.assign((size_t)(Q - 1) * n, 0);
+  }
+  // rows of the nodes [n0, n1) into one chunk (the chunks run on host
+  // threads; departure-point rows go straight to their slots)
+  struct Chunk {
+    std::vector<int> dst, ptr, col, bnodes;
+    std::vector<double> w, cst;
+    int rc = NAT_OK;
+    char err[256] = {0};
+  };
+  auto work = [&](long long n0, long long n1, Chunk& C) {
+  std::vector<int>& dst = C.dst;
+  std::vector<int>& ptr = C.ptr;
+  std::vector<int>& col = C.col;
+  std::vector<int>& bnodes = C.bnodes;
+  std::vector<double>& w = C.w;
+  std::vector<double>& cst = C.cst;
+  for (long long node = n0; node < n1; ++node) {
     int idx[3] = {(int)(node % s->n_ax[0]), (int)((node / s->n_ax[0]) % s->n_ax[1]),
                   (int)(node / ((long long)s->n_ax[0] * s->n_ax[1]))};
     double x[3] = {0, 0, 0};
@@ -1282,7 +1424,7 @@ int build_wall_rows(nat_solver* s) {
       if (hits[alpha] != 0) wall_node = true;
     }
     if (!wall_node && !s->mapped) continue;
-    bnodes.push_back((int)node);
+    if (!dp) bnodes.push_back((int)node);
     for (int alpha = 1; alpha < Q; ++alpha) {
       const Path& P = paths[alpha];
       const bool identity = hits[alpha] < 0;
@@ -1294,38 +1436,69 @@ int build_wall_rows(nat_solver* s) {
       for (int a = 0; a < 3; ++a)
         for (int j = 0; j < PMAX1; ++j) l1[a][j] = (a >= D && j == 0) ? 1.0 : 0.0;
       double ud[3] = {0, 0, 0};
-      if (!identity && s->mapped && !q1_inverse(s, cell, P.dep, ud))
-        return fail(s, NAT_ERR_UNSUPPORTED,
-                    "the inverse map of cell (%d %d %d) failed at a departure point; the mesh is too distorted "
-                    "for this time step",
-                    cell[0], cell[1], cell[2]);
+      if (!identity && s->mapped && !q1_inverse(s, cell, P.dep, ud)) {
+        C.rc = NAT_ERR_UNSUPPORTED;
+        snprintf(C.err, sizeof(C.err),
+                 "the inverse map of cell (%d %d %d) failed at a departure point; the mesh is too distorted "
+                 "for this time step",
+                 cell[0], cell[1], cell[2]);
+        return;
+      }
+      double uu[3] = {0, 0, 0};  // unit coordinates of the departure point
       for (int a = 0; a < D; ++a) {
         if (identity) {
           cell[a] = own[a];
+          uu[a] = xi[idx[a] % PER];
           for (int j = 0; j <= p; ++j) l1[a][j] = (j == idx[a] % PER) ? 1.0 : 0.0;
           continue;
         }
         double ul = s->mapped ? ud[a] : (P.dep[a] - cell[a] * s->h[a]) / s->h[a];
         if (fabs(ul) < 1e-10) ul = 0.0;
         if (fabs(ul - 1.0) < 1e-10) ul = 1.0;
+        uu[a] = ul;
         for (int j = 0; j <= p; ++j) l1[a][j] = lagrange(p, xi, j, ul);
       }
       const double c = P.c;
       const int np1 = p + 1;
       const int nloc = D == 3 ? np1 * np1 * np1 : np1 * np1;
       double wrest = 0.0, wgrest = 0.0;
+      bool tiny = false;
       for (int li = 0; li < nloc; ++li) {
         const int lx = li % np1, ly = (li / np1) % np1, lz = D == 3 ? li / (np1 * np1) : 0;
         const double v = l1[0][lx] * l1[1][ly] * (D == 3 ? l1[2][lz] : 1.0);
-        if (fabs(v) < 1e-10) continue;  // SemiLagrangian.cpp:483
+        if (fabs(v) < 1e-10) {  // SemiLagrangian.cpp:483
+          if (v != 0.0) tiny = true;
+          continue;
+        }
+        wrest += v * s->rest[sdir];
+        wgrest += v * grest[sdir];
+        if (dp) continue;
         // the FE_Q node p of the last cell of a periodic axis is node 0
         const int ix = (cell[0] * PER + lx) % s->n_ax[0], iy = (cell[1] * PER + ly) % s->n_ax[1],
                   iz = (cell[2] * PER + lz) % s->n_ax[2];
         const long long src = ((long long)iz * s->n_ax[1] + iy) * s->n_ax[0] + ix;
         col.push_back((int)(sdir * n + src));
         w.push_back(v);
-        wrest += v * s->rest[sdir];
-        wgrest += v * grest[sdir];
+      }
+      if (dp) {
+        // departure-point row: first node of the cell, unit point, constants, flags
+        const long long r = (long long)(alpha - 1) * n + node;
+        const long long first =
+            ((long long)(cell[2] * PER) * s->n_ax[1] + cell[1] * PER) * s->n_ax[0] + cell[0] * PER;
+        mp_base[r] = (int)(sdir * n + first);
+        for (int a = 0; a < D; ++a) mp_u[((long long)(alpha - 1) * D + a) * n + node] = uu[a];
+        mp_c[2 * r] = c;                                // plain f
+        mp_c[2 * r + 1] = c + wrest - s->rest[alpha];  // f - w_i storage
+        unsigned char fl = tiny ? MAP_TINY : 0;
+        for (int a = 0; a < D; ++a)
+          if (PER == p && cell[a] == N[a] - 1) fl |= (unsigned char)(1u << a);  // FE_Q wrap
+        mp_flags[r] = fl;
+        continue;
+      }
+      if (col.size() > (size_t)INT32_MAX) {
+        C.rc = NAT_ERR_UNSUPPORTED;
+        snprintf(C.err, sizeof(C.err), "sparse rows exceed 2^31 entries; use fewer nodes");
+        return;
       }
       dst.push_back((int)(alpha * n + node));
       ptr.push_back((int)col.size());
@@ -1335,6 +1508,32 @@ int build_wall_rows(nat_solver* s) {
       cst.push_back(wgrest - grest[alpha]);       // g - w_i g_ref storage
     }
   }
+  };
+  const int nthr = (int)std::max<long long>(1, std::min<long long>(std::thread::hardware_concurrency(), n / 256));
+  std::vector<Chunk> chunks(nthr);
+  {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthr; ++t)
+      th.emplace_back(work, n * t / nthr, n * (t + 1) / nthr, std::ref(chunks[t]));
+    for (auto& t : th) t.join();
+  }
+  for (const Chunk& C : chunks)
+    if (C.rc) return fail(s, C.rc, "%s", C.err);
+  std::vector<int> dst, ptr(1, 0), col, bnodes;
+  std::vector<double> w, cst;
+  for (Chunk& C : chunks) {
+    const size_t off = col.size();
+    if (off + C.col.size() > (size_t)INT32_MAX)
+      return fail(s, NAT_ERR_UNSUPPORTED, "sparse rows exceed 2^31 entries; use fewer nodes");
+    for (int v : C.ptr) ptr.push_back((int)(v + off));
+    dst.insert(dst.end(), C.dst.begin(), C.dst.end());
+    col.insert(col.end(), C.col.begin(), C.col.end());
+    bnodes.insert(bnodes.end(), C.bnodes.begin(), C.bnodes.end());
+    w.insert(w.end(), C.w.begin(), C.w.end());
+    cst.insert(cst.end(), C.cst.begin(), C.cst.end());
+    C = Chunk();
+  }
+  if (dp) return upload_mapped_rows(s, mp_base, mp_u, mp_c, mp_flags);
   s->nbn = (int)bnodes.size();
   s->nbr = (int)dst.size();
   if (s->nbr == 0) return NAT_OK;
@@ -1469,6 +1668,7 @@ int nat_destroy(nat_solver* s) {
   cudaFree(s->d_br_c);
   cudaFree(s->d_bn_node);
   cudaFree(s->d_mw);
+  free_mapped_rows(s);
   delete s;
   return NAT_OK;
 }
@@ -1716,6 +1916,18 @@ int nat_create(const nat_spec* spec, nat_solver** out) {
     s->ks_coll = pick(coll);
     s->ks_stream = pick(L_COLL_NONE);
   }
+  if (!s->thermal && spec->vertices) {
+    auto mk = [&](int c) -> const void* {
+      switch (spec->stencil) {
+        case NAT_D2Q9: return mapped_kernel_d2q9(c, spec->precision, spec->order);
+        case NAT_D3Q19: return mapped_kernel_d3q19(c, spec->precision, spec->order);
+        case NAT_D3Q27: return mapped_kernel_d3q27(c, spec->precision, spec->order);
+      }
+      return nullptr;
+    };
+    s->mp_step = mk(coll);
+    s->mp_stream = mk(L_COLL_NONE);
+  }
   if (!s->thermal && !s->ks_coll.step) {
     // the reference throws for these combinations too
     // (collision/BGKIncompressible.cpp:54-55, collision/KBCStandard.cpp:79-81)
@@ -1882,6 +2094,12 @@ int nat_stream(nat_solver* s, double t, double* dt_out) {
   (void)t;
   if (!s) return NAT_ERR_INVALID_ARG;
   int rc = NAT_OK;
+  if (s->mapped && !s->thermal) {
+    rc = launch_mapped(s, false, 0);
+    if (rc) return rc;
+    if (dt_out) *dt_out = s->dt;
+    return NAT_OK;
+  }
   if (s->mapped) {
     // every row is a sparse row; the rest population stays
     s->cur = 1 - s->cur;
@@ -1986,6 +2204,11 @@ int nat_step_async(nat_solver* s, int n_steps, int write_macro) {
   for (int k = 0; k < n_steps; ++k) {
     const int wm = (write_macro && k == n_steps - 1) ? 1 : 0;
     int rc = NAT_OK;
+    if (s->mapped && !s->thermal) {
+      rc = launch_mapped(s, true, wm);  // every node from its departure-point rows
+      if (rc) return rc;
+      continue;
+    }
     if (s->mapped)
       s->cur = 1 - s->cur;  // every node is stepped from its sparse rows
     else
@@ -2080,7 +2303,7 @@ int nat_set_kernel_variant(nat_solver* s, int variant) {
 
 int nat_kernel_variant(const nat_solver* s) {
   if (!s) return -1;
-  if (s->mapped) return 8;
+  if (s->mapped && !s->thermal) return 8;
   return s->thermal ? 5 : (s->use_v2 ? s->kind : 1);
 }
 
@@ -2155,7 +2378,7 @@ int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
 
 int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* threads, int64_t* smem_bytes) {
   if (!s) return NAT_ERR_INVALID_ARG;
-  if (s->mapped) {
+  if (s->mapped && !s->thermal) {
     if (variant) *variant = 8;
     if (tile_nodes) tile_nodes[0] = tile_nodes[1] = tile_nodes[2] = 1;
     if (threads) *threads = 128;
