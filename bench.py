@@ -158,13 +158,13 @@ def time_e2e(sol, torch, f_host, rho_h, u_h, steps: int):
     """C-ABI calls with host buffers: upload f, one step, read rho/u."""
     sol.upload_f(f_host)
     sol.step(1)
-    sol.download_macro()
+    sol.download_macro(rho_h, u_h)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
         sol.upload_f(f_host)
         sol.step(1)
-        r, u = sol.download_macro()
+        r, u = sol.download_macro(rho_h, u_h)
     torch.cuda.synchronize()
     return (time.perf_counter() - t0) / steps
 
@@ -391,7 +391,10 @@ def run_ours(args):
     f_host = torch.from_numpy(f0).pin_memory().numpy()
     sol.upload_f(f0)
     e2e_steps = max(5, min(50, args.steps // 20))
-    e2e_s = time_e2e(sol, torch, f_host, None, None, e2e_steps)
+    # page-locked result buffers (the f buffer above is page-locked too)
+    rho_h = torch.empty(sol.n_ref, dtype=torch.float64).pin_memory().numpy()
+    u_h = torch.empty((sol.D, sol.n_ref), dtype=torch.float64).pin_memory().numpy()
+    e2e_s = time_e2e(sol, torch, f_host, rho_h, u_h, e2e_steps)
     h2d = f0.nbytes
     d2h = 8 * (1 + sol.D) * sol.n_ref
     # correctness guard on the measured state: finite, mass near 1

@@ -299,6 +299,18 @@ int nat_kernel_variant(const nat_solver* s);
  * trial steps run on the solver's own buffers (no allocation). */
 int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen);
 
+/* Report of the last nat_autotune (no counterpart in the reference): returns
+ * the number of candidates timed and writes, for the first `max` of them,
+ * the mean ms per step (L2-warm, back-to-back steps) and five ints each in
+ * desc: kernel variant, nodes per CTA along x, y, z, threads per CTA.
+ * Either pointer may be NULL; -1 for a NULL handle. */
+int nat_autotune_report(const nat_solver* s, int max, float* ms_per_step, int* desc);
+
+/* Use candidate `index` of the list nat_autotune times (same order, same
+ * variant filter; no counterpart in the reference): a fixed, reproducible
+ * kernel choice without timing, and the way the tests reach every kernel. */
+int nat_select_candidate(nat_solver* s, int index);
+
 /* The fused-step kernel in use: variant (1 generic, 2 tile, 3 row-segment),
  * nodes per CTA along each axis, threads per CTA, dynamic shared memory. */
 int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* threads,

@@ -55,7 +55,7 @@ EXPORTS = [
     "nat_upload_f", "nat_download_f", "nat_download_macro", "nat_upload_macro", "nat_stream",
     "nat_collide", "nat_step", "nat_step_async", "nat_status", "nat_last_error",
     "nat_mass_energy", "nat_device_f", "nat_launch_count", "nat_version", "nat_set_kernel_variant",
-    "nat_kernel_variant", "nat_autotune", "nat_kernel_info",
+    "nat_kernel_variant", "nat_autotune", "nat_autotune_report", "nat_select_candidate", "nat_kernel_info",
     "nat_server_create", "nat_server_destroy", "nat_server_submit", "nat_server_step", "nat_server_poll",
     "nat_server_result", "nat_server_stats", "nat_server_last_error", "nat_mass_energy_noalloc",
     "nat_set_thermal", "nat_get_thermal", "nat_upload_g", "nat_download_g", "nat_download_thermal",
@@ -143,6 +143,8 @@ def load_library(path: str | None = None):
                                           C.POINTER(C.c_double), vp, vp]
     L.nat_kernel_variant.argtypes = [vp]
     L.nat_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.nat_autotune_report.argtypes = [vp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_int)]
+    L.nat_select_candidate.argtypes = [vp, C.c_int]
     L.nat_kernel_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), i64p]
     L.nat_set_thermal.argtypes = [vp, C.POINTER(_Thermal)]
     L.nat_get_thermal.argtypes = [vp, C.POINTER(_Thermal)]
@@ -303,9 +305,16 @@ class Solver:
         self._check(self._L.nat_download_f(self._h, _dp(out)))
         return out
 
-    def download_macro(self):
-        rho = np.empty(self.n_ref)
-        u = np.empty((self.D, self.n_ref))
+    def download_macro(self, rho: np.ndarray = None, u: np.ndarray = None):
+        """rho (n_ref) and u (D, n_ref) of the last collision, into the given
+        float64 arrays when passed (e.g. page-locked ones, so the copy runs as
+        DMA), else into new ones."""
+        if rho is None:
+            rho = np.empty(self.n_ref)
+        if u is None:
+            u = np.empty((self.D, self.n_ref))
+        if rho.shape != (self.n_ref,) or u.shape != (self.D, self.n_ref):
+            raise ValueError("rho / u have the wrong shape")
         self._check(self._L.nat_download_macro(self._h, _dp(rho), _dp(u)))
         return rho, u
 
@@ -359,6 +368,22 @@ class Solver:
         nc, ch = C.c_int(), C.c_int()
         self._check(self._L.nat_autotune(self._h, int(steps), C.byref(nc), C.byref(ch)))
         return nc.value, ch.value
+
+    def select_candidate(self, index: int):
+        """Use candidate `index` of the autotuner's list (no timing)."""
+        self._check(self._L.nat_select_candidate(self._h, int(index)))
+
+    def autotune_report(self) -> list:
+        """Per candidate of the last autotune: dict(variant, tile_nodes,
+        threads, ms_per_step)."""
+        n = int(self._L.nat_autotune_report(self._h, 0, None, None))
+        if n <= 0:
+            return []
+        ms = (C.c_float * n)()
+        desc = (C.c_int * (5 * n))()
+        self._L.nat_autotune_report(self._h, n, ms, desc)
+        return [dict(variant=desc[5 * i], tile_nodes=[desc[5 * i + 1], desc[5 * i + 2], desc[5 * i + 3]],
+                     threads=desc[5 * i + 4], ms_per_step=float(ms[i])) for i in range(n)]
 
     def kernel_info(self) -> dict:
         v, th = C.c_int(), C.c_int()

@@ -7,7 +7,7 @@ namespace natgpu {
 
 namespace {
 
-template <class S, int COLL, int P, bool DG, int WY, int MINB>
+template <class S, int COLL, int P, bool DG, int WY, int MINB, bool ZS = false>
 RowLaunch sentry(int coll) {
   RowLaunch e;
   e.stencil = S::ID;
@@ -17,7 +17,7 @@ RowLaunch sentry(int coll) {
   e.dg = DG;
   e.wy = WY;
   e.wz = 1;
-  e.fn = (const void*)&k_sl_row<S, float, COLL, P, DG, WY, 1, true, MINB>;
+  e.fn = (const void*)&k_sl_row<S, float, COLL, P, DG, WY, 1, true, MINB, ZS>;
   return e;
 }
 
@@ -25,6 +25,10 @@ template <class S, int COLL, int P>
 void add_orders(std::vector<RowLaunch>& t, int coll) {
   t.push_back(sentry<S, COLL, P, true, 4, 8>(coll));
   t.push_back(sentry<S, COLL, P, false, 4, 8>(coll));
+  // z sharing: two cells of rows per CTA
+  constexpr int WD = 2 * (P + 1), WQ = 2 * P;
+  t.push_back(sentry<S, COLL, P, true, WD, 65536 / (32 * WD * 64), true>(coll));
+  t.push_back(sentry<S, COLL, P, false, WQ, 65536 / (32 * WQ * 64), true>(coll));
   if constexpr (P < PMAX) add_orders<S, COLL, P + 1>(t, coll);
 }
 

@@ -104,6 +104,10 @@ struct nat_solver {
   unsigned char* d_mp_flags = nullptr;
   const void* mp_step = nullptr;    // kernels for this stencil / model / order / precision
   const void* mp_stream = nullptr;
+  // report of the last nat_autotune: per candidate ms per step, kind, nodes
+  // per CTA along x, y, z and threads per CTA
+  std::vector<float> at_ms;
+  std::vector<int> at_desc;  // 5 ints per candidate
 };
 
 namespace {
@@ -2307,6 +2311,39 @@ int nat_kernel_variant(const nat_solver* s) {
   return s->thermal ? 5 : (s->use_v2 ? s->kind : 1);
 }
 
+// The kernels nat_autotune times, in its order: the specialised candidates
+// that apply (filtered by the kernel variant setting), then the generic
+// kernel unless a specialised one is required.
+static int tune_candidates(nat_solver* s, std::vector<Cand>* cand, int* ncand) {
+  int smem_optin = 0;
+  CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device),
+     "device attribute");
+  const int coll_sel = coll_selector(s->spec.collision);
+  *cand = s->variant == 1 ? std::vector<Cand>() : v2_candidates(s, coll_sel, smem_optin);
+  if (s->variant >= 3) {
+    std::vector<Cand> keep;
+    for (const Cand& k : *cand)
+      if (variant_kind(s->variant) == k.kind) keep.push_back(k);
+    cand->swap(keep);
+  }
+  *ncand = (int)cand->size() + (s->variant >= 2 ? 0 : 1);  // + the generic kernel
+  return NAT_OK;
+}
+
+int nat_select_candidate(nat_solver* s, int index) {
+  if (!s) return NAT_ERR_INVALID_ARG;
+  if (s->thermal || s->mapped) return index == 0 ? NAT_OK : fail(s, NAT_ERR_INVALID_ARG, "one kernel only");
+  std::vector<Cand> cand;
+  int ncand = 0;
+  int rc = tune_candidates(s, &cand, &ncand);
+  if (rc) return rc;
+  if (index < 0 || index >= ncand) return fail(s, NAT_ERR_INVALID_ARG, "candidate %d of %d", index, ncand);
+  if (index < (int)cand.size()) return use_candidate(s, cand[index]);
+  s->use_v2 = false;
+  s->kind = 1;
+  return NAT_OK;
+}
+
 int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
   if (!s || steps < 1) return NAT_ERR_INVALID_ARG;
   if (s->thermal || s->mapped) {
@@ -2314,18 +2351,10 @@ int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
     if (chosen) *chosen = 0;
     return NAT_OK;
   }
-  int smem_optin = 0;
-  CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device),
-     "device attribute");
-  const int coll_sel = coll_selector(s->spec.collision);
-  std::vector<Cand> cand = s->variant == 1 ? std::vector<Cand>() : v2_candidates(s, coll_sel, smem_optin);
-  if (s->variant >= 3) {
-    std::vector<Cand> keep;
-    for (const Cand& k : cand)
-      if (variant_kind(s->variant) == k.kind) keep.push_back(k);
-    cand.swap(keep);
-  }
-  const int ncand = (int)cand.size() + (s->variant >= 2 ? 0 : 1);  // + the generic kernel
+  std::vector<Cand> cand;
+  int ncand = 0;
+  int rc0 = tune_candidates(s, &cand, &ncand);
+  if (rc0) return rc0;
   if (n_candidates) *n_candidates = ncand;
   if (ncand == 0) return fail(s, NAT_ERR_UNSUPPORTED, "no kernel applies");
   // keep the state: back it up in the staging buffer (Q * n_ref doubles >= f)
@@ -2338,6 +2367,8 @@ int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
   CK(cudaEventCreate(&e1), "event");
   float best = 1e30f;
   int best_i = -1;
+  s->at_ms.clear();
+  s->at_desc.clear();
   for (int i = 0; i < ncand; ++i) {
     int rc;
     if (i < (int)cand.size()) {
@@ -2347,6 +2378,16 @@ int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
       rc = NAT_OK;
     }
     if (rc) break;
+    int desc[5] = {0, 0, 0, 0, 0};
+    {
+      int tn[3], th = 0;
+      int64_t sm = 0;
+      nat_kernel_info(s, &desc[0], tn, &th, &sm);
+      desc[1] = tn[0];
+      desc[2] = tn[1];
+      desc[3] = tn[2];
+      desc[4] = th;
+    }
     rc = nat_step_async(s, 1, 0);  // warm-up
     if (rc) break;
     cudaEventRecord(e0, s->stream);
@@ -2356,6 +2397,8 @@ int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
     CK(cudaEventSynchronize(e1), "autotune sync");
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
+    s->at_ms.push_back(ms / steps);
+    s->at_desc.insert(s->at_desc.end(), desc, desc + 5);
     if (ms < best) {
       best = ms;
       best_i = i;
@@ -2374,6 +2417,17 @@ int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
   if (best_i < (int)cand.size()) return use_candidate(s, cand[best_i]);
   s->use_v2 = false;
   return NAT_OK;
+}
+
+int nat_autotune_report(const nat_solver* s, int max, float* ms_per_step, int* desc) {
+  if (!s || max < 0) return -1;
+  const int n = (int)s->at_ms.size();
+  for (int i = 0; i < n && i < max; ++i) {
+    if (ms_per_step) ms_per_step[i] = s->at_ms[i];
+    if (desc)
+      for (int k = 0; k < 5; ++k) desc[5 * i + k] = s->at_desc[5 * i + k];
+  }
+  return n;
 }
 
 int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* threads, int64_t* smem_bytes) {

@@ -446,6 +446,45 @@ def test_shared_state_row_kernel_matches_oracle(gpu_lib, case):
     assert rel_l2(u, u1) <= 1e-6
 
 
+# Every kernel the autotuner can choose, one by one (nat_select_candidate):
+# the row-segment kernels in all their CTA shapes (incl. the z-sharing form),
+# the row-group, bulk-copy, tile and generic kernels.
+EVERY_CASES = [
+    ("D3Q19", (4, 4, 2), 4, True, "BGK_STANDARD", "fp32dev"),
+    ("D3Q19", (3, 4, 3), 2, False, "BGK_STANDARD", "fp32dev"),
+    ("D3Q27", (3, 4, 2), 3, True, "BGK_STANDARD", "fp32dev"),
+    ("D3Q27", (4, 4, 2), 3, False, "KBC_STANDARD", "fp32dev"),
+    ("D3Q19", (4, 4, 2), 4, True, "BGK_STANDARD", "fp64"),
+    ("D2Q9", (8, 8), 4, True, "BGK_STANDARD", "fp32dev"),
+]
+
+
+@pytest.mark.parametrize("case", EVERY_CASES, ids=[_ids(c[:5]) + "-" + c[5] for c in EVERY_CASES])
+def test_every_autotune_candidate_matches_oracle(gpu_lib, case):
+    stencil, cells, p, dg, model, precision = case
+    st, mesh, dt, tau, spec = make_case(stencil, cells, p, dg, model, precision=precision)
+    f0 = periodic_state(mesh, st, seed=29)
+    S = O.SLOperator(mesh, st, dt)
+    f1, rho1, u1 = oracle_step(S, st, model, tau, f0, 3)
+    with N.Solver(spec) as sol:
+        sol.upload_f(f0)
+        n, _ = sol.autotune(1)
+        kinds = [r["variant"] for r in sol.autotune_report()]
+    assert n >= 1 and len(kinds) == n
+    tol = 1e-6 if precision == "fp32dev" else 1e-12
+    for i in range(n):
+        with N.Solver(spec) as sol:
+            sol.select_candidate(i)
+            assert sol.kernel_variant == kinds[i]
+            sol.upload_f(f0)
+            sol.step(3)
+            f = sol.download_f()
+            rho, u = sol.download_macro()
+        assert rel_l2(f, f1) <= tol, (i, kinds[i])
+        assert rel_l2(rho, rho1) <= tol
+        assert rel_l2(u, u1) <= (1e-6 if precision == "fp32dev" else 1e-11)
+
+
 # Row-group kernel (sl_rowg.cuh, kernel kind 7): G warps own a whole x row
 # (32 (G - 1) < nx <= 32 G, G = 2..4).
 ROWG_CASES = [
