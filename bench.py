@@ -289,6 +289,55 @@ def bench_compressible(torch, stream, flush, steps: int = 200, warmup: int = 5, 
     return out
 
 
+MAPPED = {"name": "lubrication_sine_d2q9_bgk_sl_dg_p4_256x64", "refinement": 6, "order": 4, "Ma": 0.1,
+          "viscosity": 1e-3, "cfl": 0.4, "bottom_velocity": 0.05}
+
+
+def bench_mapped(torch, stream, flush, steps: int = 100, warmup: int = 5):
+    """MappingQ1 cells: the LubricationSine channel (the reference's
+    non-Cartesian benchmark) refined to 256 x 64 cells, D2Q9 BGK, FE_DGQ
+    p = 4 (409,600 nodes), moving bottom wall; the departure-point kernel in
+    FP32 deviation storage and in FP64, each device-timed."""
+    import natrium_gb300 as N
+    from natrium_gb300 import problems as P
+    c = MAPPED
+    V = P.lubrication_sine_grid(refinement=c["refinement"])
+    cells = tuple(s - 1 for s in V.shape[:2])
+    scaling = math.sqrt(3) / c["Ma"]
+    U = c["bottom_velocity"] * scaling
+    out = {"workload": c["name"], "unit": UNIT}
+    for precision in ("fp32dev", "fp64"):
+        spec = N.SolverSpec(stencil="D2Q9", order=c["order"], cells=cells, length=(1.0, 0.25), scaling=scaling,
+                            viscosity=c["viscosity"], cfl=c["cfl"], collision="BGK_STANDARD", precision=precision,
+                            topology="dg", periodic=(True, False, True), vertices=V)
+        t0 = time.perf_counter()
+        sol = N.Solver(spec)
+        t_create = time.perf_counter() - t0
+        sol.set_boundary(2, "VELOCITY_BOUNCE_BACK", np.array([U, 0.0, 0.0]))
+        sol.set_stream(stream.cuda_stream)
+        X = P.mapped_node_coords(V, c["order"], "dg")
+        u = P.lubrication_sine_velocity(X, U, 0.25, 0.05)
+        sol.upload_f(P.equilibrium("D2Q9", scaling, np.ones(sol.n_ref), u))
+        n_steps = steps if precision == "fp32dev" else max(20, steps // 4)
+        per, launches = time_device(sol, torch, stream, flush, n_steps, warmup)
+        ms = sum(per) / n_steps
+        n = sol.n_dev
+        es = 8 if precision == "fp64" else 4
+        # f read and written once, plus the rows: base, D unit coordinates,
+        # constant, flags per (node, direction)
+        row_bytes = (sol.Q - 1) * (4 + 2 * es + es + 1)
+        alg = n * (2 * sol.Q * es + row_bytes)
+        out[precision] = {"ms_per_step": ms, "value": n / (ms * 1e-3), "gpu_launches": launches,
+                          "algorithmic_bytes_per_launch": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9,
+                          "create_s": t_create, "kernel": f"k_mapped<D2Q9,{'double' if es == 8 else 'float'},BGK,4>",
+                          "kernel_variant": sol.kernel_variant}
+        out["nodes"] = n
+        sol.close()
+    out["value"] = out["fp32dev"]["value"]
+    out["cells"] = list(cells)
+    return out
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -341,6 +390,9 @@ def run_ours(args):
         dist.init_process_group("nccl")
     stream = torch.cuda.Stream()
     flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+    if args.mapped_only:
+        print(json.dumps(bench_mapped(torch, stream, flush, steps=args.steps, warmup=args.warmup)))
+        return 0
     if args.compressible_only:
         print(json.dumps(bench_compressible(torch, stream, flush, steps=args.steps, warmup=args.warmup,
                                             full_run=not args.profile)))
@@ -433,6 +485,7 @@ def run_ours(args):
         return 0
     cpu = cpu_baseline() if ws == 1 else None
     compressible = None if args.no_compressible else bench_compressible(torch, stream, flush)
+    mapped = None if args.no_mapped else bench_mapped(torch, stream, flush)
     serving = None
     if not args.no_serving:
         from natrium_gb300 import serving as SV
@@ -474,6 +527,7 @@ def run_ours(args):
         "speedup_vs_fp64_plain": ms64 / ms,
         "serving": serving,
         "compressible": compressible,
+        "mapped": mapped,
         "state_ok": ok,
     }
     print(json.dumps(line))
@@ -495,6 +549,9 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="lean run for ncu: FP32 device timing only (no e2e, FP64 leg, CPU baseline or clocks)")
     ap.add_argument("--no-compressible", action="store_true", help="skip the compressible D2Q25H leg")
+    ap.add_argument("--no-mapped", action="store_true", help="skip the mapped-mesh (LubricationSine) leg")
+    ap.add_argument("--mapped-only", action="store_true",
+                    help="time only the mapped-mesh leg (prints its JSON object)")
     ap.add_argument("--compressible-only", action="store_true",
                     help="time only the compressible D2Q25H leg (prints its JSON object)")
     args = ap.parse_args()

@@ -69,6 +69,8 @@ __device__ __forceinline__ void lagrange_values(Real u, const LagrangeTab<Real>&
   }
 }
 
+// (One direction per loop iteration: unrolling two, which overlaps their row
+// loads and gathers, measured 25 % slower in 2-D and 7 % in 3-D.)
 template <class S, class Real, int COLL, int P>
 __global__ void __launch_bounds__(MAP_THREADS) k_mapped(const StepParams prm, const MappedRows<Real> R,
                                                       const LagrangeTab<Real> L) {
@@ -84,8 +86,9 @@ __global__ void __launch_bounds__(MAP_THREADS) k_mapped(const StepParams prm, co
   for (int node0 = blockIdx.x * MAP_THREADS; node0 < n; node0 += gridDim.x * MAP_THREADS) {
     const int node = node0 + threadIdx.x;
     const bool live = node < n;
+    if (!live) continue;
 #pragma unroll 1
-    for (int a = 1; a < Q && live; ++a) {
+    for (int a = 1; a < Q; ++a) {
       const long long r = (long long)(a - 1) * n + node;
       const int base = __ldg(R.base + r);
       const unsigned fl = __ldg(R.flags + r);
@@ -138,7 +141,6 @@ __global__ void __launch_bounds__(MAP_THREADS) k_mapped(const StepParams prm, co
       }
       vs[a - 1][threadIdx.x] = acc + __ldg(R.cst + r);
     }
-    if (!live) continue;
     Real v[Q];
     v[0] = fin[node];
 #pragma unroll
