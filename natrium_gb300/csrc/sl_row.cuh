@@ -280,20 +280,44 @@ __device__ __forceinline__ void row_body(const RowArgs<Real>& prm, const Real* s
     (void)dz;
     (void)dy;
     (void)dx;
+    // Row offsets of the window in the rotated order (slot 0 is the
+    // dominant row), computed once per direction in the z-sharing form
+    // (there the yz-diagonals do not go through yz()).  The other forms
+    // compute them inline: holding the offsets across the two yz() calls of
+    // an x direction spills at 64 registers (measured 19 % slower).
+    constexpr bool HOIST = ZWY > 0;
+    int zo[NJZ], yo[NJY];
+    if constexpr (HOIST) {
+#pragma unroll
+      for (int jz = 0; jz < NJZ; ++jz) {
+        const int rz = j0z + jz;
+        zo[jz] = wrap(zs + (rz > P ? rz - (P + 1) : rz), nz) * nxy;
+      }
+#pragma unroll
+      for (int jy = 0; jy < NJY; ++jy) {
+        const int ry = j0y + jy;
+        yo[jy] = wrap(ys + (ry > P ? ry - (P + 1) : ry), ny) * nx;
+      }
+    }
     // yz-factored value at x position gx
     auto yz = [&](int gx) -> Real {
       Real zv[P + 1];
 #pragma unroll
       for (int jz = 0; jz < NJZ; ++jz) {
-        // rotated window order: slot 0 is the dominant row
-        const int rz = j0z + jz;
-        const int gz = wrap(zs + (rz > P ? rz - (P + 1) : rz), nz);
         Real yv[P + 1];
+        if constexpr (HOIST) {
+          const Real* __restrict__ px = src + gx;
 #pragma unroll
-        for (int jy = 0; jy < NJY; ++jy) {
-          const int ry = j0y + jy;
-          const int gy = wrap(ys + (ry > P ? ry - (P + 1) : ry), ny);
-          yv[jy] = __ldg(src + gz * nxy + gy * nx + gx);
+          for (int jy = 0; jy < NJY; ++jy) yv[jy] = __ldg(px + (zo[jz] + yo[jy]));
+        } else {
+          const int rz = j0z + jz;
+          const int gz = wrap(zs + (rz > P ? rz - (P + 1) : rz), nz);
+#pragma unroll
+          for (int jy = 0; jy < NJY; ++jy) {
+            const int ry = j0y + jy;
+            const int gy = wrap(ys + (ry > P ? ry - (P + 1) : ry), ny);
+            yv[jy] = __ldg(src + gz * nxy + gy * nx + gx);
+          }
         }
         if constexpr (sy != 0)
           zv[jz] = wsum<DEV, P>(sw[1][dy][cy], yv);
@@ -315,12 +339,9 @@ __device__ __forceinline__ void row_body(const RowArgs<Real>& prm, const Real* s
       for (int uu = zwarp; uu < U; uu += ZWY) {
         const int gy = wrap(ybase + uu, ny);
         Real zv[P + 1];
+        const Real* __restrict__ pr = src + gy * nx + gxx;
 #pragma unroll
-        for (int jz = 0; jz <= P; ++jz) {
-          const int rz = j0z + jz;
-          const int gz = wrap(zs + (rz > P ? rz - (P + 1) : rz), nz);
-          zv[jz] = __ldg(src + gz * nxy + gy * nx + gxx);
-        }
+        for (int jz = 0; jz <= P; ++jz) zv[jz] = __ldg(pr + zo[jz]);
         Z[uu * 32 + lane] = wsum<DEV, P>(sw[2][dz][cz], zv);
       }
       __syncthreads();
