@@ -2173,7 +2173,7 @@ static int launch_wall_nodes(nat_solver* s, int write_macro) {
                                     s->stream);
     }
     if (e != cudaSuccess) return cuda_fail(s, e, "two-population wall nodes");
-    s->launches++;
+    s->launches += 2;  // rows, then the collision of the nodes
     return NAT_OK;
   }
   // the step's buffers: launch_* toggled cur, so the input is the other one

@@ -439,18 +439,38 @@ __global__ void __launch_bounds__(32 * TH_WARPS, (sizeof(Real) == 4 ? 2 : 1))
   }
 }
 
-// Fused step of the wall nodes (nodes with a departure path that meets a
-// wall face): f and g gathered through the host-built rows of the node
-// (row k (Q - 1) + alpha - 1; constants: slot 0 / 1 for f in FP64 / FP32
-// deviation storage, 2 / 3 for g), relaxWithG, one write.  Runs after the
-// fused kernel of the whole lattice and overwrites the wall nodes.
+// Wall nodes of the two-population model, in two passes that keep the GPU
+// busy although the wall nodes are few:
+//  1. k_thermal_rows: one thread per sparse row (node, direction) streams f
+//     and g of that row into the output buffers (constant slots: f, g);
+//  2. k_thermal_collide_nodes: one thread per wall node collides its streamed
+//     values (rest population from the input) and writes f, g and the fields.
+// (One thread walking all 24 rows of its node, ~430 dependent loads, left
+// the few hundred warps latency-bound: ~50 us for 3,000 nodes.)
 template <class Real>
-__global__ void __launch_bounds__(128) k_thermal_wall_nodes(const __grid_constant__ ThermalStepT<Real> P, int nbn,
-                                                            const int* __restrict__ bnode,
-                                                            const int* __restrict__ ptr,
-                                                            const int* __restrict__ col, const Real* __restrict__ w,
-                                                            const double* __restrict__ cst) {
+__global__ void __launch_bounds__(256) k_thermal_rows(const __grid_constant__ ThermalStepT<Real> P, int nrows,
+                                                      const int* __restrict__ bnode, const int* __restrict__ ptr,
+                                                      const int* __restrict__ col, const Real* __restrict__ w,
+                                                      const double* __restrict__ cst) {
   constexpr bool DEV = sizeof(Real) == 4;
+  const int n = P.n;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
+    const int node = bnode[r / (TH_Q - 1)];
+    const int a = r % (TH_Q - 1) + 1;
+    Real af = Real(cst[4 * r + (DEV ? 1 : 0)]), ag = Real(cst[4 * r + (DEV ? 3 : 2)]);
+    for (int j = ptr[r]; j < ptr[r + 1]; ++j) {
+      const int c = col[j];
+      af = fma(w[j], P.f_in[c], af);
+      ag = fma(w[j], P.g_in[c], ag);
+    }
+    P.f_out[(long long)a * n + node] = af;
+    P.g_out[(long long)a * n + node] = ag;
+  }
+}
+
+template <class Real>
+__global__ void __launch_bounds__(128) k_thermal_collide_nodes(const __grid_constant__ ThermalStepT<Real> P, int nbn,
+                                                               const int* __restrict__ bnode) {
   const int n = P.n;
   int bad = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nbn; k += gridDim.x * blockDim.x) {
@@ -460,14 +480,8 @@ __global__ void __launch_bounds__(128) k_thermal_wall_nodes(const __grid_constan
     g[0] = P.g_in[node];
 #pragma unroll
     for (int a = 1; a < TH_Q; ++a) {
-      const int r = k * (TH_Q - 1) + a - 1;
-      Real af = Real(cst[4 * r + (DEV ? 1 : 0)]), ag = Real(cst[4 * r + (DEV ? 3 : 2)]);
-      for (int j = ptr[r]; j < ptr[r + 1]; ++j) {
-        af = fma(w[j], P.f_in[col[j]], af);
-        ag = fma(w[j], P.g_in[col[j]], ag);
-      }
-      f[a] = af;
-      g[a] = ag;
+      f[a] = P.f_out[(long long)a * n + node];
+      g[a] = P.g_out[(long long)a * n + node];
     }
     Real ux = Real(0), uy = Real(0);
     double rho, T, kn;
