@@ -289,6 +289,70 @@ def bench_compressible(torch, stream, flush, steps: int = 200, warmup: int = 5, 
     return out
 
 
+MIXED = {"name": "tgv3d_d3q27_kbc_sl_dg_p3_32x32x32", "stencil": "D3Q27", "collision": "KBC_STANDARD",
+         "order": 3, "cells": (32, 32, 32), "Ma": 0.1, "Re": 1600.0, "cfl": 0.4, "steps": 2000, "every": 100}
+
+
+def bench_mixed(torch, stream, flush, steps: int = None):
+    """The mixed-precision accuracy configuration: 3-D Taylor-Green, D3Q27
+    KBC, 32^3 hexahedra, FE_DGQ p = 3 (2,097,152 nodes x 27), Ma 0.1,
+    Re 1600, 2000 steps.  The FP32 deviation path and the FP64 path run side
+    by side from the same initial f; every 100 steps the relative L2
+    difference of u and rho is recorded (the FP64 path is the oracle-pinned
+    one), and each path's device time per step is reported."""
+    import natrium_gb300 as N
+    from natrium_gb300 import problems as P
+    c = MIXED
+    steps = steps or c["steps"]
+    scaling = math.sqrt(3) / c["Ma"]
+    sols = {}
+    for prec in ("fp64", "fp32dev"):
+        spec = N.SolverSpec(stencil=c["stencil"], order=c["order"], cells=c["cells"], length=(2 * math.pi,) * 3,
+                            scaling=scaling, viscosity=1.0 / c["Re"], cfl=c["cfl"], collision=c["collision"],
+                            precision=prec, topology="dg")
+        sol = N.Solver(spec)
+        sol.set_stream(stream.cuda_stream)
+        X = P.node_coords(c["cells"], c["order"], spec.length, "dg")
+        rho, u = P.taylor_green_3d(X, c["Ma"])
+        sol.upload_f(P.equilibrium(c["stencil"], scaling, rho, u))
+        sol.autotune(3)
+        sols[prec] = sol
+    rl2 = lambda a, b: float(np.sqrt(np.sum((a - b) ** 2) / np.sum(b ** 2)))
+    curve, ms = [], {"fp64": 0.0, "fp32dev": 0.0}
+    done = 0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    while done < steps:
+        k = min(c["every"], steps - done)
+        out = {}
+        for prec, sol in sols.items():
+            torch.cuda.synchronize()
+            e0.record(stream)
+            sol.step_async(k, True)
+            e1.record(stream)
+            sol.status()
+            ms[prec] += e0.elapsed_time(e1)
+            out[prec] = sol.download_macro()
+        done += k
+        curve.append({"step": done, "rel_l2_u": rl2(out["fp32dev"][1], out["fp64"][1]),
+                      "rel_l2_rho": rl2(out["fp32dev"][0], out["fp64"][0])})
+    n = sols["fp64"].n_dev
+    res = {"workload": c["name"], "nodes": n, "steps": steps, "unit": UNIT,
+           "fp32dev": {"ms_per_step": ms["fp32dev"] / steps, "value": n * steps / (ms["fp32dev"] * 1e-3),
+                       "kernel": sols["fp32dev"].kernel_info()},
+           "fp64": {"ms_per_step": ms["fp64"] / steps, "value": n * steps / (ms["fp64"] * 1e-3),
+                    "kernel": sols["fp64"].kernel_info()},
+           "speedup_fp32dev_vs_fp64": ms["fp64"] / ms["fp32dev"],
+           "max_rel_l2_u": max(r["rel_l2_u"] for r in curve), "max_rel_l2_rho": max(r["rel_l2_rho"] for r in curve),
+           "every_100_steps": curve,
+           "storage": "FP32 f - w_i with FP32 arithmetic and FP64 departure weights (no BF16/FP16 operands: "
+                      "the 1e-6 velocity target rules them out)",
+           "timing": "device events around each 100-step block, L2 not flushed (2.1 M nodes x 27 x 4 B = "
+                     "226 MB per f buffer exceeds the L2)"}
+    for sol in sols.values():
+        sol.close()
+    return res
+
+
 MAPPED = {"name": "lubrication_sine_d2q9_bgk_sl_dg_p4_256x64", "refinement": 6, "order": 4, "Ma": 0.1,
           "viscosity": 1e-3, "cfl": 0.4, "bottom_velocity": 0.05}
 
@@ -393,6 +457,9 @@ def run_ours(args):
     if args.mapped_only:
         print(json.dumps(bench_mapped(torch, stream, flush, steps=args.steps, warmup=args.warmup)))
         return 0
+    if args.mixed_only:
+        print(json.dumps(bench_mixed(torch, stream, flush)))
+        return 0
     if args.compressible_only:
         print(json.dumps(bench_compressible(torch, stream, flush, steps=args.steps, warmup=args.warmup,
                                             full_run=not args.profile)))
@@ -486,6 +553,7 @@ def run_ours(args):
     cpu = cpu_baseline() if ws == 1 else None
     compressible = None if args.no_compressible else bench_compressible(torch, stream, flush)
     mapped = None if args.no_mapped else bench_mapped(torch, stream, flush)
+    mixed = None if args.no_mixed else bench_mixed(torch, stream, flush)
     serving = None
     if not args.no_serving:
         from natrium_gb300 import serving as SV
@@ -528,6 +596,7 @@ def run_ours(args):
         "serving": serving,
         "compressible": compressible,
         "mapped": mapped,
+        "mixed_d3q27": mixed,
         "state_ok": ok,
     }
     print(json.dumps(line))
@@ -550,6 +619,9 @@ def main():
                     help="lean run for ncu: FP32 device timing only (no e2e, FP64 leg, CPU baseline or clocks)")
     ap.add_argument("--no-compressible", action="store_true", help="skip the compressible D2Q25H leg")
     ap.add_argument("--no-mapped", action="store_true", help="skip the mapped-mesh (LubricationSine) leg")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the D3Q27 KBC FP32-vs-FP64 accuracy leg")
+    ap.add_argument("--mixed-only", action="store_true",
+                    help="run only the D3Q27 KBC FP32-vs-FP64 accuracy leg (prints its JSON object)")
     ap.add_argument("--mapped-only", action="store_true",
                     help="time only the mapped-mesh leg (prints its JSON object)")
     ap.add_argument("--compressible-only", action="store_true",
