@@ -234,6 +234,8 @@ def _compressible_leg(torch, stream, flush, precision, steps, warmup, full_run):
     open_boundaries(sol)
     sol.set_stream(stream.cuda_stream)
     sol.init_thermal(rho, u, T)
+    if precision != "fp64":
+        sol.autotune(10)  # FP32: register or shared-memory form of the fused kernel
     per, launches = time_device(sol, torch, stream, flush, steps, warmup)
     ms = sum(per) / steps
     n = sol.n_dev
@@ -241,7 +243,8 @@ def _compressible_leg(torch, stream, flush, precision, steps, warmup, full_run):
     out = {"precision": precision, "ms_per_step": ms, "value": n / (ms * 1e-3), "gpu_launches": launches,
            "algorithmic_bytes_per_launch": 2 * 2 * sol.Q * es * n,
            "achieved_gbs": 2 * 2 * sol.Q * es * n / (ms * 1e-3) / 1e9,
-           "kernel": f"k_thermal_step<{'double' if es == 8 else 'float'},true>"}
+           "kernel": f"k_thermal_step<{'double' if es == 8 else 'float'},true>", "kernel_variant": sol.kernel_variant,
+           "autotune": sol.autotune_report()}
     fields = None
     if full_run:
         sol.init_thermal(rho, u, T)

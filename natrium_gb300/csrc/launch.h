@@ -85,8 +85,9 @@ void rowt_kernels_d3q27_kbc(std::vector<RowLaunch>& v);
 // Compressible two-population model on D2Q25H (k_thermal.cu): fused
 // stream(f, g) (+ relaxWithG), collision only, equilibrium initialisation;
 // FP64 and FP32-deviation forms.
-cudaError_t launch_thermal_step(const ThermalStepT<double>& P, bool collide, cudaStream_t st);
-cudaError_t launch_thermal_step(const ThermalStepT<float>& P, bool collide, cudaStream_t st);
+// form: 0 register form, 1 / 2 shared-memory forms (FP32 only)
+cudaError_t launch_thermal_step(const ThermalStepT<double>& P, bool collide, cudaStream_t st, int form);
+cudaError_t launch_thermal_step(const ThermalStepT<float>& P, bool collide, cudaStream_t st, int form);
 cudaError_t launch_thermal_collide(const ThermalPointT<double>& P, int grid, cudaStream_t st);
 cudaError_t launch_thermal_collide(const ThermalPointT<float>& P, int grid, cudaStream_t st);
 cudaError_t launch_thermal_init(const ThermalPointT<double>& P, void* f, void* g, bool fp32, int grid,

@@ -77,6 +77,7 @@ struct nat_solver {
   ThermalModelT<float> tmf;
   ThermalTablesT<double> tt;
   ThermalTablesT<float> ttf;
+  int th_form = 0;  // fused kernel form: 0 registers, 1 / 2 shared memory (FP32)
   // wall boundaries (non-periodic axes): per face kind and wall velocity, and
   // the rows of the streaming operator whose departure path meets a wall
   bool walls = false;
@@ -958,9 +959,10 @@ ThermalPointT<Real> thermal_point_params(nat_solver* s, int in_init, const Therm
 int launch_thermal(nat_solver* s, bool collide, int write_macro) {
   cudaError_t e;
   if (s->spec.precision == NAT_FP64)
-    e = launch_thermal_step(thermal_step_params<double>(s, write_macro, s->tt, s->tm), collide, s->stream);
+    e = launch_thermal_step(thermal_step_params<double>(s, write_macro, s->tt, s->tm), collide, s->stream, 0);
   else
-    e = launch_thermal_step(thermal_step_params<float>(s, write_macro, s->ttf, s->tmf), collide, s->stream);
+    e = launch_thermal_step(thermal_step_params<float>(s, write_macro, s->ttf, s->tmf), collide, s->stream,
+                            s->th_form);
   if (e != cudaSuccess) return cuda_fail(s, e, "two-population stream-collide launch");
   s->launches++;
   s->cur = 1 - s->cur;
@@ -2308,7 +2310,8 @@ int nat_set_kernel_variant(nat_solver* s, int variant) {
 int nat_kernel_variant(const nat_solver* s) {
   if (!s) return -1;
   if (s->mapped && !s->thermal) return 8;
-  return s->thermal ? 5 : (s->use_v2 ? s->kind : 1);
+  if (s->thermal) return s->th_form == 0 ? 5 : 8 + s->th_form;
+  return s->use_v2 ? s->kind : 1;
 }
 
 // The kernels nat_autotune times, in its order: the specialised candidates
@@ -2332,6 +2335,11 @@ static int tune_candidates(nat_solver* s, std::vector<Cand>* cand, int* ncand) {
 
 int nat_select_candidate(nat_solver* s, int index) {
   if (!s) return NAT_ERR_INVALID_ARG;
+  if (s->thermal && s->spec.precision != NAT_FP64 && !s->mapped) {
+    if (index < 0 || index > 2) return fail(s, NAT_ERR_INVALID_ARG, "candidate %d of 3", index);
+    s->th_form = index;
+    return NAT_OK;
+  }
   if (s->thermal || s->mapped) return index == 0 ? NAT_OK : fail(s, NAT_ERR_INVALID_ARG, "one kernel only");
   std::vector<Cand> cand;
   int ncand = 0;
@@ -2344,8 +2352,65 @@ int nat_select_candidate(nat_solver* s, int index) {
   return NAT_OK;
 }
 
+// The two-population fused kernel in FP32: time its three forms (f and g
+// backed up in the staging buffer, which holds Q n_ref doubles >= 2 Q n_dev
+// floats) and keep the fastest.
+static int autotune_thermal(nat_solver* s, int steps, int* n_candidates, int* chosen) {
+  const size_t pop = sizeof(float) * (size_t)s->Q * s->n_dev;
+  const int cur0 = s->cur, form0 = s->th_form;
+  CK(cudaMemcpyAsync(s->staging, s->f[cur0], pop, cudaMemcpyDeviceToDevice, s->stream), "autotune backup");
+  CK(cudaMemcpyAsync((char*)s->staging + pop, s->g[cur0], pop, cudaMemcpyDeviceToDevice, s->stream),
+     "autotune backup");
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0), "event");
+  CK(cudaEventCreate(&e1), "event");
+  s->at_ms.clear();
+  s->at_desc.clear();
+  float best = 1e30f;
+  int best_i = -1, rc = NAT_OK;
+  for (int form = 0; form < 3 && !rc; ++form) {
+    s->th_form = form;
+    rc = nat_step_async(s, 1, 0);
+    if (rc) break;
+    cudaEventRecord(e0, s->stream);
+    rc = nat_step_async(s, steps, 0);
+    cudaEventRecord(e1, s->stream);
+    if (rc) break;
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = cuda_fail(s, cudaGetLastError(), "autotune sync");
+      break;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const int desc[5] = {form == 0 ? 5 : 8 + form, 32, 1, 1, 32 * (form == 0 ? TH_WARPS : TH_WARPS_SS)};
+    s->at_ms.push_back(ms / steps);
+    s->at_desc.insert(s->at_desc.end(), desc, desc + 5);
+    if (ms < best) {
+      best = ms;
+      best_i = form;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s->cur = cur0;
+  CK(cudaMemcpyAsync(s->f[cur0], s->staging, pop, cudaMemcpyDeviceToDevice, s->stream), "autotune restore");
+  CK(cudaMemcpyAsync(s->g[cur0], (char*)s->staging + pop, pop, cudaMemcpyDeviceToDevice, s->stream),
+     "autotune restore");
+  CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "status clear");
+  CK(cudaStreamSynchronize(s->stream), "autotune restore sync");
+  if (rc) {
+    s->th_form = form0;
+    return rc;
+  }
+  s->th_form = best_i;
+  if (n_candidates) *n_candidates = 3;
+  if (chosen) *chosen = best_i;
+  return NAT_OK;
+}
+
 int nat_autotune(nat_solver* s, int steps, int* n_candidates, int* chosen) {
   if (!s || steps < 1) return NAT_ERR_INVALID_ARG;
+  if (s->thermal && s->spec.precision != NAT_FP64 && !s->mapped) return autotune_thermal(s, steps, n_candidates, chosen);
   if (s->thermal || s->mapped) {
     if (n_candidates) *n_candidates = 1;
     if (chosen) *chosen = 0;
@@ -2440,13 +2505,13 @@ int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* t
     return NAT_OK;
   }
   if (s->thermal) {
-    if (variant) *variant = 5;
+    if (variant) *variant = nat_kernel_variant(s);
     if (tile_nodes) {
       tile_nodes[0] = 32;
       tile_nodes[1] = 1;
       tile_nodes[2] = 1;
     }
-    if (threads) *threads = 32 * TH_WARPS;
+    if (threads) *threads = 32 * (s->th_form == 0 ? TH_WARPS : TH_WARPS_SS);
     if (smem_bytes) *smem_bytes = 0;
     return NAT_OK;
   }

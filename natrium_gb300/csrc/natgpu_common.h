@@ -84,6 +84,7 @@ struct StepParams {
 };
 
 constexpr int TH_WARPS = 8;   // warps per CTA of the fused kernel
+constexpr int TH_WARPS_SS = 4;  // warps per CTA of its shared-memory (FP32) form
 constexpr int TH_BWMAX = 64;  // x buffer width bound: 32 nodes + window halo
 constexpr int TH_Q = 25;
 constexpr int TH_NG = 9;

@@ -143,8 +143,10 @@ __device__ __forceinline__ Real eq_member(Real Em1, Real Ox, Real Oy, Real Oxy) 
 // ones.  With given_u the velocity (unscaled) is the prescribed one
 // (initialisation procedure), otherwise it is computed.  Returns the status
 // bits (density underflow / NaN).
-template <class Real>
-__device__ __forceinline__ int thermal_relax(const ThermalModelT<Real>& M, Real (&f)[TH_Q], Real (&g)[TH_Q],
+// f, g: the node's 25 + 25 values, indexable by direction (register arrays,
+// or SmemPop views of a warp's shared-memory slots)
+template <class Real, class FA, class GA>
+__device__ __forceinline__ int thermal_relax(const ThermalModelT<Real>& M, FA& f, GA& g,
                                              bool given_u, Real& ux, Real& uy, double& rho_o, double& T_o,
                                              double& kn_o) {
   constexpr bool DEV = sizeof(Real) == 4;
@@ -318,13 +320,34 @@ __device__ __forceinline__ Real th_wsum(const Real* w, const Real (&v)[PMAX1], i
 }
 
 // Fused step: stream f and g (same operator), then (COLLIDE) relaxWithG.
-template <class Real, bool COLLIDE>
-__global__ void __launch_bounds__(32 * TH_WARPS, (sizeof(Real) == 4 ? 2 : 1))
+// The populations of one lane kept in its warp's shared-memory slots
+// (stride 32 between directions).
+template <class Real>
+struct SmemPop {
+  Real* p;
+  __device__ __forceinline__ Real& operator[](int i) const { return p[i * 32]; }
+};
+
+// FORM 0: W warps per CTA, f and g of the node in 50 registers (FP32:
+// 126 registers, 16 resident warps per SM).  FORM 1 / 2: 4 warps per CTA,
+// the streamed f and g wait in the warp's shared-memory slots and the
+// collision works on them there; the registers are capped for 5 / 6
+// resident CTAs (20 / 24 warps per SM; the collision's temporaries then
+// spill a little).  The autotuner picks the form.
+template <int FORM, bool F32>
+constexpr int th_minb() {
+  return FORM == 1 ? 5 : (FORM == 2 ? 6 : (F32 ? 2 : 1));
+}
+
+template <class Real, bool COLLIDE, int W = TH_WARPS, int FORM = 0>
+__global__ void __launch_bounds__(32 * W, (th_minb<FORM, sizeof(Real) == 4>()))
     k_thermal_step(const __grid_constant__ ThermalStepT<Real> P) {
   __shared__ Real swx[ND_MAX][PER_MAX][PMAX1];
   __shared__ int soffx[ND_MAX][PER_MAX];
   __shared__ int sj0x[ND_MAX][PER_MAX];
-  __shared__ Real bufs[TH_WARPS][4][TH_BWMAX + 1];
+  constexpr bool SS = FORM > 0;
+  __shared__ Real bufs[W][4][TH_BWMAX + 1];
+  __shared__ Real pops[SS ? W : 1][2][SS ? TH_Q : 1][32];
   for (int i = threadIdx.x; i < ND_MAX * PER_MAX * PMAX1; i += blockDim.x)
     (&swx[0][0][0])[i] = (&P.tb.w[0][0][0][0])[i];
   for (int i = threadIdx.x; i < ND_MAX * PER_MAX; i += blockDim.x) {
@@ -334,7 +357,7 @@ __global__ void __launch_bounds__(32 * TH_WARPS, (sizeof(Real) == 4 ? 2 : 1))
   __syncthreads();
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wid = blockIdx.x * TH_WARPS + warp;
+  const int wid = blockIdx.x * W + warp;
   if (wid >= P.nseg * P.ny) return;  // warp-uniform
   const int nx = P.nx, ny = P.ny, n = P.n;
   const int p = P.tb.p, per = P.tb.per;
@@ -348,7 +371,8 @@ __global__ void __launch_bounds__(32 * TH_WARPS, (sizeof(Real) == 4 ? 2 : 1))
   const int gxa = ((x0 + P.tb.xl + lane) % nx + nx) % nx;
   const bool hasb = lane + 32 < P.tb.bw;
 
-  Real fs[TH_Q], gs[TH_Q];
+  // the step on the node's populations fs, gs (registers or shared memory)
+  auto body = [&](auto& fs, auto& gs) {
   fs[0] = P.f_in[node];
   gs[0] = P.g_in[node];
 
@@ -436,6 +460,14 @@ __global__ void __launch_bounds__(32 * TH_WARPS, (sizeof(Real) == 4 ? 2 : 1))
   for (int q = 0; q < TH_Q; ++q) {
     P.f_out[(long long)q * n + node] = fs[q];
     P.g_out[(long long)q * n + node] = gs[q];
+  }
+  };
+  if constexpr (SS) {
+    SmemPop<Real> fsm{&pops[warp][0][0][lane]}, gsm{&pops[warp][1][0][lane]};
+    body(fsm, gsm);
+  } else {
+    Real fs[TH_Q], gs[TH_Q];
+    body(fs, gs);
   }
 }
 

@@ -214,6 +214,36 @@ def test_fp32_200_steps_close_to_oracle(gpu_lib, settings):
     assert rel_l2(u, u1) <= 1e-4
 
 
+@pytest.mark.parametrize("form", [0, 1, 2], ids=["registers", "smem-20-warps", "smem-24-warps"])
+@pytest.mark.parametrize("settings", [N.ThermalSettings(), N.ThermalSettings(prandtl=0.71, prandtl_set=True,
+                                                                             sutherland=True)],
+                         ids=["default", "prandtl-sutherland"])
+def test_fp32_kernel_forms_close_to_oracle(gpu_lib, form, settings):
+    """The three forms of the FP32 fused kernel (nat_select_candidate: f and
+    g in registers, or in shared memory with 20 / 24 resident warps)."""
+    st, mesh, dt, tau, spec = thermal_case((6, 6), 3, True, scaling=1.2)
+    rho0, u0, T0, f0, g0 = thermal_state(mesh, st, seed=9, gamma=settings.gamma)
+    S = O.SLOperator(mesh, st, dt)
+    f1, g1 = f0.copy(), g0.copy()
+    r1, u1, T1, m1 = S.step_compressible(f1, g1, tau, _th(settings), nsteps=3)
+    with N.Solver(_spec32(spec)) as sol:
+        sol.set_thermal(settings)
+        sol.select_candidate(form)
+        assert sol.kernel_variant == (5 if form == 0 else 8 + form)
+        sol.upload_f(f0)
+        sol.upload_g(g0)
+        sol.step(3)
+        f, g = sol.download_f(), sol.download_g()
+        T, _ = sol.download_thermal()
+        n, ch = sol.autotune(2)
+        rep = sol.autotune_report()
+        assert n == 3 and len(rep) == 3 and sol.kernel_variant == rep[ch]["variant"]
+        assert rel_l2(sol.download_f(), f) <= 1e-7  # the autotuner restored f
+    assert rel_l2(f, f1) <= 1e-6
+    assert rel_l2(g, g1) <= 1e-6
+    assert rel_l2(T, T1) <= 1e-6
+
+
 def test_fp32_initialisation_and_uniform_state(gpu_lib):
     st, mesh, dt, tau, spec = thermal_case((4, 4), 2, False, scaling=1.1)
     n = mesh.n_nodes
