@@ -193,7 +193,9 @@ int nat_mass_energy(nat_solver* s, double* mass, double* kinetic_energy);
  * nodes are rejected (NAT_ERR_INVALID_ARG).  The first call on a device looks
  * up the array's device address (make it before any stream capture); calls
  * whose kernels overlap on the GPU share the array and race.  Calls no
- * cudaMalloc / cudaFree.  Deterministic: fixed reduction order. */
+ * cudaMalloc / cudaFree.  Deterministic: fixed reduction order.  The node
+ * weights are those of the Cartesian box (cell_size); a mapped mesh's
+ * weights depend on its cells' Jacobians: use nat_mass_energy there. */
 #define NAT_NOALLOC_MAX_NODES 16777216LL
 int nat_mass_energy_noalloc(const double* rho_dev, const double* u_dev, int dim, const int n_axis[3],
                             int order, int topology, const double cell_size[3], double* out_dev,
