@@ -412,6 +412,18 @@ def dist_env():
     return ws, rank, local
 
 
+def aggregate_ranks(torch, ws: int, total_ms: float, nodes: int, steps: int, device="cuda"):
+    """Replicas: every rank timed `steps` steps of its own `nodes`-node solve.
+    Returns the slowest rank's total (all ranks must call this; a MAX
+    all-reduce, no data-path collective) and the whole-job throughput
+    ws * nodes * steps / that time."""
+    if ws > 1:
+        t = torch.tensor([total_ms], device=device, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, ws * nodes * steps / (total_ms * 1e-3)
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -499,14 +511,9 @@ def run_ours(args):
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
-    total_ms = sum(per)
-    if ws > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    ms = total_ms / args.steps
     nodes = sol.n_dev
-    value = ws * nodes * args.steps / (total_ms * 1e-3)
+    total_ms, value = aggregate_ranks(torch, ws, sum(per), nodes, args.steps)
+    ms = total_ms / args.steps
     Q = sol.Q
 
     # --- e2e through the C ABI with host buffers -------------------------------
@@ -517,6 +524,8 @@ def run_ours(args):
     rho_h = torch.empty(sol.n_ref, dtype=torch.float64).pin_memory().numpy()
     u_h = torch.empty((sol.D, sol.n_ref), dtype=torch.float64).pin_memory().numpy()
     e2e_s = time_e2e(sol, torch, f_host, rho_h, u_h, e2e_steps)
+    e2e_ms, _ = aggregate_ranks(torch, ws, e2e_s * 1e3, nodes, 1)  # slowest rank
+    e2e_s = e2e_ms * 1e-3
     h2d = f0.nbytes
     d2h = 8 * (1 + sol.D) * sol.n_ref
     # correctness guard on the measured state: finite, mass near 1
