@@ -481,7 +481,7 @@ def run_ours(args):
         return 0
 
     # --- FP32-deviation path (headline) -------------------------------------
-    spec = spec_for("fp32dev")
+    spec = spec_for(args.profile_precision if args.profile else "fp32dev")
     f0 = initial_state(spec)
     sol = N.Solver(spec)
     sol.set_stream(stream.cuda_stream)
@@ -627,6 +627,8 @@ def main():
                     help="fused kernel: 0 autotuned, 1 generic, 3 tile, 4 row-segment, 6 bulk-copy row-segment, "
                          "7 row-group")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
+    ap.add_argument("--profile-precision", default="fp32dev", choices=["fp32dev", "fp64"],
+                    help="with --profile: the path to time (the headline FP32 deviation path or plain FP64)")
     ap.add_argument("--profile", action="store_true",
                     help="lean run for ncu: FP32 device timing only (no e2e, FP64 leg, CPU baseline or clocks)")
     ap.add_argument("--no-compressible", action="store_true", help="skip the compressible D2Q25H leg")
