@@ -2178,17 +2178,20 @@ static int launch_wall_nodes(nat_solver* s, int write_macro) {
     s->launches += 2;  // rows, then the collision of the nodes
     return NAT_OK;
   }
-  // the step's buffers: launch_* toggled cur, so the input is the other one
+  // the step's buffers: launch_* toggled cur, so the input is the other one;
+  // the rows first (one thread per row), then the nodes' collision
+  int rc = launch_wall_rows(s, s->f[1 - s->cur], s->f[s->cur], false);
+  if (rc) return rc;
   StepParams P = step_params(s, s->f[1 - s->cur], s->f[s->cur], 1, write_macro, 0);
   void* args[2];
   WallNodes<double> W64;
   WallNodes<float> W32;
   args[0] = &P;
   if (s->spec.precision == NAT_FP64) {
-    W64 = {s->nbn, s->d_bn_node, s->d_br_ptr, s->d_br_col, s->d_br_w, s->d_br_c, 0};
+    W64 = {s->nbn, s->d_bn_node};
     args[1] = &W64;
   } else {
-    W32 = {s->nbn, s->d_bn_node, s->d_br_ptr, s->d_br_col, s->d_br_wf, s->d_br_c, 1};
+    W32 = {s->nbn, s->d_bn_node};
     args[1] = &W32;
   }
   CK(cudaLaunchKernel(s->ks_coll.wallnode, dim3((s->nbn + 127) / 128), dim3(128), args, 0, s->stream),

@@ -320,19 +320,18 @@ __global__ void __launch_bounds__(NT) k_sl_step(const StepParams P) {
 // row k (Q - 1) + alpha - 1 holding sum_j w_j f_in[col_j] + cst[4 row + slot].
 template <class Real>
 struct WallNodes {
-  int nbn;
-  const int* node;
-  const int* ptr;
-  const int* col;
-  const Real* w;
-  const double* cst;
-  int slot;
+  int nbn;           // wall nodes
+  const int* node;   // their lattice indices
 };
 
-// Fused step of the wall nodes: gather their streamed values through the
-// sparse rows, collide, write f (and rho/u on output steps).  Runs after the
-// fused kernel of the whole lattice and overwrites the wall nodes, whose
-// periodic-window values there are not the wall's.
+// Collision of the wall nodes.  Their sparse rows have just been streamed
+// into f_out by k_wall_rows (one thread per row); this takes the streamed
+// values from there and the rest population from f_in, collides, and writes
+// f (and rho/u on output steps).  Runs after the fused kernel of the whole
+// lattice and overwrites the wall nodes, whose periodic-window values there
+// are not the wall's.  (One thread walking all Q-1 rows of its node was
+// latency-bound: a few thousand wall nodes are too few warps to hide ~300
+// dependent loads each.)
 template <class S, class Real, int COLL>
 __global__ void __launch_bounds__(128) k_wall_nodes(const StepParams P, const WallNodes<Real> W) {
   constexpr bool DEV = sizeof(Real) == 4;
@@ -346,12 +345,7 @@ __global__ void __launch_bounds__(128) k_wall_nodes(const StepParams P, const Wa
     Real v[Q];
     v[0] = fin[node];
 #pragma unroll
-    for (int a = 1; a < Q; ++a) {
-      const int r = k * (Q - 1) + a - 1;
-      Real acc = Real(W.cst[4 * r + W.slot]);
-      for (int j = W.ptr[r]; j < W.ptr[r + 1]; ++j) acc = fma(W.w[j], fin[W.col[j]], acc);
-      v[a] = acc;
-    }
+    for (int a = 1; a < Q; ++a) v[a] = fout[(long long)a * n + node];
     Real u[3] = {0, 0, 0};
     Real rho = Real(1);
     Real pre[Q];
