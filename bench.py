@@ -163,8 +163,9 @@ def time_e2e(sol, torch, f_host, rho_h, u_h, steps: int):
     t0 = time.perf_counter()
     for _ in range(steps):
         sol.upload_f(f_host)
-        sol.step(1)
+        sol.step_async(1, True)              # enqueue; the download below synchronises
         r, u = sol.download_macro(rho_h, u_h)
+        sol.status()                         # the step's density check, every step
     torch.cuda.synchronize()
     return (time.perf_counter() - t0) / steps
 
