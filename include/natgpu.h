@@ -116,7 +116,9 @@ typedef struct nat_solver nat_solver;
 
 /* Create a solver: allocates device buffers on the current CUDA device and
  * assembles the streaming operator for dt (SemiLagrangian::setDeltaT ->
- * updateSparsityPattern/reassemble, advection/SemiLagrangian.h:175-179). */
+ * updateSparsityPattern/reassemble, advection/SemiLagrangian.h:175-179).
+ * Q x nodes must stay below 2^31 (32-bit indexing in the kernels; e.g.
+ * 113 M nodes of D3Q19): larger lattices get NAT_ERR_UNSUPPORTED. */
 int nat_create(const nat_spec* spec, nat_solver** out);
 int nat_destroy(nat_solver* s);
 

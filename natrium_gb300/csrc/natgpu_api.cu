@@ -1963,6 +1963,11 @@ int nat_create(const nat_spec* spec, nat_solver** out) {
   for (int q = 0; q < s->Q; ++q)
     s->rest[q] = spec->collision == NAT_BGK_INCOMPRESSIBLE ? inc_rest(q) : hs.w[q];
   *out = s;
+  // the kernels index one population buffer (Q blocks of n nodes) with 32-bit
+  // integers: refuse lattices beyond that before anything is allocated
+  if ((long long)s->Q * std::max(s->n_dev, s->n_ref) >= (long long)INT32_MAX)
+    return fail(s, NAT_ERR_UNSUPPORTED, "lattice too large: Q x nodes = %lld must stay below 2^31",
+                (long long)s->Q * std::max(s->n_dev, s->n_ref));
   s->spec.vertices = nullptr;  // not retained: the grid is copied
   CK(cudaGetDevice(&s->device), "cudaGetDevice");
   if (spec->vertices) {

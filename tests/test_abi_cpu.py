@@ -69,3 +69,14 @@ def test_last_error_null_handle():
     buf = C.create_string_buffer(64)
     assert L.nat_last_error(None, buf, 64) == 0
     assert buf.value == b"null handle"
+
+
+def test_lattice_beyond_32bit_indexing_is_refused_without_gpu():
+    # 200^3 cells of p = 4 DG: 10^9 nodes x 19 populations > 2^31 -- refused
+    # before anything is allocated or launched
+    spec = N.SolverSpec(stencil="D3Q19", order=4, cells=(200, 200, 200), length=(1, 1, 1), scaling=1.0,
+                        viscosity=0.1, topology="dg", precision="fp32dev")
+    with pytest.raises(N.NatError) as ei:
+        N.Solver(spec)
+    assert ei.value.code == N.NAT_ERR_UNSUPPORTED
+    assert "2^31" in str(ei.value)
