@@ -149,6 +149,22 @@ def lubrication_sine_grid(length: float = 1.0, average_height: float = 0.25, amp
     return np.stack([xr, yr / H * upper], -1)
 
 
+def sinusoidal_shear_grid(length: float = 1.0, average_height: float = 1.0, amplitude: float = 0.1,
+                          cell_aspect_ratio: float = 1.0, refinement: int = 2) -> np.ndarray:
+    """Vertices of the SinusoidalShear2D gap (benchmarks/SinusoidalShear2D.cpp:33-52 and
+    .h:80-105): the unit square of 1 / aspect x 1 cells refined `refinement` times, mapped by
+    x -> L x_r, x_r = x - 0.019 A / 0.49 sin(4 pi x), and
+    y -> y_r(y) (H + A sin(2 pi x_r)), y_r(y) = 1/2 + tanh(pi (y - 1/2)) / (2 tanh(pi / 2)).
+    x is periodic; the bottom (y = 0, moving) and the wavy top are walls."""
+    H, A = average_height, amplitude
+    nx = int(1.0 / cell_aspect_ratio) * 2 ** refinement
+    ny = 2 ** refinement
+    X, Y = np.meshgrid(np.linspace(0.0, 1.0, nx + 1), np.linspace(0.0, 1.0, ny + 1), indexing="ij")
+    xr = X - 0.019 * A / 0.49 * np.sin(4 * math.pi * X)
+    yr = 0.5 + 0.5 * np.tanh((Y - 0.5) * math.pi) / math.tanh(0.5 * math.pi)
+    return np.stack([length * xr, yr * (H + A * np.sin(2 * math.pi * xr))], -1)
+
+
 def lubrication_sine_velocity(X: np.ndarray, bottom_velocity: float, average_height: float, amplitude: float):
     """Initial velocity (LubricationSine.cpp:78-87): u = U (1 - y / (H - A))^2, v = 0."""
     upper = average_height - amplitude

@@ -87,6 +87,19 @@ def test_lubrication_sine_channel_constant_streaming(p):
     assert S.wall_hits > 0
 
 
+@pytest.mark.parametrize("p", [2, 3])
+def test_sinusoidal_shear_gap_constant_streaming(p):
+    V = P.sinusoidal_shear_grid(refinement=2)
+    cells = tuple(s - 1 for s in V.shape[:2])
+    assert np.abs(V[-1, :, 0] - V[0, :, 0] - 1.0).max() < 1e-12  # one translation along x
+    st = O.stencil("D2Q9", 1.0)
+    m = O.Mesh(2, cells, p, True, (1.0, 1.0), bc=(0, 0, 1, 1, 0, 0), uw=((0, 0, 0),) * 6, vertices=V)
+    dt = O.time_step(m.h_min(), p, st.max_speed, 0.4)
+    S = O.SLOperator(m, st, dt)
+    assert np.abs(S.stream(np.ones((9, m.n_nodes))) - 1.0).max() < 1e-14
+    assert S.wall_hits > 0
+
+
 def test_periodic_axis_needs_one_translation():
     V = P.wavy_grid((3, 3), (1.0, 1.0), 0.1)
     V[-1, 1, 1] += 0.01  # x+ face no longer a translate of the x- face
@@ -222,6 +235,30 @@ def test_lubrication_sine_channel_matches_oracle(gpu_lib, precision):
     tol = 1e-12 if precision == "fp64" else 1e-6
     assert rel_l2(f, f1) <= tol
     assert rel_l2(u, u1) <= (1e-11 if precision == "fp64" else 1e-5)
+
+
+@pytest.mark.gpu
+def test_sinusoidal_shear_gap_matches_oracle(gpu_lib):
+    V = P.sinusoidal_shear_grid(refinement=2)
+    cells = tuple(s - 1 for s in V.shape[:2])
+    scaling = math.sqrt(3) / 0.1
+    U = 0.05 * scaling
+    bc = (0, 0, 1, 1, 0, 0)
+    uw = ((0, 0, 0), (0, 0, 0), (U, 0, 0), (0, 0, 0), (0, 0, 0), (0, 0, 0))
+    st, m, dt, tau, spec = _mapped_case("D2Q9", cells, 3, True, V, bc=bc, uw=uw, nu=0.01, model="KBC_STANDARD")
+    f0 = _state(m, st, seed=11)
+    S = O.SLOperator(m, st, dt)
+    f1 = f0.copy()
+    rho1, u1 = np.zeros(m.n_nodes), np.zeros((2, m.n_nodes))
+    for _ in range(3):
+        f1 = S.stream(f1)
+        O.collide(st, "KBC_STANDARD", tau, f1, rho1, u1)
+    with N.Solver(spec) as sol:
+        sol.set_boundary(2, "VELOCITY_BOUNCE_BACK", np.array([U, 0.0, 0.0]))
+        sol.upload_f(f0)
+        sol.step(3)
+        f = sol.download_f()
+    assert rel_l2(f, f1) <= 1e-12
 
 
 @pytest.mark.gpu
