@@ -6,6 +6,9 @@ Oracle known answers, restated from the reference's own tests
 y = 1 moving with u = (0.01, 0), nu = 0.2, D2Q9, scaling 1, FE_Q:
   * p = 1, CFL 0.4, 10 steps from rest: the mean density stays 1 within 1e-10;
   * p = 2, CFL 1, 100 steps: |u - 0.01| <= 1e-3 and |v| <= 1e-5 at every node.
+The boundary handler's hit counts on CouetteFlow2D
+(boundaries/SemiLagrangianBoundaryHandler_test.cpp): 102 hits at dt = 0.001,
+204 at dt = 0.1.
 GPU parity (DG topology, through the C ABI): relative L2 <= 1e-12 per step in
 FP64 and <= 1e-6 in FP32 deviation storage against the oracle's tracker.
 """
@@ -45,6 +48,22 @@ def test_bounce_back_wall_velocity_known_answer():
     rho, u = S.step_bgk(f, tau, 100)
     assert np.abs(u[0] - 0.01).max() <= 1e-3
     assert np.abs(u[1]).max() <= 1e-5
+
+
+@pytest.mark.parametrize("dt,layers", [(0.001, 1), (0.1, 2)])
+def test_wall_hit_counts_known_answer(dt, layers):
+    """SemiLagrangianBoundaryHandler_DataStructures_test / _offSupportHits_test
+    (boundaries/SemiLagrangianBoundaryHandler_test.cpp:98-176): CouetteFlow2D on
+    [0, 1]^2, refinement 3 (8 x 8 cells), FE_Q p = 2, D2Q9, walls at y = 0 and
+    y = 1, periodic x.  A small step hits the walls from the support points on
+    them only: (2^3 * 2 * 2 + 2) points x 3 directions = 102 hits; dt = 0.1
+    reaches the second node layer: twice that."""
+    st = O.stencil("D2Q9", 1.0)
+    uw = ((0, 0, 0), (0, 0, 0), (0, 0, 0), (0.1, 0, 0), (0, 0, 0), (0, 0, 0))
+    m = O.Mesh(2, (8, 8), 2, False, (1.0, 1.0), bc=(0, 0, 1, 1, 0, 0), uw=uw)
+    S = O.SLOperator(m, st, dt)
+    n_points = 2 ** 3 * 2 * 2 + 2
+    assert S.wall_hits == layers * n_points * 3
 
 
 def test_bounce_back_rows_reverse_the_population():
