@@ -203,6 +203,24 @@ def test_mass_energy_reduction(gpu_lib):
     assert m == pytest.approx(_mass(mesh, rho1), rel=1e-12)
 
 
+def test_physical_properties_known_answers(gpu_lib):
+    """solver/PhysicalProperties_test.cpp:46-91.  Mass of CouetteFlow2D on the unit
+    square (rho = 1): 1 within 1e-4 %.  Kinetic energy of the ShearLayer2D
+    initial state (Minion & Brown: u0 = 1, kappa = 80, nu = 1e-4, refinement 3
+    -> 8 x 8 cells, scaling 10, FE_Q p = 2): 0.476 within 10 %."""
+    from natrium_gb300 import problems as P
+    spec = N.SolverSpec(stencil="D2Q9", order=2, cells=(8, 8), length=(1.0, 1.0), scaling=10.0, viscosity=1e-4,
+                        cfl=0.4, topology="feq")
+    X = P.node_coords((8, 8), 2, (1.0, 1.0), "feq")
+    rho, u = P.shear_layer_2d(X, kappa=80.0, delta=0.05, L=1.0)
+    with N.Solver(spec) as sol:
+        sol.upload_f(P.equilibrium("D2Q9", 10.0, rho, u))
+        sol.collide()  # rho and u (scaled) from the moments of f
+        m, e = sol.mass_energy()
+    assert m == pytest.approx(1.0, rel=1e-6)
+    assert e == pytest.approx(0.476, rel=0.10)
+
+
 def _mass(mesh, rho):
     # sum_cells sum_q rho w_q |J| via the oracle's quadrature (KE with |u| = 1)
     one = np.ones((mesh.dim, rho.size)) / math.sqrt(mesh.dim)
