@@ -391,9 +391,11 @@ def bench_mapped(torch, stream, flush, steps: int = 100, warmup: int = 5):
         ms = sum(per) / n_steps
         n = sol.n_dev
         es = 8 if precision == "fp64" else 4
-        # f read and written once, plus the rows: base, D unit coordinates,
-        # constant, flags per (node, direction)
-        row_bytes = (sol.Q - 1) * (4 + 2 * es + es + 1)
+        # f read and written once, plus the rows per (node, direction): base,
+        # D unit coordinates (FP32) or D (p + 1) Lagrange values (FP64),
+        # constant, flags
+        per_row = 2 * es if es == 4 else 2 * (c["order"] + 1) * es
+        row_bytes = (sol.Q - 1) * (4 + per_row + es + 1)
         alg = n * (2 * sol.Q * es + row_bytes)
         out[precision] = {"ms_per_step": ms, "value": n / (ms * 1e-3), "gpu_launches": launches,
                           "algorithmic_bytes_per_launch": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9,

@@ -1391,7 +1391,8 @@ int build_wall_rows(nat_solver* s) {
   if (dp) {
     if ((long long)Q * n > INT32_MAX) return fail(s, NAT_ERR_UNSUPPORTED, "Q x nodes exceeds 2^31");
     mp_base.assign((size_t)(Q - 1) * n, 0);
-    mp_u.assign((size_t)(Q - 1) * D * n, 0.0);
+    // FP32: unit coordinates; FP64: the 1-D Lagrange values (sl_mapped.cuh)
+    mp_u.assign((size_t)(Q - 1) * D * n * (s->spec.precision == NAT_FP64 ? p + 1 : 1), 0.0);
     mp_c.assign((size_t)2 * (Q - 1) * n, 0.0);
     mp_flags.assign((size_t)(Q - 1) * n, 0);
   }
@@ -1492,7 +1493,13 @@ int build_wall_rows(nat_solver* s) {
         const long long first =
             ((long long)(cell[2] * PER) * s->n_ax[1] + cell[1] * PER) * s->n_ax[0] + cell[0] * PER;
         mp_base[r] = (int)(sdir * n + first);
-        for (int a = 0; a < D; ++a) mp_u[((long long)(alpha - 1) * D + a) * n + node] = uu[a];
+        if (s->spec.precision == NAT_FP64) {
+          for (int a = 0; a < D; ++a)
+            for (int j = 0; j <= p; ++j)
+              mp_u[(((long long)(alpha - 1) * D + a) * (p + 1) + j) * n + node] = l1[a][j];
+        } else {
+          for (int a = 0; a < D; ++a) mp_u[((long long)(alpha - 1) * D + a) * n + node] = uu[a];
+        }
         mp_c[2 * r] = c;                                // plain f
         mp_c[2 * r + 1] = c + wrest - s->rest[alpha];  // f - w_i storage
         unsigned char fl = tiny ? MAP_TINY : 0;

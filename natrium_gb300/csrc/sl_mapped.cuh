@@ -7,7 +7,8 @@
 // values are products of 1-D Lagrange polynomials at the departure point's
 // UNIT coordinates, so a row is fully described by
 //   base   source index of the cell's first node (source direction * n + node),
-//   u[D]   unit coordinates of the departure point in that cell,
+//   u[D]   unit coordinates of the departure point in that cell (FP32; the
+//          FP64 form stores the D (P+1) 1-D Lagrange values instead),
 //   cst    additive constant (bounce-back wall terms, deviation-form offset),
 //   flags  bits 0-2: the local node p of this cell along x / y / z is node 0
 //          of the axis (FE_Q, last cell of a periodic axis); bit 3: the row
@@ -37,7 +38,8 @@ constexpr unsigned MAP_TINY = 8u;
 template <class Real>
 struct MappedRows {
   const int* base;             // (Q-1) n
-  const Real* u;               // (Q-1) D n: [(a-1) D + d] n + node
+  const Real* u;               // FP32: unit coordinates, (Q-1) D n: [(a-1) D + d] n + node;
+                               // FP64: 1-D Lagrange values, [((a-1) D + d) (P+1) + j] n + node
   const Real* cst;             // (Q-1) n
   const unsigned char* flags;  // (Q-1) n
   int nax[3];                  // lattice nodes per axis
@@ -92,12 +94,25 @@ __global__ void __launch_bounds__(MAP_THREADS) k_mapped(const StepParams prm, co
       const long long r = (long long)(a - 1) * n + node;
       const int base = __ldg(R.base + r);
       const unsigned fl = __ldg(R.flags + r);
-      const Real* ur = R.u + (long long)(a - 1) * D * n + node;
       Real lx[NP], ly[NP], lz[NP];
-      lagrange_values<P>(__ldg(ur), L, lx);
-      lagrange_values<P>(__ldg(ur + n), L, ly);
-      if constexpr (D == 3) lagrange_values<P>(__ldg(ur + 2 * n), L, lz);
-      else lz[0] = Real(1);
+      if constexpr (sizeof(Real) == 8) {
+        // FP64: the 1-D Lagrange values are stored (the FP64 pipe is the
+        // bound; evaluating them here cost as much as the gather itself)
+        const Real* lr = R.u + (long long)(a - 1) * D * NP * n + node;
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {
+          lx[j] = __ldg(lr + (long long)j * n);
+          ly[j] = __ldg(lr + (long long)(NP + j) * n);
+          if constexpr (D == 3) lz[j] = __ldg(lr + (long long)(2 * NP + j) * n);
+        }
+        if constexpr (D == 2) lz[0] = Real(1);
+      } else {
+        const Real* ur = R.u + (long long)(a - 1) * D * n + node;
+        lagrange_values<P>(__ldg(ur), L, lx);
+        lagrange_values<P>(__ldg(ur + n), L, ly);
+        if constexpr (D == 3) lagrange_values<P>(__ldg(ur + 2 * n), L, lz);
+        else lz[0] = Real(1);
+      }
       // offsets of the local nodes; node p wraps to node 0 of the axis on the
       // last FE_Q cell of a periodic axis
       int ox[NP], oy[NP], oz[NZ];
