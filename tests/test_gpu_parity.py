@@ -203,6 +203,39 @@ def test_mass_energy_reduction(gpu_lib):
     assert m == pytest.approx(_mass(mesh, rho1), rel=1e-12)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
+def test_tgv2d_integration_known_answer(gpu_lib, precision):
+    """The reference's semi-Lagrangian Taylor-Green integration test
+    (ConvergenceTestSemiLagrangianPeriodic, IntegrationTestCases.cpp:885-961),
+    run on the device: 8 x 8 cells, FE_Q p = 4, D2Q9 BGK, nu = 1, Ma = 0.05,
+    CFL 0.4; after t = 1 / (2 nu), E_kin / E_kin(0) = e^-2 within 1e-2 and the
+    velocity's relative L2 error against the analytic decay below 5e-2."""
+    import json
+    import os
+    from natrium_gb300 import problems as P
+    with open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")) as fh:
+        c = json.load(fh)["tgv2d_sl"]
+    Ma, nu, p = c["Ma"], c["viscosity"], c["order"]
+    n = 2 ** c["refinement"]
+    scaling = math.sqrt(3) / Ma
+    spec = N.SolverSpec(stencil="D2Q9", order=p, cells=(n, n), length=(2 * math.pi,) * 2, scaling=scaling,
+                        viscosity=nu, cfl=c["cfl"], collision="BGK_STANDARD", precision=precision, topology="feq")
+    X = P.node_coords((n, n), p, spec.length, "feq")
+    rho0, u0 = P.taylor_green_2d(X, Ma)
+    with N.Solver(spec) as sol:
+        sol.upload_macro(rho0, u0)  # E_kin(0) of the initial fields
+        _, e0 = sol.mass_energy()
+        nsteps = int(round(1.0 / (2 * nu) / sol.dt))
+        sol.upload_f(P.equilibrium("D2Q9", scaling, rho0, u0))
+        sol.step(nsteps)
+        _, e1 = sol.mass_energy()
+        rho, u = sol.download_macro()
+        t = nsteps * sol.dt
+    assert abs(e1 / e0 - math.exp(-2)) < c["ekin_tol"]
+    ua = np.stack([np.sin(X[:, 0]) * np.cos(X[:, 1]), -np.cos(X[:, 0]) * np.sin(X[:, 1])]) * math.exp(-2 * nu * t)
+    assert rel_l2(u, ua) < c["l2_velocity_tol"]
+
+
 def test_physical_properties_known_answers(gpu_lib):
     """solver/PhysicalProperties_test.cpp:46-91.  Mass of CouetteFlow2D on the unit
     square (rho = 1): 1 within 1e-4 %.  Kinetic energy of the ShearLayer2D
