@@ -264,7 +264,8 @@ int nat_init_thermal(nat_solver* s, const double* rho_host, const double* u_host
  * iteration, time, stencil scaling and FE order, and the f vectors): one
  * binary file with a header (those fields plus the lattice) and f (and g for
  * NAT_BGK_COMPRESSIBLE) in the reference layout, FP64.  Loading checks that
- * lattice, stencil, order and scaling are the handle's. */
+ * lattice, stencil, order and scaling are the handle's, and for a mapped
+ * mesh its vertex grid (by a hash of the vertex array's bytes). */
 int nat_checkpoint_save(nat_solver* s, const char* path, int64_t iteration, double time);
 int nat_checkpoint_load(nat_solver* s, const char* path, int64_t* iteration, double* time);
 

@@ -1,0 +1,143 @@
+// Internal to libnatgpu.so: the solver handle and the helpers its
+// translation units share.
+//   natgpu_api.cu  creation, stepping, transfers, reductions, kernel choice;
+//   tracker.cu     the host departure-path tracker: wall rows, mapped-mesh
+//                  (MappingQ1) rows and mesh setup;
+//   io.cu          checkpoint and solution output.
+// Not part of the C ABI (include/natgpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/natgpu.h"
+#include "launch.h"
+#include "natgpu_common.h"
+#include "sl_step_v2.cuh"
+
+struct nat_solver {
+  nat_spec spec;
+  int D = 0, Q = 0;
+  int period = 0;
+  int n_ax[3] = {1, 1, 1};      // device lattice per axis
+  int n_ref_ax[3] = {1, 1, 1};  // reference layout per axis
+  long long n_dev = 0, n_ref = 0;
+  double dt = 0, tau = 0, h[3] = {1, 1, 1};
+  double cs2_scaled = 0;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  void* f[2] = {nullptr, nullptr};
+  int cur = 0;
+  double* rho = nullptr;
+  double* u = nullptr;
+  double* staging = nullptr;  // Q * n_ref doubles
+  double* red = nullptr;      // reduction results (2 doubles)
+  int* status = nullptr;
+  natgpu::SLTables* d_tab = nullptr;
+  natgpu::SLTables h_tab;
+  int B[3] = {1, 1, 1};
+  int ntiles = 0;
+  size_t smem_step = 0;
+  natgpu::KernelSet ks_coll, ks_stream;
+  std::string err;
+  long long launches = 0;
+  double rest[32];
+  // specialised kernel (sl_step_v2.cuh)
+  int variant = 0;  // 0 auto, 1 generic only, 2 specialised required
+  bool use_v2 = false;  // a specialised kernel (tile or row) is in use
+  int kind = 1;         // 1 generic, 2 tile, 3 row
+  natgpu::V2Launch v2;
+  natgpu::RowLaunch row;
+  natgpu::SpecWeights<double> w64;
+  natgpu::SpecWeights<float> w32;
+  // compressible two-population model (D2Q25H)
+  bool thermal = false;
+  nat_thermal th;
+  void* g[2] = {nullptr, nullptr};  // second population, same layout and type as f
+  double* T = nullptr;              // temperature
+  double* mask = nullptr;           // shock sensor (Knudsen estimate)
+  double gref = 3.0;                // FP32 deviation storage of g: g - w_i gref
+  natgpu::ThermalModelT<double> tm;
+  natgpu::ThermalModelT<float> tmf;
+  natgpu::ThermalTablesT<double> tt;
+  natgpu::ThermalTablesT<float> ttf;
+  int th_form = 0;  // fused kernel form: 0 registers, 1 / 2 shared memory (FP32)
+  // wall boundaries (non-periodic axes): per face kind and wall velocity, and
+  // the rows of the streaming operator whose departure path meets a wall
+  bool walls = false;
+  int bc[6] = {0, 0, 0, 0, 0, 0};
+  double uw[6][3] = {{0}};
+  int nbr = 0;                   // boundary rows
+  int* d_br_dst = nullptr;       // destination index dir * n_dev + node
+  int* d_br_ptr = nullptr;       // nbr + 1 offsets into col / w
+  int* d_br_col = nullptr;       // source index dir * n_dev + node
+  double* d_br_w = nullptr;      // Lagrange weights (FP64)
+  float* d_br_wf = nullptr;      // the same in float
+  double* d_br_c = nullptr;      // per row: f const, f const (deviation form), g const, g const (deviation)
+  int nbn = 0;                   // wall nodes: nodes with a row that meets a wall; their
+  int* d_bn_node = nullptr;      // Q - 1 rows are rows k (Q-1) .. k (Q-1) + Q - 2 above
+  // MappingQ1 cells: every node is a "wall node" (all rows sparse), the
+  // Cartesian fused kernels are not used
+  bool mapped = false;
+  std::vector<double> vtx;       // grid vertices, x fastest, 3 doubles each
+  double pv[3][3] = {{0}};       // periodic translation of each axis
+  double* d_mw = nullptr;        // per-node quadrature weight (mass / energy)
+  // departure-point rows (sl_mapped.cuh), one population only
+  int* d_mp_base = nullptr;
+  void* d_mp_u = nullptr;        // Real
+  void* d_mp_c = nullptr;        // Real
+  unsigned char* d_mp_flags = nullptr;
+  const void* mp_step = nullptr;    // kernels for this stencil / model / order / precision
+  const void* mp_stream = nullptr;
+  // report of the last nat_autotune: per candidate ms per step, kind, nodes
+  // per CTA along x, y, z and threads per CTA
+  std::vector<float> at_ms;
+  std::vector<int> at_desc;  // 5 ints per candidate
+};
+
+namespace natgpu {
+namespace api {
+
+// error text into the handle, returns the code
+int fail(nat_solver* s, int code, const char* fmt, ...);
+int cuda_fail(nat_solver* s, cudaError_t e, const char* what);
+
+// stencil metadata (host)
+struct HostStencil {
+  int D, Q;
+  double e[32][3];  // unscaled velocities
+  double w[32];
+  // per-axis displacement classes: count and scaled speed of each (the
+  // departure point is x - dt * cls along the axis)
+  int nd;
+  double cls[ND_MAX];
+};
+
+bool get_host_stencil(int id, HostStencil* out, double scaling);
+// Gauss-Lobatto points on [0, 1], Lagrange basis value l_j(x), GL weights
+void gl_points(int p, double* xi);
+double lagrange(int p, const double* xi, int j, double x);
+void gl_weights(int p, const double* xi, double* wq);
+
+struct Dims {
+  int nx, ny, nz;    // device lattice
+  int rx, ry, rz;    // reference lattice
+};
+
+// tracker.cu
+int build_wall_rows(nat_solver* s);
+int launch_wall_rows(nat_solver* s, const void* in, void* out, bool g_pop);
+void free_mapped_rows(nat_solver* s);
+int setup_mapping(nat_solver* s, const double* vertices, double* hmin);
+void node_point(const nat_solver* s, const int* c, const int* l, const double* xi, double* x);
+
+}  // namespace api
+}  // namespace natgpu
+
+#define CK(call, what)                              \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return cuda_fail(s, e_, what); \
+  } while (0)

@@ -6,6 +6,7 @@ same f bit for bit as the uninterrupted run; the VTU output carries the
 lattice nodes, the p^D sub-cells of every element and the fields of the last
 collision.
 """
+import dataclasses
 import math
 import os
 import xml.etree.ElementTree as ET
@@ -76,6 +77,34 @@ def test_checkpoint_of_another_lattice_is_refused(gpu_lib, tmp_path):
     with N.Solver(spec) as c:
         with pytest.raises(N.NatError):
             c.load_checkpoint(str(bad))
+
+
+def test_checkpoint_of_a_mapped_mesh(gpu_lib, tmp_path):
+    """Resume on the same vertex grid is bitwise; another grid of the same
+    size is refused."""
+    from natrium_gb300 import problems as P
+    V = P.wavy_grid((4, 4), (1.0, 1.0), 0.1)
+    spec = N.SolverSpec(stencil="D2Q9", order=2, cells=(4, 4), length=(1.0, 1.0), scaling=10.0, viscosity=1e-3,
+                        topology="dg", vertices=V)
+    X = P.mapped_node_coords(V, 2, "dg")
+    u = 0.05 * np.stack([np.sin(2 * np.pi * X[:, 1]), np.cos(2 * np.pi * X[:, 0])]) * 10.0
+    f0 = P.equilibrium("D2Q9", 10.0, np.ones(X.shape[0]), u)
+    path = str(tmp_path / "mapped.ckpt")
+    with N.Solver(spec) as a:
+        a.upload_f(f0)
+        a.step(3)
+        a.save_checkpoint(path, iteration=3, time=3 * a.dt)
+        a.step(2)
+        fa = a.download_f()
+    with N.Solver(spec) as b:
+        it, t = b.load_checkpoint(path)
+        assert it == 3
+        b.step(2)
+        assert np.array_equal(b.download_f(), fa)
+    other = dataclasses.replace(spec, vertices=P.wavy_grid((4, 4), (1.0, 1.0), 0.05))
+    with N.Solver(other) as c:
+        with pytest.raises(N.NatError):
+            c.load_checkpoint(path)
 
 
 @pytest.mark.parametrize("dg", [False, True])
