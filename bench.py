@@ -196,10 +196,15 @@ def cpu_baseline(sample_cells=(8, 8, 8), steps=5):
     t0 = time.perf_counter()
     S.step_bgk(f, tau, steps, threads)
     el = (time.perf_counter() - t0) / steps
+    # the same sample on one thread (one timed step)
+    t0 = time.perf_counter()
+    S.step_bgk(f, tau, 1, 1)
+    el1 = time.perf_counter() - t0
     return {"value": mesh.n_nodes / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "value_1_thread": mesh.n_nodes / el1,
             "sample": f"{w['stencil']} BGK FE_DGQ p={w['order']}, {sample_cells[0]}^3 cells "
                       f"({mesh.n_nodes} nodes), {steps} timed steps of copy + CSR SpMV + collide, FP64, "
-                      f"{threads} OpenMP threads"}
+                      f"{threads} OpenMP threads (value_1_thread: one step on one thread)"}
 
 
 COMPRESSIBLE = dict(
