@@ -219,6 +219,23 @@ int nat_mass_energy_noalloc(const double* rho_dev, const double* u_dev, int dim,
 #define NAT_BC_DO_NOTHING 2
 int nat_set_boundary(nat_solver* s, int face, int kind, const double u_wall[3]);
 
+/* Constant body force (ProblemDescription::setExternalForce with
+ * ConstantExternalForce; SolverConfiguration::setForcingScheme), applied by
+ * the advanced collision of the time loop (collision_advanced/
+ * CollisionOperator.h:76-90, AuxiliaryCollisionFunctions.h:332-414):
+ *   NAT_FORCE_SHIFTING_VELOCITY: equilibrium velocity u + tau dt F / rho;
+ *   NAT_FORCE_EXACT_DIFFERENCE: after relaxation
+ *     f += f^eq(rho, u + dt F / rho) - f^eq(rho, u);
+ * both report u + dt F / (2 rho).  force[0..D-1] in scaled units (like u).
+ * BGK_STANDARD only (NAT_ERR_UNSUPPORTED otherwise; the reference's GUO
+ * scheme is not implemented in the advanced path either).  Not applied with
+ * a prescribed velocity (nat_collide with in_init).  With a force the step
+ * runs in the generic fused kernel.  NAT_FORCE_NONE switches it off. */
+#define NAT_FORCE_NONE 0
+#define NAT_FORCE_SHIFTING_VELOCITY 1
+#define NAT_FORCE_EXACT_DIFFERENCE 2
+int nat_set_force(nat_solver* s, int scheme, const double force[3]);
+
 /* ---- compressible two-population model (NAT_BGK_COMPRESSIBLE) ---------- */
 /* Equilibrium of the collision (SolverConfiguration equilibrium scheme). */
 #define NAT_EQ_BGK 0     /* second order, collision_advanced/Equilibria.h:66-83 */

@@ -45,6 +45,7 @@ NAT_ERR_UNSUPPORTED = 7
 STENCILS = {"D2Q9": 0, "D3Q19": 1, "D3Q27": 2, "D2Q25H": 3}
 STENCIL_DQ = {"D2Q9": (2, 9), "D3Q19": (3, 19), "D3Q27": (3, 27), "D2Q25H": (2, 25)}
 COLLISIONS = {"BGK_STANDARD": 0, "BGK_INCOMPRESSIBLE": 1, "KBC_STANDARD": 2, "BGK_COMPRESSIBLE": 3}
+FORCE_SCHEMES = {"NONE": 0, "SHIFTING_VELOCITY": 1, "EXACT_DIFFERENCE": 2}
 EQUILIBRIA = {"BGK": 0, "QUARTIC": 1}
 TOPOLOGIES = {"feq": 0, "dg": 1}
 PRECISIONS = {"fp64": 0, "fp32dev": 1}
@@ -59,7 +60,8 @@ EXPORTS = [
     "nat_server_create", "nat_server_destroy", "nat_server_submit", "nat_server_step", "nat_server_poll",
     "nat_server_result", "nat_server_stats", "nat_server_last_error", "nat_mass_energy_noalloc",
     "nat_set_thermal", "nat_get_thermal", "nat_upload_g", "nat_download_g", "nat_download_thermal",
-    "nat_init_thermal", "nat_set_boundary", "nat_checkpoint_save", "nat_checkpoint_load", "nat_write_vtu",
+    "nat_init_thermal", "nat_set_boundary", "nat_set_force", "nat_checkpoint_save", "nat_checkpoint_load",
+    "nat_write_vtu",
 ]
 
 
@@ -153,6 +155,7 @@ def load_library(path: str | None = None):
     L.nat_download_thermal.argtypes = [vp, dp, dp]
     L.nat_init_thermal.argtypes = [vp, dp, dp, dp]
     L.nat_set_boundary.argtypes = [vp, C.c_int, C.c_int, dp]
+    L.nat_set_force.argtypes = [vp, C.c_int, dp]
     L.nat_checkpoint_save.argtypes = [vp, C.c_char_p, C.c_int64, C.c_double]
     L.nat_checkpoint_load.argtypes = [vp, C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_double)]
     L.nat_write_vtu.argtypes = [vp, C.c_char_p]
@@ -411,6 +414,13 @@ class Solver:
         self._check(self._L.nat_write_vtu(self._h, os.fsencode(path)))
 
     # -- wall boundaries -------------------------------------------------------------
+    def set_force(self, scheme: str = "SHIFTING_VELOCITY", force=(0.0, 0.0, 0.0)):
+        """Constant body force in scaled units (ConstantExternalForce) with the
+        forcing scheme NONE, SHIFTING_VELOCITY or EXACT_DIFFERENCE."""
+        F = np.zeros(3)
+        F[: len(force)] = force
+        self._check(self._L.nat_set_force(self._h, FORCE_SCHEMES[scheme], _dp(F)))
+
     def set_boundary(self, face: int, kind: str = "VELOCITY_BOUNCE_BACK", u_wall=(0.0, 0.0, 0.0)):
         """Kind of wall face `face` (0 x-, 1 x+, 2 y-, 3 y+, 4 z-, 5 z+) of a
         non-periodic axis: VELOCITY_BOUNCE_BACK (wall velocity u_wall, scaled)

@@ -117,6 +117,55 @@ __device__ __forceinline__ Real collide_bgk(Real (&v)[S::Q], Real inv_tau,
 }
 
 // ---------------------------------------------------------------------------
+// BGK with a constant body force F: the advanced collision of the time loop
+// (CollisionOperator.h:76-90, AuxiliaryCollisionFunctions.h:332-414).
+// dF = dt F / scaling (unscaled momentum gained per step).
+//   scheme 1 (SHIFTING_VELOCITY): equilibrium velocity u + tau dF / rho;
+//   scheme 2 (EXACT_DIFFERENCE): relax with u, then
+//     f += f^eq(rho, u + dF / rho) - f^eq(rho, u);
+// both report the velocity u + dF / (2 rho).  Not applied with a prescribed
+// velocity (inInitializationProcedure).  Returns rho.
+// ---------------------------------------------------------------------------
+template <class S, bool DEV, bool COMP, class Real>
+__device__ __forceinline__ Real collide_bgk_force(Real (&v)[S::Q], Real inv_tau, Real tau, Real (&u)[3],
+                                                  bool given_u, const Real (&dF)[3], int scheme) {
+  if (given_u) return collide_bgk<S, DEV, COMP>(v, inv_tau, u, true);
+  Real m0, j[3];
+  moments<S, COMP>(v, m0, j);
+  const Real rho = DEV ? (Real(1) + m0) : m0;
+  const Real inv = Real(1) / rho;
+  u[0] = j[0] * inv;
+  u[1] = j[1] * inv;
+  u[2] = (S::D == 3) ? j[2] * inv : Real(0);
+  Real ue[3] = {u[0], u[1], u[2]};
+  if (scheme == 1)
+    for (int a = 0; a < S::D; ++a) ue[a] += tau * dF[a] * inv;
+  Real us[3] = {ue[0], ue[1], ue[2]};
+  if (scheme == 2)
+    for (int a = 0; a < S::D; ++a) us[a] += dF[a] * inv;
+  const Real uu = Real(1.5) * (ue[0] * ue[0] + ue[1] * ue[1] + ue[2] * ue[2]);
+  const Real uus = Real(1.5) * (us[0] * us[0] + us[1] * us[1] + us[2] * us[2]);
+  static_for<0, S::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    const Real ee = Real(3) * edot<S, i>(ue);
+    const Real poly = ee * (Real(1) + Real(0.5) * ee) - uu;
+    Real eq;
+    if constexpr (DEV)
+      eq = Real(S::w(i)) * (m0 + rho * poly);
+    else
+      eq = Real(S::w(i)) * rho * (Real(1) + poly);
+    v[i] = v[i] - inv_tau * (v[i] - eq);
+    if (scheme == 2) {
+      const Real es = Real(3) * edot<S, i>(us);
+      const Real polys = es * (Real(1) + Real(0.5) * es) - uus;
+      v[i] += Real(S::w(i)) * rho * (polys - poly);
+    }
+  });
+  for (int a = 0; a < S::D; ++a) u[a] += Real(0.5) * dF[a] * inv;
+  return rho;
+}
+
+// ---------------------------------------------------------------------------
 // BGK incompressible, D2Q9 only (collision/BGKIncompressible.cpp:62-190):
 // feq_0 = -4 sigma rho + 4/9 (1 + usq), feq_1..4 = lambda rho + 1/9 (1 + ...),
 // feq_5..8 = gamma rho + rho/36 (1 + ...), lambda = 1/3, gamma = 1/12,
@@ -278,12 +327,14 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
 }
 
 // Mass / momentum projection of the FP32 collision: removes the float
-// rounding defect of the conserved moments (post - pre) through the rest and
-// the axis populations, so that the collision conserves them exactly up to
-// the (unbiased) rounding of small differences.
+// rounding defect of the conserved moments (post - pre - target, target the
+// momentum a body force adds) through the rest and the axis populations, so
+// that the collision conserves them exactly up to the (unbiased) rounding of
+// small differences.
 template <class S, class Real>
-__device__ __forceinline__ void conserve(Real (&v)[S::Q], const Real (&pre)[S::Q]) {
-  Real dm = 0, dj[3] = {0, 0, 0};
+__device__ __forceinline__ void conserve(Real (&v)[S::Q], const Real (&pre)[S::Q],
+                                         const Real (&target)[3] = {Real(0), Real(0), Real(0)}) {
+  Real dm = 0, dj[3] = {-target[0], -target[1], -target[2]};
   static_for<0, S::Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
     const Real d = v[i] - pre[i];
@@ -308,5 +359,28 @@ __device__ __forceinline__ void conserve(Real (&v)[S::Q], const Real (&pre)[S::Q
   });
   v[0] -= dm;
 }
+
+// BGK of a StepParams kernel: plain, or with the body force of the handle.
+// FORCE = false compiles the plain collision only (the force term costs
+// registers that a latency-bound kernel needs for resident warps).
+template <class S, bool DEV, bool COMP, bool FORCE = true, class Real, class Prm>
+__device__ __forceinline__ Real bgk_collide(const Prm& P, Real (&v)[S::Q], const Real (&pre)[S::Q], Real (&u)[3],
+                                            bool given_u) {
+  Real rho;
+  if (!FORCE || P.force_scheme == 0) {
+    rho = collide_bgk<S, DEV, COMP>(v, Real(1) / Real(P.tau), u, given_u);
+    if constexpr (DEV) {
+      if (!given_u) conserve<S>(v, pre);
+    }
+  } else {
+    const Real dF[3] = {Real(P.dF[0]), Real(P.dF[1]), Real(P.dF[2])};
+    rho = collide_bgk_force<S, DEV, COMP>(v, Real(1) / Real(P.tau), Real(P.tau), u, given_u, dF, P.force_scheme);
+    if constexpr (DEV) {
+      if (!given_u) conserve<S>(v, pre, dF);
+    }
+  }
+  return rho;
+}
+
 
 }  // namespace natgpu

@@ -7,6 +7,7 @@ namespace natgpu {
 
 template <class Real>
 static const void* pick(int coll, int p) {
+  if (coll == L_COLL_BGK_FORCE) return mapped_for_order<SD3Q19, Real, COLL_BGK, true>(p);
   switch (coll) {
     case L_COLL_NONE: return mapped_for_order<SD3Q19, Real, COLL_NONE>(p);
     case L_COLL_BGK: return mapped_for_order<SD3Q19, Real, COLL_BGK>(p);

@@ -26,7 +26,9 @@ KernelSet kernels_d3q19(int coll, int prec);
 KernelSet kernels_d3q27(int coll, int prec);
 
 // departure-point kernels of mapped meshes (sl_mapped.cuh) for order p;
-// NULL when the combination is not instantiated
+// NULL when the combination is not instantiated.  coll L_COLL_BGK_FORCE: the
+// BGK form with the body-force term.
+constexpr int L_COLL_BGK_FORCE = 100;
 const void* mapped_kernel_d2q9(int coll, int prec, int p);
 const void* mapped_kernel_d3q19(int coll, int prec, int p);
 const void* mapped_kernel_d3q27(int coll, int prec, int p);

@@ -438,6 +438,8 @@ StepParams step_params(nat_solver* s, const void* fin, void* fout, int collide,
   P.write_macro = write_macro;
   P.in_init = in_init;
   P.collide = collide;
+  P.force_scheme = s->force_scheme;
+  for (int a = 0; a < 3; ++a) P.dF[a] = s->dt * s->force[a] / s->spec.scaling;
   return P;
 }
 
@@ -487,7 +489,7 @@ int launch_mapped_t(nat_solver* s, const void* kern, int collide, int write_macr
 }
 
 int launch_mapped(nat_solver* s, bool collide, int write_macro) {
-  const void* k = collide ? s->mp_step : s->mp_stream;
+  const void* k = collide ? (s->force_scheme ? s->mp_step_force : s->mp_step) : s->mp_stream;
   if (!k) return fail(s, NAT_ERR_UNSUPPORTED, "no departure-point kernel for this configuration");
   return s->spec.precision == NAT_FP64 ? launch_mapped_t<double>(s, k, collide, write_macro)
                                        : launch_mapped_t<float>(s, k, collide, write_macro);
@@ -632,6 +634,10 @@ int select_v2(nat_solver* s, int coll_sel, int smem_optin) {
   s->use_v2 = false;
   s->kind = 1;
   if (s->variant == 1) return NAT_OK;
+  // a body force runs in the generic kernel only
+  if (s->force_scheme)
+    return s->variant >= 2 ? fail(s, NAT_ERR_UNSUPPORTED, "with a body force only the generic kernel runs")
+                           : NAT_OK;
   std::vector<Cand> all = v2_candidates(s, coll_sel, smem_optin), c;
   for (const Cand& k : all)
     if (s->variant <= 2 || variant_kind(s->variant) == k.kind) c.push_back(k);
@@ -1125,6 +1131,7 @@ int nat_create(const nat_spec* spec, nat_solver** out) {
     };
     s->mp_step = mk(coll);
     s->mp_stream = mk(L_COLL_NONE);
+    if (coll == L_COLL_BGK) s->mp_step_force = mk(L_COLL_BGK_FORCE);
   }
   if (!s->thermal && !s->ks_coll.step) {
     // the reference throws for these combinations too
@@ -1529,6 +1536,7 @@ static int tune_candidates(nat_solver* s, std::vector<Cand>* cand, int* ncand) {
       if (variant_kind(s->variant) == k.kind) keep.push_back(k);
     cand->swap(keep);
   }
+  if (s->force_scheme) cand->clear();  // a body force runs in the generic kernel only
   *ncand = (int)cand->size() + (s->variant >= 2 ? 0 : 1);  // + the generic kernel
   return NAT_OK;
 }
@@ -1727,6 +1735,21 @@ int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* t
   if (threads)
     *threads = k == 2 ? s->v2.nth : (k == 7 ? 32 * s->row.g * s->row.wy : (row ? 32 * s->row.wy * s->row.wz : STEP_THREADS));
   if (smem_bytes) *smem_bytes = (int64_t)(k == 2 ? s->v2.smem : (row ? s->row.smem : s->smem_step));
+  return NAT_OK;
+}
+
+int nat_set_force(nat_solver* s, int scheme, const double force[3]) {
+  if (!s || scheme < NAT_FORCE_NONE || scheme > NAT_FORCE_EXACT_DIFFERENCE || (scheme && !force))
+    return NAT_ERR_INVALID_ARG;
+  if (scheme && (s->thermal || s->spec.collision != NAT_BGK_STANDARD))
+    return fail(s, NAT_ERR_UNSUPPORTED, "a body force acts in the BGK_STANDARD collision only");
+  s->force_scheme = scheme;
+  for (int a = 0; a < 3; ++a) s->force[a] = (scheme && a < s->D) ? force[a] : 0.0;
+  if (scheme) {
+    // the specialised kernels have no force term: the generic kernel runs
+    s->use_v2 = false;
+    s->kind = 1;
+  }
   return NAT_OK;
 }
 

@@ -81,6 +81,10 @@ struct StepParams {
   int write_macro;
   int in_init;
   int collide;  // 0: stream only
+  // constant body force (BGK only): 0 none, 1 shifting velocity, 2 exact
+  // difference; dF = dt F / scaling, the momentum a node gains per step
+  int force_scheme;
+  double dF[3];
 };
 
 constexpr int TH_WARPS = 8;   // warps per CTA of the fused kernel

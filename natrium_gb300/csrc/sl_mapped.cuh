@@ -73,7 +73,7 @@ __device__ __forceinline__ void lagrange_values(Real u, const LagrangeTab<Real>&
 
 // (One direction per loop iteration: unrolling two, which overlaps their row
 // loads and gathers, measured 25 % slower in 2-D and 7 % in 3-D.)
-template <class S, class Real, int COLL, int P>
+template <class S, class Real, int COLL, int P, bool FORCE = false>
 __global__ void __launch_bounds__(MAP_THREADS) k_mapped(const StepParams prm, const MappedRows<Real> R,
                                                       const LagrangeTab<Real> L) {
   constexpr bool DEV = sizeof(Real) == 4;
@@ -166,8 +166,7 @@ __global__ void __launch_bounds__(MAP_THREADS) k_mapped(const StepParams prm, co
 #pragma unroll
     for (int q = 0; q < Q; ++q) pre[q] = v[q];
     if constexpr (COLL == COLL_BGK) {
-      rho = collide_bgk<S, DEV, DEV>(v, Real(1) / Real(prm.tau), u, false);
-      if constexpr (DEV) conserve<S>(v, pre);
+      rho = bgk_collide<S, DEV, DEV, FORCE>(prm, v, pre, u, false);
     } else if constexpr (COLL == COLL_BGK_INC) {
       rho = collide_bgk_inc<DEV, DEV>(v, Real(1) / Real(prm.tau), u, false);
     } else if constexpr (COLL == COLL_KBC) {
@@ -190,16 +189,17 @@ __global__ void __launch_bounds__(MAP_THREADS) k_mapped(const StepParams prm, co
   if (bad) atomicOr(prm.status, bad);
 }
 
-// the instantiation of one order (1..PMAX), NULL outside that range
-template <class S, class Real, int COLL>
+// the instantiation of one order (1..PMAX), NULL outside that range;
+// FORCE: the BGK form with the body-force term
+template <class S, class Real, int COLL, bool FORCE = false>
 const void* mapped_for_order(int p) {
   switch (p) {
-    case 1: return (const void*)&k_mapped<S, Real, COLL, 1>;
-    case 2: return (const void*)&k_mapped<S, Real, COLL, 2>;
-    case 3: return (const void*)&k_mapped<S, Real, COLL, 3>;
-    case 4: return (const void*)&k_mapped<S, Real, COLL, 4>;
-    case 5: return (const void*)&k_mapped<S, Real, COLL, 5>;
-    case 6: return (const void*)&k_mapped<S, Real, COLL, 6>;
+    case 1: return (const void*)&k_mapped<S, Real, COLL, 1, FORCE>;
+    case 2: return (const void*)&k_mapped<S, Real, COLL, 2, FORCE>;
+    case 3: return (const void*)&k_mapped<S, Real, COLL, 3, FORCE>;
+    case 4: return (const void*)&k_mapped<S, Real, COLL, 4, FORCE>;
+    case 5: return (const void*)&k_mapped<S, Real, COLL, 5, FORCE>;
+    case 6: return (const void*)&k_mapped<S, Real, COLL, 6, FORCE>;
   }
   return nullptr;
 }

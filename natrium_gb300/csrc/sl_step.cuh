@@ -288,8 +288,7 @@ __global__ void __launch_bounds__(NT) k_sl_step(const StepParams P) {
       for (int q = 0; q < Q; ++q) pre[q] = fs[k][q];
     }
     if constexpr (COLL == COLL_BGK) {
-      rho = collide_bgk<S, DEV, DEV>(fs[k], Real(1) / Real(P.tau), u, false);
-      if constexpr (DEV) conserve<S>(fs[k], pre);
+      rho = bgk_collide<S, DEV, DEV>(P, fs[k], pre, u, false);
     } else if constexpr (COLL == COLL_BGK_INC) {
       rho = collide_bgk_inc<DEV, DEV>(fs[k], Real(1) / Real(P.tau), u, false);
     } else if constexpr (COLL == COLL_KBC) {
@@ -352,8 +351,7 @@ __global__ void __launch_bounds__(128) k_wall_nodes(const StepParams P, const Wa
 #pragma unroll
     for (int q = 0; q < Q; ++q) pre[q] = v[q];
     if constexpr (COLL == COLL_BGK) {
-      rho = collide_bgk<S, DEV, DEV>(v, Real(1) / Real(P.tau), u, false);
-      if constexpr (DEV) conserve<S>(v, pre);
+      rho = bgk_collide<S, DEV, DEV>(P, v, pre, u, false);
     } else if constexpr (COLL == COLL_BGK_INC) {
       rho = collide_bgk_inc<DEV, DEV>(v, Real(1) / Real(P.tau), u, false);
     } else if constexpr (COLL == COLL_KBC) {
@@ -406,11 +404,8 @@ __global__ void __launch_bounds__(256) k_collide(const StepParams P) {
         if (!given) conserve<S>(v, pre);
       }
     } else {
-      rho = collide_bgk<S, DEV, DEV>(v, Real(1) / Real(P.tau), u, given);
       // with a prescribed velocity the momentum is not a collision invariant
-      if constexpr (DEV) {
-        if (!given) conserve<S>(v, pre);
-      }
+      rho = bgk_collide<S, DEV, DEV>(P, v, pre, u, given);
     }
     if (!(rho >= Real(1e-10))) bad |= (rho != rho) ? ST_NAN : ST_DENSITY;
     P.rho[i] = (double)rho;

@@ -66,6 +66,9 @@ struct nat_solver {
   int th_form = 0;  // fused kernel form: 0 registers, 1 / 2 shared memory (FP32)
   // wall boundaries (non-periodic axes): per face kind and wall velocity, and
   // the rows of the streaming operator whose departure path meets a wall
+  // constant body force (NAT_FORCE_*), F in scaled units
+  int force_scheme = 0;
+  double force[3] = {0, 0, 0};
   bool walls = false;
   int bc[6] = {0, 0, 0, 0, 0, 0};
   double uw[6][3] = {{0}};
@@ -91,6 +94,7 @@ struct nat_solver {
   unsigned char* d_mp_flags = nullptr;
   const void* mp_step = nullptr;    // kernels for this stencil / model / order / precision
   const void* mp_stream = nullptr;
+  const void* mp_step_force = nullptr;  // BGK with the body-force term
   // report of the last nat_autotune: per candidate ms per step, kind, nodes
   // per CTA along x, y, z and threads per CTA
   std::vector<float> at_ms;

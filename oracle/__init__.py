@@ -78,6 +78,8 @@ def lib():
         L.orc_sl_bconst.argtypes = [C.c_void_p, C.c_int, dp]
         L.orc_sl_wall_hits.argtypes = [C.c_void_p]
         L.orc_collide_bgk.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int64, dp, dp, dp, C.c_int, C.c_int]
+        L.orc_collide_bgk_force.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int64, dp, dp, dp,
+                                            C.c_int, C.c_int, dp, C.c_int]
         L.orc_equilibrium.argtypes = [C.c_int, C.c_double, C.c_int64, dp, dp, dp]
         L.orc_bgk_collide_single_point.argtypes = [C.c_int, C.c_double, C.c_double, dp]
         L.orc_collide_bgk_incompressible_d2q9.argtypes = [C.c_double, C.c_double, C.c_int64, dp, dp, dp, C.c_int]
@@ -341,6 +343,20 @@ def _check(rc):
 def collide_bgk(st: Stencil, tau: float, f, rho, u, in_init=False, nthreads=1):
     n = f.shape[1]
     _check(lib().orc_collide_bgk(st.id, st.scaling, tau, n, _dp(f), _dp(rho), _dp(u), int(in_init), nthreads))
+
+
+# forcing schemes of the advanced collision (SolverConfiguration::setForcingScheme)
+FORCE_NONE, FORCE_SHIFTING_VELOCITY, FORCE_EXACT_DIFFERENCE = 0, 1, 2
+
+
+def collide_bgk_force(st: Stencil, tau: float, dt: float, f, rho, u, scheme: int, force, in_init=False,
+                      nthreads=1):
+    """Advanced BGK with a constant body force (scaled units)."""
+    F = np.zeros(3)
+    F[: len(force)] = force
+    n = f.shape[1]
+    _check(lib().orc_collide_bgk_force(st.id, st.scaling, tau, dt, n, _dp(f), _dp(rho), _dp(u), int(in_init),
+                                       int(scheme), _dp(F), nthreads))
 
 
 def collide_bgk_incompressible_d2q9(st: Stencil, tau: float, f, rho, u, in_init=False):

@@ -1002,9 +1002,55 @@ int orc_sl_wall_hits(const orc_sl* s) { return s ? s->n_wall_hits : -1; }
  * (AuxiliaryCollisionFunctions.h:63-68,177).  u arrays hold the scaled
  * velocity (u_unscaled * scaling).  Returns ORC_ERR_DENSITY if any density
  * is below 1e-10 (AuxiliaryCollisionFunctions.h:45-59). */
-int orc_collide_bgk(int stencil, double scaling, double tau, int64_t n,
-                    double* f, double* rho, double* u, int in_init,
-                    int nthreads) {
+/* Advanced BGK (CollisionOperator.h:26-111 with BGKCollision::relax and
+ * BGKEquilibrium).  With a constant body force (scheme 1 SHIFTING_VELOCITY,
+ * 2 EXACT_DIFFERENCE; force in scaled units, dt the time step), as
+ * CollisionOperator.h:76-90 applies it when the problem has an external
+ * force (AuxiliaryCollisionFunctions.h:332-414):
+ *   u_raw += dt F / (2 rho)                     (SHIFTING: before relax;
+ *                                                EXACT: after it)
+ *   SHIFTING: velocity += tau dt F / (rho scaling) before the equilibrium;
+ *   EXACT: after relax, velocity += dt F / (rho scaling) and
+ *          f += feq(shifted velocity) - feq.
+ * The force is left out with a prescribed velocity (in_init). */
+static void advanced_bgk_feq(int stencil, int D, int Q, const double e[32][3], const double* w, double cs2, double dens,
+                    const double* vel, double* feq) {
+  int pq, j;
+  if (stencil == ORC_D2Q9) {
+    /* Equilibria.h:33-63 */
+    double prefactor = 1. / cs2, sp, usq, mixed, wt;
+    sp = vel[0] * vel[0] + vel[1] * vel[1];
+    usq = -sp / (2 * cs2);
+    wt = 4. / 9. * dens;
+    feq[0] = wt * (1 + usq);
+    wt = 1. / 9. * dens;
+    mixed = prefactor * (vel[0]);
+    feq[1] = wt * (1 + mixed * (1 + 0.5 * mixed) + usq);
+    feq[3] = wt * (1 - mixed * (1 - 0.5 * mixed) + usq);
+    mixed = prefactor * (vel[1]);
+    feq[2] = wt * (1 + mixed * (1 + 0.5 * mixed) + usq);
+    feq[4] = wt * (1 - mixed * (1 - 0.5 * mixed) + usq);
+    wt = 1. / 36. * dens;
+    mixed = prefactor * (vel[0] + vel[1]);
+    feq[5] = wt * (1 + mixed * (1 + 0.5 * mixed) + usq);
+    feq[7] = wt * (1 - mixed * (1 - 0.5 * mixed) + usq);
+    mixed = prefactor * (-vel[0] + vel[1]);
+    feq[6] = wt * (1 + mixed * (1 + 0.5 * mixed) + usq);
+    feq[8] = wt * (1 - mixed * (1 - 0.5 * mixed) + usq);
+  } else {
+    /* Equilibria.h:66-83 */
+    double uu = 0.0;
+    for (j = 0; j < D; j++) uu += -(vel[j] * vel[j]) / (2.0 * cs2);
+    for (pq = 0; pq < Q; pq++) {
+      double ue = 0.0;
+      for (j = 0; j < D; j++) ue += (vel[j] * e[pq][j]) / cs2;
+      feq[pq] = w[pq] * dens * (1 + ue * (1 + 0.5 * (ue)) + uu);
+    }
+  }
+}
+
+int orc_collide_bgk_force(int stencil, double scaling, double tau, double dt, int64_t n, double* f, double* rho,
+                          double* u, int in_init, int scheme, const double* force, int nthreads) {
   int D, Q, bad = 0;
   double es[3 * 32], w[32], cs2s, vmax;
   double e[32][3];
@@ -1039,47 +1085,38 @@ int orc_collide_bgk(int stencil, double scaling, double tau, int64_t n,
         vel[j] = vel[j] * 1.0 / dens;
       }
     }
+    const int forced = scheme != 0 && !in_init;
     if (!in_init) {
       for (j = 0; j < D; j++) u[(int64_t)j * n + ii] = vel[j] * scaling;
+      if (forced && scheme == 1) {
+        /* applyMacroscopicForces, applyForces */
+        for (j = 0; j < D; j++) u[(int64_t)j * n + ii] += 0.5 * dt * force[j] / dens;
+        for (j = 0; j < D; j++) vel[j] += tau * dt * force[j] / dens / scaling;
+      }
     } else {
       for (j = 0; j < D; j++) vel[j] = u[(int64_t)j * n + ii] / scaling;
     }
-    if (stencil == ORC_D2Q9) {
-      /* Equilibria.h:33-63 */
-      double prefactor = 1. / cs2, sp, usq, mixed, wt;
-      sp = vel[0] * vel[0] + vel[1] * vel[1];
-      usq = -sp / (2 * cs2);
-      wt = 4. / 9. * dens;
-      feq[0] = wt * (1 + usq);
-      wt = 1. / 9. * dens;
-      mixed = prefactor * (vel[0]);
-      feq[1] = wt * (1 + mixed * (1 + 0.5 * mixed) + usq);
-      feq[3] = wt * (1 - mixed * (1 - 0.5 * mixed) + usq);
-      mixed = prefactor * (vel[1]);
-      feq[2] = wt * (1 + mixed * (1 + 0.5 * mixed) + usq);
-      feq[4] = wt * (1 - mixed * (1 - 0.5 * mixed) + usq);
-      wt = 1. / 36. * dens;
-      mixed = prefactor * (vel[0] + vel[1]);
-      feq[5] = wt * (1 + mixed * (1 + 0.5 * mixed) + usq);
-      feq[7] = wt * (1 - mixed * (1 - 0.5 * mixed) + usq);
-      mixed = prefactor * (-vel[0] + vel[1]);
-      feq[6] = wt * (1 + mixed * (1 + 0.5 * mixed) + usq);
-      feq[8] = wt * (1 - mixed * (1 - 0.5 * mixed) + usq);
-    } else {
-      /* Equilibria.h:66-83 */
-      double uu = 0.0;
-      for (j = 0; j < D; j++) uu += -(vel[j] * vel[j]) / (2.0 * cs2);
-      for (pq = 0; pq < Q; pq++) {
-        double ue = 0.0;
-        for (j = 0; j < D; j++) ue += (vel[j] * e[pq][j]) / cs2;
-        feq[pq] = w[pq] * dens * (1 + ue * (1 + 0.5 * (ue)) + uu);
-      }
-    }
+    advanced_bgk_feq(stencil, D, Q, e, w, cs2, dens, vel, feq);
     /* CollisionSchemes.h:38-40 */
     for (pq = 0; pq < Q; pq++) fl[pq] -= 1. / tau * (fl[pq] - feq[pq]);
+    if (forced && scheme == 2) {
+      /* postCollisionApplyForces (EXACT_DIFFERENCE) */
+      double shifted[32];
+      for (j = 0; j < D; j++) {
+        vel[j] += dt * force[j] / dens / scaling;
+        u[(int64_t)j * n + ii] += 0.5 * dt * force[j] / dens;
+      }
+      advanced_bgk_feq(stencil, D, Q, e, w, cs2, dens, vel, shifted);
+      for (pq = 0; pq < Q; pq++) fl[pq] += shifted[pq] - feq[pq];
+    }
     for (pq = 0; pq < Q; pq++) f[(int64_t)pq * n + ii] = fl[pq];
   }
   return bad ? ORC_ERR_DENSITY : ORC_OK;
+}
+
+int orc_collide_bgk(int stencil, double scaling, double tau, int64_t n, double* f, double* rho, double* u,
+                    int in_init, int nthreads) {
+  return orc_collide_bgk_force(stencil, scaling, tau, 0.0, n, f, rho, u, in_init, 0, NULL, nthreads);
 }
 
 /* Legacy equilibrium, BGKStandard::getEquilibriumDistribution
