@@ -12,7 +12,9 @@ static KernelSet pick_d2q9(int coll) {
       return {(const void*)&k_sl_step<S, Real, COLL_NONE, STEP_NPT>, nullptr, nullptr};
     case L_COLL_BGK:
       return {(const void*)&k_sl_step<S, Real, COLL_BGK, STEP_NPT>,
-              (const void*)&k_collide<S, Real, COLL_BGK>, (const void*)&k_wall_nodes<S, Real, COLL_BGK>};
+              (const void*)&k_collide<S, Real, COLL_BGK>, (const void*)&k_wall_nodes<S, Real, COLL_BGK>,
+              (const void*)&k_sl_step<S, Real, COLL_BGK, STEP_NPT, true>,
+              (const void*)&k_collide<S, Real, COLL_BGK, true>, (const void*)&k_wall_nodes<S, Real, COLL_BGK, true>};
     case L_COLL_BGK_INC:
       return {(const void*)&k_sl_step<S, Real, COLL_BGK_INC, STEP_NPT>,
               (const void*)&k_collide<S, Real, COLL_BGK_INC>, (const void*)&k_wall_nodes<S, Real, COLL_BGK_INC>};

@@ -12,7 +12,9 @@ static KernelSet pick_d3q19(int coll) {
       return {(const void*)&k_sl_step<S, Real, COLL_NONE, STEP_NPT>, nullptr, nullptr};
     case L_COLL_BGK:
       return {(const void*)&k_sl_step<S, Real, COLL_BGK, STEP_NPT>,
-              (const void*)&k_collide<S, Real, COLL_BGK>, (const void*)&k_wall_nodes<S, Real, COLL_BGK>};
+              (const void*)&k_collide<S, Real, COLL_BGK>, (const void*)&k_wall_nodes<S, Real, COLL_BGK>,
+              (const void*)&k_sl_step<S, Real, COLL_BGK, STEP_NPT, true>,
+              (const void*)&k_collide<S, Real, COLL_BGK, true>, (const void*)&k_wall_nodes<S, Real, COLL_BGK, true>};
     default:
       return {nullptr, nullptr, nullptr};
   }

@@ -18,6 +18,10 @@ struct KernelSet {
   const void* step;      // fused stream(+collide) kernel, NULL if unsupported
   const void* collide;   // collide-only kernel, NULL for COLL_NONE
   const void* wallnode;  // fused step of the wall nodes (k_wall_nodes), NULL for COLL_NONE
+  // the same three with the body-force term (BGK only, else NULL)
+  const void* step_force = nullptr;
+  const void* collide_force = nullptr;
+  const void* wallnode_force = nullptr;
 };
 
 // prec: 0 = FP64, 1 = FP32 deviation

@@ -448,7 +448,8 @@ int launch_step(nat_solver* s, const KernelSet& ks, int collide, int write_macro
   void* fout = s->f[1 - s->cur];
   StepParams P = step_params(s, fin, fout, collide, write_macro, 0);
   void* args[] = {&P};
-  cudaError_t e = cudaLaunchKernel(ks.step, dim3(s->ntiles), dim3(STEP_THREADS), args,
+  const void* fn = (s->force_scheme && collide && ks.step_force) ? ks.step_force : ks.step;
+  cudaError_t e = cudaLaunchKernel(fn, dim3(s->ntiles), dim3(STEP_THREADS), args,
                                    s->smem_step, s->stream);
   if (e != cudaSuccess) return cuda_fail(s, e, "stream-collide launch");
   s->launches++;
@@ -1348,7 +1349,8 @@ static int launch_collide(nat_solver* s, int in_init) {
   }
   StepParams P = step_params(s, s->f[s->cur], s->f[s->cur], 1, 1, in_init);
   void* args[] = {&P};
-  CK(cudaLaunchKernel(s->ks_coll.collide, dim3(grid_for(s->n_dev)), dim3(256), args, 0, s->stream),
+  const void* fn = (s->force_scheme && s->ks_coll.collide_force) ? s->ks_coll.collide_force : s->ks_coll.collide;
+  CK(cudaLaunchKernel(fn, dim3(grid_for(s->n_dev)), dim3(256), args, 0, s->stream),
      "collide launch");
   s->launches++;
   return NAT_OK;
@@ -1398,7 +1400,8 @@ static int launch_wall_nodes(nat_solver* s, int write_macro) {
     W32 = {s->nbn, s->d_bn_node};
     args[1] = &W32;
   }
-  CK(cudaLaunchKernel(s->ks_coll.wallnode, dim3((s->nbn + 127) / 128), dim3(128), args, 0, s->stream),
+  const void* fn = (s->force_scheme && s->ks_coll.wallnode_force) ? s->ks_coll.wallnode_force : s->ks_coll.wallnode;
+  CK(cudaLaunchKernel(fn, dim3((s->nbn + 127) / 128), dim3(128), args, 0, s->stream),
      "wall nodes launch");
   s->launches++;
   return NAT_OK;

@@ -102,7 +102,8 @@ __host__ __device__ constexpr double rest_state(int i) {
 
 // Fused step kernel.  Real: arithmetic/storage type (double: plain FP64;
 // float: deviation storage).  NPT: lattice nodes owned per thread.
-template <class S, class Real, int COLL, int NPT>
+// FORCE: the BGK form with the body-force term (bgk_collide)
+template <class S, class Real, int COLL, int NPT, bool FORCE = false>
 __global__ void __launch_bounds__(NT) k_sl_step(const StepParams P) {
   constexpr bool DEV = sizeof(Real) == 4;
   constexpr int Q = S::Q;
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(NT) k_sl_step(const StepParams P) {
       for (int q = 0; q < Q; ++q) pre[q] = fs[k][q];
     }
     if constexpr (COLL == COLL_BGK) {
-      rho = bgk_collide<S, DEV, DEV>(P, fs[k], pre, u, false);
+      rho = bgk_collide<S, DEV, DEV, FORCE>(P, fs[k], pre, u, false);
     } else if constexpr (COLL == COLL_BGK_INC) {
       rho = collide_bgk_inc<DEV, DEV>(fs[k], Real(1) / Real(P.tau), u, false);
     } else if constexpr (COLL == COLL_KBC) {
@@ -331,7 +332,7 @@ struct WallNodes {
 // are not the wall's.  (One thread walking all Q-1 rows of its node was
 // latency-bound: a few thousand wall nodes are too few warps to hide ~300
 // dependent loads each.)
-template <class S, class Real, int COLL>
+template <class S, class Real, int COLL, bool FORCE = false>
 __global__ void __launch_bounds__(128) k_wall_nodes(const StepParams P, const WallNodes<Real> W) {
   constexpr bool DEV = sizeof(Real) == 4;
   constexpr int Q = S::Q;
@@ -351,7 +352,7 @@ __global__ void __launch_bounds__(128) k_wall_nodes(const StepParams P, const Wa
 #pragma unroll
     for (int q = 0; q < Q; ++q) pre[q] = v[q];
     if constexpr (COLL == COLL_BGK) {
-      rho = bgk_collide<S, DEV, DEV>(P, v, pre, u, false);
+      rho = bgk_collide<S, DEV, DEV, FORCE>(P, v, pre, u, false);
     } else if constexpr (COLL == COLL_BGK_INC) {
       rho = collide_bgk_inc<DEV, DEV>(v, Real(1) / Real(P.tau), u, false);
     } else if constexpr (COLL == COLL_KBC) {
@@ -373,7 +374,7 @@ __global__ void __launch_bounds__(128) k_wall_nodes(const StepParams P, const Wa
 }
 
 // Collision only (CollisionModel::collideAll on the device state), in place.
-template <class S, class Real, int COLL>
+template <class S, class Real, int COLL, bool FORCE = false>
 __global__ void __launch_bounds__(256) k_collide(const StepParams P) {
   constexpr bool DEV = sizeof(Real) == 4;
   constexpr int Q = S::Q;
@@ -405,7 +406,7 @@ __global__ void __launch_bounds__(256) k_collide(const StepParams P) {
       }
     } else {
       // with a prescribed velocity the momentum is not a collision invariant
-      rho = bgk_collide<S, DEV, DEV>(P, v, pre, u, given);
+      rho = bgk_collide<S, DEV, DEV, FORCE>(P, v, pre, u, given);
     }
     if (!(rho >= Real(1e-10))) bad |= (rho != rho) ? ST_NAN : ST_DENSITY;
     P.rho[i] = (double)rho;
