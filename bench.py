@@ -12,7 +12,10 @@ value:   node updates/s of the FP32-deviation path with f resident in HBM
          256 MiB write between timed steps, outside the events).
 e2e:     the same metric through the C ABI with host buffers: each step
          uploads f (FP64, pinned host memory), runs the step and reads rho
-         and u back.
+         and u back.  Pipelined: step k's upload runs on the handle's copy
+         stream while step k-1 is stepped and read back (asynchronous
+         read-back tickets); the blocking one-step-at-a-time loop is
+         reported beside it (e2e.serial), with the measured host link.
 fp64_plain: the plain FP64 path on the same workload.
 roofline: algorithmic bytes per step = 2 Q s_f per node (f read once,
          written once) over the measured HBM copy bandwidth.
@@ -155,7 +158,8 @@ def time_device(sol, torch, stream, flush, steps: int, warmup: int):
 
 
 def time_e2e(sol, torch, f_host, rho_h, u_h, steps: int):
-    """C-ABI calls with host buffers: upload f, one step, read rho/u."""
+    """C-ABI calls with host buffers, one step at a time: upload f, one step,
+    blocking read of rho/u, status check.  Returns s per step."""
     sol.upload_f(f_host)
     sol.step(1)
     sol.download_macro(rho_h, u_h)
@@ -166,6 +170,51 @@ def time_e2e(sol, torch, f_host, rho_h, u_h, steps: int):
         sol.step_async(1, True)              # enqueue; the download below synchronises
         r, u = sol.download_macro(rho_h, u_h)
         sol.status()                         # the step's density check, every step
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / steps
+
+
+def measure_link(torch, nbytes: int, reps: int = 5):
+    """Host link bandwidth (GB/s) of copies of nbytes between page-locked host
+    memory and the device, each direction alone (CUDA events)."""
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            dst.copy_(src, non_blocking=True)
+        b.record()
+        torch.cuda.synchronize()
+        out[name] = nbytes * reps / (a.elapsed_time(b) * 1e-3) / 1e9
+    return out
+
+
+def time_e2e_pipelined(sol, torch, f_host, rho_bufs, u_bufs, steps: int):
+    """The same calls pipelined: every step still uploads its whole f from
+    page-locked host memory and reads its rho/u back, but the read-back is
+    asynchronous (a ticket) and the host waits for step k-1's results only
+    after enqueueing step k, so step k's upload (its own copy stream) runs
+    while step k-1 is stepped and read back.  Each wait checks the status of
+    its step.  Returns s per step."""
+    def run(n):
+        prev = None
+        for k in range(n):
+            sol.upload_f(f_host)
+            sol.step_async(1, True)
+            t = sol.download_macro_async(rho_bufs[k % 2], u_bufs[k % 2])
+            if prev is not None:
+                sol.wait(prev)               # step k-1's rho/u are on the host
+            prev = t
+        sol.wait(prev)
+
+    run(3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run(steps)
     torch.cuda.synchronize()
     return (time.perf_counter() - t0) / steps
 
@@ -531,9 +580,22 @@ def run_ours(args):
     # page-locked result buffers (the f buffer above is page-locked too)
     rho_h = torch.empty(sol.n_ref, dtype=torch.float64).pin_memory().numpy()
     u_h = torch.empty((sol.D, sol.n_ref), dtype=torch.float64).pin_memory().numpy()
-    e2e_s = time_e2e(sol, torch, f_host, rho_h, u_h, e2e_steps)
-    e2e_ms, _ = aggregate_ranks(torch, ws, e2e_s * 1e3, nodes, 1)  # slowest rank
+    link = measure_link(torch, f0.nbytes)
+    serial_s = time_e2e(sol, torch, f_host, rho_h, u_h, e2e_steps)
+    serial_ms, _ = aggregate_ranks(torch, ws, serial_s * 1e3, nodes, 1)  # slowest rank
+    rho_b = [rho_h, torch.empty(sol.n_ref, dtype=torch.float64).pin_memory().numpy()]
+    u_b = [u_h, torch.empty((sol.D, sol.n_ref), dtype=torch.float64).pin_memory().numpy()]
+    e2e_s = time_e2e_pipelined(sol, torch, f_host, rho_b, u_b, 4 * e2e_steps)
+    e2e_ms, _ = aggregate_ranks(torch, ws, e2e_s * 1e3, nodes, 1)
     e2e_s = e2e_ms * 1e-3
+    # the pipelined read-backs equal the blocking one of the same state
+    sol.upload_f(f0)
+    sol.step(1)
+    r_ref, u_ref = sol.download_macro()
+    sol.upload_f(f0)
+    sol.step_async(1, True)
+    sol.wait(sol.download_macro_async(rho_b[1], u_b[1]))
+    pipeline_ok = bool(np.array_equal(rho_b[1], r_ref) and np.array_equal(u_b[1], u_ref))
     h2d = f0.nbytes
     d2h = 8 * (1 + sol.D) * sol.n_ref
     # correctness guard on the measured state: finite, mass near 1
@@ -607,7 +669,13 @@ def run_ours(args):
                      "autotune": {"candidates": ncand, "chosen": chosen}},
         "cpu_baseline": cpu,
         "e2e": {"value": ws * nodes / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_s * 1e3},
+                "ms_per_step": e2e_s * 1e3,
+                "mode": "pipelined: upload of step k on its own copy stream while step k-1 is stepped and its "
+                        "rho/u read back; every step uploads its f and reads its rho/u, status checked per step",
+                "link": link, "link_floor_ms": h2d / (link["h2d_gbs"] * 1e6),
+                "serial": {"value": ws * nodes / (serial_ms * 1e-3), "ms_per_step": serial_ms,
+                           "mode": "upload, step, blocking read-back, one step at a time"},
+                "pipeline_matches_blocking": pipeline_ok},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "fp64_plain": {"value": ws * nodes / (ms64 * 1e-3), "ms_per_step": ms64, "steps": steps64,

@@ -138,12 +138,32 @@ int nat_set_dt(nat_solver* s, double dt);
  * the legacy default stream. */
 int nat_set_stream(nat_solver* s, void* cuda_stream);
 
-/* Copy f (host, reference layout, Q * n_ref doubles) to the device. */
+/* Copy f (host, reference layout, Q * n_ref doubles) to the device.
+ * Enqueued without waiting: the copy runs on the handle's own copy stream
+ * into one of two input staging buffers, and the conversion to the device
+ * layout on the handle's stream waits for it.  Work enqueued later on the
+ * handle's stream sees the new f.  With page-locked f_host the copy is
+ * asynchronous: keep f_host unchanged until a later synchronising call
+ * (nat_status, nat_wait, a blocking download) returns. */
 int nat_upload_f(nat_solver* s, const double* f_host);
 /* Copy f back to the host (reference layout; periodic duplicates filled). */
 int nat_download_f(nat_solver* s, double* f_host);
 /* Copy rho (n_ref) and u (D * n_ref, scaled) of the last collision. */
 int nat_download_macro(nat_solver* s, double* rho_host, double* u_host);
+/* The read-back of nat_download_macro, enqueued without waiting.  *ticket
+ * receives a number for nat_wait; rho_host and u_host (page-locked for an
+ * asynchronous copy) must stay valid and are filled once nat_wait(ticket)
+ * returns.  The device status word is read and cleared with it, so the
+ * ticket carries the status of the steps enqueued since the previous read of
+ * it.  Used to pipeline host I/O: the upload of the next f runs while this
+ * read-back is in flight. */
+int nat_download_macro_async(nat_solver* s, double* rho_host, double* u_host,
+                             uint64_t* ticket);
+/* Wait until the read-back of a ticket is on the host; returns its status
+ * (NAT_OK, NAT_ERR_DENSITY_UNDERFLOW, NAT_ERR_NAN).  Up to 8 tickets are
+ * tracked; issuing a ninth waits for the oldest, and its status, if nobody
+ * waited for it, is returned by the next nat_wait. */
+int nat_wait(nat_solver* s, uint64_t ticket);
 /* Copy rho and scaled u from the host to the device (the input of a
  * collision with in_init != 0). */
 int nat_upload_macro(nat_solver* s, const double* rho_host,

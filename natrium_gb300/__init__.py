@@ -61,7 +61,7 @@ EXPORTS = [
     "nat_server_result", "nat_server_stats", "nat_server_last_error", "nat_mass_energy_noalloc",
     "nat_set_thermal", "nat_get_thermal", "nat_upload_g", "nat_download_g", "nat_download_thermal",
     "nat_init_thermal", "nat_set_boundary", "nat_set_force", "nat_checkpoint_save", "nat_checkpoint_load",
-    "nat_write_vtu",
+    "nat_write_vtu", "nat_download_macro_async", "nat_wait",
 ]
 
 
@@ -129,6 +129,8 @@ def load_library(path: str | None = None):
     L.nat_download_f.argtypes = [vp, dp]
     L.nat_download_macro.argtypes = [vp, dp, dp]
     L.nat_upload_macro.argtypes = [vp, dp, dp]
+    L.nat_download_macro_async.argtypes = [vp, dp, dp, C.POINTER(C.c_uint64)]
+    L.nat_wait.argtypes = [vp, C.c_uint64]
     L.nat_stream.argtypes = [vp, C.c_double, dp]
     L.nat_collide.argtypes = [vp, C.c_int]
     L.nat_step.argtypes = [vp, C.c_int]
@@ -235,6 +237,7 @@ class Solver:
     def __init__(self, spec: SolverSpec):
         self.spec = spec
         self._L = load_library()
+        self._pending = {}  # ticket -> host arrays of an asynchronous read-back
         self._h = C.c_void_p()
         cs = spec.c()
         rc = self._L.nat_create(C.byref(cs), C.byref(self._h))
@@ -264,8 +267,9 @@ class Solver:
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
-            self._L.nat_destroy(self._h)
+            self._L.nat_destroy(self._h)  # waits for outstanding read-backs
             self._h = C.c_void_p()
+            self._pending = {}
 
     def __del__(self):
         try:
@@ -320,6 +324,33 @@ class Solver:
             raise ValueError("rho / u have the wrong shape")
         self._check(self._L.nat_download_macro(self._h, _dp(rho), _dp(u)))
         return rho, u
+
+    def download_macro_async(self, rho: np.ndarray, u: np.ndarray) -> int:
+        """Enqueue the read-back of rho (n_ref) and u (D, n_ref) into the given
+        C-contiguous float64 arrays (page-locked ones for an asynchronous
+        copy) and return a ticket; the arrays are filled, and the status of
+        the steps before it checked, by wait(ticket).  The arrays are kept
+        alive here until then."""
+        if rho.shape != (self.n_ref,) or u.shape != (self.D, self.n_ref):
+            raise ValueError("rho / u have the wrong shape")
+        for a in (rho, u):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or not a.flags.writeable:
+                raise ValueError("rho / u must be writeable C-contiguous float64 arrays")
+        t = C.c_uint64()
+        self._check(self._L.nat_download_macro_async(self._h, _dp(rho), _dp(u), C.byref(t)))
+        self._pending[t.value] = (rho, u)
+        # issuing ticket t waited for ticket t - 8 (its slot was reused)
+        for old in [k for k in self._pending if k <= t.value - 8]:
+            del self._pending[old]
+        return t.value
+
+    def wait(self, ticket: int):
+        """Wait for the read-back of a ticket; raises CollisionException when
+        a step before it met a density below 1e-10 or a NaN."""
+        try:
+            self._check(self._L.nat_wait(self._h, ticket))
+        finally:
+            self._pending.pop(ticket, None)
 
     def upload_macro(self, rho: np.ndarray, u: np.ndarray):
         rho = np.ascontiguousarray(rho, dtype=np.float64)

@@ -944,6 +944,25 @@ static int launch_wall_nodes(nat_solver* s, int write_macro);
 
 int nat_destroy(nat_solver* s) {
   if (!s) return NAT_OK;
+  // outstanding copies into host memory and from the input staging buffers
+  for (int k = 0; k < nat_solver::NTICKET; ++k)
+    if (s->tk_ev[k]) {
+      cudaEventSynchronize(s->tk_ev[k]);
+      cudaEventDestroy(s->tk_ev[k]);
+    }
+  if (s->h2d) {
+    cudaStreamSynchronize(s->h2d);
+    cudaStreamDestroy(s->h2d);
+  }
+  for (int k = 0; k < 2; ++k) {
+    if (s->in_free[k]) {
+      cudaEventSynchronize(s->in_free[k]);
+      cudaEventDestroy(s->in_free[k]);
+    }
+    if (s->in_full[k]) cudaEventDestroy(s->in_full[k]);
+    cudaFree(s->in_stage[k]);
+  }
+  cudaFreeHost(s->tk_status);
   cudaFree(s->f[0]);
   cudaFree(s->f[1]);
   cudaFree(s->rho);
@@ -1241,18 +1260,49 @@ int nat_set_stream(nat_solver* s, void* stream) {
   return NAT_OK;
 }
 
+// The copy stream, events and input staging buffers of nat_upload_f.
+static int ensure_upload_path(nat_solver* s) {
+  if (s->h2d) return NAT_OK;
+  const size_t bytes = sizeof(double) * (size_t)s->Q * s->n_ref;
+  for (int k = 0; k < 2; ++k) {
+    if (cudaMalloc((void**)&s->in_stage[k], bytes) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(s->in_stage[0]);
+      s->in_stage[0] = nullptr;
+      return fail(s, NAT_ERR_OOM, "cudaMalloc(%zu) failed (input staging)", bytes);
+    }
+  }
+  for (int k = 0; k < 2; ++k) {
+    CK(cudaEventCreateWithFlags(&s->in_full[k], cudaEventDisableTiming), "upload events");
+    CK(cudaEventCreateWithFlags(&s->in_free[k], cudaEventDisableTiming), "upload events");
+  }
+  // non-blocking: no implicit ordering against the legacy default stream
+  CK(cudaStreamCreateWithFlags(&s->h2d, cudaStreamNonBlocking), "copy stream");
+  return NAT_OK;
+}
+
 int nat_upload_f(nat_solver* s, const double* f_host) {
   if (!s || !f_host) return NAT_ERR_INVALID_ARG;
-  CK(cudaMemcpyAsync(s->staging, f_host, sizeof(double) * s->Q * s->n_ref,
-                     cudaMemcpyHostToDevice, s->stream), "upload f");
+  int rc = ensure_upload_path(s);
+  if (rc) return rc;
+  const int k = s->in_slot;
+  // the copy waits for the conversion that last read this buffer; the
+  // conversion below waits for the copy
+  CK(cudaStreamWaitEvent(s->h2d, s->in_free[k], 0), "upload order");
+  CK(cudaMemcpyAsync(s->in_stage[k], f_host, sizeof(double) * s->Q * s->n_ref, cudaMemcpyHostToDevice, s->h2d),
+     "upload f");
+  CK(cudaEventRecord(s->in_full[k], s->h2d), "upload event");
+  CK(cudaStreamWaitEvent(s->stream, s->in_full[k], 0), "upload order");
   Dims d = dims_of(s);
   const int g = grid_for(s->n_dev * s->Q);
   if (s->spec.precision == NAT_FP64)
-    k_upload<double><<<g, 256, 0, s->stream>>>(s->staging, (double*)s->f[s->cur], d, s->Q, s->red + 2);
+    k_upload<double><<<g, 256, 0, s->stream>>>(s->in_stage[k], (double*)s->f[s->cur], d, s->Q, s->red + 2);
   else
-    k_upload<float><<<g, 256, 0, s->stream>>>(s->staging, (float*)s->f[s->cur], d, s->Q, s->red + 2);
+    k_upload<float><<<g, 256, 0, s->stream>>>(s->in_stage[k], (float*)s->f[s->cur], d, s->Q, s->red + 2);
   CK(cudaGetLastError(), "upload kernel");
   s->launches++;
+  CK(cudaEventRecord(s->in_free[k], s->stream), "upload event");
+  s->in_slot = 1 - k;
   return NAT_OK;
 }
 
@@ -1284,6 +1334,65 @@ int nat_download_macro(nat_solver* s, double* rho_host, double* u_host) {
   CK(cudaMemcpyAsync(u_host, s->staging + s->n_ref, sizeof(double) * s->D * s->n_ref,
                      cudaMemcpyDeviceToHost, s->stream), "download u");
   CK(cudaStreamSynchronize(s->stream), "download sync");
+  return NAT_OK;
+}
+
+int nat_download_macro_async(nat_solver* s, double* rho_host, double* u_host, uint64_t* ticket) {
+  if (!s || !rho_host || !u_host || !ticket) return NAT_ERR_INVALID_ARG;
+  if (!s->tk_status) {
+    CK(cudaHostAlloc((void**)&s->tk_status, sizeof(int) * nat_solver::NTICKET, cudaHostAllocDefault),
+       "ticket status words");
+    memset(s->tk_status, 0, sizeof(int) * nat_solver::NTICKET);
+    for (int k = 0; k < nat_solver::NTICKET; ++k)
+      CK(cudaEventCreateWithFlags(&s->tk_ev[k], cudaEventDisableTiming), "ticket events");
+  }
+  const unsigned long long t = s->tk_next;
+  const int k = (int)(t % nat_solver::NTICKET);
+  if (s->tk_held[k]) {
+    // the slot's old ticket: wait for it and keep its status for the next wait
+    CK(cudaEventSynchronize(s->tk_ev[k]), "ticket reuse");
+    s->tk_lost |= s->tk_status[k];
+    s->tk_status[k] = 0;
+    s->tk_held[k] = 0;
+  }
+  Dims d = dims_of(s);
+  k_fields_to_ref<<<grid_for(s->n_ref), 256, 0, s->stream>>>(s->rho, s->staging, d, 1);
+  k_fields_to_ref<<<grid_for(s->n_ref * s->D), 256, 0, s->stream>>>(s->u, s->staging + s->n_ref, d, s->D);
+  CK(cudaGetLastError(), "macro kernel");
+  s->launches += 2;
+  CK(cudaMemcpyAsync(rho_host, s->staging, sizeof(double) * s->n_ref, cudaMemcpyDeviceToHost, s->stream),
+     "download rho");
+  CK(cudaMemcpyAsync(u_host, s->staging + s->n_ref, sizeof(double) * s->D * s->n_ref, cudaMemcpyDeviceToHost,
+                     s->stream),
+     "download u");
+  // the status of the steps since the previous read of it, then cleared
+  CK(cudaMemcpyAsync(&s->tk_status[k], s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "status read");
+  CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "status clear");
+  CK(cudaEventRecord(s->tk_ev[k], s->stream), "ticket event");
+  s->tk_held[k] = t;
+  s->tk_next = t + 1;
+  *ticket = t;
+  return NAT_OK;
+}
+
+int nat_wait(nat_solver* s, uint64_t ticket) {
+  if (!s) return NAT_ERR_INVALID_ARG;
+  if (ticket == 0 || ticket >= s->tk_next) return fail(s, NAT_ERR_INVALID_ARG, "unknown ticket %llu",
+                                                       (unsigned long long)ticket);
+  const int k = (int)(ticket % nat_solver::NTICKET);
+  int st = 0;
+  if (s->tk_held[k] == ticket) {
+    CK(cudaEventSynchronize(s->tk_ev[k]), "ticket wait");
+    st = s->tk_status[k];
+    s->tk_status[k] = 0;
+  }
+  // an older ticket whose slot was reused is complete already; its status,
+  // like that of every reused slot nobody waited for, is in tk_lost
+  st |= s->tk_lost;
+  s->tk_lost = 0;
+  if (st & ST_NAN) return fail(s, NAT_ERR_NAN, "NaN density in collision");
+  if (st) return fail(s, NAT_ERR_DENSITY_UNDERFLOW,
+                      "Densities too small (< 1e-10) for collisions. Decrease time step size.");
   return NAT_OK;
 }
 

@@ -64,11 +64,11 @@ struct nat_solver {
   natgpu::ThermalTablesT<double> tt;
   natgpu::ThermalTablesT<float> ttf;
   int th_form = 0;  // fused kernel form: 0 registers, 1 / 2 shared memory (FP32)
-  // wall boundaries (non-periodic axes): per face kind and wall velocity, and
-  // the rows of the streaming operator whose departure path meets a wall
   // constant body force (NAT_FORCE_*), F in scaled units
   int force_scheme = 0;
   double force[3] = {0, 0, 0};
+  // wall boundaries (non-periodic axes): per face kind and wall velocity, and
+  // the rows of the streaming operator whose departure path meets a wall
   bool walls = false;
   int bc[6] = {0, 0, 0, 0, 0, 0};
   double uw[6][3] = {{0}};
@@ -99,6 +99,26 @@ struct nat_solver {
   // per CTA along x, y, z and threads per CTA
   std::vector<float> at_ms;
   std::vector<int> at_desc;  // 5 ints per candidate
+  // Pipelined host transfers.  nat_upload_f copies into one of two input
+  // staging buffers on its own stream (h2d); the conversion kernel on the
+  // solver's stream waits for that copy, and the next copy into the same
+  // buffer waits for the conversion.  So the copy of the next state runs
+  // while the current one is stepped and read back.  Created on first use.
+  cudaStream_t h2d = nullptr;
+  double* in_stage[2] = {nullptr, nullptr};  // Q * n_ref doubles each
+  cudaEvent_t in_full[2] = {nullptr, nullptr};
+  cudaEvent_t in_free[2] = {nullptr, nullptr};
+  int in_slot = 0;
+  // Asynchronous read-backs (nat_download_macro_async): ticket t uses slot
+  // t % NTICKET, an event on the solver's stream and a page-locked copy of
+  // the device status word taken right before it.  Reusing a slot first
+  // waits for its old ticket and keeps that ticket's status in tk_lost.
+  static constexpr int NTICKET = 8;
+  cudaEvent_t tk_ev[NTICKET] = {};
+  unsigned long long tk_held[NTICKET] = {};  // ticket issued in each slot (0 none)
+  int* tk_status = nullptr;                  // page-locked, NTICKET words
+  unsigned long long tk_next = 1;            // next ticket; 0 is never issued
+  int tk_lost = 0;
 };
 
 namespace natgpu {
