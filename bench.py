@@ -351,18 +351,49 @@ MIXED = {"name": "tgv3d_d3q27_kbc_sl_dg_p3_32x32x32", "stencil": "D3Q27", "colli
          "order": 3, "cells": (32, 32, 32), "Ma": 0.1, "Re": 1600.0, "cfl": 0.4, "steps": 2000, "every": 100}
 
 
-def bench_mixed(torch, stream, flush, steps: int = None):
+def bench_mixed(torch, stream, flush, steps: int = None, profile: bool = False, candidate: int = -1):
     """The mixed-precision accuracy configuration: 3-D Taylor-Green, D3Q27
     KBC, 32^3 hexahedra, FE_DGQ p = 3 (2,097,152 nodes x 27), Ma 0.1,
     Re 1600, 2000 steps.  The FP32 deviation path and the FP64 path run side
     by side from the same initial f; every 100 steps the relative L2
     difference of u and rho is recorded (the FP64 path is the oracle-pinned
-    one), and each path's device time per step is reported."""
+    one), and each path's device time per step is reported.
+
+    profile: the FP32 path alone, 3 warm-up and `steps` timed steps, with
+    the autotuner's choice (its report is returned, with the chosen index) or,
+    with candidate >= 0, that candidate of its list without timing (then the
+    3 warm-up steps are the only launches of the kernel before the timed
+    ones, for a one-launch capture)."""
     import natrium_gb300 as N
     from natrium_gb300 import problems as P
     c = MIXED
     steps = steps or c["steps"]
     scaling = math.sqrt(3) / c["Ma"]
+    if profile:
+        spec = N.SolverSpec(stencil=c["stencil"], order=c["order"], cells=c["cells"], length=(2 * math.pi,) * 3,
+                            scaling=scaling, viscosity=1.0 / c["Re"], cfl=c["cfl"], collision=c["collision"],
+                            precision="fp32dev", topology="dg")
+        with N.Solver(spec) as sol:
+            sol.set_stream(stream.cuda_stream)
+            X = P.node_coords(c["cells"], c["order"], spec.length, "dg")
+            rho, u = P.taylor_green_3d(X, c["Ma"])
+            sol.upload_f(P.equilibrium(c["stencil"], scaling, rho, u))
+            rep, chosen = [], candidate
+            if candidate >= 0:
+                sol.select_candidate(candidate)
+            else:
+                _, chosen = sol.autotune(3)
+                rep = sol.autotune_report()
+            sol.step_async(3, False)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sol.step_async(steps, False)
+            e1.record(stream)
+            sol.status()
+            ms = e0.elapsed_time(e1) / steps
+            return {"workload": c["name"], "nodes": sol.n_dev, "ms_per_step": ms, "kernel": sol.kernel_info(),
+                    "candidate": chosen, "autotune": rep}
     sols = {}
     for prec in ("fp64", "fp32dev"):
         spec = N.SolverSpec(stencil=c["stencil"], order=c["order"], cells=c["cells"], length=(2 * math.pi,) * 3,
@@ -530,7 +561,8 @@ def run_ours(args):
         print(json.dumps(bench_mapped(torch, stream, flush, steps=args.steps, warmup=args.warmup)))
         return 0
     if args.mixed_only:
-        print(json.dumps(bench_mixed(torch, stream, flush)))
+        print(json.dumps(bench_mixed(torch, stream, flush, steps=args.steps if args.profile else None,
+                                     profile=args.profile, candidate=args.candidate)))
         return 0
     if args.compressible_only:
         print(json.dumps(bench_compressible(torch, stream, flush, steps=args.steps, warmup=args.warmup,
@@ -703,6 +735,8 @@ def main():
                     help="fused kernel: 0 autotuned, 1 generic, 3 tile, 4 row-segment, 6 bulk-copy row-segment, "
                          "7 row-group")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
+    ap.add_argument("--candidate", type=int, default=-1,
+                    help="with --mixed-only --profile: use this autotuner candidate without timing")
     ap.add_argument("--profile-precision", default="fp32dev", choices=["fp32dev", "fp64"],
                     help="with --profile: the path to time (the headline FP32 deviation path or plain FP64)")
     ap.add_argument("--profile", action="store_true",

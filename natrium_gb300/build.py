@@ -18,7 +18,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libnatgpu.so")
 
-SOURCES = ["natgpu_api.cu", "k_d2q9.cu", "k_d3q19.cu", "k_d3q27.cu", "k_v2.cu", "k_row_d2q9.cu",
+SOURCES = ["natgpu_api.cu", "k_d2q9.cu", "k_d3q19.cu", "k_d3q27.cu", "k_v2.cu", "k_v2_small.cu", "k_row_d2q9.cu",
            "k_row_d3q19.cu", "k_row_d3q27.cu", "serve.cu",
            "natgpu_noalloc.cu", "k_thermal.cu", "k_rowt_d3q19.cu", "k_rowt_d3q27_bgk.cu",
            "k_rowt_d3q27_kbc.cu", "k_row_ss_d3q19.cu", "k_row_ss_d3q27.cu",

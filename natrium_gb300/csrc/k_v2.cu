@@ -1,33 +1,11 @@
 // Instantiations of the specialised fused kernel (sl_step_v2.cuh) and the
 // lookup used by the host API.  One entry per (stencil, collision,
 // precision, order, topology) with its tile shape in cells and CTA size.
-#include "launch.h"
-#include "sl_step_v2.cuh"
+#include "v2_entry.cuh"
 
 namespace natgpu {
 
 namespace {
-
-template <class S, class Real, int COLL, int P, bool DG, int CX, int CY, int CZ, int NTH>
-V2Launch entry(int coll) {
-  V2Launch e;
-  e.stencil = S::ID;
-  e.coll = coll;
-  e.prec = sizeof(Real) == 8 ? 0 : 1;
-  e.P = P;
-  e.dg = DG;
-  e.cells[0] = CX;
-  e.cells[1] = CY;
-  e.cells[2] = CZ;
-  e.nth = NTH;
-  e.fn = (const void*)&k_sl_step_v2<S, Real, COLL, P, DG, CX, CY, CZ, NTH>;
-  e.smem = v2_smem_bytes<S, Real, P, DG, CX, CY, CZ>();
-  using TL = Tile<S, P, DG, CX, CY, CZ, sizeof(Real)>;
-  e.B[0] = TL::BX;
-  e.B[1] = TL::BY;
-  e.B[2] = TL::BZ;
-  return e;
-}
 
 const std::vector<V2Launch>& table() {
   static const std::vector<V2Launch> t = {
@@ -53,7 +31,10 @@ const std::vector<V2Launch>& table() {
 std::vector<V2Launch> find_v2(int stencil, int coll, int prec, int P, bool dg, const int cells[3], int dim,
                               int nx) {
   std::vector<V2Launch> out;
-  for (const V2Launch& e : table()) {
+  std::vector<V2Launch> all = table();
+  const std::vector<V2Launch>& more = v2_table_small_tiles();
+  all.insert(all.end(), more.begin(), more.end());
+  for (const V2Launch& e : all) {
     if (e.stencil != stencil || e.coll != coll || e.prec != prec || e.P != P || e.dg != dg) continue;
     bool ok = true;
     for (int a = 0; a < dim; ++a)

@@ -358,8 +358,11 @@ __device__ __forceinline__ void run_phase(Real* const (&reg)[3], Real* const (&s
   });
 }
 
-template <class S, class Real, int COLL, int P, bool DG, int CX, int CY, int CZ, int NTH>
-__global__ void __launch_bounds__(NTH, 1) k_sl_step_v2(const __grid_constant__ StepParams2<Real> prm) {
+// MINB: resident CTAs per SM the register allocation is sized for (small
+// tiles run several CTAs per SM, so that one computes while another waits at
+// a barrier).
+template <class S, class Real, int COLL, int P, bool DG, int CX, int CY, int CZ, int NTH, int MINB = 1>
+__global__ void __launch_bounds__(NTH, MINB) k_sl_step_v2(const __grid_constant__ StepParams2<Real> prm) {
   constexpr bool DEV = sizeof(Real) == 4;
   using TL = Tile<S, P, DG, CX, CY, CZ, sizeof(Real)>;
   constexpr int Q = S::Q;
