@@ -640,10 +640,12 @@ def run_ours(args):
     sol64 = N.Solver(spec64)
     sol64.set_stream(stream.cuda_stream)
     sol64.upload_f(f0)
+    at64 = []
     if args.variant:
         sol64.set_kernel_variant(args.variant)
     else:
         sol64.autotune(3)
+        at64 = sol64.autotune_report()
     kinfo64 = sol64.kernel_info()
     steps64 = max(3, args.steps // 4)
     per64, _ = time_device(sol64, torch, stream, flush, steps64, args.warmup)
@@ -711,7 +713,7 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "fp64_plain": {"value": ws * nodes / (ms64 * 1e-3), "ms_per_step": ms64, "steps": steps64,
-                       "roofline_frac": ach64 / hbm, "achieved_gbs": ach64, "kernel": kinfo64},
+                       "roofline_frac": ach64 / hbm, "achieved_gbs": ach64, "kernel": kinfo64, "autotune": at64},
         "speedup_vs_fp64_plain": ms64 / ms,
         "serving": serving,
         "compressible": compressible,

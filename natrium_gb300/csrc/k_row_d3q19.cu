@@ -6,7 +6,7 @@ namespace natgpu {
 
 namespace {
 
-template <class S, class Real, int COLL, int P, bool DG, int WY, int WZ>
+template <class S, class Real, int COLL, int P, bool DG, int WY, int WZ, bool ZS = false>
 RowLaunch rentry(int coll) {
   RowLaunch e;
   e.stencil = S::ID;
@@ -16,7 +16,7 @@ RowLaunch rentry(int coll) {
   e.dg = DG;
   e.wy = WY;
   e.wz = WZ;
-  e.fn = (const void*)&k_sl_row<S, Real, COLL, P, DG, WY, WZ>;
+  e.fn = (const void*)&k_sl_row<S, Real, COLL, P, DG, WY, WZ, false, (sizeof(Real) == 4 ? 2 : 1), ZS>;
   return e;
 }
 
@@ -30,6 +30,11 @@ void add_orders(std::vector<RowLaunch>& t, int coll) {
   t.push_back(rentry<S, float, COLL, P, false, WY2, WZ>(coll));
   t.push_back(rentry<S, double, COLL, P, true, WY, WZ>(coll));
   t.push_back(rentry<S, double, COLL, P, false, WY, WZ>(coll));
+  // FP64 with z sharing (a CTA of two cells of rows): the z-factored rows of
+  // the yz-diagonal directions are computed once per CTA, which takes about
+  // half of those directions' FP64 multiply-adds off the FP64 pipe
+  t.push_back(rentry<S, double, COLL, P, true, 2 * (P + 1), 1, true>(coll));
+  t.push_back(rentry<S, double, COLL, P, false, 2 * P, 1, true>(coll));
   if constexpr (P < PMAX) add_orders<S, COLL, P + 1>(t, coll);
 }
 
