@@ -394,7 +394,7 @@ def bench_mixed(torch, stream, flush, steps: int = None, profile: bool = False, 
             ms = e0.elapsed_time(e1) / steps
             return {"workload": c["name"], "nodes": sol.n_dev, "ms_per_step": ms, "kernel": sol.kernel_info(),
                     "candidate": chosen, "autotune": rep}
-    sols = {}
+    sols, reports = {}, {}
     for prec in ("fp64", "fp32dev"):
         spec = N.SolverSpec(stencil=c["stencil"], order=c["order"], cells=c["cells"], length=(2 * math.pi,) * 3,
                             scaling=scaling, viscosity=1.0 / c["Re"], cfl=c["cfl"], collision=c["collision"],
@@ -405,6 +405,7 @@ def bench_mixed(torch, stream, flush, steps: int = None, profile: bool = False, 
         rho, u = P.taylor_green_3d(X, c["Ma"])
         sol.upload_f(P.equilibrium(c["stencil"], scaling, rho, u))
         sol.autotune(3)
+        reports[prec] = sol.autotune_report()
         sols[prec] = sol
     rl2 = lambda a, b: float(np.sqrt(np.sum((a - b) ** 2) / np.sum(b ** 2)))
     curve, ms = [], {"fp64": 0.0, "fp32dev": 0.0}
@@ -427,9 +428,9 @@ def bench_mixed(torch, stream, flush, steps: int = None, profile: bool = False, 
     n = sols["fp64"].n_dev
     res = {"workload": c["name"], "nodes": n, "steps": steps, "unit": UNIT,
            "fp32dev": {"ms_per_step": ms["fp32dev"] / steps, "value": n * steps / (ms["fp32dev"] * 1e-3),
-                       "kernel": sols["fp32dev"].kernel_info()},
+                       "kernel": sols["fp32dev"].kernel_info(), "autotune": reports["fp32dev"]},
            "fp64": {"ms_per_step": ms["fp64"] / steps, "value": n * steps / (ms["fp64"] * 1e-3),
-                    "kernel": sols["fp64"].kernel_info()},
+                    "kernel": sols["fp64"].kernel_info(), "autotune": reports["fp64"]},
            "speedup_fp32dev_vs_fp64": ms["fp64"] / ms["fp32dev"],
            "max_rel_l2_u": max(r["rel_l2_u"] for r in curve), "max_rel_l2_rho": max(r["rel_l2_rho"] for r in curve),
            "every_100_steps": curve,

@@ -508,6 +508,8 @@ EVERY_CASES = [
     # DG p = 3 with cells divisible by every D3Q27 tile (4 x 2 x 2 down to 4 x 1 x 1)
     ("D3Q27", (4, 2, 2), 3, True, "KBC_STANDARD", "fp32dev"),
     ("D3Q27", (4, 2, 2), 3, True, "BGK_STANDARD", "fp32dev"),
+    ("D3Q27", (4, 2, 2), 3, True, "KBC_STANDARD", "fp64"),
+    ("D3Q27", (3, 4, 2), 3, False, "BGK_STANDARD", "fp64"),
     ("D3Q19", (4, 4, 2), 4, True, "BGK_STANDARD", "fp64"),
     ("D2Q9", (8, 8), 4, True, "BGK_STANDARD", "fp32dev"),
 ]
