@@ -160,7 +160,7 @@ int nat_download_macro(nat_solver* s, double* rho_host, double* u_host);
 int nat_download_macro_async(nat_solver* s, double* rho_host, double* u_host,
                              uint64_t* ticket);
 /* Wait until the read-back of a ticket is on the host; returns its status
- * (NAT_OK, NAT_ERR_DENSITY_UNDERFLOW, NAT_ERR_NAN).  Up to 8 tickets are
+ * (NAT_OK, NAT_ERR_DENSITY_UNDERFLOW, NAT_ERR_NAN, NAT_ERR_TIMEOUT).  Up to 8 tickets are
  * tracked; issuing a ninth waits for the oldest, and its status, if nobody
  * waited for it, is returned by the next nat_wait. */
 int nat_wait(nat_solver* s, uint64_t ticket);
@@ -189,8 +189,18 @@ int nat_step(nat_solver* s, int n_steps);
 int nat_step_async(nat_solver* s, int n_steps, int write_macro);
 
 /* Synchronise the handle's stream and return the device status
- * (NAT_OK, NAT_ERR_DENSITY_UNDERFLOW, NAT_ERR_NAN); clears it. */
+ * (NAT_OK, NAT_ERR_DENSITY_UNDERFLOW, NAT_ERR_NAN, or NAT_ERR_TIMEOUT when
+ * a bulk-copy kernel's wait for a copy ran out and a step is incomplete);
+ * clears it. */
 int nat_status(nat_solver* s);
+
+/* Limit of every wait of the bulk-copy kernels (tile and bulk-copy row
+ * kernels) for a copy, in polls of its mbarrier; default 2^24.  A wait that
+ * runs out sets NAT_ERR_TIMEOUT in the status, waits (bounded) for the
+ * copies it still has in flight and stops its tile, so a lost copy cannot
+ * hang the GPU.  0 makes every such wait run out at once: the way to test
+ * that path without a fault. */
+int nat_set_wait_limit(nat_solver* s, uint32_t polls);
 
 /* Copy the text of the last error into buf (always NUL terminated). */
 int nat_last_error(const nat_solver* s, char* buf, size_t len);

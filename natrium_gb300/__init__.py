@@ -61,7 +61,7 @@ EXPORTS = [
     "nat_server_result", "nat_server_stats", "nat_server_last_error", "nat_mass_energy_noalloc",
     "nat_set_thermal", "nat_get_thermal", "nat_upload_g", "nat_download_g", "nat_download_thermal",
     "nat_init_thermal", "nat_set_boundary", "nat_set_force", "nat_checkpoint_save", "nat_checkpoint_load",
-    "nat_write_vtu", "nat_download_macro_async", "nat_wait",
+    "nat_write_vtu", "nat_download_macro_async", "nat_wait", "nat_set_wait_limit",
 ]
 
 
@@ -131,6 +131,7 @@ def load_library(path: str | None = None):
     L.nat_upload_macro.argtypes = [vp, dp, dp]
     L.nat_download_macro_async.argtypes = [vp, dp, dp, C.POINTER(C.c_uint64)]
     L.nat_wait.argtypes = [vp, C.c_uint64]
+    L.nat_set_wait_limit.argtypes = [vp, C.c_uint32]
     L.nat_stream.argtypes = [vp, C.c_double, dp]
     L.nat_collide.argtypes = [vp, C.c_int]
     L.nat_step.argtypes = [vp, C.c_int]
@@ -380,6 +381,13 @@ class Solver:
 
     def status(self):
         self._check(self._L.nat_status(self._h))
+
+    def set_wait_limit(self, polls: int):
+        """Limit of each wait of the bulk-copy kernels for a copy (mbarrier
+        polls; default 2^24).  A wait that runs out ends the step with
+        NatError(NAT_ERR_TIMEOUT) instead of hanging; 0 makes every such wait
+        run out at once (tests that path)."""
+        self._check(self._L.nat_set_wait_limit(self._h, int(polls)))
 
     def mass_energy(self):
         m, e = C.c_double(), C.c_double()

@@ -671,6 +671,7 @@ int launch_v2_t(nat_solver* s, const SpecWeights<Real>& W, int write_macro) {
   P.tau = s->tau;
   P.scaling = s->spec.scaling;
   P.write_macro = write_macro;
+  P.wait_polls = s->wait_polls;
   P.W = W;
   const int grid = P.ntx * P.nty * (s->n_ax[2] / s->v2.B[2]);
   void* args[] = {&P};
@@ -697,6 +698,7 @@ int launch_row_t(nat_solver* s, const SpecWeights<Real>& W, int write_macro) {
   P.tau = s->tau;
   P.scaling = s->spec.scaling;
   P.write_macro = write_macro;
+  P.wait_polls = s->wait_polls;
   P.W = W;
   int grid = P.nseg * (P.ny / s->row.wy) * (P.nz / s->row.wz);
   int nth = 32 * s->row.wy * s->row.wz;
@@ -1337,6 +1339,15 @@ int nat_download_macro(nat_solver* s, double* rho_host, double* u_host) {
   return NAT_OK;
 }
 
+// The error of a non-zero device status word: a wait that ran out first (the
+// step did not complete), then NaN, then a density below 1e-10.
+static int status_error(nat_solver* s, int st) {
+  if (st & ST_TIMEOUT)
+    return fail(s, NAT_ERR_TIMEOUT, "a wait for a bulk copy ran out; the step is incomplete");
+  if (st & ST_NAN) return fail(s, NAT_ERR_NAN, "NaN density in collision");
+  return fail(s, NAT_ERR_DENSITY_UNDERFLOW, "Densities too small (< 1e-10) for collisions. Decrease time step size.");
+}
+
 int nat_download_macro_async(nat_solver* s, double* rho_host, double* u_host, uint64_t* ticket) {
   if (!s || !rho_host || !u_host || !ticket) return NAT_ERR_INVALID_ARG;
   if (!s->tk_status) {
@@ -1390,10 +1401,7 @@ int nat_wait(nat_solver* s, uint64_t ticket) {
   // like that of every reused slot nobody waited for, is in tk_lost
   st |= s->tk_lost;
   s->tk_lost = 0;
-  if (st & ST_NAN) return fail(s, NAT_ERR_NAN, "NaN density in collision");
-  if (st) return fail(s, NAT_ERR_DENSITY_UNDERFLOW,
-                      "Densities too small (< 1e-10) for collisions. Decrease time step size.");
-  return NAT_OK;
+  return st ? status_error(s, st) : NAT_OK;
 }
 
 int nat_upload_macro(nat_solver* s, const double* rho_host, const double* u_host) {
@@ -1552,6 +1560,12 @@ int nat_step(nat_solver* s, int n_steps) {
   return nat_status(s);
 }
 
+int nat_set_wait_limit(nat_solver* s, uint32_t polls) {
+  if (!s) return NAT_ERR_INVALID_ARG;
+  s->wait_polls = polls;
+  return NAT_OK;
+}
+
 int nat_status(nat_solver* s) {
   if (!s) return NAT_ERR_INVALID_ARG;
   int st = 0;
@@ -1559,9 +1573,7 @@ int nat_status(nat_solver* s) {
   CK(cudaStreamSynchronize(s->stream), "status sync");
   if (st) {
     CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "status clear");
-    if (st & ST_NAN) return fail(s, NAT_ERR_NAN, "NaN density in collision");
-    return fail(s, NAT_ERR_DENSITY_UNDERFLOW,
-                "Densities too small (< 1e-10) for collisions. Decrease time step size.");
+    return status_error(s, st);
   }
   return NAT_OK;
 }

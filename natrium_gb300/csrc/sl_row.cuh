@@ -45,6 +45,7 @@ struct RowParams {
   double tau;
   double scaling;
   int write_macro;
+  unsigned wait_polls;  // bulk-copy row kernel: limit of each wait for a stage (MBAR_MAX_POLLS)
   SpecWeights<Real> W;  // [axis][sign][class][j]
 };
 

@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(32 * WY * WZ, (sizeof(Real) == 4 ? 2 : 1))
     (void)dz;
     (void)dx;
     if (fail_at) return;
-    if (!mbar_wait(&bar[s], parity, MBAR_MAX_POLLS)) {
+    if (!mbar_wait(&bar[s], parity, prm.wait_polls)) {
       fail_at = A;
       return;
     }

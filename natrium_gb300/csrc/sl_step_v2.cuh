@@ -57,6 +57,7 @@ struct StepParams2 {
   double tau;
   double scaling;
   int write_macro;
+  unsigned wait_polls;  // limit of each wait for a region copy (MBAR_MAX_POLLS)
   SpecWeights<Real> W;
 };
 
@@ -413,10 +414,21 @@ __global__ void __launch_bounds__(NTH, MINB) k_sl_step_v2(const __grid_constant_
     constexpr int A = PH + 1;  // direction whose region is consumed now
     if (!ok) return;
     if constexpr (A < Q) {
-      if (!mbar_wait(&bars[(A - 1) % 3], ((A - 1) / 3) & 1, MBAR_MAX_POLLS)) s_abort = 1;
+      if (!mbar_wait(&bars[(A - 1) % 3], ((A - 1) / 3) & 1, prm.wait_polls)) s_abort = 1;
     }
     __syncthreads();
     if (s_abort) {
+      // copies still in flight: directions A .. max(A + 1, 3), issued and
+      // not yet waited for; wait for them (bounded) before the CTA exits
+      if constexpr (A < Q) {
+        constexpr int HI = A + 1 > 3 ? A + 1 : 3;
+        constexpr int LAST = HI < Q - 1 ? HI : Q - 1;
+        if (threadIdx.x == 0)
+          static_for<A, LAST + 1>([&](auto J) {
+            constexpr int D = decltype(J)::value;
+            mbar_wait(&bars[(D - 1) % 3], ((D - 1) / 3) & 1, MBAR_MAX_POLLS);
+          });
+      }
       ok = false;
       return;
     }
@@ -428,7 +440,7 @@ __global__ void __launch_bounds__(NTH, MINB) k_sl_step_v2(const __grid_constant_
     run_phase<S, Real, P, DG, DEV, CX, CY, CZ, PH, NTH>(reg, st1, st2, sb, prm.W);
   });
   if (!ok) {
-    // a bulk copy never completed: report and stop this tile
+    // a wait for a bulk copy ran out: report and stop this tile
     if (threadIdx.x == 0) atomicOr(prm.status, ST_TIMEOUT);
     return;
   }

@@ -119,6 +119,9 @@ struct nat_solver {
   int* tk_status = nullptr;                  // page-locked, NTICKET words
   unsigned long long tk_next = 1;            // next ticket; 0 is never issued
   int tk_lost = 0;
+  // limit of each wait of the bulk-copy kernels for a copy (polls of the
+  // mbarrier); 0 makes every such wait run out at once
+  unsigned wait_polls = natgpu::MBAR_MAX_POLLS;
 };
 
 namespace natgpu {
