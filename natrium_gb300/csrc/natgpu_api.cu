@@ -1263,22 +1263,22 @@ int nat_set_stream(nat_solver* s, void* stream) {
 }
 
 // The copy stream, events and input staging buffers of nat_upload_f.
+// Each piece is created once; a call after a failed one creates what is
+// still missing (nat_destroy frees whatever exists).
 static int ensure_upload_path(nat_solver* s) {
   if (s->h2d) return NAT_OK;
   const size_t bytes = sizeof(double) * (size_t)s->Q * s->n_ref;
   for (int k = 0; k < 2; ++k) {
-    if (cudaMalloc((void**)&s->in_stage[k], bytes) != cudaSuccess) {
+    if (!s->in_stage[k] && cudaMalloc((void**)&s->in_stage[k], bytes) != cudaSuccess) {
       cudaGetLastError();
-      cudaFree(s->in_stage[0]);
-      s->in_stage[0] = nullptr;
+      s->in_stage[k] = nullptr;
       return fail(s, NAT_ERR_OOM, "cudaMalloc(%zu) failed (input staging)", bytes);
     }
+    if (!s->in_full[k]) CK(cudaEventCreateWithFlags(&s->in_full[k], cudaEventDisableTiming), "upload events");
+    if (!s->in_free[k]) CK(cudaEventCreateWithFlags(&s->in_free[k], cudaEventDisableTiming), "upload events");
   }
-  for (int k = 0; k < 2; ++k) {
-    CK(cudaEventCreateWithFlags(&s->in_full[k], cudaEventDisableTiming), "upload events");
-    CK(cudaEventCreateWithFlags(&s->in_free[k], cudaEventDisableTiming), "upload events");
-  }
-  // non-blocking: no implicit ordering against the legacy default stream
+  // last: its presence marks the path complete.  Non-blocking: no implicit
+  // ordering against the legacy default stream
   CK(cudaStreamCreateWithFlags(&s->h2d, cudaStreamNonBlocking), "copy stream");
   return NAT_OK;
 }
@@ -1350,12 +1350,14 @@ static int status_error(nat_solver* s, int st) {
 
 int nat_download_macro_async(nat_solver* s, double* rho_host, double* u_host, uint64_t* ticket) {
   if (!s || !rho_host || !u_host || !ticket) return NAT_ERR_INVALID_ARG;
-  if (!s->tk_status) {
-    CK(cudaHostAlloc((void**)&s->tk_status, sizeof(int) * nat_solver::NTICKET, cudaHostAllocDefault),
-       "ticket status words");
-    memset(s->tk_status, 0, sizeof(int) * nat_solver::NTICKET);
+  if (!s->tk_ev[nat_solver::NTICKET - 1]) {  // created last: the ring is complete
+    if (!s->tk_status) {
+      CK(cudaHostAlloc((void**)&s->tk_status, sizeof(int) * nat_solver::NTICKET, cudaHostAllocDefault),
+         "ticket status words");
+      memset(s->tk_status, 0, sizeof(int) * nat_solver::NTICKET);
+    }
     for (int k = 0; k < nat_solver::NTICKET; ++k)
-      CK(cudaEventCreateWithFlags(&s->tk_ev[k], cudaEventDisableTiming), "ticket events");
+      if (!s->tk_ev[k]) CK(cudaEventCreateWithFlags(&s->tk_ev[k], cudaEventDisableTiming), "ticket events");
   }
   const unsigned long long t = s->tk_next;
   const int k = (int)(t % nat_solver::NTICKET);
