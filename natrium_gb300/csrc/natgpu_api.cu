@@ -1324,17 +1324,26 @@ int nat_download_f(nat_solver* s, double* f_host) {
   return NAT_OK;
 }
 
-int nat_download_macro(nat_solver* s, double* rho_host, double* u_host) {
-  if (!s || !rho_host || !u_host) return NAT_ERR_INVALID_ARG;
+// rho and u in the reference layout (staging buffer), then copied to the
+// host, all enqueued on the handle's stream.
+static int enqueue_macro_readback(nat_solver* s, double* rho_host, double* u_host) {
   Dims d = dims_of(s);
   k_fields_to_ref<<<grid_for(s->n_ref), 256, 0, s->stream>>>(s->rho, s->staging, d, 1);
   k_fields_to_ref<<<grid_for(s->n_ref * s->D), 256, 0, s->stream>>>(s->u, s->staging + s->n_ref, d, s->D);
   CK(cudaGetLastError(), "macro kernel");
   s->launches += 2;
-  CK(cudaMemcpyAsync(rho_host, s->staging, sizeof(double) * s->n_ref, cudaMemcpyDeviceToHost,
-                     s->stream), "download rho");
-  CK(cudaMemcpyAsync(u_host, s->staging + s->n_ref, sizeof(double) * s->D * s->n_ref,
-                     cudaMemcpyDeviceToHost, s->stream), "download u");
+  CK(cudaMemcpyAsync(rho_host, s->staging, sizeof(double) * s->n_ref, cudaMemcpyDeviceToHost, s->stream),
+     "download rho");
+  CK(cudaMemcpyAsync(u_host, s->staging + s->n_ref, sizeof(double) * s->D * s->n_ref, cudaMemcpyDeviceToHost,
+                     s->stream),
+     "download u");
+  return NAT_OK;
+}
+
+int nat_download_macro(nat_solver* s, double* rho_host, double* u_host) {
+  if (!s || !rho_host || !u_host) return NAT_ERR_INVALID_ARG;
+  int rc = enqueue_macro_readback(s, rho_host, u_host);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(s->stream), "download sync");
   return NAT_OK;
 }
@@ -1368,16 +1377,8 @@ int nat_download_macro_async(nat_solver* s, double* rho_host, double* u_host, ui
     s->tk_status[k] = 0;
     s->tk_held[k] = 0;
   }
-  Dims d = dims_of(s);
-  k_fields_to_ref<<<grid_for(s->n_ref), 256, 0, s->stream>>>(s->rho, s->staging, d, 1);
-  k_fields_to_ref<<<grid_for(s->n_ref * s->D), 256, 0, s->stream>>>(s->u, s->staging + s->n_ref, d, s->D);
-  CK(cudaGetLastError(), "macro kernel");
-  s->launches += 2;
-  CK(cudaMemcpyAsync(rho_host, s->staging, sizeof(double) * s->n_ref, cudaMemcpyDeviceToHost, s->stream),
-     "download rho");
-  CK(cudaMemcpyAsync(u_host, s->staging + s->n_ref, sizeof(double) * s->D * s->n_ref, cudaMemcpyDeviceToHost,
-                     s->stream),
-     "download u");
+  int rc = enqueue_macro_readback(s, rho_host, u_host);
+  if (rc) return rc;
   // the status of the steps since the previous read of it, then cleared
   CK(cudaMemcpyAsync(&s->tk_status[k], s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "status read");
   CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "status clear");
