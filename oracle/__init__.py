@@ -3,9 +3,9 @@
 TEST INFRASTRUCTURE ONLY: a numpy/ctypes front-end for ``natoracle.c``, the
 plain-C FP64 restatement of NATriuM's reference algorithm (see the header of
 ``natoracle.c`` for the reference file:line each function follows).  Only the
-tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may use
-it, and only as the checker.  The product package ``natrium_gb300`` never
-imports it.
+tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg and
+reference arm may use it: to check results and as the timed CPU baseline.  The
+product package ``natrium_gb300`` never imports it.
 
 Parity status: pinned against the known answers and invariants of the
 reference's own tests; the reference itself cannot be built or run (deal.II,

@@ -3,9 +3,10 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This file is a plain-C (FP64) restatement of
  * NATriuM's reference algorithm for the hot path.  It is used by the tests,
- * by __graft_entry__.smoke() and by bench.py's CPU-baseline leg, always as the
- * checker and never as the thing measured or shipped.  The product path
- * (natrium_gb300/, libnatgpu.so) never links, loads or calls it.
+ * by __graft_entry__.smoke() and by bench.py's CPU-baseline leg and reference
+ * arm: to check results and as the timed CPU baseline, never as the product
+ * path that is measured or shipped.  The product path (natrium_gb300/,
+ * libnatgpu.so) never links, loads or calls it.
  *
  * Parity status: the reference (deal.II 9.3.3 + Trilinos 13.0.1 + p4est +
  * Boost + MPI) cannot be compiled or run here, so there are no outputs of the

@@ -1,7 +1,7 @@
 """The CPU oracle against the known answers of the reference's own tests.
 
-These pin the oracle (test infrastructure) before it is trusted as the
-checker of the CUDA path.  The expected values come from
+These pin the oracle (test infrastructure) before the CUDA path is compared
+against it.  The expected values come from
 tests/golden/known_answers.json, parsed out of the reference's test sources
 by tests/golden/make_golden.py.
 """
