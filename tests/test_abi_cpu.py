@@ -80,3 +80,16 @@ def test_lattice_beyond_32bit_indexing_is_refused_without_gpu():
         N.Solver(spec)
     assert ei.value.code == N.NAT_ERR_UNSUPPORTED
     assert "2^31" in str(ei.value)
+
+
+def test_transfer_entry_points_check_arguments_without_gpu():
+    """The pipelined-transfer and wait-limit entry points reject a null handle
+    or null buffers before touching CUDA."""
+    L = N.load_library()
+    t = C.c_uint64(7)
+    buf = (C.c_double * 4)()
+    assert L.nat_download_macro_async(None, buf, buf, C.byref(t)) == N.NAT_ERR_INVALID_ARG
+    assert t.value == 7  # untouched
+    assert L.nat_wait(None, 1) == N.NAT_ERR_INVALID_ARG
+    assert L.nat_set_wait_limit(None, 0) == N.NAT_ERR_INVALID_ARG
+    assert L.nat_upload_f(None, buf) == N.NAT_ERR_INVALID_ARG
