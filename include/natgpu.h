@@ -135,7 +135,8 @@ int nat_get_dt(const nat_solver* s, double* dt, double* tau);
 int nat_set_dt(nat_solver* s, double dt);
 
 /* Bind the handle to a CUDA stream (cudaStream_t passed as void*); NULL =
- * the legacy default stream. */
+ * the legacy default stream.  Work already enqueued on the previous stream
+ * is ordered before work enqueued on the new one. */
 int nat_set_stream(nat_solver* s, void* cuda_stream);
 
 /* Copy f (host, reference layout, Q * n_ref doubles) to the device.

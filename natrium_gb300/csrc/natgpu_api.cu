@@ -1258,7 +1258,18 @@ int nat_set_dt(nat_solver* s, double dt) {
 
 int nat_set_stream(nat_solver* s, void* stream) {
   if (!s) return NAT_ERR_INVALID_ARG;
-  s->stream = (cudaStream_t)stream;
+  cudaStream_t ns = (cudaStream_t)stream;
+  if (ns != s->stream) {
+    // what is enqueued on the old stream (an upload's conversion, a step)
+    // comes before anything enqueued on the new one
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "stream switch");
+    cudaError_t e = cudaEventRecord(ev, s->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ns, ev, 0);
+    cudaEventDestroy(ev);  // released once the recorded work completes
+    if (e != cudaSuccess) return cuda_fail(s, e, "stream switch");
+  }
+  s->stream = ns;
   return NAT_OK;
 }
 
