@@ -7,15 +7,12 @@ lattice nodes, the p^D sub-cells of every element and the fields of the last
 collision.
 """
 import dataclasses
-import math
-import os
 import xml.etree.ElementTree as ET
 
 import numpy as np
 import pytest
 
 import natrium_gb300 as N
-import oracle as O
 from tests.gpu_cases import make_case, periodic_state, thermal_case, thermal_state
 
 pytestmark = pytest.mark.gpu

@@ -1,7 +1,5 @@
 """Continuous-batching server: each result is the same alone and in the
 mix, matches the single-solve path, and admission by HBM footprint works."""
-import math
-
 import numpy as np
 import pytest
 
