@@ -54,7 +54,7 @@ extern "C" {
 #define NAT_ERR_CUDA 6
 #define NAT_ERR_UNSUPPORTED 7
 
-/* ---- stencils (stencils/*.cpp of the reference) ------------------------ */
+/* ---- stencils (the stencils/ directory of the reference) --------------- */
 #define NAT_D2Q9 0
 #define NAT_D3Q19 1
 #define NAT_D3Q27 2

@@ -1136,7 +1136,7 @@ int nat_create(const nat_spec* spec, nat_solver** out) {
       case NAT_D3Q19: return kernels_d3q19(c, spec->precision);
       case NAT_D3Q27: return kernels_d3q27(c, spec->precision);
     }
-    return {nullptr, nullptr};
+    return KernelSet{};
   };
   if (!s->thermal) {
     s->ks_coll = pick(coll);

@@ -288,6 +288,8 @@ __device__ __forceinline__ void row_body(const RowArgs<Real>& prm, const Real* s
     // an x direction spills at 64 registers (measured 19 % slower).
     constexpr bool HOIST = ZWY > 0;
     int zo[NJZ], yo[NJY];
+    (void)zo;
+    (void)yo;
     if constexpr (HOIST) {
 #pragma unroll
       for (int jz = 0; jz < NJZ; ++jz) {
