@@ -93,3 +93,25 @@ def test_transfer_entry_points_check_arguments_without_gpu():
     assert L.nat_wait(None, 1) == N.NAT_ERR_INVALID_ARG
     assert L.nat_set_wait_limit(None, 0) == N.NAT_ERR_INVALID_ARG
     assert L.nat_upload_f(None, buf) == N.NAT_ERR_INVALID_ARG
+
+
+def test_async_readback_validates_host_arrays_without_gpu():
+    """Solver.download_macro_async checks the host arrays before any C call
+    (a handle-less Solver: the checks must raise before the library is
+    reached)."""
+    import numpy as np
+
+    sol = N.Solver.__new__(N.Solver)
+    sol.n_ref, sol.D = 10, 2
+    sol._pending = {}
+    sol._L = None  # any C call would fail with AttributeError, not ValueError
+    good_r, good_u = np.empty(10), np.empty((2, 10))
+    for r, u in [(np.empty(9), good_u), (good_r, np.empty((3, 10))), (good_r.astype(np.float32), good_u),
+                 (good_r, np.empty((10, 2)).T), (np.empty(20)[::2], good_u)]:
+        with pytest.raises(ValueError):
+            sol.download_macro_async(r, u)
+    ro = np.empty(10)
+    ro.flags.writeable = False
+    with pytest.raises(ValueError):
+        sol.download_macro_async(ro, good_u)
+    assert sol._pending == {}
