@@ -223,10 +223,12 @@ int nat_mass_energy(nat_solver* s, double* mass, double* kinetic_energy);
  * out_dev[1] = kinetic energy, in device memory, written on cuda_stream.
  * The only scratch is a 64 KiB file-scope device array that every GPU
  * loading the library holds until exit; inputs above NAT_NOALLOC_MAX_NODES
- * nodes are rejected (NAT_ERR_INVALID_ARG).  The first call on a device looks
- * up the array's device address (make it before any stream capture); calls
- * whose kernels overlap on the GPU share the array and race.  Calls no
- * cudaMalloc / cudaFree.  Deterministic: fixed reduction order.  The node
+ * nodes are rejected (NAT_ERR_INVALID_ARG), and so is an axis whose node count
+ * is not a whole number of cells (a multiple of p for FE_Q, of p + 1 for DG).
+ * The first call on a device looks up the array's device address (make it
+ * before any stream capture; after a cudaDeviceReset the next call looks it
+ * up again); calls whose kernels overlap on the GPU share the array and race.
+ * Calls no cudaMalloc / cudaFree.  Deterministic: fixed reduction order.  The node
  * weights are those of the Cartesian box (cell_size); a mapped mesh's
  * weights depend on its cells' Jacobians: use nat_mass_energy there. */
 #define NAT_NOALLOC_MAX_NODES 16777216LL

@@ -14,9 +14,12 @@
 // Contract:
 //   * at most NAT_NOALLOC_MAX_NODES lattice nodes per call (larger inputs are
 //     rejected with NAT_ERR_INVALID_ARG and a message);
+//   * every axis holds whole cells (a multiple of p nodes for FE_Q with the
+//     periodic duplicates folded, of p + 1 for DG), else NAT_ERR_INVALID_ARG;
 //   * the first call on a device looks up the device address of g_partials
 //     (cudaGetSymbolAddress) with that device current; make that first call
-//     before capturing any stream, later calls do no set-up;
+//     before capturing any stream, later calls do no set-up (a call after a
+//     cudaDeviceReset sees a new context id and looks the address up again);
 //   * every call shares g_partials: calls whose kernels overlap on the GPU
 //     (different streams, or different host threads) race on it and must be
 //     serialised by the caller;
@@ -34,6 +37,7 @@
 
 #include "../../include/natgpu.h"
 #include "natgpu_common.h"
+#include "solver.h"
 
 namespace {
 
@@ -116,39 +120,41 @@ __global__ void __launch_bounds__(NA_THREADS) k_me_final(const double* __restric
   }
 }
 
-// per-device address of g_partials, looked up once per device
+// Device address of g_partials, looked up once per device and CUDA context.
+// The context id is part of the key so that a cudaDeviceReset between calls
+// (which destroys the context and the module holding g_partials) leads to a
+// fresh look-up instead of a stale address.
+struct AddrEntry {
+  unsigned long long ctx_id;
+  double* addr;
+};
 std::mutex g_mtx;
-double* g_addr[64] = {nullptr};
+AddrEntry g_addr[64] = {};
 
-// Gauss-Lobatto points on [0, 1] and their quadrature weights (host, no
-// allocation)
-void gl_rule(int p, double* xi, double* wq) {
-  xi[0] = 0.0;
-  xi[p] = 1.0;
-  for (int j = 1; j < p; ++j) {
-    long double x = -cosl(3.14159265358979323846264338327950288L * j / p);
-    for (int it = 0; it < 100; ++it) {
-      long double p0 = 1, p1 = x, d0 = 0, d1 = 1;
-      for (int k = 2; k <= p; ++k) {
-        long double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
-        long double d2 = d0 + (2 * k - 1) * p1;
-        p0 = p1; p1 = p2; d0 = d1; d1 = d2;
-      }
-      long double dx = d1 / ((2 * x * d1 - p * (p + 1) * p1) / (1 - x * x));
-      x -= dx;
-      if (fabsl(dx) < 1e-22L) break;
-    }
-    xi[j] = (double)((x + 1.0L) / 2.0L);
-  }
-  for (int j = 0; j <= p; ++j) {
-    long double x = 2.0L * xi[j] - 1.0L, p0 = 1, p1 = x;
-    for (int k = 2; k <= p; ++k) {
-      long double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
-      p0 = p1;
-      p1 = p2;
-    }
-    wq[j] = (double)(1.0L / ((long double)p * (p + 1) * p1 * p1));
-  }
+// id of the current CUDA context (cuCtxGetCurrent / cuCtxGetId, reached through
+// the runtime's driver entry points so the library does not link libcuda);
+// 0 when unavailable, which disables the reset check but not the cache
+unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  });
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
 }
 
 }  // namespace
@@ -160,9 +166,12 @@ extern "C" int nat_mass_energy_noalloc(const double* rho_dev, const double* u_de
   if (dim != 2 && dim != 3) return NAT_ERR_INVALID_ARG;
   if (order < 1 || order > natgpu::PMAX) return NAT_ERR_INVALID_ARG;
   if (topology != NAT_TOPO_FEQ && topology != NAT_TOPO_DG) return NAT_ERR_INVALID_ARG;
+  // node classes repeat with the period of a cell: p (FE_Q, periodic
+  // duplicates folded) or p + 1 (DG); an axis must hold whole cells
+  const int period = topology == NAT_TOPO_DG ? order + 1 : order;
   long long n = 1;
   for (int a = 0; a < dim; ++a) {
-    if (n_axis[a] < 1) return NAT_ERR_INVALID_ARG;
+    if (n_axis[a] < 1 || n_axis[a] % period != 0) return NAT_ERR_INVALID_ARG;
     n *= n_axis[a];
   }
   if (n > NAT_NOALLOC_MAX_NODES) return NAT_ERR_INVALID_ARG;  // beyond the scratch in g_partials
@@ -170,22 +179,24 @@ extern "C" int nat_mass_energy_noalloc(const double* rho_dev, const double* u_de
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return NAT_ERR_CUDA;
   double* partials;
   {
+    const unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> lk(g_mtx);
-    if (!g_addr[dev]) {
-      // set-up, once per device, with that device current
+    AddrEntry& e = g_addr[dev];
+    if (!e.addr || (ctx != 0 && e.ctx_id != ctx)) {
+      // set-up, once per device (and again after a reset of its context),
+      // with that device current
       void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_partials) != cudaSuccess || !p) {
-        cudaGetLastError();
-        return NAT_ERR_CUDA;
-      }
-      g_addr[dev] = static_cast<double*>(p);
+      if (cudaGetSymbolAddress(&p, g_partials) != cudaSuccess || !p) return NAT_ERR_CUDA;
+      e.addr = static_cast<double*>(p);
+      e.ctx_id = current_context_id();  // the look-up made the context current
     }
-    partials = g_addr[dev];
+    partials = e.addr;
   }
   NaQuad q;
   double xi[natgpu::PMAX1 + 1], wq[natgpu::PMAX1 + 1];
-  gl_rule(order, xi, wq);
-  q.period = topology == NAT_TOPO_DG ? order + 1 : order;
+  natgpu::api::gl_points(order, xi);  // the rule nat_mass_energy uses
+  natgpu::api::gl_weights(order, xi, wq);
+  q.period = period;
   for (int a = 0; a < 3; ++a)
     for (int c = 0; c < natgpu::PER_MAX; ++c) {
       double w = c < q.period ? wq[c] : 0.0;
@@ -197,9 +208,16 @@ extern "C" int nat_mass_energy_noalloc(const double* rho_dev, const double* u_de
   q.nz = dim == 3 ? n_axis[2] : 1;
   q.dim = dim;
   q.n = n;
-  const int nb = (int)((n + NA_NODES_PER_BLOCK - 1) / NA_NODES_PER_BLOCK);
+  int nb = (int)((n + NA_NODES_PER_BLOCK - 1) / NA_NODES_PER_BLOCK);
   cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
-  k_me_partials<<<nb, NA_THREADS, 0, st>>>(rho_dev, u_dev, q, partials);
-  k_me_final<<<1, NA_THREADS, 0, st>>>(partials, nb, out_dev);
-  return cudaGetLastError() == cudaSuccess ? NAT_OK : NAT_ERR_CUDA;
+  // each launch's own status (an earlier, unrelated error of the caller's
+  // thread is neither reported nor cleared here)
+  void* a1[] = {(void*)&rho_dev, (void*)&u_dev, (void*)&q, (void*)&partials};
+  if (cudaLaunchKernel((const void*)k_me_partials, dim3(nb), dim3(NA_THREADS), a1, 0, st) != cudaSuccess)
+    return NAT_ERR_CUDA;
+  const double* pc = partials;
+  void* a2[] = {(void*)&pc, (void*)&nb, (void*)&out_dev};
+  if (cudaLaunchKernel((const void*)k_me_final, dim3(1), dim3(NA_THREADS), a2, 0, st) != cudaSuccess)
+    return NAT_ERR_CUDA;
+  return NAT_OK;
 }

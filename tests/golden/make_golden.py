@@ -18,8 +18,10 @@
    seeded periodic inputs) that the GPU parity tests check against in
    addition to the live oracle.
 
-Usage: python tests/golden/make_golden.py [--reference /root/reference]
-Without a reference tree, step 1 is skipped and the committed JSON is kept.
+Usage: python tests/golden/make_golden.py [--reference PATH]
+PATH is the root of a NATriuM source tree; without --reference the
+environment variable NATRIUM_REFERENCE is used.  Without either (or when the
+directory does not exist), step 1 is skipped and the committed JSON is kept.
 """
 from __future__ import annotations
 
@@ -222,9 +224,10 @@ def oracle_fixtures():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("NATRIUM_REFERENCE"),
+                    help="root of the NATriuM source tree (default: $NATRIUM_REFERENCE)")
     a = ap.parse_args()
-    if os.path.isdir(a.reference):
+    if a.reference and os.path.isdir(a.reference):
         ka = known_answers(a.reference)
         with open(os.path.join(HERE, "known_answers.json"), "w") as fh:
             json.dump(ka, fh, indent=1)

@@ -115,3 +115,25 @@ def test_async_readback_validates_host_arrays_without_gpu():
     with pytest.raises(ValueError):
         sol.download_macro_async(ro, good_u)
     assert sol._pending == {}
+
+
+def test_noalloc_reduction_checks_arguments_without_gpu():
+    """nat_mass_energy_noalloc rejects, before any CUDA call, an axis that does
+    not hold whole cells: its node weights repeat with the cell's period (p
+    nodes per cell for FE_Q with the periodic duplicates folded, p + 1 for DG),
+    so the reference layout's N p + 1 FE_Q count would silently give a wrong
+    mass."""
+    L = N.load_library()
+    dummy = C.c_void_p(16)  # never dereferenced: every case is rejected before a launch
+    h = (C.c_double * 3)(1.0, 1.0, 1.0)
+    for n_axis, order, topo in (((33, 32, 1), 4, N.TOPOLOGIES["feq"]),   # 8 cells p=4 + the duplicate
+                                ((32, 33, 1), 4, N.TOPOLOGIES["feq"]),
+                                ((40, 41, 1), 4, N.TOPOLOGIES["dg"]),    # not a multiple of p + 1 = 5
+                                ((0, 40, 1), 4, N.TOPOLOGIES["dg"])):
+        axes = (C.c_int * 3)(*n_axis)
+        rc = L.nat_mass_energy_noalloc(dummy, dummy, 2, axes, order, topo, h, dummy, None)
+        assert rc == N.NAT_ERR_INVALID_ARG, n_axis
+    axes = (C.c_int * 3)(32, 32, 1)
+    assert L.nat_mass_energy_noalloc(dummy, dummy, 4, axes, 4, 0, h, dummy, None) == N.NAT_ERR_INVALID_ARG
+    assert L.nat_mass_energy_noalloc(dummy, dummy, 2, axes, 0, 0, h, dummy, None) == N.NAT_ERR_INVALID_ARG
+    assert L.nat_mass_energy_noalloc(None, dummy, 2, axes, 4, 0, h, dummy, None) == N.NAT_ERR_INVALID_ARG

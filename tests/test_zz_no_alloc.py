@@ -3,12 +3,15 @@
 Some callers of this library cannot call cudaMalloc where they need the
 mass / kinetic-energy diagnostics -- work being recorded into a CUDA graph,
 hosts whose framework owns all device memory, latency-bound loops -- so this
-entry point keeps its only scratch in a fixed file-scope device array.  The
-test calls it through the C ABI twice in a row on the same fields and checks
-both results against the allocating entry point nat_mass_energy, within the
-relative tolerance the FP64 parity tests use (1e-12).  It lives in a file of
-its own that pytest collects last, and it sets up everything it needs so it
-also passes alone in a fresh process.
+entry point keeps its only scratch (one partial pair per block of 4096 nodes)
+in a fixed file-scope device array.  The tests call it through the C ABI twice
+in a row on the same fields and check both results against the allocating
+entry point nat_mass_energy, within the relative tolerance the FP64 parity
+tests use (1e-12).  The cases cover one block and many blocks with a partial
+last block, and a large call followed by a small one on other fields, so that
+partials the small call does not write are never read.  The file is collected
+last and sets up everything it needs, so it also passes alone in a fresh
+process.
 """
 import ctypes as C
 import math
@@ -20,30 +23,26 @@ import natrium_gb300 as N
 from natrium_gb300 import problems as P
 
 TOL = 1e-12
+NODES_PER_BLOCK = 4096  # of the no-allocation reduction's first pass
 
 
-@pytest.mark.gpu
-@pytest.mark.parametrize("stencil,cells,p,topology", [("D2Q9", (8, 8), 4, "feq"), ("D3Q19", (4, 4, 4), 3, "dg")])
-def test_noalloc_matches_allocating_entry_point(gpu_lib, stencil, cells, p, topology):
-    import torch
+def _solve_fields(stencil, cells, p, topology, steps):
+    """rho, u on the device lattice (periodic FE_Q duplicates folded) after a
+    few steps, and nat_mass_energy of the same state."""
     Ma = 0.1
     scaling = math.sqrt(3) / Ma
     L = (2 * math.pi,) * 3
     spec = N.SolverSpec(stencil=stencil, order=p, cells=cells, length=L, scaling=scaling, viscosity=1e-2,
                         cfl=0.4, precision="fp64", topology=topology)
     X = P.node_coords(cells, p, L, topology)
-    if len(cells) == 2:
-        rho, u = P.taylor_green_2d(X, Ma)
-    else:
-        rho, u = P.taylor_green_3d(X, Ma)
+    rho, u = P.taylor_green_2d(X, Ma) if len(cells) == 2 else P.taylor_green_3d(X, Ma)
     f0 = P.equilibrium(stencil, scaling, rho, u)
     with N.Solver(spec) as sol:
         sol.upload_f(f0)
-        sol.step(3)
+        sol.step(steps)
         mass, ke = sol.mass_energy()
         rho_r, u_r = sol.download_macro()
     dim = len(cells)
-    # device lattice order: FE_Q folds the periodic duplicate of every axis
     per = p if topology == "feq" else p + 1
     n_axis = [cells[a] * per for a in range(dim)]
     ref_axis = [n + (1 if topology == "feq" else 0) for n in n_axis]
@@ -51,28 +50,66 @@ def test_noalloc_matches_allocating_entry_point(gpu_lib, stencil, cells, p, topo
     sl = tuple(slice(0, n) for n in reversed(n_axis))
     rho_d = np.ascontiguousarray(rho_r.reshape(shape)[sl].ravel())
     u_d = np.ascontiguousarray(np.stack([u_r[a].reshape(shape)[sl].ravel() for a in range(dim)]))
+    h = [L[a] / cells[a] if a < dim else 1.0 for a in range(3)]
+    return dict(rho=rho_d, u=u_d, dim=dim, n_axis=n_axis, p=p, topology=topology, h=h, mass=mass, ke=ke)
+
+
+def _call(lib, case, torch, out):
     dev = torch.device("cuda:0")
-    t_rho = torch.from_numpy(rho_d).to(dev)
-    t_u = torch.from_numpy(u_d).to(dev)
-    out = torch.zeros(2, dtype=torch.float64, device=dev)
-    lib = N.load_library()
-    axes = (C.c_int * 3)(*(n_axis + [1] * (3 - dim)))
-    h = (C.c_double * 3)(*[L[a] / cells[a] if a < dim else 1.0 for a in range(3)])
+    t_rho = torch.from_numpy(case["rho"]).to(dev)
+    t_u = torch.from_numpy(case["u"]).to(dev)
+    axes = (C.c_int * 3)(*(case["n_axis"] + [1] * (3 - case["dim"])))
+    h = (C.c_double * 3)(*case["h"])
     stream = torch.cuda.current_stream().cuda_stream
-    topo = N.TOPOLOGIES[topology]
-    results = []
-    for _ in range(2):
-        out.zero_()
-        rc = lib.nat_mass_energy_noalloc(C.c_void_p(t_rho.data_ptr()), C.c_void_p(t_u.data_ptr()), dim, axes, p,
-                                         topo, h, C.c_void_p(out.data_ptr()), C.c_void_p(stream))
-        assert rc == N.NAT_OK
-        torch.cuda.synchronize()
-        results.append(out.cpu().numpy().copy())
-    for m2, e2 in results:
-        assert abs(m2 - mass) <= TOL * abs(mass)
-        assert abs(e2 - ke) <= TOL * abs(ke)
+    rc = lib.nat_mass_energy_noalloc(C.c_void_p(t_rho.data_ptr()), C.c_void_p(t_u.data_ptr()), case["dim"], axes,
+                                     case["p"], N.TOPOLOGIES[case["topology"]], h, C.c_void_p(out.data_ptr()),
+                                     C.c_void_p(stream))
+    assert rc == N.NAT_OK
+    torch.cuda.synchronize()
+    return out.cpu().numpy().copy()
+
+
+def _check(res, case):
+    m2, e2 = res
+    assert abs(m2 - case["mass"]) <= TOL * abs(case["mass"])
+    assert abs(e2 - case["ke"]) <= TOL * abs(case["ke"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("stencil,cells,p,topology", [
+    ("D2Q9", (8, 8), 4, "feq"),        # 1,024 nodes: one block
+    ("D3Q19", (4, 4, 4), 3, "dg"),     # 4,096 nodes: one full block
+    ("D2Q9", (64, 65), 4, "feq"),      # 66,560 nodes: 17 blocks, the last one partial
+])
+def test_noalloc_matches_allocating_entry_point(gpu_lib, stencil, cells, p, topology):
+    import torch
+    case = _solve_fields(stencil, cells, p, topology, 3)
+    n = int(np.prod(case["n_axis"]))
+    out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda:0")
+    results = [_call(gpu_lib, case, torch, out) for _ in range(2)]
+    for r in results:
+        _check(r, case)
     # fixed reduction order: the two calls agree bit for bit
     assert np.array_equal(results[0], results[1])
+    if n > NODES_PER_BLOCK:
+        assert n % NODES_PER_BLOCK != 0  # the partial last block is exercised
+
+
+@pytest.mark.gpu
+def test_noalloc_large_then_small_call_reads_no_stale_partials(gpu_lib):
+    """A call over many blocks leaves its partials in the shared array; a
+    following call over fewer blocks, on other fields, must read only its own
+    (and the large one, repeated, must again give its own result)."""
+    import torch
+    big = _solve_fields("D2Q9", (64, 65), 4, "feq", 2)      # 17 blocks
+    small = _solve_fields("D3Q19", (2, 3, 2), 4, "dg", 1)   # 1,500 nodes: 1 block
+    out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda:0")
+    r_big = _call(gpu_lib, big, torch, out)
+    r_small = _call(gpu_lib, small, torch, out)
+    r_big2 = _call(gpu_lib, big, torch, out)
+    _check(r_big, big)
+    _check(r_small, small)
+    assert np.array_equal(r_big, r_big2)
 
 
 @pytest.mark.gpu
