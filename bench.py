@@ -7,18 +7,23 @@ periodic cube [0, 2 pi)^3 with 16^3 hexahedra and FE_DGQ order 4 (125
 nodes / cell, 512,000 nodes x 19), Ma = 0.1, Re = 1600, CFL = 0.4;
 synthetic analytic initial state, equilibrium-initialised.
 
-value:   node updates/s of the FP32-deviation path with f resident in HBM
-         (device time from CUDA events around each step; L2 flushed by a
-         256 MiB write between timed steps, outside the events).
+value:   node updates/s of the plain FP64 path (the reference's own
+         arithmetic) with f resident in HBM (device time from CUDA events
+         around each step; L2 flushed by a 256 MiB write between timed steps,
+         outside the events).
 e2e:     the same metric through the C ABI with host buffers: each step
          uploads f (FP64, pinned host memory), runs the step and reads rho
          and u back.  Pipelined: step k's upload runs on the handle's copy
          stream while step k-1 is stepped and read back (asynchronous
          read-back tickets); the blocking one-step-at-a-time loop is
          reported beside it (e2e.serial), with the measured host link.
-fp64_plain: the plain FP64 path on the same workload.
-roofline: algorithmic bytes per step = 2 Q s_f per node (f read once,
-         written once) over the measured HBM copy bandwidth.
+roofline: the FP64 kernel is bound by the FP64 pipe, not by HBM: achieved =
+         executed FP64 flops per launch (one ncu capture) over the live launch
+         time, against the FP64 peak measured in the same run (cuBLAS DGEMM);
+         the HBM fraction (algorithmic bytes 2 Q s_f per node) beside it.
+fp32dev: the mixed-precision form (f - w_i stored in FP32) on the same
+         workload: device rate, speed-up over FP64, HBM roofline, its own e2e
+         and its error against the FP64 path after 1000 steps.
 cpu_baseline: the CPU oracle (FP64 restatement of the reference algorithm:
          copy + per-direction CSR SpMV + collide sweep, OpenMP) on a bounded
          sample of the same workload.
@@ -136,15 +141,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def time_device(sol, torch, stream, flush, steps: int, warmup: int):
+def time_device(sol, torch, stream, flush, steps: int, warmup: int, nvtx: str = None):
     """Per-step CUDA-event timing on the solver's stream, L2 flushed between
-    steps outside the events.  Returns (per-step ms list, launches)."""
+    steps outside the events.  Returns (per-step ms list, launches).  With
+    nvtx, the timed steps are enclosed in an NVTX range of that name."""
     for _ in range(warmup):
         sol.step_async(1, write_macro=False)
         with torch.cuda.stream(stream):
             flush.add_(1.0)
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    if nvtx:
+        torch.cuda.nvtx.range_push(nvtx)
     l0 = sol.launches
     for k in range(steps):
         ev[k][0].record(stream)
@@ -152,9 +160,12 @@ def time_device(sol, torch, stream, flush, steps: int, warmup: int):
         ev[k][1].record(stream)
         with torch.cuda.stream(stream):
             flush.add_(1.0)
+    launches = sol.launches - l0
+    if nvtx:
+        torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     sol.status()
-    return [a.elapsed_time(b) for a, b in ev], sol.launches - l0
+    return [a.elapsed_time(b) for a, b in ev], launches
 
 
 def time_e2e(sol, torch, f_host, rho_h, u_h, steps: int):
@@ -513,6 +524,14 @@ def aggregate_ranks(torch, ws: int, total_ms: float, nodes: int, steps: int, dev
     return total_ms, ws * nodes * steps / (total_ms * 1e-3)
 
 
+def bench_config(nodes: int, ws: int) -> dict:
+    """The workload as both arms name it (identical keys and values)."""
+    w = WORKLOAD
+    return {"workload": w["name"], "nodes": nodes, "stencil": w["stencil"], "collision": w["collision"],
+            "order": w["order"], "topology": w["topology"], "cells": list(w["cells"]), "Ma": w["Ma"], "Re": w["Re"],
+            "cfl": w["cfl"], "storage": "fp64 (plain)", "parallelism": f"replicas x{ws}"}
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -536,8 +555,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic TGV3D state)",
-        "config": {"workload": w["name"], "nodes": mesh.n_nodes, "stencil": w["stencil"], "order": w["order"],
-                   "topology": w["topology"], "cells": list(w["cells"])},
+        "config": bench_config(mesh.n_nodes, args.gpus),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"full workload, {args.steps} steps; the reference (deal.II/Trilinos) cannot "
                                    "be built, its algorithm is restated in oracle/natoracle.c"},
@@ -545,6 +563,72 @@ def run_reference(args):
     }
     print(json.dumps(line))
     return 0
+
+
+def fp64_peak_tflops(torch, n: int = 4096, reps: int = 3) -> float:
+    """Measured FP64 peak of this GPU: cuBLAS DGEMM (torch float64 matmul) of
+    n^3, 2 n^3 flops, best of reps, CUDA events."""
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    c = a @ b
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) * 1e-3)
+    del a, b, c
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def fp64_profile():
+    """Executed FP64 flops and DRAM traffic per launch of the FP64 kernel, from
+    one ncu capture (profiles/fp64_flops.json)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "fp64_flops.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return None
+
+
+def time_e2e_legs(sol, torch, ws, f0, nodes, e2e_steps):
+    """The e2e legs of one solver: link bandwidth, the serial loop and the
+    pipelined loop (the reported value), and the check that a pipelined
+    read-back equals the blocking one."""
+    f_host = torch.from_numpy(f0).pin_memory().numpy()
+    rho_h = torch.empty(sol.n_ref, dtype=torch.float64).pin_memory().numpy()
+    u_h = torch.empty((sol.D, sol.n_ref), dtype=torch.float64).pin_memory().numpy()
+    link = measure_link(torch, f0.nbytes)
+    serial_s = time_e2e(sol, torch, f_host, rho_h, u_h, e2e_steps)
+    serial_ms, _ = aggregate_ranks(torch, ws, serial_s * 1e3, nodes, 1)
+    rho_b = [rho_h, torch.empty(sol.n_ref, dtype=torch.float64).pin_memory().numpy()]
+    u_b = [u_h, torch.empty((sol.D, sol.n_ref), dtype=torch.float64).pin_memory().numpy()]
+    e2e_s = time_e2e_pipelined(sol, torch, f_host, rho_b, u_b, 4 * e2e_steps)
+    e2e_ms, _ = aggregate_ranks(torch, ws, e2e_s * 1e3, nodes, 1)
+    sol.upload_f(f0)
+    sol.step(1)
+    r_ref, u_ref = sol.download_macro()
+    sol.upload_f(f0)
+    sol.step_async(1, True)
+    sol.wait(sol.download_macro_async(rho_b[1], u_b[1]))
+    pipeline_ok = bool(np.array_equal(rho_b[1], r_ref) and np.array_equal(u_b[1], u_ref))
+    h2d = f0.nbytes
+    d2h = 8 * (1 + sol.D) * sol.n_ref
+    return {"value": ws * nodes / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+            "mode": "pipelined: upload of step k on its own copy stream while step k-1 is stepped and its "
+                    "rho/u read back; every step uploads its f (FP64, reference layout, page-locked) and reads "
+                    "its rho/u, status checked per step",
+            "link": link, "link_floor_ms": h2d / (link["h2d_gbs"] * 1e6),
+            "serial": {"value": ws * nodes / (serial_ms * 1e-3), "ms_per_step": serial_ms,
+                       "mode": "upload, step, blocking read-back, one step at a time"},
+            "pipeline_matches_blocking": pipeline_ok}
+
+
+KERNEL_NAMES = {1: "k_sl_step", 2: "k_sl_step_v2", 3: "k_sl_row", 6: "k_sl_rowt", 7: "k_sl_rowg"}
 
 
 def run_ours(args):
@@ -570,98 +654,111 @@ def run_ours(args):
                                             full_run=not args.profile)))
         return 0
 
-    # --- FP32-deviation path (headline) -------------------------------------
-    spec = spec_for(args.profile_precision if args.profile else "fp32dev")
-    f0 = initial_state(spec)
-    sol = N.Solver(spec)
-    sol.set_stream(stream.cuda_stream)
-    sol.upload_f(f0)
-    if args.variant:
-        sol.set_kernel_variant(args.variant)
-        ncand, chosen = 1, 0
-    else:
-        ncand, chosen = sol.autotune(10)
-    kinfo = sol.kernel_info()
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
     vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
     try:
         smi_index = int(vis.split(",")[local]) if vis else local
     except (ValueError, IndexError):
         smi_index = local
+
     if args.profile:
-        per, launches = time_device(sol, torch, stream, flush, args.steps, args.warmup)
-        print(json.dumps({"profile_run": True, "ms_per_step": sum(per) / args.steps, "launches": launches,
-                          "kernel": kinfo}))
-        sol.close()
+        spec = spec_for(args.profile_precision)
+        f0 = initial_state(spec)
+        with N.Solver(spec) as sol:
+            sol.set_stream(stream.cuda_stream)
+            sol.upload_f(f0)
+            if args.variant:
+                sol.set_kernel_variant(args.variant)
+            elif args.candidate >= 0:
+                sol.select_candidate(args.candidate)
+            else:
+                sol.autotune(10)
+            # the timed steps sit in an NVTX range "timed" (ncu --nvtx-include timed/)
+            per, launches = time_device(sol, torch, stream, flush, args.steps, args.warmup, nvtx="timed")
+            print(json.dumps({"profile_run": True, "precision": args.profile_precision,
+                              "ms_per_step": sum(per) / args.steps, "launches": launches,
+                              "kernel": sol.kernel_info()}))
         return 0
+
+    dgemm = fp64_peak_tflops(torch)
+
+    # --- headline: the plain FP64 path (the reference's own arithmetic) --------
+    spec = spec_for("fp64")
+    f0 = initial_state(spec)
+    sol = N.Solver(spec)
+    sol.set_stream(stream.cuda_stream)
+    sol.upload_f(f0)
+    at64 = []
+    if args.variant:
+        sol.set_kernel_variant(args.variant)
+        ncand, chosen = 1, 0
+    else:
+        ncand, chosen = sol.autotune(5)
+        at64 = sol.autotune_report()
+    kinfo = sol.kernel_info()
+    sol.upload_f(f0)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
     with ClockSampler(smi_index) as clk:
         per, launches = time_device(sol, torch, stream, flush, args.steps, args.warmup)
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
     nodes = sol.n_dev
+    Q = sol.Q
     total_ms, value = aggregate_ranks(torch, ws, sum(per), nodes, args.steps)
     ms = total_ms / args.steps
-    Q = sol.Q
-
-    # --- e2e through the C ABI with host buffers -------------------------------
-    f_host = torch.from_numpy(f0).pin_memory().numpy()
-    sol.upload_f(f0)
-    e2e_steps = max(5, min(50, args.steps // 20))
-    # page-locked result buffers (the f buffer above is page-locked too)
-    rho_h = torch.empty(sol.n_ref, dtype=torch.float64).pin_memory().numpy()
-    u_h = torch.empty((sol.D, sol.n_ref), dtype=torch.float64).pin_memory().numpy()
-    link = measure_link(torch, f0.nbytes)
-    serial_s = time_e2e(sol, torch, f_host, rho_h, u_h, e2e_steps)
-    serial_ms, _ = aggregate_ranks(torch, ws, serial_s * 1e3, nodes, 1)  # slowest rank
-    rho_b = [rho_h, torch.empty(sol.n_ref, dtype=torch.float64).pin_memory().numpy()]
-    u_b = [u_h, torch.empty((sol.D, sol.n_ref), dtype=torch.float64).pin_memory().numpy()]
-    e2e_s = time_e2e_pipelined(sol, torch, f_host, rho_b, u_b, 4 * e2e_steps)
-    e2e_ms, _ = aggregate_ranks(torch, ws, e2e_s * 1e3, nodes, 1)
-    e2e_s = e2e_ms * 1e-3
-    # the pipelined read-backs equal the blocking one of the same state
-    sol.upload_f(f0)
-    sol.step(1)
-    r_ref, u_ref = sol.download_macro()
-    sol.upload_f(f0)
-    sol.step_async(1, True)
-    sol.wait(sol.download_macro_async(rho_b[1], u_b[1]))
-    pipeline_ok = bool(np.array_equal(rho_b[1], r_ref) and np.array_equal(u_b[1], u_ref))
-    h2d = f0.nbytes
-    d2h = 8 * (1 + sol.D) * sol.n_ref
-    # correctness guard on the measured state: finite, mass near 1
+    e2e = time_e2e_legs(sol, torch, ws, f0, nodes, max(5, min(50, args.steps // 4)))
     rho, u = sol.download_macro()
     ok = bool(np.all(np.isfinite(rho)) and abs(float(np.mean(rho)) - 1.0) < 1e-2)
     sol.close()
 
-    # --- plain FP64 path ---------------------------------------------------------
-    spec64 = spec_for("fp64")
-    sol64 = N.Solver(spec64)
-    sol64.set_stream(stream.cuda_stream)
-    sol64.upload_f(f0)
-    at64 = []
+    # --- FP32 deviation storage (the mixed-precision form) -------------------------
+    spec32 = spec_for("fp32dev")
+    sol32 = N.Solver(spec32)
+    sol32.set_stream(stream.cuda_stream)
+    sol32.upload_f(f0)
     if args.variant:
-        sol64.set_kernel_variant(args.variant)
+        sol32.set_kernel_variant(args.variant)
+        ncand32, chosen32 = 1, 0
     else:
-        sol64.autotune(3)
-        at64 = sol64.autotune_report()
-    kinfo64 = sol64.kernel_info()
-    steps64 = max(3, args.steps // 4)
-    per64, _ = time_device(sol64, torch, stream, flush, steps64, args.warmup)
-    ms64 = sum(per64) / steps64
-    sol64.close()
+        ncand32, chosen32 = sol32.autotune(10)
+    kinfo32 = sol32.kernel_info()
+    sol32.upload_f(f0)
+    steps32 = max(args.steps, 20)
+    per32, launches32 = time_device(sol32, torch, stream, flush, steps32, args.warmup)
+    total32, value32 = aggregate_ranks(torch, ws, sum(per32), nodes, steps32)
+    ms32 = total32 / steps32
+    e2e32 = time_e2e_legs(sol32, torch, ws, f0, nodes, max(5, min(50, args.steps // 4)))
+    # accuracy against the FP64 path (the path pinned to the oracle), same start
+    acc_steps = 1000
+    sol32.upload_f(f0)
+    sol32.step(acc_steps)
+    r32, u32 = sol32.download_macro()
+    sol32.close()
+    with N.Solver(spec) as s64:
+        s64.set_stream(stream.cuda_stream)
+        s64.upload_f(f0)
+        s64.step(acc_steps)
+        r64, u64 = s64.download_macro()
+    rl2 = lambda a, b: float(np.sqrt(np.sum((a - b) ** 2) / np.sum(b ** 2)))
 
     hbm, peak_kind = peaks()
-    alg_bytes = 2 * Q * 4 * nodes
-    achieved = alg_bytes / (ms * 1e-3) / 1e9
     alg64 = 2 * Q * 8 * nodes
-    ach64 = alg64 / (ms64 * 1e-3) / 1e9
+    alg32 = 2 * Q * 4 * nodes
+    prof = fp64_profile()
+    traffic64 = flops64 = busy64 = None
+    if prof and prof.get("workload") == WORKLOAD["name"] and prof.get("kernel_variant") == kinfo["variant"] \
+            and prof.get("tile_nodes") == kinfo["tile_nodes"]:
+        traffic64 = prof.get("dram_bytes_per_launch")
+        flops64 = prof.get("fp64_flops_per_launch")
+        busy64 = prof.get("fp64_pipe_busy")
     tr = traffic_from_profile()
-    traffic = None
-    if tr and tr.get("workload") == WORKLOAD["name"] and kinfo["variant"] == 3:
-        traffic = tr.get("dram_bytes_per_launch")
+    traffic32 = None
+    if tr and tr.get("workload") == WORKLOAD["name"] and tr.get("kernel_variant", 3) == kinfo32["variant"]:
+        traffic32 = tr.get("dram_bytes_per_launch")
+    ach64_gbs = alg64 / (ms * 1e-3) / 1e9
+    fp64_tflops = flops64 / (ms * 1e-3) / 1e12 if flops64 else None
 
     if rank != 0:
         if ws > 1:
@@ -676,7 +773,7 @@ def run_ours(args):
         from natrium_gb300 import serving as SV
         arr, reqs = SV.workload(512, seed=0, rate=200.0)
         serving = SV.run_workload(arr, reqs)
-        seq = SV.run_sequential(reqs[:32], "fp64")
+        seq = SV.run_sequential(reqs[:args.fp64_sample], "fp64")
         cap = SV.run_workload(np.zeros(len(reqs)), reqs)
         serving["capacity"] = {"solves_per_s": cap["solves_per_s"], "wall_s": cap["wall_s"],
                                "latency_p50_s": cap["latency_p50_s"], "latency_p99_s": cap["latency_p99_s"],
@@ -685,37 +782,42 @@ def run_ours(args):
         serving.update({"workload": "512 D2Q9 solves (TGV / shear layer, BGK / KBC, N in {4..64}, p 2-6, "
                                     "Ma 0.02-0.1, Re 100-5000, 50-2000 steps), Poisson 200 req/s, seed 0, "
                                     "FP32 deviation storage",
-                        "fp64_one_at_a_time": {**seq, "sample": "first 32 requests of the same stream"}})
+                        "fp64_one_at_a_time": {**seq, "sample": f"first {args.fp64_sample} requests of the same "
+                                                                "stream"}})
+    kname = KERNEL_NAMES.get(kinfo["variant"], str(kinfo["variant"]))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (analytic Taylor-Green initial state, equilibrium-initialised)",
-        "config": {"workload": WORKLOAD["name"], "nodes": nodes, "stencil": WORKLOAD["stencil"],
-                   "collision": WORKLOAD["collision"], "order": WORKLOAD["order"], "topology": WORKLOAD["topology"],
-                   "cells": list(WORKLOAD["cells"]), "storage": "fp32 deviation f - w_i",
-                   "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
-                   "parallelism": f"replicas x{ws}"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": alg_bytes,
-                     "kernel": {1: "k_sl_step", 2: "k_sl_step_v2", 3: "k_sl_row", 6: "k_sl_rowt", 7: "k_sl_rowg"}[kinfo["variant"]]
-                               + "<D3Q19,float,BGK>",
-                     "tile_nodes": kinfo["tile_nodes"], "threads": kinfo["threads"],
-                     "autotune": {"candidates": ncand, "chosen": chosen}},
+        "config": bench_config(nodes, ws),
+        "l2": "flushed between timed steps (256 MiB write, outside the timed events)",
+        "roofline": {"bound": "fp64", "achieved": fp64_tflops, "peak": dgemm, "unit": "TFLOP/s",
+                     "frac": fp64_tflops / dgemm if fp64_tflops else None, "traffic": traffic64,
+                     "peak_kind": "measured in this run: cuBLAS DGEMM 4096^3 (torch float64 matmul), best of 3",
+                     "achieved_from": "executed FP64 flops per launch (2 DFMA + DADD + DMUL, one ncu capture, "
+                                      "profiles/fp64_flops.json) / the live mean launch time",
+                     "fp64_pipe_busy_ncu": busy64,
+                     "hbm": {"achieved": ach64_gbs, "peak": hbm, "unit": "GB/s", "frac": ach64_gbs / hbm,
+                             "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg64},
+                     "kernel": kname + "<D3Q19,double,BGK>", "tile_nodes": kinfo["tile_nodes"],
+                     "threads": kinfo["threads"], "autotune": {"candidates": ncand, "chosen": chosen,
+                                                               "report": at64}},
         "cpu_baseline": cpu,
-        "e2e": {"value": ws * nodes / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_s * 1e3,
-                "mode": "pipelined: upload of step k on its own copy stream while step k-1 is stepped and its "
-                        "rho/u read back; every step uploads its f and reads its rho/u, status checked per step",
-                "link": link, "link_floor_ms": h2d / (link["h2d_gbs"] * 1e6),
-                "serial": {"value": ws * nodes / (serial_ms * 1e-3), "ms_per_step": serial_ms,
-                           "mode": "upload, step, blocking read-back, one step at a time"},
-                "pipeline_matches_blocking": pipeline_ok},
+        "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk.summary(),
-        "fp64_plain": {"value": ws * nodes / (ms64 * 1e-3), "ms_per_step": ms64, "steps": steps64,
-                       "roofline_frac": ach64 / hbm, "achieved_gbs": ach64, "kernel": kinfo64, "autotune": at64},
-        "speedup_vs_fp64_plain": ms64 / ms,
+        "fp32dev": {"value": value32, "ms_per_step": ms32, "steps": steps32, "gpu_launches": launches32,
+                    "storage": "fp32 deviation f - w_i, FP32 arithmetic, FP64 departure weights",
+                    "speedup_vs_fp64_plain": ms / ms32,
+                    "roofline": {"bound": "hbm", "achieved": alg32 / (ms32 * 1e-3) / 1e9, "peak": hbm,
+                                 "unit": "GB/s", "frac": alg32 / (ms32 * 1e-3) / 1e9 / hbm, "traffic": traffic32,
+                                 "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg32,
+                                 "kernel": KERNEL_NAMES.get(kinfo32["variant"], str(kinfo32["variant"]))
+                                           + "<D3Q19,float,BGK>",
+                                 "tile_nodes": kinfo32["tile_nodes"], "threads": kinfo32["threads"],
+                                 "autotune": {"candidates": ncand32, "chosen": chosen32}},
+                    "e2e": e2e32,
+                    "error_vs_fp64": {"steps": acc_steps, "rel_l2_u": rl2(u32, u64), "rel_l2_rho": rl2(r32, r64)}},
         "serving": serving,
         "compressible": compressible,
         "mapped": mapped,
@@ -739,11 +841,14 @@ def main():
                          "7 row-group")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--candidate", type=int, default=-1,
-                    help="with --mixed-only --profile: use this autotuner candidate without timing")
-    ap.add_argument("--profile-precision", default="fp32dev", choices=["fp32dev", "fp64"],
-                    help="with --profile: the path to time (the headline FP32 deviation path or plain FP64)")
+                    help="with --profile: use this autotuner candidate without timing")
+    ap.add_argument("--profile-precision", default="fp64", choices=["fp32dev", "fp64"],
+                    help="with --profile: the path to time (the headline plain FP64 path or FP32 deviation)")
     ap.add_argument("--profile", action="store_true",
-                    help="lean run for ncu: FP32 device timing only (no e2e, FP64 leg, CPU baseline or clocks)")
+                    help="lean run for ncu: device timing of one path only (no e2e, other legs, CPU baseline "
+                         "or clocks)")
+    ap.add_argument("--fp64-sample", type=int, default=128,
+                    help="serving: requests of the stream timed one at a time on the plain FP64 path")
     ap.add_argument("--no-compressible", action="store_true", help="skip the compressible D2Q25H leg")
     ap.add_argument("--no-mapped", action="store_true", help="skip the mapped-mesh (LubricationSine) leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the D3Q27 KBC FP32-vs-FP64 accuracy leg")

@@ -259,14 +259,23 @@ int nat_set_boundary(nat_solver* s, int face, int kind, const double u_wall[3]);
  *   NAT_FORCE_SHIFTING_VELOCITY: equilibrium velocity u + tau dt F / rho;
  *   NAT_FORCE_EXACT_DIFFERENCE: after relaxation
  *     f += f^eq(rho, u + dt F / rho) - f^eq(rho, u);
- * both report u + dt F / (2 rho).  force[0..D-1] in scaled units (like u).
- * BGK_STANDARD only (NAT_ERR_UNSUPPORTED otherwise; the reference's GUO
- * scheme is not implemented in the advanced path either).  Not applied with
+ *   NAT_FORCE_GUO: the legacy BGKStandard::collideAll scheme
+ *     (collision/BGKStandard.cpp:128-133, 222-225 for D2Q9; :374-380,
+ *     470-473 for D3Q19; the advanced path throws for it): equilibrium velocity
+ *     u' = u + dt F / (2 rho), then f_i += dt w_i (1 - omega/2) (p (e_i.F - u'.F)
+ *     + p^2 (e_i.u')(e_i.F)), p = scaling / c_s^2, with unit e_i and scaled u',
+ *     F (collision/ExternalForceFunctions.h:119-200).  D2Q9 and D3Q19 only
+ *     (the reference sends D3Q27 to the generic BGK::collideAll, which has no
+ *     force).  For D3Q19 the reference adds the source term to a copy that it
+ *     does not store, so only the shifted equilibrium acts: kept as written.
+ * All report u + dt F / (2 rho).  force[0..D-1] in scaled units (like u).
+ * BGK_STANDARD only (NAT_ERR_UNSUPPORTED otherwise).  Not applied with
  * a prescribed velocity (nat_collide with in_init).  With a force the step
  * runs in the generic fused kernel.  NAT_FORCE_NONE switches it off. */
 #define NAT_FORCE_NONE 0
 #define NAT_FORCE_SHIFTING_VELOCITY 1
 #define NAT_FORCE_EXACT_DIFFERENCE 2
+#define NAT_FORCE_GUO 3
 int nat_set_force(nat_solver* s, int scheme, const double force[3]);
 
 /* ---- compressible two-population model (NAT_BGK_COMPRESSIBLE) ---------- */

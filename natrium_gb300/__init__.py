@@ -45,7 +45,7 @@ NAT_ERR_UNSUPPORTED = 7
 STENCILS = {"D2Q9": 0, "D3Q19": 1, "D3Q27": 2, "D2Q25H": 3}
 STENCIL_DQ = {"D2Q9": (2, 9), "D3Q19": (3, 19), "D3Q27": (3, 27), "D2Q25H": (2, 25)}
 COLLISIONS = {"BGK_STANDARD": 0, "BGK_INCOMPRESSIBLE": 1, "KBC_STANDARD": 2, "BGK_COMPRESSIBLE": 3}
-FORCE_SCHEMES = {"NONE": 0, "SHIFTING_VELOCITY": 1, "EXACT_DIFFERENCE": 2}
+FORCE_SCHEMES = {"NONE": 0, "SHIFTING_VELOCITY": 1, "EXACT_DIFFERENCE": 2, "GUO": 3}
 EQUILIBRIA = {"BGK": 0, "QUARTIC": 1}
 TOPOLOGIES = {"feq": 0, "dg": 1}
 PRECISIONS = {"fp64": 0, "fp32dev": 1}
@@ -455,7 +455,8 @@ class Solver:
     # -- wall boundaries -------------------------------------------------------------
     def set_force(self, scheme: str = "SHIFTING_VELOCITY", force=(0.0, 0.0, 0.0)):
         """Constant body force in scaled units (ConstantExternalForce) with the
-        forcing scheme NONE, SHIFTING_VELOCITY or EXACT_DIFFERENCE."""
+        forcing scheme NONE, SHIFTING_VELOCITY, EXACT_DIFFERENCE (the advanced
+        collision) or GUO (the legacy BGKStandard collision, D2Q9 and D3Q19)."""
         F = np.zeros(3)
         F[: len(force)] = force
         self._check(self._L.nat_set_force(self._h, FORCE_SCHEMES[scheme], _dp(F)))

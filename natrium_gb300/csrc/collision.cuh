@@ -118,17 +118,33 @@ __device__ __forceinline__ Real collide_bgk(Real (&v)[S::Q], Real inv_tau,
 
 // ---------------------------------------------------------------------------
 // BGK with a constant body force F: the advanced collision of the time loop
-// (CollisionOperator.h:76-90, AuxiliaryCollisionFunctions.h:332-414).
+// (CollisionOperator.h:76-90, AuxiliaryCollisionFunctions.h:332-414) and the
+// legacy BGKStandard's GUO scheme (collision/BGKStandard.cpp:128-133, 222-225
+// for D2Q9; :374-380, 470-473 for D3Q19).
 // dF = dt F / scaling (unscaled momentum gained per step).
 //   scheme 1 (SHIFTING_VELOCITY): equilibrium velocity u + tau dF / rho;
 //   scheme 2 (EXACT_DIFFERENCE): relax with u, then
 //     f += f^eq(rho, u + dF / rho) - f^eq(rho, u);
-// both report the velocity u + dF / (2 rho).  Not applied with a prescribed
-// velocity (inInitializationProcedure).  Returns rho.
+//   scheme 3 (GUO): equilibrium velocity u' = u + dF / (2 rho), then
+//     f_i += w_i (1 - omega/2) (3 e_i.dF - 3 scaling u'.dF + 9 (e_i.u')(e_i.dF))
+//     (collision/ExternalForceFunctions.h:119-200, applyGuoForcingD2Q9, written
+//     in unscaled variables: its u.F term carries the stencil scaling, as in
+//     the reference).  For D3Q19 the reference adds that source term to a
+//     local copy after the relaxed values are stored (BGKStandard.cpp:441-473),
+//     so only the shifted equilibrium acts; restated as written.
+// All report the velocity u + dF / (2 rho).  Not applied with a prescribed
+// velocity (inInitializationProcedure).  Returns rho; tgt receives the mass
+// and momentum the collision adds (the FP32 projection's targets).
 // ---------------------------------------------------------------------------
+template <class S>
+__host__ __device__ constexpr bool guo_source() {
+  return S::Q == 9;  // D2Q9; the D3Q19 source term is discarded by the reference
+}
+
 template <class S, bool DEV, bool COMP, class Real>
 __device__ __forceinline__ Real collide_bgk_force(Real (&v)[S::Q], Real inv_tau, Real tau, Real (&u)[3],
-                                                  bool given_u, const Real (&dF)[3], int scheme) {
+                                                  bool given_u, const Real (&dF)[3], int scheme, Real scaling,
+                                                  Real (&tgt)[4]) {
   if (given_u) return collide_bgk<S, DEV, COMP>(v, inv_tau, u, true);
   Real m0, j[3];
   moments<S, COMP>(v, m0, j);
@@ -140,11 +156,15 @@ __device__ __forceinline__ Real collide_bgk_force(Real (&v)[S::Q], Real inv_tau,
   Real ue[3] = {u[0], u[1], u[2]};
   if (scheme == 1)
     for (int a = 0; a < S::D; ++a) ue[a] += tau * dF[a] * inv;
+  if (scheme == 3)
+    for (int a = 0; a < S::D; ++a) ue[a] += Real(0.5) * dF[a] * inv;
   Real us[3] = {ue[0], ue[1], ue[2]};
   if (scheme == 2)
     for (int a = 0; a < S::D; ++a) us[a] += dF[a] * inv;
   const Real uu = Real(1.5) * (ue[0] * ue[0] + ue[1] * ue[1] + ue[2] * ue[2]);
   const Real uus = Real(1.5) * (us[0] * us[0] + us[1] * us[1] + us[2] * us[2]);
+  const Real guo = (Real(1) - Real(0.5) * inv_tau);  // 1 - omega / 2
+  const Real uF = ue[0] * dF[0] + ue[1] * dF[1] + ue[2] * dF[2];
   static_for<0, S::Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
     const Real ee = Real(3) * edot<S, i>(ue);
@@ -160,8 +180,27 @@ __device__ __forceinline__ Real collide_bgk_force(Real (&v)[S::Q], Real inv_tau,
       const Real polys = es * (Real(1) + Real(0.5) * es) - uus;
       v[i] += Real(S::w(i)) * rho * (polys - poly);
     }
+    if constexpr (guo_source<S>()) {
+      if (scheme == 3) {
+        const Real eF = edot<S, i>(dF);
+        const Real eu = edot<S, i>(ue);
+        v[i] += Real(S::w(i)) * guo * (Real(3) * eF - Real(3) * scaling * uF + Real(9) * eu * eF);
+      }
+    }
   });
   for (int a = 0; a < S::D; ++a) u[a] += Real(0.5) * dF[a] * inv;
+  // mass and momentum added: dF for schemes 1 and 2; for GUO the relaxation
+  // towards u' adds omega dF / 2 and the source term (1 - omega/2) dF, and the
+  // source's mass is 3 (1 - omega/2)(1 - scaling) u'.dF
+  tgt[0] = Real(0);
+  for (int a = 0; a < 3; ++a) tgt[1 + a] = dF[a];
+  if (scheme == 3) {
+    if constexpr (guo_source<S>()) {
+      tgt[0] = Real(3) * guo * (Real(1) - scaling) * uF;
+    } else {
+      for (int a = 0; a < 3; ++a) tgt[1 + a] = Real(0.5) * inv_tau * dF[a];
+    }
+  }
   return rho;
 }
 
@@ -328,13 +367,14 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
 
 // Mass / momentum projection of the FP32 collision: removes the float
 // rounding defect of the conserved moments (post - pre - target, target the
-// momentum a body force adds) through the rest and the axis populations, so
+// mass and momentum a body force adds) through the rest and the axis populations, so
 // that the collision conserves them exactly up to the (unbiased) rounding of
 // small differences.
 template <class S, class Real>
 __device__ __forceinline__ void conserve(Real (&v)[S::Q], const Real (&pre)[S::Q],
-                                         const Real (&target)[3] = {Real(0), Real(0), Real(0)}) {
-  Real dm = 0, dj[3] = {-target[0], -target[1], -target[2]};
+                                         const Real (&target)[3] = {Real(0), Real(0), Real(0)},
+                                         Real mass_target = Real(0)) {
+  Real dm = -mass_target, dj[3] = {-target[0], -target[1], -target[2]};
   static_for<0, S::Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
     const Real d = v[i] - pre[i];
@@ -374,9 +414,14 @@ __device__ __forceinline__ Real bgk_collide(const Prm& P, Real (&v)[S::Q], const
     }
   } else {
     const Real dF[3] = {Real(P.dF[0]), Real(P.dF[1]), Real(P.dF[2])};
-    rho = collide_bgk_force<S, DEV, COMP>(v, Real(1) / Real(P.tau), Real(P.tau), u, given_u, dF, P.force_scheme);
+    Real tgt[4];
+    rho = collide_bgk_force<S, DEV, COMP>(v, Real(1) / Real(P.tau), Real(P.tau), u, given_u, dF, P.force_scheme,
+                                          Real(P.scaling), tgt);
     if constexpr (DEV) {
-      if (!given_u) conserve<S>(v, pre, dF);
+      if (!given_u) {
+        const Real tj[3] = {tgt[1], tgt[2], tgt[3]};
+        conserve<S>(v, pre, tj, tgt[0]);
+      }
     }
   }
   return rho;

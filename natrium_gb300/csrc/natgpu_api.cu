@@ -1877,10 +1877,13 @@ int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* t
 }
 
 int nat_set_force(nat_solver* s, int scheme, const double force[3]) {
-  if (!s || scheme < NAT_FORCE_NONE || scheme > NAT_FORCE_EXACT_DIFFERENCE || (scheme && !force))
+  if (!s || scheme < NAT_FORCE_NONE || scheme > NAT_FORCE_GUO || (scheme && !force))
     return NAT_ERR_INVALID_ARG;
   if (scheme && (s->thermal || s->spec.collision != NAT_BGK_STANDARD))
     return fail(s, NAT_ERR_UNSUPPORTED, "a body force acts in the BGK_STANDARD collision only");
+  if (scheme == NAT_FORCE_GUO && s->spec.stencil != NAT_D2Q9 && s->spec.stencil != NAT_D3Q19)
+    return fail(s, NAT_ERR_UNSUPPORTED,
+                "the GUO scheme exists for D2Q9 and D3Q19 only (the legacy BGKStandard collision)");
   s->force_scheme = scheme;
   for (int a = 0; a < 3; ++a) s->force[a] = (scheme && a < s->D) ? force[a] : 0.0;
   if (scheme) {

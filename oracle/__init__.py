@@ -346,7 +346,8 @@ def collide_bgk(st: Stencil, tau: float, f, rho, u, in_init=False, nthreads=1):
 
 
 # forcing schemes of the advanced collision (SolverConfiguration::setForcingScheme)
-FORCE_NONE, FORCE_SHIFTING_VELOCITY, FORCE_EXACT_DIFFERENCE = 0, 1, 2
+# (3: GUO, the legacy BGKStandard scheme, collision/BGKStandard.cpp:222-225, 470-473)
+FORCE_NONE, FORCE_SHIFTING_VELOCITY, FORCE_EXACT_DIFFERENCE, FORCE_GUO = 0, 1, 2, 3
 
 
 def collide_bgk_force(st: Stencil, tau: float, dt: float, f, rho, u, scheme: int, force, in_init=False,

@@ -1050,6 +1050,9 @@ static void advanced_bgk_feq(int stencil, int D, int Q, const double e[32][3], c
   }
 }
 
+static int collide_bgk_legacy_guo(int stencil, double scaling, double tau, double dt, int64_t n, double* f,
+                                  double* rho, double* u, int in_init, const double* force);
+
 int orc_collide_bgk_force(int stencil, double scaling, double tau, double dt, int64_t n, double* f, double* rho,
                           double* u, int in_init, int scheme, const double* force, int nthreads) {
   int D, Q, bad = 0;
@@ -1064,6 +1067,7 @@ int orc_collide_bgk_force(int stencil, double scaling, double tau, double dt, in
       for (a = 0; a < 3; a++) e[i][a] = es[3 * i + a] / scaling;
   }
   const double cs2 = cs2s / (scaling * scaling);
+  if (scheme == 3) return collide_bgk_legacy_guo(stencil, scaling, tau, dt, n, f, rho, u, in_init, force);
   (void)nthreads;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static) reduction(| : bad) num_threads(nthreads > 0 ? nthreads : 1)
@@ -1111,6 +1115,78 @@ int orc_collide_bgk_force(int stencil, double scaling, double tau, double dt, in
       for (pq = 0; pq < Q; pq++) fl[pq] += shifted[pq] - feq[pq];
     }
     for (pq = 0; pq < Q; pq++) f[(int64_t)pq * n + ii] = fl[pq];
+  }
+  return bad ? ORC_ERR_DENSITY : ORC_OK;
+}
+
+/* The legacy BGKStandard collision with the GUO forcing scheme, in the
+ * reference's scaled variables: collideAllD2Q9 (collision/BGKStandard.cpp:
+ * 64-239; velocity :128-133, equilibrium :142-175, relaxation :177-186,
+ * source :222-225) with applyGuoForcingD2Q9 (collision/
+ * ExternalForceFunctions.h:119-200), and collideAllD3Q19 (BGKStandard.cpp:
+ * 241-477; velocity :374-380).  In collideAllD3Q19 the relaxed values are
+ * written to the global vectors (:441-459) and the source term then goes to
+ * the local copy f_i, which is not stored again (:466-473): only the shifted
+ * equilibrium acts.  Restated as written.  force: scaled units. */
+static int collide_bgk_legacy_guo(int stencil, double scaling, double tau, double dt, int64_t n, double* f,
+                                  double* rho, double* u, int in_init, const double* force) {
+  int D, Q, bad = 0;
+  double es[3 * 32], w[32], cs2, vmax;
+  int64_t ii;
+  if (orc_stencil(stencil, scaling, &D, &Q, es, w, &cs2, &vmax) != ORC_OK) return ORC_ERR_ARG;
+  if (stencil != ORC_D2Q9 && stencil != ORC_D3Q19) return ORC_ERR_ARG;
+  const double prefactor = scaling / cs2;
+  const double relax_factor = -1.0 / tau; /* BGK.cpp:13-16 with the legacy tau - 1/2 */
+  const double omega = -relax_factor;
+  for (ii = 0; ii < n; ii++) {
+    double fl[32], feq[32], vel[3] = {0, 0, 0}, dens = 0.0;
+    int i, a;
+    for (i = 0; i < Q; i++) fl[i] = f[(int64_t)i * n + ii];
+    for (i = 0; i < Q; i++) dens += fl[i];
+    rho[ii] = dens;
+    if (dens < 1e-10 || dens != dens) {
+      bad = 1;
+      continue;
+    }
+    if (!in_init) {
+      for (a = 0; a < D; a++) {
+        double m = 0.0;
+        for (i = 0; i < Q; i++) m += fl[i] * (es[3 * i + a] / scaling);
+        vel[a] = scaling / dens * m;
+      }
+      for (a = 0; a < D; a++) {
+        vel[a] += 0.5 * dt * force[a] / dens;
+        u[(int64_t)a * n + ii] = vel[a];
+      }
+    } else {
+      for (a = 0; a < D; a++) vel[a] = u[(int64_t)a * n + ii];
+    }
+    double sp = 0.0;
+    for (a = 0; a < D; a++) sp += vel[a] * vel[a];
+    const double usq = -sp / (2 * cs2);
+    for (i = 0; i < Q; i++) {
+      double eu = 0.0;
+      for (a = 0; a < D; a++) eu += (es[3 * i + a] / scaling) * vel[a];
+      const double mixed = prefactor * eu;
+      feq[i] = w[i] * dens * (1 + mixed * (1 + 0.5 * mixed) + usq);
+    }
+    for (i = 0; i < Q; i++) fl[i] += relax_factor * (fl[i] - feq[i]);
+    if (stencil == ORC_D2Q9 && !in_init) {
+      double ug_fg = 0.0;
+      for (a = 0; a < D; a++) ug_fg += vel[a] * force[a];
+      const double one_min_omega_half = 1 - 0.5 * omega;
+      for (i = 0; i < Q; i++) {
+        double eia_ua = 0.0, eig_fg = 0.0;
+        for (a = 0; a < D; a++) {
+          eia_ua += (es[3 * i + a] / scaling) * vel[a];
+          eig_fg += (es[3 * i + a] / scaling) * force[a];
+        }
+        const double s_i = w[i] * one_min_omega_half *
+                           (prefactor * (eig_fg - ug_fg) + prefactor * prefactor * (eia_ua * eig_fg));
+        fl[i] += dt * s_i;
+      }
+    }
+    for (i = 0; i < Q; i++) f[(int64_t)i * n + ii] = fl[i];
   }
   return bad ? ORC_ERR_DENSITY : ORC_OK;
 }

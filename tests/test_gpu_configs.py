@@ -1,0 +1,304 @@
+"""The five benchmark configurations at their stated sizes, on the GPU through
+the C ABI, against the CPU oracle (the FP64 restatement of the reference's
+copy + per-direction CSR SpMV + collide sweep).
+
+* C1: 2-D Taylor-Green, D2Q9 BGK, FE_DGQ p = 4, 8 x 8 cells (1,600 nodes),
+  Ma 0.05, Re 1000 (L = 2 pi), CFL 0.4, equilibrium-initialised, the density
+  with the sign of the configuration (1 - Ma^2/4 (cos 2x + cos 2y)); 100 steps,
+  FP64 within 1e-12 relative L2 of the oracle after every step.
+* C2: 3-D Taylor-Green, D3Q19 BGK, FE_DGQ p = 4, 16^3 cells (512,000 nodes),
+  Ma 0.1, Re 1600, CFL 0.4: FP64 within 1e-12 of the oracle after each of 5
+  steps; the kinetic-energy curve E_kin(t) of 1000 steps (every 100 steps)
+  within 1e-12 of the oracle's (FP64) and 1e-6 (FP32 deviation storage); FP32
+  deviation storage within 1e-6 of FP64 in u after 1000 steps.
+* C3: 3-D Taylor-Green, D3Q27 KBC, FE_DGQ p = 3.  The oracle's CSR of the full
+  32^3 mesh has 1.5e9 entries (18 GB) and its assembly is single-threaded, so
+  FP64 parity is taken (a) directly at 16^3 cells (262,144 nodes, 2.3 GB of
+  CSR) and (b) at the full 32^3 size (2,097,152 nodes) on an input of period
+  16 cells: the periodic Cartesian operator is translation-invariant by cells,
+  so the 32^3 step of that input equals, block by block, the oracle's step of
+  one period on a 16^3 mesh of the same cell size, time step and tau.  FP32
+  deviation storage stays within 1e-6 of FP64 in u over 2000 steps at 32^3.
+* C4: four-quadrant Riemann problem, D2Q25H compressible BGK (quartic
+  equilibrium, g population), FE_DGQ p = 2, 128 x 128 cells (147,456 nodes),
+  do-nothing faces on all four sides: FP64 f, g, rho, u, T within 1e-12 of the
+  oracle after each of 5 steps.
+(The serving configuration is checked in tests/test_serving.py.)
+"""
+import math
+
+import numpy as np
+import pytest
+
+import natrium_gb300 as N
+import oracle as O
+from natrium_gb300 import problems as P
+from tests.gpu_cases import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+
+
+def _threads():
+    return O.max_threads()
+
+
+# ---------------------------------------------------------------------------
+# C1
+# ---------------------------------------------------------------------------
+
+def test_c1_tgv2d_dg_p4_100_steps_per_step(gpu_lib):
+    Ma, Re, p, cells, L = 0.05, 1000.0, 4, (8, 8), 2 * math.pi
+    st = O.stencil("D2Q9", math.sqrt(3) / Ma)
+    mesh = O.Mesh(2, cells, p, True, (L, L, L))
+    assert mesh.n_nodes == 1600
+    dt = O.time_step(mesh.h_min(), p, st.max_speed, 0.4)
+    nu = 1.0 * L / Re  # U0 = 1 (scaled), characteristic length 2 pi (TaylorGreenVortex2D.cpp:22)
+    tau = nu / (dt * st.cs2) + 0.5
+    rho0, u0 = O.tgv2d_init(mesh.coords(), Ma, rho_sign=-1.0)
+    f = O.equilibrium(st, rho0, np.ascontiguousarray(u0))
+    S = O.SLOperator(mesh, st, dt)
+    spec = N.SolverSpec(stencil="D2Q9", order=p, cells=cells, length=(L, L), scaling=st.scaling, viscosity=nu,
+                        cfl=0.4, collision="BGK_STANDARD", precision="fp64", topology="dg")
+    rho = np.zeros(mesh.n_nodes)
+    u = np.zeros((2, mesh.n_nodes))
+    worst = 0.0
+    with N.Solver(spec) as sol:
+        assert sol.dt == pytest.approx(dt, rel=1e-15)
+        assert sol.tau == pytest.approx(tau, rel=1e-14)
+        sol.upload_f(f)
+        for k in range(100):
+            f = S.stream(f)
+            O.collide(st, "BGK_STANDARD", tau, f, rho, u)
+            sol.step(1)
+            g = sol.download_f()
+            worst = max(worst, rel_l2(g, f))
+            assert worst <= TOL64, k
+        r, v = sol.download_macro()
+    assert rel_l2(r, rho) <= TOL64
+    assert rel_l2(v, u) <= 1e-11
+
+
+# ---------------------------------------------------------------------------
+# C2
+# ---------------------------------------------------------------------------
+
+C2 = dict(stencil="D3Q19", cells=(16, 16, 16), p=4, Ma=0.1, Re=1600.0, L=2 * math.pi)
+
+
+@pytest.fixture(scope="module")
+def c2_oracle():
+    c = C2
+    st = O.stencil(c["stencil"], math.sqrt(3) / c["Ma"])
+    mesh = O.Mesh(3, c["cells"], c["p"], True, (c["L"],) * 3)
+    assert mesh.n_nodes == 512000
+    dt = O.time_step(mesh.h_min(), c["p"], st.max_speed, 0.4)
+    nu = 1.0 / c["Re"]  # U0 = 1, characteristic length 1 (TaylorGreenVortex3D.cpp:21)
+    tau = nu / (dt * st.cs2) + 0.5
+    rho0, u0 = O.tgv3d_init(mesh.coords(), c["Ma"])
+    f0 = O.equilibrium(st, rho0, np.ascontiguousarray(u0))
+    return dict(st=st, mesh=mesh, dt=dt, nu=nu, tau=tau, f0=f0, S=O.SLOperator(mesh, st, dt))
+
+
+def _c2_spec(o, precision):
+    c = C2
+    return N.SolverSpec(stencil=c["stencil"], order=c["p"], cells=c["cells"], length=(c["L"],) * 3,
+                        scaling=o["st"].scaling, viscosity=o["nu"], cfl=0.4, collision="BGK_STANDARD",
+                        precision=precision, topology="dg")
+
+
+def test_c2_tgv3d_16cubed_p4_fp64_per_step(gpu_lib, c2_oracle):
+    o = c2_oracle
+    f = o["f0"].copy()
+    with N.Solver(_c2_spec(o, "fp64")) as sol:
+        assert sol.n_ref == 512000
+        assert sol.dt == pytest.approx(o["dt"], rel=1e-15)
+        sol.upload_f(o["f0"])
+        for k in range(5):
+            rho, u = o["S"].step_bgk(f, o["tau"], 1, _threads())
+            sol.step(1)
+            assert rel_l2(sol.download_f(), f) <= TOL64, k
+        r, v = sol.download_macro()
+    assert rel_l2(r, rho) <= TOL64
+    assert rel_l2(v, u) <= 1e-11
+
+
+def test_c2_tgv3d_kinetic_energy_curve_against_oracle(gpu_lib, c2_oracle):
+    """E_kin(t) every 100 steps over 1000 steps (PhysicalProperties::
+    kineticEnergy, solver/PhysicalProperties.cpp:80-132, Gauss-Lobatto
+    quadrature): the GPU FP64 curve within 1e-12 relative of the oracle's,
+    the FP32 deviation curve within 1e-6; the curve decays monotonically."""
+    o = c2_oracle
+    f = o["f0"].copy()
+    curve = []
+    for _ in range(10):
+        rho, u = o["S"].step_bgk(f, o["tau"], 100, _threads())
+        curve.append(O.kinetic_energy(o["mesh"], rho, u))
+    ref = np.array(curve)
+    assert np.all(np.diff(ref) < 0)
+    for precision, tol in (("fp64", TOL64), ("fp32dev", 1e-6)):
+        got = []
+        with N.Solver(_c2_spec(o, precision)) as sol:
+            sol.upload_f(o["f0"])
+            for _ in range(10):
+                sol.step(100)
+                got.append(sol.mass_energy()[1])
+        err = np.abs(np.array(got) - ref) / ref
+        assert np.max(err) <= tol, (precision, err)
+
+
+def test_c2_fp32_deviation_against_fp64_1000_steps(gpu_lib, c2_oracle):
+    o = c2_oracle
+    out = {}
+    for precision in ("fp64", "fp32dev"):
+        with N.Solver(_c2_spec(o, precision)) as sol:
+            sol.upload_f(o["f0"])
+            sol.step(1000)
+            out[precision] = sol.download_macro()
+    assert rel_l2(out["fp32dev"][1], out["fp64"][1]) <= 1e-6
+    assert rel_l2(out["fp32dev"][0], out["fp64"][0]) <= 1e-7
+
+
+# ---------------------------------------------------------------------------
+# C3
+# ---------------------------------------------------------------------------
+
+def _tgv3d_k(X, Ma, k):
+    """The Taylor-Green state of wavenumber k (k = 1: TaylorGreenVortex3D)."""
+    return O.tgv3d_init(np.ascontiguousarray(X * k), Ma)
+
+
+def _c3_oracle(cells, L, k, nsteps):
+    Ma, Re, p = 0.1, 1600.0, 3
+    st = O.stencil("D3Q27", math.sqrt(3) / Ma)
+    mesh = O.Mesh(3, cells, p, True, (L,) * 3)
+    dt = O.time_step(mesh.h_min(), p, st.max_speed, 0.4)
+    nu = 1.0 / Re
+    tau = nu / (dt * st.cs2) + 0.5
+    rho0, u0 = _tgv3d_k(mesh.coords(), Ma, k)
+    f0 = O.equilibrium(st, rho0, np.ascontiguousarray(u0))
+    S = O.SLOperator(mesh, st, dt)
+    f = f0.copy()
+    rho = np.zeros(mesh.n_nodes)
+    u = np.zeros((3, mesh.n_nodes))
+    steps = []
+    for _ in range(nsteps):
+        f = S.stream(f, _threads())
+        O.collide(st, "KBC_STANDARD", tau, f, rho, u)
+        steps.append(f.copy())
+    return dict(st=st, mesh=mesh, dt=dt, nu=nu, tau=tau, f0=f0, steps=steps, rho=rho.copy(), u=u.copy())
+
+
+def _c3_spec(o, cells, L, precision, dt=None):
+    return N.SolverSpec(stencil="D3Q27", order=3, cells=cells, length=(L,) * 3, scaling=o["st"].scaling,
+                        viscosity=o["nu"], cfl=0.4, dt=dt if dt is not None else 0.0, collision="KBC_STANDARD",
+                        precision=precision, topology="dg")
+
+
+def test_c3_tgv3d_kbc_16cubed_fp64_per_step(gpu_lib):
+    cells, L = (16, 16, 16), 2 * math.pi
+    o = _c3_oracle(cells, L, 1.0, 5)
+    assert o["mesh"].n_nodes == 262144
+    with N.Solver(_c3_spec(o, cells, L, "fp64")) as sol:
+        assert sol.dt == pytest.approx(o["dt"], rel=1e-15)
+        sol.upload_f(o["f0"])
+        for k in range(5):
+            sol.step(1)
+            assert rel_l2(sol.download_f(), o["steps"][k]) <= TOL64, k
+        r, v = sol.download_macro()
+    assert rel_l2(r, o["rho"]) <= TOL64
+    assert rel_l2(v, o["u"]) <= 1e-11
+
+
+def test_c3_tgv3d_kbc_32cubed_fp64_period16_against_oracle(gpu_lib):
+    """Full size (32^3 cells, 2,097,152 nodes): an input of period 16 cells
+    (the Taylor-Green state of wavenumber 2 on [0, 2 pi)^3) against the
+    oracle's run of one period (16^3 cells on [0, pi)^3: same cell size,
+    time step and tau), 3 steps, every one of the 8 periods compared."""
+    o = _c3_oracle((16, 16, 16), math.pi, 2.0, 3)
+    cells, L = (32, 32, 32), 2 * math.pi
+    mesh = O.Mesh(3, cells, 3, True, (L,) * 3)
+    assert mesh.n_nodes == 2097152
+    rho0, u0 = _tgv3d_k(mesh.coords(), 0.1, 2.0)
+    f0 = O.equilibrium(o["st"], rho0, np.ascontiguousarray(u0))
+    Q, n1, n2 = 27, 64, 128
+    with N.Solver(_c3_spec(o, cells, L, "fp64")) as sol:
+        assert sol.dt == pytest.approx(o["dt"], rel=1e-15)  # same h_min, same CFL rule
+        assert sol.tau == pytest.approx(o["tau"], rel=1e-14)
+        sol.upload_f(f0)
+        for k in range(3):
+            sol.step(1)
+            g = sol.download_f().reshape(Q, n2, n2, n2)
+            ref = o["steps"][k].reshape(Q, n1, n1, n1)
+            for bz in (0, n1):
+                for by in (0, n1):
+                    for bx in (0, n1):
+                        blk = g[:, bz:bz + n1, by:by + n1, bx:bx + n1]
+                        assert rel_l2(blk, ref) <= TOL64, (k, bx, by, bz)
+
+
+def test_c3_fp32_deviation_against_fp64_2000_steps(gpu_lib):
+    """The mixed-precision configuration at full size: FP32 f - w_i storage
+    against the FP64 path (pinned to the oracle above) after 500, 1000, 1500
+    and 2000 steps: relative L2 of u within 1e-6, of rho within 1e-7."""
+    cells, L, Ma = (32, 32, 32), 2 * math.pi, 0.1
+    scaling = math.sqrt(3) / Ma
+    X = P.node_coords(cells, 3, (L,) * 3, "dg")
+    rho0, u0 = P.taylor_green_3d(X, Ma)
+    f0 = P.equilibrium("D3Q27", scaling, rho0, u0)
+    sols = {}
+    try:
+        for precision in ("fp64", "fp32dev"):
+            spec = N.SolverSpec(stencil="D3Q27", order=3, cells=cells, length=(L,) * 3, scaling=scaling,
+                                viscosity=1 / 1600.0, cfl=0.4, collision="KBC_STANDARD", precision=precision,
+                                topology="dg")
+            sols[precision] = N.Solver(spec)
+            sols[precision].upload_f(f0)
+        for block in range(4):
+            out = {}
+            for precision, sol in sols.items():
+                sol.step(500)
+                out[precision] = sol.download_macro()
+            assert rel_l2(out["fp32dev"][1], out["fp64"][1]) <= 1e-6, block
+            assert rel_l2(out["fp32dev"][0], out["fp64"][0]) <= 1e-7, block
+    finally:
+        for sol in sols.values():
+            sol.close()
+
+
+# ---------------------------------------------------------------------------
+# C4
+# ---------------------------------------------------------------------------
+
+def test_c4_riemann_d2q25h_128sq_p2_fp64_per_step(gpu_lib):
+    cells, p, nu, vu = (128, 128), 2, 1e-3, 1.58
+    st = O.stencil("D2Q25H", 1.0)
+    DN = 2  # do-nothing faces x-, x+, y-, y+
+    mesh = O.Mesh(2, cells, p, True, (1.0, 1.0, 1.0), bc=(DN, DN, DN, DN, 0, 0))
+    assert mesh.n_nodes == 147456
+    dt = O.time_step(mesh.h_min(), p, st.max_speed, 0.4)
+    tau = nu / (dt * st.cs2) + 0.5
+    rho0, u0, T0 = P.riemann_2d(mesh.coords(), vu, 1.0)
+    f0, g0 = O.thermal_init(st, rho0, np.ascontiguousarray(u0), T0)
+    S = O.SLOperator(mesh, st, dt)
+    spec = N.SolverSpec(stencil="D2Q25H", order=p, cells=cells, length=(1.0, 1.0), scaling=1.0, viscosity=nu,
+                        cfl=0.4, collision="BGK_COMPRESSIBLE", precision="fp64", topology="dg",
+                        periodic=(False, False, True))
+    f, g = f0.copy(), g0.copy()
+    with N.Solver(spec) as sol:
+        for face in range(4):
+            sol.set_boundary(face, "DO_NOTHING")
+        assert sol.dt == pytest.approx(dt, rel=1e-15)
+        sol.upload_f(f0)
+        sol.upload_g(g0)
+        for k in range(5):
+            rho, u, T, _ = S.step_compressible(f, g, tau, nthreads=_threads())
+            sol.step(1)
+            assert rel_l2(sol.download_f(), f) <= TOL64, k
+            assert rel_l2(sol.download_g(), g) <= TOL64, k
+        r, v = sol.download_macro()
+        Tg, _ = sol.download_thermal()
+    assert rel_l2(r, rho) <= TOL64
+    assert rel_l2(v, u) <= 1e-11
+    assert rel_l2(Tg, T) <= TOL64

@@ -159,6 +159,39 @@ def test_uniform_state_is_stationary_on_device(gpu_lib):
     assert np.abs(m).max() < 1e-12
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
+@pytest.mark.parametrize("T0", [1.1, 1.2])
+def test_quartic_equilibrium_moment_recovery_on_device(gpu_lib, T0, precision):
+    """The known answers of the reference's Equilibrium_D2Q19H_test and
+    Equilibrium_D3Q45_test (test/collision_advanced/Equilibrium_test.cpp:
+    111-206), run on this build's compressible stencil D2Q25H on the device:
+    the quartic equilibrium at rho = 1, u = (0.1, 0.2), T = 1.1 (1.2), scaling
+    1, c_s^2 = 1/3, returns its density and velocity (BOOST_CHECK_CLOSE
+    10e-6 %, i.e. 1e-7 relative); here also its temperature, from the
+    device collision's moments of f and g."""
+    spec = N.SolverSpec(stencil="D2Q25H", order=2, cells=(2, 2), length=(1.0, 1.0), scaling=1.0, viscosity=1.0,
+                        dt=0.1, collision="BGK_COMPRESSIBLE", precision=precision, topology="dg")
+    st = O.stencil("D2Q25H", 1.0)
+    with N.Solver(spec) as sol:
+        n = sol.n_ref
+        rho0 = np.ones(n)
+        u0 = np.stack([np.full(n, 0.1), np.full(n, 0.2)])
+        sol.init_thermal(rho0, u0, np.full(n, T0))
+        f = sol.download_f()
+        sol.collide()
+        rho, u = sol.download_macro()
+        T, _ = sol.download_thermal()
+    e = st.e_unit[:, :2]
+    r = f.sum(0)
+    v = (e.T @ f) / r
+    tol = 1e-7
+    assert np.allclose(r, 1.0, rtol=tol, atol=0)
+    assert np.allclose(v[0], 0.1, rtol=tol, atol=0) and np.allclose(v[1], 0.2, rtol=tol, atol=0)
+    assert np.allclose(rho, 1.0, rtol=tol, atol=0)
+    assert np.allclose(u[0], 0.1, rtol=tol, atol=0) and np.allclose(u[1], 0.2, rtol=tol, atol=0)
+    assert np.allclose(T, T0, rtol=tol, atol=0)
+
+
 def test_density_underflow_is_reported(gpu_lib):
     st, mesh, dt, tau, spec = thermal_case((2, 2), 2, True)
     n = mesh.n_nodes
