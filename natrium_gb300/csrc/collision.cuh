@@ -84,10 +84,25 @@ __device__ __forceinline__ Real edot(const Real (&u)[3]) {
   return r;
 }
 
+// index of the direction opposite to i (e_opp = -e_i)
+template <class S>
+__host__ __device__ constexpr int opp(int i) {
+  for (int j = 0; j < S::Q; ++j)
+    if (S::e(j, 0) == -S::e(i, 0) && S::e(j, 1) == -S::e(i, 1) && S::e(j, 2) == -S::e(i, 2)) return j;
+  return -1;
+}
+
 // ---------------------------------------------------------------------------
 // BGK with the second-order equilibrium
 // (collision_advanced/CollisionSchemes.h:28-41, Equilibria.h:33-83).
 // Returns the density.  If given_u, u is input (inInitializationProcedure).
+//
+// Evaluated per pair of opposite directions (i, i'): with c = e_i . u,
+//   feq_{i,i'} = w rho (1 - 1.5 u^2 + 4.5 c^2) +- 3 w rho c,
+// and the relaxation f + omega (feq - f) = (1 - omega) f + omega feq, so a
+// pair costs one even and one odd term (the same arithmetic as the
+// reference's per-direction form, regrouped; in the deviation storage the
+// even term carries w m0 instead of w).
 // ---------------------------------------------------------------------------
 template <class S, bool DEV, bool COMP, class Real>
 __device__ __forceinline__ Real collide_bgk(Real (&v)[S::Q], Real inv_tau,
@@ -102,16 +117,24 @@ __device__ __forceinline__ Real collide_bgk(Real (&v)[S::Q], Real inv_tau,
     u[2] = (S::D == 3) ? j[2] * inv : Real(0);
   }
   const Real uu = Real(1.5) * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  const Real keep = Real(1) - inv_tau;  // 1 - omega
+  const Real orho = inv_tau * rho;
+  // even part without the 4.5 c^2 term, times omega: omega w (rho (1 - uu))
+  // (plain) or omega w (m0 - rho uu) (deviation)
+  const Real base = DEV ? inv_tau * m0 - orho * uu : orho - orho * uu;
   static_for<0, S::Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
-    const Real ue = Real(3) * edot<S, i>(u);
-    const Real poly = ue * (Real(1) + Real(0.5) * ue) - uu;
-    Real eq;
-    if constexpr (DEV)
-      eq = Real(S::w(i)) * (m0 + rho * poly);
-    else
-      eq = Real(S::w(i)) * rho * (Real(1) + poly);
-    v[i] = v[i] - inv_tau * (v[i] - eq);
+    constexpr int o = opp<S>(i);
+    if constexpr (i == 0) {
+      v[0] = fma(v[0], keep, Real(S::w(0)) * base);
+    } else if constexpr (i < o) {
+      const Real c = edot<S, i>(u);
+      const Real ow = Real(S::w(i)) * orho;                       // omega w rho
+      const Real even = fma(Real(4.5) * ow * c, c, Real(S::w(i)) * base);
+      const Real odd = Real(3) * ow * c;
+      v[i] = fma(v[i], keep, even + odd);
+      v[o] = fma(v[o], keep, even - odd);
+    }
   });
   return rho;
 }
@@ -311,22 +334,37 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
     dm[a][2] = pm1 - sm1 - sm1 * pm1;                      // base*post - 1
     dm[a][0] = (-sm1 - pm1) / (Real(1) + pm1);             // base/post - 1
   }
-  Real feq[S::Q], df[S::Q];
-  static_for<0, S::Q>([&](auto I) {
+  // q_i = prod_a (1 + d_a) - 1 of direction i, f^eq_i = w_i rho (1 + q_i)
+  auto qof = [&](auto I) -> Real {
     constexpr int i = decltype(I)::value;
-    Real q = Real(0);  // prod_a (1 + d_a) - 1
+    Real q = Real(0);
 #pragma unroll
     for (int a = 0; a < S::D; ++a) {
       const int c = (a == 0 ? S::e(i, 0) : (a == 1 ? S::e(i, 1) : S::e(i, 2))) + 1;
       const Real d = dm[a][c];
       q = q + d + q * d;
     }
+    return q;
+  };
+  // 1 / f^eq_i = (1 / (w_i rho)) prod_a 1 / (1 + d_a): nine reciprocals
+  // instead of one division per direction
+  Real rinv[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) rinv[a][c] = Real(1) / (Real(1) + dm[a][c]);
+  const Real irho = Real(1) / rho;
+  // f - f^eq (the only per-direction array kept; f^eq and the shear part
+  // are recomputed where needed, which keeps the register footprint small)
+  Real df[S::Q];
+  static_for<0, S::Q>([&](auto I) {
+    constexpr int i = decltype(I)::value;
+    const Real q = qof(I);
     const Real w = Real(S::w(i));
-    feq[i] = w * rho * (Real(1) + q);
     if constexpr (DEV)
       df[i] = v[i] - w * (m0 * (Real(1) + q) + q);
     else
-      df[i] = v[i] - feq[i];
+      df[i] = v[i] - w * rho * (Real(1) + q);
   });
   // second-moment differences of f - feq
   Real M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
@@ -344,13 +382,14 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
   M[2][0] = M[0][2];
   M[2][1] = M[1][2];
   Real ss = Real(0), sh = Real(0);
-  Real ds[S::Q];
   static_for<0, S::Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
-    ds[i] = kbc_shear<S, i>(M);
-    const Real dh = df[i] - ds[i];
-    const Real inv = Real(1) / feq[i];
-    ss += ds[i] * dh * inv;
+    const Real ds = kbc_shear<S, i>(M);
+    const Real dh = df[i] - ds;
+    Real inv = irho * Real(1.0 / S::w(i));
+#pragma unroll
+    for (int a = 0; a < S::D; ++a) inv *= rinv[a][(a == 0 ? S::e(i, 0) : (a == 1 ? S::e(i, 1) : S::e(i, 2))) + 1];
+    ss += ds * dh * inv;
     sh += dh * dh * inv;
   });
   const Real beta = Real(0.5) / tau;
@@ -359,8 +398,9 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
   if (sh < Real(1e-16)) gamma = Real(2);
   static_for<0, S::Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
-    const Real dh = df[i] - ds[i];
-    v[i] = v[i] - beta * (Real(2) * ds[i] + gamma * dh);
+    const Real ds = kbc_shear<S, i>(M);
+    const Real dh = df[i] - ds;
+    v[i] = v[i] - beta * (Real(2) * ds + gamma * dh);
   });
   return rho;
 }
