@@ -398,9 +398,11 @@ def bench_mixed(torch, stream, flush, steps: int = None, profile: bool = False, 
             sol.step_async(3, False)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.nvtx.range_push("timed")  # ncu --nvtx-include timed/
             e0.record(stream)
             sol.step_async(steps, False)
             e1.record(stream)
+            torch.cuda.nvtx.range_pop()
             sol.status()
             ms = e0.elapsed_time(e1) / steps
             return {"workload": c["name"], "nodes": sol.n_dev, "ms_per_step": ms, "kernel": sol.kernel_info(),
@@ -628,7 +630,7 @@ def time_e2e_legs(sol, torch, ws, f0, nodes, e2e_steps):
             "pipeline_matches_blocking": pipeline_ok}
 
 
-KERNEL_NAMES = {1: "k_sl_step", 2: "k_sl_step_v2", 3: "k_sl_row", 6: "k_sl_rowt", 7: "k_sl_rowg"}
+KERNEL_NAMES = {1: "k_sl_step", 2: "k_sl_step_v2", 3: "k_sl_row", 6: "k_sl_rowt", 7: "k_sl_rowg", 11: "k_sl_cell"}
 
 
 def run_ours(args):
@@ -676,7 +678,7 @@ def run_ours(args):
             per, launches = time_device(sol, torch, stream, flush, args.steps, args.warmup, nvtx="timed")
             print(json.dumps({"profile_run": True, "precision": args.profile_precision,
                               "ms_per_step": sum(per) / args.steps, "launches": launches,
-                              "kernel": sol.kernel_info()}))
+                              "kernel": sol.kernel_info(), "autotune": sol.autotune_report()}))
         return 0
 
     dgemm = fp64_peak_tflops(torch)
@@ -847,7 +849,7 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="lean run for ncu: device timing of one path only (no e2e, other legs, CPU baseline "
                          "or clocks)")
-    ap.add_argument("--fp64-sample", type=int, default=128,
+    ap.add_argument("--fp64-sample", type=int, default=512,
                     help="serving: requests of the stream timed one at a time on the plain FP64 path")
     ap.add_argument("--no-compressible", action="store_true", help="skip the compressible D2Q25H leg")
     ap.add_argument("--no-mapped", action="store_true", help="skip the mapped-mesh (LubricationSine) leg")

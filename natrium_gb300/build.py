@@ -23,7 +23,7 @@ SOURCES = ["natgpu_api.cu", "k_d2q9.cu", "k_d3q19.cu", "k_d3q27.cu", "k_v2.cu", 
            "natgpu_noalloc.cu", "k_thermal.cu", "k_rowt_d3q19.cu", "k_rowt_d3q27_bgk.cu",
            "k_rowt_d3q27_kbc.cu", "k_row_ss_d3q19.cu", "k_row_ss_d3q27.cu",
            "k_rowg_d3q19.cu", "k_rowg_d3q27.cu", "k_mapped_d2q9.cu", "k_mapped_d3q19.cu",
-           "k_mapped_d3q27.cu", "tracker.cu", "io.cu"]
+           "k_mapped_d3q27.cu", "tracker.cu", "io.cu", "k_cell.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

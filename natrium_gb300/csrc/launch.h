@@ -71,8 +71,10 @@ struct RowLaunch {
   int wy, wz;
   const void* fn;
   int kind = 3;      // 3: row kernel (sl_row.cuh), 6: bulk-copy row kernel (sl_rowt.cuh),
-                     // 7: row-group kernel (sl_rowg.cuh; wy = rows per CTA)
-  int g = 0;         // kind 7: warps per x row (32 (g - 1) < nx <= 32 g)
+                     // 7: row-group kernel (sl_rowg.cuh; wy = rows per CTA),
+                     // 11: cell-row kernel (sl_cell.cuh; wy = rows per CTA)
+  int g = 0;         // kind 7: warps per x row (32 (g - 1) < nx <= 32 g); kind 11: cells per x row
+  int warps = 0;     // kind 11: warps per CTA
   size_t smem = 0;   // dynamic shared memory (kind 6)
   int align = 1;     // nx must be a multiple of this (kind 6: aligned row copies)
   int min_nx = 0;    // and at least this (kind 6: at most two pieces per row)
@@ -87,6 +89,7 @@ void row_ss_kernels_d3q27(std::vector<RowLaunch>& v);
 void rowt_kernels_d3q19(std::vector<RowLaunch>& v);
 void rowt_kernels_d3q27_bgk(std::vector<RowLaunch>& v);
 void rowt_kernels_d3q27_kbc(std::vector<RowLaunch>& v);
+void cell_kernels(std::vector<RowLaunch>& v);
 
 // Compressible two-population model on D2Q25H (k_thermal.cu): fused
 // stream(f, g) (+ relaxWithG), collision only, equilibrium initialisation;

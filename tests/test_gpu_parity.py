@@ -512,6 +512,13 @@ EVERY_CASES = [
     ("D3Q27", (3, 4, 2), 3, False, "BGK_STANDARD", "fp64"),
     ("D3Q19", (4, 4, 2), 4, True, "BGK_STANDARD", "fp64"),
     ("D2Q9", (8, 8), 4, True, "BGK_STANDARD", "fp32dev"),
+    # cell-row kernel shapes (nx = L (p + 1), L = 16 or 32 cells per x row)
+    ("D3Q27", (16, 2, 2), 3, True, "KBC_STANDARD", "fp32dev"),
+    ("D3Q27", (32, 2, 1), 3, True, "BGK_STANDARD", "fp32dev"),
+    ("D3Q27", (32, 2, 1), 3, True, "KBC_STANDARD", "fp64"),
+    ("D3Q19", (16, 4, 2), 4, True, "BGK_STANDARD", "fp32dev"),
+    ("D3Q19", (16, 4, 2), 4, True, "BGK_STANDARD", "fp64"),
+    ("D3Q19", (32, 2, 1), 3, True, "BGK_STANDARD", "fp32dev"),
 ]
 
 
