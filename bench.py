@@ -504,6 +504,38 @@ def bench_mapped(torch, stream, flush, steps: int = 100, warmup: int = 5):
         sol.close()
     out["value"] = out["fp32dev"]["value"]
     out["cells"] = list(cells)
+    out["departure_search"] = bench_departure_search()
+    return out
+
+
+def bench_departure_search(cells=(32, 32, 32), order=2):
+    """Setup of a mapped mesh: the departure-point search with the MappingQ1
+    Newton inverse (SemiLagrangian.cpp:525-757, SemiLagrangianTools.cpp:15-64)
+    for every (node, direction) of D3Q19, FE_DGQ p = 2 on a deformed periodic
+    grid of 32^3 cells (884,736 nodes x 18 rows): nat_create (which searches
+    on the device), then the search alone on the device and on all host
+    threads (the same tracker code, rows equal bit for bit)."""
+    import natrium_gb300 as N
+    from natrium_gb300 import problems as P
+    L = (1.0, 1.0, 1.0)
+    V = P.wavy_grid(cells, L, 0.05)
+    scaling = math.sqrt(3) / 0.1
+    spec = N.SolverSpec(stencil="D3Q19", order=order, cells=cells, length=L, scaling=scaling, viscosity=1e-3,
+                        cfl=0.4, collision="BGK_STANDARD", precision="fp32dev", topology="dg", vertices=V)
+    t0 = time.perf_counter()
+    sol = N.Solver(spec)
+    t_create = time.perf_counter() - t0
+    sol.mapped_rows("device", copy=False)  # warm (module and allocations)
+    t0 = time.perf_counter()
+    sol.mapped_rows("device", copy=False)
+    t_dev = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sol.mapped_rows("host", copy=False)
+    t_host = time.perf_counter() - t0
+    out = {"mesh": f"D3Q19 FE_DGQ p={order}, {cells[0]}^3 deformed cells", "nodes": sol.n_dev,
+           "rows": (sol.Q - 1) * sol.n_dev, "create_s": t_create, "search_device_s": t_dev,
+           "search_host_s": t_host, "host_threads": os.cpu_count(), "speedup_device_vs_host": t_host / t_dev}
+    sol.close()
     return out
 
 

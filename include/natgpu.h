@@ -335,6 +335,20 @@ int nat_checkpoint_load(nat_solver* s, const char* path, int64_t* iteration, dou
  * and, for NAT_BGK_COMPRESSIBLE, T and shock_sensor, from the last collision. */
 int nat_write_vtu(nat_solver* s, const char* path);
 
+/* Departure-point rows of a mapped one-population mesh (no counterpart in
+ * the reference, whose tracker fills the sparse matrix directly,
+ * SemiLagrangian.cpp:145-522): searched again by the host tracker (where = 0,
+ * all host threads) or the device tracker (where = 1, one GPU thread per
+ * row; the one nat_create uses), without changing the handle's own rows, and
+ * copied to the host arrays that are not NULL.  Rows are direction-major,
+ * node-minor: (Q-1) n_dev of them.  base: int32 per row; flags: uint8 per row;
+ * u: per row D unit coordinates (float, NAT_FP32_DEV) or D (p+1) 1-D Lagrange
+ * values (double, NAT_FP64), stored [row direction][axis][j][node]; c: per row
+ * the additive constant (float deviation form / double plain).  Both trackers
+ * use the same code without floating-point contraction and give the same rows
+ * bit for bit.  NAT_ERR_UNSUPPORTED for other handles. */
+int nat_mapped_rows(nat_solver* s, int where, int32_t* base, void* u, void* c, uint8_t* flags);
+
 /* Device pointers of the current distribution buffer (Q blocks of n_dev
  * values, double for NAT_FP64 and float (f - w_i) for NAT_FP32_DEV). */
 int nat_device_f(nat_solver* s, void** f_dev);

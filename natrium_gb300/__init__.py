@@ -57,7 +57,7 @@ EXPORTS = [
     "nat_collide", "nat_step", "nat_step_async", "nat_status", "nat_last_error",
     "nat_mass_energy", "nat_device_f", "nat_launch_count", "nat_version", "nat_set_kernel_variant",
     "nat_kernel_variant", "nat_autotune", "nat_autotune_report", "nat_select_candidate", "nat_kernel_info",
-    "nat_server_create", "nat_server_destroy", "nat_server_submit", "nat_server_step", "nat_server_poll",
+    "nat_mapped_rows", "nat_server_create", "nat_server_destroy", "nat_server_submit", "nat_server_step", "nat_server_poll",
     "nat_server_result", "nat_server_stats", "nat_server_last_error", "nat_mass_energy_noalloc",
     "nat_set_thermal", "nat_get_thermal", "nat_upload_g", "nat_download_g", "nat_download_thermal",
     "nat_init_thermal", "nat_set_boundary", "nat_set_force", "nat_checkpoint_save", "nat_checkpoint_load",
@@ -159,6 +159,7 @@ def load_library(path: str | None = None):
     L.nat_init_thermal.argtypes = [vp, dp, dp, dp]
     L.nat_set_boundary.argtypes = [vp, C.c_int, C.c_int, dp]
     L.nat_set_force.argtypes = [vp, C.c_int, dp]
+    L.nat_mapped_rows.argtypes = [vp, C.c_int, vp, vp, vp, vp]
     L.nat_checkpoint_save.argtypes = [vp, C.c_char_p, C.c_int64, C.c_double]
     L.nat_checkpoint_load.argtypes = [vp, C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_double)]
     L.nat_write_vtu.argtypes = [vp, C.c_char_p]
@@ -453,6 +454,28 @@ class Solver:
         self._check(self._L.nat_write_vtu(self._h, os.fsencode(path)))
 
     # -- wall boundaries -------------------------------------------------------------
+    def mapped_rows(self, where: str = "device", copy: bool = True):
+        """Departure-point rows of a mapped one-population mesh, searched by
+        the host tracker (where="host") or the device tracker ("device"):
+        (base int32 [(Q-1) n], u, c, flags uint8 [(Q-1) n]) with u and c
+        float32 (FP32 deviation storage: unit coordinates, deviation
+        constant) or float64 (FP64: 1-D Lagrange values, plain constant).
+        copy=False runs the search only (for timing) and returns None."""
+        fp64 = self.spec.precision == "fp64"
+        dt = np.float64 if fp64 else np.float32
+        nr = (self.Q - 1) * self.n_dev
+        per = self.D * (self.spec.order + 1 if fp64 else 1)
+        if copy:
+            base = np.empty(nr, dtype=np.int32)
+            u = np.empty(nr * per, dtype=dt)
+            c = np.empty(nr, dtype=dt)
+            fl = np.empty(nr, dtype=np.uint8)
+            ptrs = [a.ctypes.data_as(C.c_void_p) for a in (base, u, c, fl)]
+        else:
+            ptrs = [None] * 4
+        self._check(self._L.nat_mapped_rows(self._h, {"host": 0, "device": 1}[where], *ptrs))
+        return (base, u, c, fl) if copy else None
+
     def set_force(self, scheme: str = "SHIFTING_VELOCITY", force=(0.0, 0.0, 0.0)):
         """Constant body force in scaled units (ConstantExternalForce) with the
         forcing scheme NONE, SHIFTING_VELOCITY, EXACT_DIFFERENCE (the advanced

@@ -26,6 +26,9 @@ SOURCES = ["natgpu_api.cu", "k_d2q9.cu", "k_d3q19.cu", "k_d3q27.cu", "k_v2.cu", 
            "k_mapped_d3q27.cu", "tracker.cu", "io.cu", "k_cell.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# the departure-path tracker runs on the host and on the device and must give
+# the same rows bit for bit: no floating-point contraction on either side
+FILE_FLAGS = {"tracker.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 
 
 def nvcc() -> str:
@@ -53,7 +56,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src: str) -> str:
         obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
-        cmd = [nv, *FLAGS, *ARCH, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nv, *FLAGS, *FILE_FLAGS.get(src, []), *ARCH, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")

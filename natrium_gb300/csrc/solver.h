@@ -92,6 +92,7 @@ struct nat_solver {
   void* d_mp_u = nullptr;        // Real
   void* d_mp_c = nullptr;        // Real
   unsigned char* d_mp_flags = nullptr;
+  bool track_on_host = false;    // departure-point rows by the host tracker (else the device's)
   const void* mp_step = nullptr;    // kernels for this stencil / model / order / precision
   const void* mp_stream = nullptr;
   const void* mp_step_force = nullptr;  // BGK with the body-force term
@@ -158,6 +159,9 @@ int build_wall_rows(nat_solver* s);
 int launch_wall_rows(nat_solver* s, const void* in, void* out, bool g_pop);
 void free_mapped_rows(nat_solver* s);
 int setup_mapping(nat_solver* s, const double* vertices, double* hmin);
+int host_mapped_rows(nat_solver* s, std::vector<int>& base, std::vector<unsigned char>& u,
+                     std::vector<unsigned char>& c, std::vector<unsigned char>& flags);
+int device_mapped_rows(nat_solver* s, int** d_base, void** d_u, void** d_c, unsigned char** d_flags);
 void node_point(const nat_solver* s, const int* c, const int* l, const double* xi, double* x);
 
 }  // namespace api

@@ -5,7 +5,13 @@
 //  - the sparse rows of the wall nodes (k_wall_rows streams them);
 //  - the departure-point rows of mapped meshes (sl_mapped.cuh) and the mapped
 //    mesh's setup (period vectors, Jacobian quadrature weights).
-// Runs once per time step size, on all host threads.
+// The departure-point rows of mapped meshes are searched on the device
+// (k_track_rows, one thread per row) with the same tracker functions as the
+// host (track.cuh; this file is compiled without floating-point
+// contraction, so both give the same rows bit for bit); the host search on
+// all host threads remains for wall rows, two-population mapped meshes and
+// as the reference the test compares the device rows with.  Runs once per
+// time step size.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -18,6 +24,7 @@
 
 #include "sl_mapped.cuh"
 #include "solver.h"
+#include "track.cuh"
 
 namespace natgpu {
 namespace api {
@@ -40,218 +47,123 @@ __global__ void k_wall_rows(int nbr, const int* __restrict__ dst, const int* __r
   }
 }
 
-// First face of the axis-aligned cell [lo, lo + h] crossed by the segment
-// p_in -> p_out (unit coordinates snapped at 1e-10; the x face is taken
-// first, later faces only when strictly earlier); -1 if p_out lies in the
-// closed cell.  Writes the crossing point.  Restates
-// SemiLagrangian::faceCrossedFirst for MappingCartesian (SemiLagrangian.cpp:525-699).
-int face_crossed_first(int D, const double* lo, const double* h, const double* p_in, const double* p_out,
-                       double* p_b) {
-  double pi[3], po[3], lambda = 100.0;
-  int face = -1;
-  auto snap = [](double v) { return fabs(v) < 1e-10 ? 0.0 : (fabs(v - 1.0) < 1e-10 ? 1.0 : v); };
-  for (int a = 0; a < D; ++a) {
-    pi[a] = snap((p_in[a] - lo[a]) / h[a]);
-    po[a] = snap((p_out[a] - lo[a]) / h[a]);
+// The tracker's view of a solver (track.cuh), its vertex pointer `vtx` in
+// host or device memory.
+TrackGeom make_geom(const nat_solver* s, const double* vtx) {
+  TrackGeom g;
+  memset(&g, 0, sizeof g);
+  HostStencil hs;
+  get_host_stencil(s->spec.stencil, &hs, s->spec.scaling);
+  g.D = s->D;
+  g.Q = s->Q;
+  g.p = s->spec.order;
+  g.PER = s->period;
+  g.mapped = s->mapped ? 1 : 0;
+  g.n = s->n_dev;
+  g.dt = s->dt;
+  g.cs2_scaled = s->cs2_scaled;
+  gl_points(g.p, g.xi);
+  for (int a = 0; a < 3; ++a) {
+    g.n_ax[a] = s->n_ax[a];
+    g.N[a] = s->spec.cells[a];
+    g.periodic[a] = s->spec.periodic[a];
+    g.h[a] = s->h[a];
+    for (int b = 0; b < 3; ++b) g.pv[a][b] = s->pv[a][b];
   }
-  for (int a = 0; a < D; ++a) {
-    double lam;
-    int f;
-    if (po[a] < 0) {
-      lam = (0 - pi[a]) / (po[a] - pi[a]);
-      f = 2 * a;
-    } else if (po[a] > 1) {
-      lam = (1 - pi[a]) / (po[a] - pi[a]);
-      f = 2 * a + 1;
-    } else {
-      continue;
-    }
-    if (a == 0 || lam < lambda) {
-      lambda = lam;
-      face = f;
-    }
+  for (int f = 0; f < 6; ++f) {
+    g.bc[f] = s->bc[f];
+    for (int a = 0; a < 3; ++a) g.uw[f][a] = s->uw[f][a];
   }
-  if (face < 0) return -1;
-  for (int a = 0; a < D; ++a) p_b[a] = lo[a] + snap(pi[a] + (po[a] - pi[a]) * lambda) * h[a];
-  return face;
+  for (int i = 0; i < g.Q; ++i) {
+    for (int a = 0; a < 3; ++a) g.es[i][a] = a < g.D ? hs.e[i][a] * s->spec.scaling : 0.0;
+    g.w[i] = hs.w[i];
+    g.rest[i] = s->rest[i];
+  }
+  for (int i = 0; i < g.Q; ++i) {
+    g.opp[i] = 0;
+    for (int j = 0; j < g.Q; ++j)
+      if (g.es[j][0] == -g.es[i][0] && g.es[j][1] == -g.es[i][1] && g.es[j][2] == -g.es[i][2]) g.opp[i] = j;
+  }
+  g.vtx = vtx;
+  return g;
 }
 
-// ---- MappingQ1: multilinear image of the unit cell from its 2^D vertices ----
+// the vertex grid alone (cell maps of setup and output)
+TrackGeom vertex_geom(const nat_solver* s) {
+  TrackGeom g;
+  memset(&g, 0, sizeof g);
+  g.D = s->D;
+  g.mapped = s->mapped ? 1 : 0;
+  for (int a = 0; a < 3; ++a) {
+    g.N[a] = s->spec.cells[a];
+    g.h[a] = s->h[a];
+  }
+  g.vtx = s->vtx.data();
+  return g;
+}
+
 const double* grid_vertex(const nat_solver* s, int i, int j, int k) {
-  const int n0 = s->spec.cells[0] + 1, n1 = s->D > 1 ? s->spec.cells[1] + 1 : 1;
-  return s->vtx.data() + 3 * (((long long)k * n1 + j) * n0 + i);
-}
-
-// x(u) of cell c, and the Jacobian dx_r/du_a when J is not null
-void q1_map(const nat_solver* s, const int* c, const double* u, double* x, double (*J)[3]) {
-  const int D = s->D;
-  for (int r = 0; r < 3; ++r) {
-    x[r] = 0.0;
-    if (J)
-      for (int a = 0; a < 3; ++a) J[r][a] = 0.0;
-  }
-  for (int k = 0; k < (1 << D); ++k) {
-    const int b[3] = {k & 1, (k >> 1) & 1, (k >> 2) & 1};
-    double phi = 1.0, dphi[3];
-    for (int a = 0; a < D; ++a) phi *= b[a] ? u[a] : 1.0 - u[a];
-    for (int a = 0; a < D; ++a) {
-      dphi[a] = b[a] ? 1.0 : -1.0;
-      for (int q = 0; q < D; ++q)
-        if (q != a) dphi[a] *= b[q] ? u[q] : 1.0 - u[q];
-    }
-    const double* v = grid_vertex(s, c[0] + b[0], D > 1 ? c[1] + b[1] : 0, D > 2 ? c[2] + b[2] : 0);
-    for (int r = 0; r < D; ++r) {
-      x[r] += phi * v[r];
-      if (J)
-        for (int a = 0; a < D; ++a) J[r][a] += dphi[a] * v[r];
-    }
-  }
-}
-
-double det3(const double (*M)[3]) {
-  return M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) - M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
-         M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
-}
-
-double q1_det(int D, const double (*J)[3]) { return D == 2 ? J[0][0] * J[1][1] - J[0][1] * J[1][0] : det3(J); }
-
-// J du = r (Cramer's rule); false for a singular J
-bool q1_solve(int D, const double (*J)[3], const double* r, double* du) {
-  const double det = q1_det(D, J);
-  if (det == 0.0) return false;
-  if (D == 2) {
-    du[0] = (J[1][1] * r[0] - J[0][1] * r[1]) / det;
-    du[1] = (-J[1][0] * r[0] + J[0][0] * r[1]) / det;
-    return true;
-  }
-  for (int col = 0; col < 3; ++col) {
-    double M[3][3];
-    for (int row = 0; row < 3; ++row)
-      for (int a = 0; a < 3; ++a) M[row][a] = a == col ? r[row] : J[row][a];
-    du[col] = det3(M) / det;
-  }
-  return true;
-}
-
-// Unit coordinates of x in cell c (the reference calls
-// MappingQ1::transform_real_to_unit_cell): Newton's method from the cell
-// centre, each step halved (up to 12 times) until the residual decreases;
-// converged once a step is below 1e-14.  False when it cannot converge (the
-// reference's ExcTransformationFailed).
-bool q1_inverse(const nat_solver* s, const int* c, const double* x, double* u) {
-  const int D = s->D;
-  double y[3], J[3][3], r[3] = {0, 0, 0}, res = 0.0;
-  for (int a = 0; a < 3; ++a) u[a] = a < D ? 0.5 : 0.0;
-  q1_map(s, c, u, y, J);
-  for (int a = 0; a < D; ++a) {
-    r[a] = y[a] - x[a];
-    res += r[a] * r[a];
-  }
-  for (int it = 0; it < 100; ++it) {
-    double du[3] = {0, 0, 0}, step = 1.0, stp = 0.0;
-    bool ok = false;
-    if (!q1_solve(D, J, r, du)) return false;
-    for (int a = 0; a < D; ++a) stp += du[a] * du[a];
-    for (int k = 0; k <= 12; ++k, step *= 0.5) {
-      double un[3] = {u[0], u[1], u[2]}, yn[3], Jn[3][3], rn[3] = {0, 0, 0}, rs = 0.0;
-      for (int a = 0; a < D; ++a) un[a] = u[a] - step * du[a];
-      q1_map(s, c, un, yn, Jn);
-      for (int a = 0; a < D; ++a) {
-        rn[a] = yn[a] - x[a];
-        rs += rn[a] * rn[a];
-      }
-      if (rs < res || rs == 0.0) {
-        for (int a = 0; a < D; ++a) {
-          u[a] = un[a];
-          r[a] = rn[a];
-        }
-        memcpy(J, Jn, sizeof(Jn));
-        res = rs;
-        ok = true;
-        break;
-      }
-    }
-    if (!ok) return stp < 1e-24;  // stuck at round-off
-    if (stp * step * step < 1e-28 || res == 0.0) return true;
-  }
-  return false;
-}
-
-// faceCrossedFirstWithoutMapping (SemiLagrangian.cpp:702-757), used when an
-// inverse map fails: each face is the plane through its first vertex with
-// the normal of its first two edges (SemiLagrangianTools.cpp:151-168); the
-// smallest lambda in [0, 1) wins.  Face vertices in the cell numbering
-// bx + 2 by + 4 bz.
-int face_crossed_first_planar(const nat_solver* s, const int* c, const double* p_in, const double* p_out,
-                              double* p_b) {
-  static const int FV2[4][2] = {{0, 2}, {1, 3}, {0, 1}, {2, 3}};
-  static const int FV3[6][3] = {{0, 2, 4}, {1, 3, 5}, {0, 4, 1}, {2, 6, 3}, {0, 1, 2}, {4, 5, 6}};
-  const int D = s->D;
-  double lambda_min = 1.0;
-  int index_min = 0;
-  for (int i = 0; i < 2 * D; ++i) {
-    const double* v[3];
-    for (int k = 0; k < D; ++k) {
-      const int cv = D == 2 ? FV2[i][k] : FV3[i][k];
-      v[k] = grid_vertex(s, c[0] + (cv & 1), c[1] + ((cv >> 1) & 1), D > 2 ? c[2] + ((cv >> 2) & 1) : 0);
-    }
-    double n[3];
-    if (D == 2) {
-      n[0] = v[1][1] - v[0][1];
-      n[1] = -(v[1][0] - v[0][0]);
-    } else {
-      double d1[3], d2[3];
-      for (int a = 0; a < 3; ++a) {
-        d1[a] = v[1][a] - v[0][a];
-        d2[a] = v[2][a] - v[0][a];
-      }
-      n[0] = d1[1] * d2[2] - d1[2] * d2[1];
-      n[1] = d1[2] * d2[0] - d1[0] * d2[2];
-      n[2] = d1[0] * d2[1] - d1[1] * d2[0];
-    }
-    double num = 0.0, den = 0.0;
-    for (int a = 0; a < D; ++a) {
-      num += (p_in[a] - v[0][a]) * n[a];
-      den += (p_in[a] - p_out[a]) * n[a];
-    }
-    const double lam = num / den;
-    if (lam < 0) continue;
-    if (lam < lambda_min) {
-      lambda_min = lam;
-      index_min = i;
-    }
-  }
-  if (lambda_min == 1) return -1;
-  for (int a = 0; a < D; ++a) p_b[a] = p_in[a] + (p_out[a] - p_in[a]) * lambda_min;
-  return index_min;
-}
-
-// faceCrossedFirst with the mapping (SemiLagrangian.cpp:525-699): the face
-// search of the unit cell on the inverse-mapped points, the crossing point
-// mapped back; the planar search when an inverse map fails
-// (SemiLagrangian.cpp:280-288).
-int face_crossed_first_q1(const nat_solver* s, const int* c, const double* p_in, const double* p_out,
-                          double* p_b) {
-  double pi[3] = {0, 0, 0}, po[3] = {0, 0, 0};
-  if (!q1_inverse(s, c, p_in, pi) || !q1_inverse(s, c, p_out, po))
-    return face_crossed_first_planar(s, c, p_in, p_out, p_b);
-  static const double lo[3] = {0, 0, 0}, one[3] = {1, 1, 1};
-  double hu[3] = {0, 0, 0};
-  const int face = face_crossed_first(s->D, lo, one, pi, po, hu);
-  if (face >= 0) q1_map(s, c, hu, p_b, nullptr);
-  return face;
+  const TrackGeom g = vertex_geom(s);
+  return tg_vertex(g, i, j, k);
 }
 
 // Position of the node at Gauss-Lobatto point (xi[l0], xi[l1], xi[l2]) of cell c.
 void node_point(const nat_solver* s, const int* c, const int* l, const double* xi, double* x) {
   x[0] = x[1] = x[2] = 0.0;
   if (s->mapped) {
+    const TrackGeom g = vertex_geom(s);
     double u[3] = {0, 0, 0};
     for (int a = 0; a < s->D; ++a) u[a] = xi[l[a]];
-    q1_map(s, c, u, x, nullptr);
+    tg_q1_map(g, c, u, x, nullptr);
     return;
   }
   for (int a = 0; a < s->D; ++a) x[a] = c[a] * s->h[a] + xi[l[a]] * s->h[a];
+}
+
+// Departure-point rows of a mapped mesh on the device: one thread per (node,
+// direction) row, the same tracker as the host (track.cuh), rows written in
+// the solve's arithmetic type.  err[0]: bit 0 an inverse map failed (err[1]
+// gets the smallest such row), bit 1 a gathered index left the Q x n state.
+template <bool F64>
+__global__ void __launch_bounds__(128, 1) k_track_rows(const TrackGeom g, int* __restrict__ base,
+                                                       void* __restrict__ uout, void* __restrict__ cout,
+                                                       unsigned char* __restrict__ flags, int* __restrict__ err) {
+  const long long nr = (long long)(g.Q - 1) * g.n;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < nr;
+       r += (long long)gridDim.x * blockDim.x) {
+    const int alpha = (int)(r / g.n) + 1;
+    const long long node = r % g.n;
+    TrackRow R;
+    if (tg_row(g, node, alpha, R)) {
+      atomicOr(err, 1);
+      atomicMin(err + 1, (int)(r < 0x7fffffffLL ? r : 0x7fffffffLL));
+      continue;
+    }
+    // every gathered index must address the Q x n state
+    const long long st[3] = {1, g.n_ax[0], (long long)g.n_ax[0] * g.n_ax[1]};
+    long long lo = R.base, hi = R.base;
+    for (int a = 0; a < g.D; ++a) {
+      if (R.flags & (1u << a)) {
+        lo += (long long)(g.p - g.n_ax[a]) * st[a];
+        hi += (long long)(g.p - 1) * st[a];
+      } else {
+        hi += (long long)g.p * st[a];
+      }
+    }
+    if (lo < 0 || hi >= (long long)g.Q * g.n) atomicOr(err, 2);
+    base[r] = (int)R.base;
+    flags[r] = R.flags;
+    if constexpr (F64) {
+      double* u = static_cast<double*>(uout);
+      for (int a = 0; a < g.D; ++a)
+        for (int j = 0; j <= g.p; ++j) u[(((long long)(alpha - 1) * g.D + a) * (g.p + 1) + j) * g.n + node] = R.l1[a][j];
+      static_cast<double*>(cout)[r] = R.c_plain;
+    } else {
+      float* u = static_cast<float*>(uout);
+      for (int a = 0; a < g.D; ++a) u[((long long)(alpha - 1) * g.D + a) * g.n + node] = (float)R.uu[a];
+      static_cast<float*>(cout)[r] = (float)R.c_dev;
+    }
+  }
 }
 
 void free_mapped_rows(nat_solver* s) {
@@ -264,46 +176,11 @@ void free_mapped_rows(nat_solver* s) {
   s->d_mp_flags = nullptr;
 }
 
-// Departure-point rows to the device in the solve's arithmetic type.
-int upload_mapped_rows(nat_solver* s, const std::vector<int>& base, const std::vector<double>& u,
-                       const std::vector<double>& c2, const std::vector<unsigned char>& flags) {
-  const bool f64 = s->spec.precision == NAT_FP64;
-  const size_t es = f64 ? 8 : 4, nr = base.size();
-  // every gathered index must address the Q x n_dev state
-  const int P = s->spec.order;
-  const long long qn = (long long)s->Q * s->n_dev;
-  const long long st[3] = {1, s->n_ax[0], (long long)s->n_ax[0] * s->n_ax[1]};
-  for (size_t r = 0; r < nr; ++r) {
-    long long lo = base[r], hi = base[r];
-    for (int a = 0; a < s->D; ++a) {
-      if (flags[r] & (1u << a)) {
-        lo += (long long)(P - s->n_ax[a]) * st[a];
-        hi += (long long)(P - 1) * st[a];
-      } else {
-        hi += (long long)P * st[a];
-      }
-    }
-    if (lo < 0 || hi >= qn)
-      return fail(s, NAT_ERR_CUDA, "internal error: departure-point row %zu addresses %lld..%lld", r, lo, hi);
-  }
-  std::vector<unsigned char> ub(u.size() * es), cb(nr * es);
-  for (size_t i = 0; i < u.size(); ++i) {
-    if (f64)
-      memcpy(&ub[i * 8], &u[i], 8);
-    else {
-      const float v = (float)u[i];
-      memcpy(&ub[i * 4], &v, 4);
-    }
-  }
-  for (size_t r = 0; r < nr; ++r) {
-    const double c = c2[2 * r + (f64 ? 0 : 1)];
-    if (f64)
-      memcpy(&cb[r * 8], &c, 8);
-    else {
-      const float v = (float)c;
-      memcpy(&cb[r * 4], &v, 4);
-    }
-  }
+// Departure-point rows built on the host (already in the device layout and
+// type) to the device.
+int upload_mapped_rows(nat_solver* s, const std::vector<int>& base, const std::vector<unsigned char>& ub,
+                       const std::vector<unsigned char>& cb, const std::vector<unsigned char>& flags) {
+  const size_t nr = base.size();
   auto alloc = [&](void** p, size_t bytes) -> bool {
     if (cudaMalloc(p, bytes) != cudaSuccess) {
       cudaGetLastError();
@@ -318,6 +195,155 @@ int upload_mapped_rows(nat_solver* s, const std::vector<int>& base, const std::v
   CK(cudaMemcpy(s->d_mp_u, ub.data(), ub.size(), cudaMemcpyHostToDevice), "mapped rows");
   CK(cudaMemcpy(s->d_mp_c, cb.data(), cb.size(), cudaMemcpyHostToDevice), "mapped rows");
   CK(cudaMemcpy(s->d_mp_flags, flags.data(), nr, cudaMemcpyHostToDevice), "mapped rows");
+  return NAT_OK;
+}
+
+// Departure-point rows of every (node, direction) of a mapped mesh, by the
+// host tracker on all host threads, into host vectors in the layout of the
+// device arrays (FP32: unit coordinates and the deviation-storage constant
+// as float; FP64: the 1-D Lagrange values and the plain constant).
+int host_mapped_rows(nat_solver* s, std::vector<int>& mp_base, std::vector<unsigned char>& mp_u,
+                     std::vector<unsigned char>& mp_c, std::vector<unsigned char>& mp_flags) {
+  const TrackGeom g = make_geom(s, s->vtx.data());
+  const bool f64 = s->spec.precision == NAT_FP64;
+  const int D = s->D, Q = s->Q, p = s->spec.order;
+  const long long n = s->n_dev;
+  const size_t es = f64 ? 8 : 4, nr = (size_t)(Q - 1) * n;
+  mp_base.assign(nr, 0);
+  mp_u.assign(nr * D * (f64 ? p + 1 : 1) * es, 0);
+  mp_c.assign(nr * es, 0);
+  mp_flags.assign(nr, 0);
+  struct Err {
+    int rc = NAT_OK;
+    long long row = -1;
+  };
+  const int nthr = (int)std::max<long long>(1, std::min<long long>(std::thread::hardware_concurrency(), n / 256));
+  std::vector<Err> errs(nthr);
+  auto work = [&](long long n0, long long n1, Err& E) {
+    for (long long node = n0; node < n1; ++node)
+      for (int alpha = 1; alpha < Q; ++alpha) {
+        const long long r = (long long)(alpha - 1) * n + node;
+        TrackRow R;
+        if (tg_row(g, node, alpha, R)) {
+          if (E.row < 0 || r < E.row) E.row = r;
+          E.rc = NAT_ERR_UNSUPPORTED;
+          return;
+        }
+        mp_base[r] = (int)R.base;
+        mp_flags[r] = R.flags;
+        if (f64) {
+          for (int a = 0; a < D; ++a)
+            for (int j = 0; j <= p; ++j)
+              memcpy(&mp_u[8 * ((((long long)(alpha - 1) * D + a) * (p + 1) + j) * n + node)], &R.l1[a][j], 8);
+          memcpy(&mp_c[8 * r], &R.c_plain, 8);
+        } else {
+          for (int a = 0; a < D; ++a) {
+            const float v = (float)R.uu[a];
+            memcpy(&mp_u[4 * (((long long)(alpha - 1) * D + a) * n + node)], &v, 4);
+          }
+          const float c = (float)R.c_dev;
+          memcpy(&mp_c[4 * r], &c, 4);
+        }
+      }
+  };
+  {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthr; ++t) th.emplace_back(work, n * t / nthr, n * (t + 1) / nthr, std::ref(errs[t]));
+    for (auto& t : th) t.join();
+  }
+  for (const Err& E : errs)
+    if (E.rc) {
+      TrackRow R;
+      tg_row(g, E.row % n, (int)(E.row / n) + 1, R);
+      return fail(s, NAT_ERR_UNSUPPORTED,
+                  "the inverse map of cell (%d %d %d) failed at a departure point; the mesh is too distorted for "
+                  "this time step",
+                  R.cell[0], R.cell[1], R.cell[2]);
+    }
+  // every gathered index must address the Q x n_dev state
+  const long long qn = (long long)Q * n;
+  const long long st[3] = {1, s->n_ax[0], (long long)s->n_ax[0] * s->n_ax[1]};
+  for (size_t r = 0; r < nr; ++r) {
+    long long lo = mp_base[r], hi = mp_base[r];
+    for (int a = 0; a < D; ++a) {
+      if (mp_flags[r] & (1u << a)) {
+        lo += (long long)(p - s->n_ax[a]) * st[a];
+        hi += (long long)(p - 1) * st[a];
+      } else {
+        hi += (long long)p * st[a];
+      }
+    }
+    if (lo < 0 || hi >= qn)
+      return fail(s, NAT_ERR_CUDA, "internal error: departure-point row %zu addresses %lld..%lld", r, lo, hi);
+  }
+  return NAT_OK;
+}
+
+// The same rows by the device tracker (k_track_rows) into device arrays
+// (allocated here); the vertex grid is copied to the device for the call.
+int device_mapped_rows(nat_solver* s, int** d_base, void** d_u, void** d_c, unsigned char** d_flags) {
+  const bool f64 = s->spec.precision == NAT_FP64;
+  const int D = s->D, Q = s->Q, p = s->spec.order;
+  const long long n = s->n_dev;
+  const size_t es = f64 ? 8 : 4, nr = (size_t)(Q - 1) * n;
+  double* d_vtx = nullptr;
+  int* d_err = nullptr;
+  *d_base = nullptr;
+  *d_u = *d_c = nullptr;
+  *d_flags = nullptr;
+  auto alloc = [&](void** ptr, size_t bytes) -> bool {
+    if (cudaMalloc(ptr, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return true;
+  };
+  auto release = [&]() {
+    cudaFree(d_vtx);
+    cudaFree(d_err);
+  };
+  if (!alloc((void**)&d_vtx, sizeof(double) * s->vtx.size()) || !alloc((void**)&d_err, 2 * sizeof(int)) ||
+      !alloc((void**)d_base, sizeof(int) * nr) || !alloc(d_u, nr * D * (f64 ? p + 1 : 1) * es) ||
+      !alloc(d_c, nr * es) || !alloc((void**)d_flags, nr)) {
+    release();
+    cudaFree(*d_base);
+    cudaFree(*d_u);
+    cudaFree(*d_c);
+    cudaFree(*d_flags);
+    *d_base = nullptr;
+    *d_u = *d_c = nullptr;
+    *d_flags = nullptr;
+    return fail(s, NAT_ERR_OOM, "cudaMalloc of the departure-point rows failed");
+  }
+  const TrackGeom g = make_geom(s, d_vtx);
+  const int h_err0[2] = {0, 0x7fffffff};
+  cudaError_t e = cudaMemcpyAsync(d_vtx, s->vtx.data(), sizeof(double) * s->vtx.size(), cudaMemcpyHostToDevice,
+                                  s->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_err, h_err0, sizeof(h_err0), cudaMemcpyHostToDevice, s->stream);
+  if (e == cudaSuccess) {
+    const long long blocks = std::min<long long>(((long long)nr + 127) / 128, 152LL * 16);
+    if (f64)
+      k_track_rows<true><<<(int)blocks, 128, 0, s->stream>>>(g, *d_base, *d_u, *d_c, *d_flags, d_err);
+    else
+      k_track_rows<false><<<(int)blocks, 128, 0, s->stream>>>(g, *d_base, *d_u, *d_c, *d_flags, d_err);
+    e = cudaGetLastError();
+    s->launches++;
+  }
+  int h_err[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h_err, d_err, sizeof(h_err), cudaMemcpyDeviceToHost, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  release();
+  if (e != cudaSuccess) return cuda_fail(s, e, "device departure-point search");
+  if (h_err[0] & 1) {
+    const TrackGeom gh = make_geom(s, s->vtx.data());
+    TrackRow R;
+    tg_row(gh, h_err[1] % n, h_err[1] / n + 1, R);
+    return fail(s, NAT_ERR_UNSUPPORTED,
+                "the inverse map of cell (%d %d %d) failed at a departure point; the mesh is too distorted for "
+                "this time step",
+                R.cell[0], R.cell[1], R.cell[2]);
+  }
+  if (h_err[0] & 2) return fail(s, NAT_ERR_CUDA, "internal error: a departure-point row addresses outside the state");
   return NAT_OK;
 }
 
@@ -336,121 +362,26 @@ int build_wall_rows(nat_solver* s) {
   s->nbn = 0;
   free_mapped_rows(s);
   if (!s->walls && !s->mapped) return NAT_OK;
-  HostStencil hs;
-  get_host_stencil(s->spec.stencil, &hs, s->spec.scaling);
-  const int D = s->D, Q = s->Q, p = s->spec.order, PER = s->period;
-  double xi[PMAX1 + 1];
-  gl_points(p, xi);
-  double es[32][3];
-  int opp[32];
-  for (int i = 0; i < Q; ++i)
-    for (int a = 0; a < 3; ++a) es[i][a] = a < D ? hs.e[i][a] * s->spec.scaling : 0.0;
-  for (int i = 0; i < Q; ++i) {
-    opp[i] = 0;
-    for (int j = 0; j < Q; ++j)
-      if (es[j][0] == -es[i][0] && es[j][1] == -es[i][1] && es[j][2] == -es[i][2]) opp[i] = j;
+  const long long n = s->n_dev;
+  // mapped meshes (one population): departure-point rows of every node
+  // (sl_mapped.cuh), searched on the device
+  if (s->mapped && !s->thermal) {
+    if ((long long)s->Q * n > INT32_MAX) return fail(s, NAT_ERR_UNSUPPORTED, "Q x nodes exceeds 2^31");
+    if (s->track_on_host) {
+      std::vector<int> base;
+      std::vector<unsigned char> u, c, flags;
+      int rc = host_mapped_rows(s, base, u, c, flags);
+      if (rc) return rc;
+      return upload_mapped_rows(s, base, u, c, flags);
+    }
+    return device_mapped_rows(s, &s->d_mp_base, &s->d_mp_u, &s->d_mp_c, &s->d_mp_flags);
   }
+  const TrackGeom g = make_geom(s, s->vtx.data());
+  const int D = s->D, Q = s->Q, p = s->spec.order, PER = s->period;
   double grest[32];
   for (int q = 0; q < Q; ++q) grest[q] = s->rest[q] * s->gref;
-  const long long n = s->n_dev;
-  const int* N = s->spec.cells;
-  // the departure path of one (node, direction): source direction, cell and
-  // point where it ends, wall term; returns the number of wall hits (-1: the
-  // lifetime cap was reached, identity row)
-  struct Path {
-    int sdir, cell[3];
-    double dep[3], c;
-  };
-  auto trace = [&](const double* x, const int* own, int alpha, Path& P) -> int {
-    // defaults (also what an identity row of the lifetime cap uses)
-    P.sdir = alpha;
-    P.c = 0.0;
-    for (int a = 0; a < 3; ++a) {
-      P.cell[a] = own[a];
-      P.dep[a] = x[a];
-    }
-    int cdir = alpha, hit_dn = 0, hits = 0, life = 0;
-    int cell[3] = {own[0], own[1], own[2]};
-    double cur[3] = {x[0], x[1], x[2]}, dep[3] = {0, 0, 0};
-    for (int a = 0; a < D; ++a) dep[a] = x[a] - s->dt * es[alpha][a];
-    double c = 0.0;
-    for (;;) {
-      if (++life > 50) {  // lifetime cap (SemiLagrangian.cpp:252-271): identity row; the
-        P.c = c;          // wall terms of the hits before it stay registered
-        return -1;
-      }
-      double lo[3], pb[3];
-      for (int a = 0; a < D; ++a) lo[a] = cell[a] * s->h[a];
-      const int face = s->mapped ? face_crossed_first_q1(s, cell, cur, dep, pb)
-                                 : face_crossed_first(D, lo, s->h, cur, dep, pb);
-      if (face < 0) break;
-      const int ax = face / 2, upper = face % 2;
-      const bool at_boundary = upper ? (cell[ax] == N[ax] - 1) : (cell[ax] == 0);
-      if (at_boundary && !s->spec.periodic[ax] && s->bc[face] == NAT_BC_VELOCITY_BOUNCE_BACK) {
-        double dist = 0.0, ve = 0.0, exu = 0.0;
-        cdir = opp[cdir];
-        for (int a = 0; a < D; ++a) {
-          dist += (dep[a] - pb[a]) * (dep[a] - pb[a]);
-          ve += es[cdir][a] * es[cdir][a];
-        }
-        dist = sqrt(dist);
-        ve = sqrt(ve);
-        for (int a = 0; a < D; ++a) {
-          cur[a] = pb[a];
-          dep[a] = cur[a] - es[cdir][a] * dist / ve;
-        }
-        for (int a = 0; a < D; ++a) exu += s->uw[face][a] * es[alpha][a];
-        c += 2.0 * hs.w[alpha] * 1.0 * exu / s->cs2_scaled;
-        ++hits;
-        continue;
-      }
-      if (at_boundary && !s->spec.periodic[ax]) {  // do-nothing
-        for (int a = 0; a < D; ++a) {
-          cur[a] = dep[a] + s->dt * es[cdir][a];
-          dep[a] = cur[a] + s->dt * es[cdir][a];
-        }
-        cdir = opp[cdir];
-        hit_dn = 1;
-        ++hits;
-        continue;
-      }
-      for (int a = 0; a < D; ++a) cur[a] = pb[a];
-      if (at_boundary) {  // periodic: translate by the axis' period vector
-        for (int a = 0; a < D; ++a) {
-          const double shift = upper ? -s->pv[ax][a] : s->pv[ax][a];
-          cur[a] += shift;
-          dep[a] += shift;
-        }
-        cell[ax] = upper ? 0 : N[ax] - 1;
-      } else {
-        cell[ax] += upper ? 1 : -1;
-      }
-    }
-    if (hit_dn) cdir = opp[cdir];  // SemiLagrangian.cpp:312-316
-    P.sdir = cdir;
-    P.c = c;
-    for (int a = 0; a < 3; ++a) {
-      P.cell[a] = cell[a];
-      P.dep[a] = dep[a];
-    }
-    return hits;
-  };
-  // mapped meshes (one population): departure-point rows of every node
-  // (sl_mapped.cuh) instead of sparse matrix rows
-  const bool dp = s->mapped && !s->thermal;
-  std::vector<int> mp_base;
-  std::vector<double> mp_u, mp_c;
-  std::vector<unsigned char> mp_flags;
-  if (dp) {
-    if ((long long)Q * n > INT32_MAX) return fail(s, NAT_ERR_UNSUPPORTED, "Q x nodes exceeds 2^31");
-    mp_base.assign((size_t)(Q - 1) * n, 0);
-    // FP32: unit coordinates; FP64: the 1-D Lagrange values (sl_mapped.cuh)
-    mp_u.assign((size_t)(Q - 1) * D * n * (s->spec.precision == NAT_FP64 ? p + 1 : 1), 0.0);
-    mp_c.assign((size_t)2 * (Q - 1) * n, 0.0);
-    mp_flags.assign((size_t)(Q - 1) * n, 0);
-  }
-  // rows of the nodes [n0, n1) into one chunk (the chunks run on host
-  // threads; departure-point rows go straight to their slots)
+  // sparse rows of the wall nodes (and of every node of a two-population
+  // mapped mesh), node range [n0, n1) into one chunk on a host thread
   struct Chunk {
     std::vector<int> dst, ptr, col, bnodes;
     std::vector<double> w, cst;
@@ -458,122 +389,89 @@ int build_wall_rows(nat_solver* s) {
     char err[256] = {0};
   };
   auto work = [&](long long n0, long long n1, Chunk& C) {
-  std::vector<int>& dst = C.dst;
-  std::vector<int>& ptr = C.ptr;
-  std::vector<int>& col = C.col;
-  std::vector<int>& bnodes = C.bnodes;
-  std::vector<double>& w = C.w;
-  std::vector<double>& cst = C.cst;
-  for (long long node = n0; node < n1; ++node) {
-    int idx[3] = {(int)(node % s->n_ax[0]), (int)((node / s->n_ax[0]) % s->n_ax[1]),
-                  (int)(node / ((long long)s->n_ax[0] * s->n_ax[1]))};
-    double x[3] = {0, 0, 0};
-    int own[3] = {0, 0, 0}, loc[3] = {0, 0, 0};
-    for (int a = 0; a < D; ++a) {
-      own[a] = idx[a] / PER;
-      loc[a] = idx[a] % PER;
-    }
-    node_point(s, own, loc, xi, x);
-    // a node is a wall node when one of its paths meets a wall; all its rows
-    // are then evaluated as sparse rows
-    Path paths[32];
-    int hits[32];
-    bool wall_node = false;
-    for (int alpha = 1; alpha < Q; ++alpha) {
-      hits[alpha] = trace(x, own, alpha, paths[alpha]);
-      if (hits[alpha] != 0) wall_node = true;
-    }
-    if (!wall_node && !s->mapped) continue;
-    if (!dp) bnodes.push_back((int)node);
-    for (int alpha = 1; alpha < Q; ++alpha) {
-      const Path& P = paths[alpha];
-      const bool identity = hits[alpha] < 0;
-      const int sdir = identity ? alpha : P.sdir;
-      int cell[3] = {own[0], own[1], own[2]};
-      if (!identity)
-        for (int a = 0; a < D; ++a) cell[a] = P.cell[a];
-      double l1[3][PMAX1];
-      for (int a = 0; a < 3; ++a)
-        for (int j = 0; j < PMAX1; ++j) l1[a][j] = (a >= D && j == 0) ? 1.0 : 0.0;
-      double ud[3] = {0, 0, 0};
-      if (!identity && s->mapped && !q1_inverse(s, cell, P.dep, ud)) {
-        C.rc = NAT_ERR_UNSUPPORTED;
-        snprintf(C.err, sizeof(C.err),
-                 "the inverse map of cell (%d %d %d) failed at a departure point; the mesh is too distorted "
-                 "for this time step",
-                 cell[0], cell[1], cell[2]);
-        return;
-      }
-      double uu[3] = {0, 0, 0};  // unit coordinates of the departure point
+    for (long long node = n0; node < n1; ++node) {
+      const int idx[3] = {(int)(node % s->n_ax[0]), (int)((node / s->n_ax[0]) % s->n_ax[1]),
+                          (int)(node / ((long long)s->n_ax[0] * s->n_ax[1]))};
+      int own[3] = {0, 0, 0}, loc[3] = {0, 0, 0};
       for (int a = 0; a < D; ++a) {
-        if (identity) {
-          cell[a] = own[a];
-          uu[a] = xi[idx[a] % PER];
-          for (int j = 0; j <= p; ++j) l1[a][j] = (j == idx[a] % PER) ? 1.0 : 0.0;
-          continue;
+        own[a] = idx[a] / PER;
+        loc[a] = idx[a] % PER;
+      }
+      double x[3];
+      tg_node_point(g, own, loc, x);
+      // a node is a wall node when one of its paths meets a wall; all its rows
+      // are then evaluated as sparse rows
+      TrackPath paths[32];
+      int hits[32];
+      bool wall_node = false;
+      for (int alpha = 1; alpha < Q; ++alpha) {
+        hits[alpha] = tg_trace(g, x, own, alpha, paths[alpha]);
+        if (hits[alpha] != 0) wall_node = true;
+      }
+      if (!wall_node && !s->mapped) continue;
+      C.bnodes.push_back((int)node);
+      for (int alpha = 1; alpha < Q; ++alpha) {
+        const TrackPath& P = paths[alpha];
+        const bool identity = hits[alpha] < 0;
+        const int sdir = identity ? alpha : P.sdir;
+        int cell[3] = {own[0], own[1], own[2]};
+        if (!identity)
+          for (int a = 0; a < D; ++a) cell[a] = P.cell[a];
+        double l1[3][PMAX1];
+        for (int a = 0; a < 3; ++a)
+          for (int j = 0; j < PMAX1; ++j) l1[a][j] = (a >= D && j == 0) ? 1.0 : 0.0;
+        double ud[3] = {0, 0, 0};
+        if (!identity && s->mapped && P.udep_ok) {
+          for (int a = 0; a < 3; ++a) ud[a] = P.udep[a];
+        } else if (!identity && s->mapped && !tg_q1_inverse(g, cell, P.dep, ud)) {
+          C.rc = NAT_ERR_UNSUPPORTED;
+          snprintf(C.err, sizeof(C.err),
+                   "the inverse map of cell (%d %d %d) failed at a departure point; the mesh is too distorted "
+                   "for this time step",
+                   cell[0], cell[1], cell[2]);
+          return;
         }
-        double ul = s->mapped ? ud[a] : (P.dep[a] - cell[a] * s->h[a]) / s->h[a];
-        if (fabs(ul) < 1e-10) ul = 0.0;
-        if (fabs(ul - 1.0) < 1e-10) ul = 1.0;
-        uu[a] = ul;
-        for (int j = 0; j <= p; ++j) l1[a][j] = lagrange(p, xi, j, ul);
-      }
-      const double c = P.c;
-      const int np1 = p + 1;
-      const int nloc = D == 3 ? np1 * np1 * np1 : np1 * np1;
-      double wrest = 0.0, wgrest = 0.0;
-      bool tiny = false;
-      for (int li = 0; li < nloc; ++li) {
-        const int lx = li % np1, ly = (li / np1) % np1, lz = D == 3 ? li / (np1 * np1) : 0;
-        const double v = l1[0][lx] * l1[1][ly] * (D == 3 ? l1[2][lz] : 1.0);
-        if (fabs(v) < 1e-10) {  // SemiLagrangian.cpp:483
-          if (v != 0.0) tiny = true;
-          continue;
+        for (int a = 0; a < D; ++a) {
+          if (identity) {
+            cell[a] = own[a];
+            for (int j = 0; j <= p; ++j) l1[a][j] = (j == idx[a] % PER) ? 1.0 : 0.0;
+            continue;
+          }
+          double ul = s->mapped ? ud[a] : (P.dep[a] - cell[a] * s->h[a]) / s->h[a];
+          if (fabs(ul) < 1e-10) ul = 0.0;
+          if (fabs(ul - 1.0) < 1e-10) ul = 1.0;
+          for (int j = 0; j <= p; ++j) l1[a][j] = tg_lagrange(p, g.xi, j, ul);
         }
-        wrest += v * s->rest[sdir];
-        wgrest += v * grest[sdir];
-        if (dp) continue;
-        // the FE_Q node p of the last cell of a periodic axis is node 0
-        const int ix = (cell[0] * PER + lx) % s->n_ax[0], iy = (cell[1] * PER + ly) % s->n_ax[1],
-                  iz = (cell[2] * PER + lz) % s->n_ax[2];
-        const long long src = ((long long)iz * s->n_ax[1] + iy) * s->n_ax[0] + ix;
-        col.push_back((int)(sdir * n + src));
-        w.push_back(v);
-      }
-      if (dp) {
-        // departure-point row: first node of the cell, unit point, constants, flags
-        const long long r = (long long)(alpha - 1) * n + node;
-        const long long first =
-            ((long long)(cell[2] * PER) * s->n_ax[1] + cell[1] * PER) * s->n_ax[0] + cell[0] * PER;
-        mp_base[r] = (int)(sdir * n + first);
-        if (s->spec.precision == NAT_FP64) {
-          for (int a = 0; a < D; ++a)
-            for (int j = 0; j <= p; ++j)
-              mp_u[(((long long)(alpha - 1) * D + a) * (p + 1) + j) * n + node] = l1[a][j];
-        } else {
-          for (int a = 0; a < D; ++a) mp_u[((long long)(alpha - 1) * D + a) * n + node] = uu[a];
+        const int np1 = p + 1;
+        const int nloc = D == 3 ? np1 * np1 * np1 : np1 * np1;
+        double wrest = 0.0, wgrest = 0.0;
+        for (int li = 0; li < nloc; ++li) {
+          const int lx = li % np1, ly = (li / np1) % np1, lz = D == 3 ? li / (np1 * np1) : 0;
+          const double v = l1[0][lx] * l1[1][ly] * (D == 3 ? l1[2][lz] : 1.0);
+          if (fabs(v) < 1e-10) continue;  // SemiLagrangian.cpp:483
+          wrest += v * s->rest[sdir];
+          wgrest += v * grest[sdir];
+          // the FE_Q node p of the last cell of a periodic axis is node 0
+          const int ix = (cell[0] * PER + lx) % s->n_ax[0], iy = (cell[1] * PER + ly) % s->n_ax[1],
+                    iz = (cell[2] * PER + lz) % s->n_ax[2];
+          const long long src = ((long long)iz * s->n_ax[1] + iy) * s->n_ax[0] + ix;
+          C.col.push_back((int)(sdir * n + src));
+          C.w.push_back(v);
         }
-        mp_c[2 * r] = c;                                // plain f
-        mp_c[2 * r + 1] = c + wrest - s->rest[alpha];  // f - w_i storage
-        unsigned char fl = tiny ? MAP_TINY : 0;
-        for (int a = 0; a < D; ++a)
-          if (PER == p && cell[a] == N[a] - 1) fl |= (unsigned char)(1u << a);  // FE_Q wrap
-        mp_flags[r] = fl;
-        continue;
+        if (C.col.size() > (size_t)INT32_MAX) {
+          C.rc = NAT_ERR_UNSUPPORTED;
+          snprintf(C.err, sizeof(C.err), "sparse rows exceed 2^31 entries; use fewer nodes");
+          return;
+        }
+        const double c = P.c;
+        C.dst.push_back((int)(alpha * n + node));
+        C.ptr.push_back((int)C.col.size());
+        C.cst.push_back(c);                           // plain f
+        C.cst.push_back(c + wrest - s->rest[alpha]);  // f - w_i storage
+        C.cst.push_back(0.0);                         // plain g: no wall term
+        C.cst.push_back(wgrest - grest[alpha]);       // g - w_i g_ref storage
       }
-      if (col.size() > (size_t)INT32_MAX) {
-        C.rc = NAT_ERR_UNSUPPORTED;
-        snprintf(C.err, sizeof(C.err), "sparse rows exceed 2^31 entries; use fewer nodes");
-        return;
-      }
-      dst.push_back((int)(alpha * n + node));
-      ptr.push_back((int)col.size());
-      cst.push_back(c);                           // plain f
-      cst.push_back(c + wrest - s->rest[alpha]);  // f - w_i storage
-      cst.push_back(0.0);                         // plain g: no wall term
-      cst.push_back(wgrest - grest[alpha]);       // g - w_i g_ref storage
     }
-  }
   };
   const int nthr = (int)std::max<long long>(1, std::min<long long>(std::thread::hardware_concurrency(), n / 256));
   std::vector<Chunk> chunks(nthr);
@@ -599,7 +497,6 @@ int build_wall_rows(nat_solver* s) {
     cst.insert(cst.end(), C.cst.begin(), C.cst.end());
     C = Chunk();
   }
-  if (dp) return upload_mapped_rows(s, mp_base, mp_u, mp_c, mp_flags);
   s->nbn = (int)bnodes.size();
   s->nbr = (int)dst.size();
   if (s->nbr == 0) return NAT_OK;
@@ -697,6 +594,7 @@ int setup_mapping(nat_solver* s, const double* vertices, double* hmin) {
     s->h[a] = s->spec.length[a] / N[a];
   }
   // cells: positive det J at the corners, smallest vertex distance
+  const TrackGeom vg = vertex_geom(s);
   const int p = s->spec.order, PER = s->period, np1 = p + 1;
   double xi[PMAX1 + 1], wq[PMAX1 + 1];
   gl_points(p, xi);
@@ -719,8 +617,8 @@ int setup_mapping(nat_solver* s, const double* vertices, double* hmin) {
           }
           const double u[3] = {(double)(i & 1), (double)((i >> 1) & 1), (double)((i >> 2) & 1)};
           double x[3], J[3][3];
-          q1_map(s, c, u, x, J);
-          if (!(q1_det(D, J) > 0))
+          tg_q1_map(vg, c, u, x, J);
+          if (!(tg_det(D, J) > 0))
             return fail(s, NAT_ERR_INVALID_ARG, "cell (%d %d %d) is inverted or degenerate", cx, cy, cz);
         }
         const int nloc = D == 3 ? np1 * np1 * np1 : np1 * np1;
@@ -728,8 +626,8 @@ int setup_mapping(nat_solver* s, const double* vertices, double* hmin) {
           const int l[3] = {li % np1, (li / np1) % np1, D == 3 ? li / (np1 * np1) : 0};
           const double u[3] = {xi[l[0]], xi[l[1]], D == 3 ? xi[l[2]] : 0.0};
           double x[3], J[3][3];
-          q1_map(s, c, u, x, J);
-          double w = q1_det(D, J);
+          tg_q1_map(vg, c, u, x, J);
+          double w = tg_det(D, J);
           for (int a = 0; a < D; ++a) w *= wq[l[a]];
           const int ix = (cx * PER + l[0]) % s->n_ax[0], iy = (cy * PER + l[1]) % s->n_ax[1],
                     iz = (cz * PER + l[2]) % s->n_ax[2];
@@ -746,3 +644,42 @@ int setup_mapping(nat_solver* s, const double* vertices, double* hmin) {
 
 }  // namespace api
 }  // namespace natgpu
+
+using namespace natgpu::api;
+
+extern "C" int nat_mapped_rows(nat_solver* s, int where, int32_t* base, void* u, void* c, uint8_t* flags) {
+  if (!s || (where != 0 && where != 1)) return NAT_ERR_INVALID_ARG;
+  if (!s->mapped || s->thermal)
+    return fail(s, NAT_ERR_UNSUPPORTED, "departure-point rows exist for mapped one-population meshes only");
+  const bool f64 = s->spec.precision == NAT_FP64;
+  const size_t es = f64 ? 8 : 4, nr = (size_t)(s->Q - 1) * s->n_dev;
+  const size_t ub = nr * s->D * (f64 ? s->spec.order + 1 : 1) * es, cb = nr * es;
+  if (where == 0) {
+    std::vector<int> b;
+    std::vector<unsigned char> uu, cc, fl;
+    const int rc = host_mapped_rows(s, b, uu, cc, fl);
+    if (rc) return rc;
+    if (base) memcpy(base, b.data(), sizeof(int) * nr);
+    if (u) memcpy(u, uu.data(), ub);
+    if (c) memcpy(c, cc.data(), cb);
+    if (flags) memcpy(flags, fl.data(), nr);
+    return NAT_OK;
+  }
+  int* d_base;
+  void *d_u, *d_c;
+  unsigned char* d_flags;
+  int rc = device_mapped_rows(s, &d_base, &d_u, &d_c, &d_flags);
+  if (rc == NAT_OK) {
+    cudaError_t e = cudaSuccess;
+    if (base && e == cudaSuccess) e = cudaMemcpy(base, d_base, sizeof(int) * nr, cudaMemcpyDeviceToHost);
+    if (u && e == cudaSuccess) e = cudaMemcpy(u, d_u, ub, cudaMemcpyDeviceToHost);
+    if (c && e == cudaSuccess) e = cudaMemcpy(c, d_c, cb, cudaMemcpyDeviceToHost);
+    if (flags && e == cudaSuccess) e = cudaMemcpy(flags, d_flags, nr, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_fail(s, e, "departure-point rows read-back");
+  }
+  cudaFree(d_base);
+  cudaFree(d_u);
+  cudaFree(d_c);
+  cudaFree(d_flags);
+  return rc;
+}

@@ -334,3 +334,53 @@ def test_mapped_grid_errors(gpu_lib):
     with pytest.raises(N.NatError) as ei:
         N.Solver(spec)
     assert ei.value.code == N.NAT_ERR_INVALID_ARG
+
+
+TRACK_CASES = [
+    (2, (4, 5), 2, True, "D2Q9", "BGK_STANDARD", "fp32dev"),
+    (2, (4, 4), 3, False, "D2Q9", "KBC_STANDARD", "fp64"),
+    (2, (5, 4), 4, True, "D2Q9", "BGK_STANDARD", "fp64"),
+    (3, (3, 3, 3), 2, True, "D3Q19", "BGK_STANDARD", "fp32dev"),
+    (3, (3, 3, 3), 2, False, "D3Q27", "KBC_STANDARD", "fp64"),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("D,cells,p,dg,stencil,model,precision", TRACK_CASES)
+def test_device_departure_search_equals_host_bitwise(gpu_lib, D, cells, p, dg, stencil, model, precision):
+    """The departure-point search and the Newton inverse of MappingQ1
+    (SemiLagrangian.cpp:525-757, SemiLagrangianTools.cpp:15-64) run on the
+    device (one thread per row, the rows nat_create uses) and on the host
+    tracker: every row is the same, bit for bit."""
+    L = (1.0, 1.0, 1.0)[:D]
+    V = P.wavy_grid(cells, L, 0.12 if D == 2 else 0.05)
+    st = O.stencil(stencil, math.sqrt(3) / 0.1)
+    m = O.Mesh(D, cells, p, dg, L, vertices=V)
+    dt = O.time_step(m.h_min(), p, st.max_speed, 0.4)
+    spec = N.SolverSpec(stencil=stencil, order=p, cells=cells, length=L, scaling=st.scaling, viscosity=2e-3,
+                        dt=dt, collision=model, precision=precision, topology="dg" if dg else "feq", vertices=V)
+    with N.Solver(spec) as sol:
+        host = sol.mapped_rows("host")
+        dev = sol.mapped_rows("device")
+    for h, d in zip(host, dev):
+        assert h.dtype == d.dtype and h.shape == d.shape
+        assert np.array_equal(h.view(np.uint8), d.view(np.uint8))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32dev", "fp64"])
+def test_device_departure_search_equals_host_in_the_lubrication_channel(gpu_lib, precision):
+    """The same in the LubricationSine channel: bounce-back walls (one moving)
+    and the wavy top wall, where paths hit walls."""
+    V = P.lubrication_sine_grid(refinement=2)
+    cells = tuple(s - 1 for s in V.shape[:2])
+    scaling = math.sqrt(3) / 0.1
+    spec = N.SolverSpec(stencil="D2Q9", order=3, cells=cells, length=(1.0, 0.25), scaling=scaling, viscosity=1e-3,
+                        cfl=0.4, collision="BGK_STANDARD", precision=precision, topology="dg",
+                        periodic=(True, False, True), vertices=V)
+    with N.Solver(spec) as sol:
+        sol.set_boundary(2, "VELOCITY_BOUNCE_BACK", np.array([0.05 * scaling, 0.0, 0.0]))
+        host = sol.mapped_rows("host")
+        dev = sol.mapped_rows("device")
+    for h, d in zip(host, dev):
+        assert np.array_equal(h.view(np.uint8), d.view(np.uint8))
