@@ -446,8 +446,14 @@ int nat_server_destroy(nat_server* s);
  * free up. */
 int nat_server_submit(nat_server* s, const nat_request* r, int64_t* id);
 /* One server step: collect finished results, admit queued requests, advance
- * every live solve by one time step (one graph launch). */
+ * every live solve by one time step (one graph launch: a kernel per group of
+ * live solves with the same order and collision model). */
 int nat_server_step(nat_server* s);
+/* Up to max_steps server steps in one call (no counterpart in the
+ * reference); stops early when no solve is live.  *steps_done (may be NULL)
+ * receives the number run.  The host runs at most 64 steps ahead of the
+ * device. */
+int nat_server_run(nat_server* s, int max_steps, int* steps_done);
 /* Ids of finished requests (up to max_ids); wait != 0 blocks until every
  * solve that has run its last step is copied out. */
 int nat_server_poll(nat_server* s, int64_t* ids, int max_ids, int* n_done, int wait);

@@ -57,7 +57,8 @@ EXPORTS = [
     "nat_collide", "nat_step", "nat_step_async", "nat_status", "nat_last_error",
     "nat_mass_energy", "nat_device_f", "nat_launch_count", "nat_version", "nat_set_kernel_variant",
     "nat_kernel_variant", "nat_autotune", "nat_autotune_report", "nat_select_candidate", "nat_kernel_info",
-    "nat_mapped_rows", "nat_server_create", "nat_server_destroy", "nat_server_submit", "nat_server_step", "nat_server_poll",
+    "nat_mapped_rows", "nat_server_create", "nat_server_destroy", "nat_server_submit", "nat_server_step", "nat_server_run",
+    "nat_server_poll",
     "nat_server_result", "nat_server_stats", "nat_server_last_error", "nat_mass_energy_noalloc",
     "nat_set_thermal", "nat_get_thermal", "nat_upload_g", "nat_download_g", "nat_download_thermal",
     "nat_init_thermal", "nat_set_boundary", "nat_set_force", "nat_checkpoint_save", "nat_checkpoint_load",

@@ -2,15 +2,16 @@
 //
 // Requests (D2Q9, BGK or KBC, FE_Q order 1-6, any cell count, own Ma / Re /
 // step count) are admitted by their HBM footprint into slots of a device
-// memory pool; every live solve advances one time step per server step, all
-// of them in ONE persistent launch: the grid strides over a device work list
-// of (slot, row, 32-node segment) items and each warp runs the row body
-// (sl_row.cuh) of its solve's order and collision model.  The step (that
-// launch plus a tick of the device step counter) is captured once as a CUDA
-// graph: the work list, the slot table and the step parity live in device
-// memory, so admissions and retirements only update data, never the graph.
-// A solve's last step writes rho / u; the host copies them out after an
-// event and frees the slot.
+// memory pool; every live solve advances one time step per server step.  A
+// server step is one CUDA graph: one kernel per (order, collision) group of
+// the live solves, as parallel branches, each specialised for its order and
+// model and walking its part of a device work list of (slot, row, 32-node
+// segment) items with the row body of sl_row.cuh.  The step counter lives in
+// device memory and the last CTA of the step advances it, so the graph needs
+// no separate tick.  Admissions and retirements rebuild the work list
+// (uploaded asynchronously from double-buffered page-locked memory) and the
+// graph; steps in between relaunch the same graph.  A solve's last step
+// writes rho / u; the host copies them out after an event and frees the slot.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
@@ -51,10 +52,8 @@ struct WorkItem {
 };
 
 template <int P, int COLL>
-__device__ __forceinline__ void serve_item(const SlotDesc& d, float* sw, float* buf, int row, int seg, int lane,
-                                           long long step) {
-  fill_row_table<float, P, false>(sw, d.W, lane, 32);
-  __syncwarp();
+__device__ __forceinline__ void serve_item(const SlotDesc& d, const float* sw, float* buf, int row, int seg,
+                                           int lane, long long step) {
   const int par = (int)((step - d.start_step) & 1);
   RowArgs<float> a;
   a.f_in = d.f[par];
@@ -73,40 +72,78 @@ __device__ __forceinline__ void serve_item(const SlotDesc& d, float* sw, float* 
   __syncwarp();
 }
 
-// Persistent batched step: warps stride over the work list.
+// group g = (order - 1) * 2 + (collision is KBC)
+constexpr int NGROUPS = 2 * PMAX;
+__host__ __device__ constexpr int serve_group(int P, int coll) { return (P - 1) * 2 + (coll == COLL_KBC ? 1 : 0); }
+
+struct GroupRange {
+  int begin, count;  // items of the group in the work list
+};
+
+// The batched step of one (order, collision) group.  Each warp takes a
+// contiguous chunk of the group's items (items of one solve are adjacent, so
+// the weight table of the solve is filled once per chunk, not per item).
+// The CTA that finishes last among all CTAs of the step's kernels
+// (total_ctas, counted on *ticket) advances the device step counter: every
+// CTA has read the counter before that.
+template <int P, int COLL>
 __global__ void __launch_bounds__(32 * SERVE_WARPS, 2)
-    k_serve_step(const SlotDesc* __restrict__ slots, const WorkItem* __restrict__ work, const int* nwork,
-                 const long long* step_ctr) {
-  constexpr int TAB = row_table_size<PMAX, false>();
-  constexpr int BW = 32 + PER_MAX + PMAX + 1;
+    k_serve_group(const SlotDesc* __restrict__ slots, const WorkItem* __restrict__ work,
+                  const GroupRange* __restrict__ groups, long long* step_ctr, unsigned* ticket,
+                  unsigned total_ctas) {
+  constexpr int TAB = row_table_size<P, false>();
+  constexpr int BW = 32 + P + P + 1;
   __shared__ float s_tab[SERVE_WARPS][TAB];
   __shared__ float s_buf[SERVE_WARPS][2 * (BW + 1)];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nw = *nwork;
+  const GroupRange gr = groups[serve_group(P, COLL)];
   const long long step = *step_ctr;
-  for (int w = blockIdx.x * SERVE_WARPS + warp; w < nw; w += gridDim.x * SERVE_WARPS) {
-    const WorkItem it = work[w];
+  const int nwarps = gridDim.x * SERVE_WARPS;
+  const int chunk = (gr.count + nwarps - 1) / nwarps;
+  const int w0 = (blockIdx.x * SERVE_WARPS + warp) * chunk;
+  const int w1 = min(w0 + chunk, gr.count);
+  int cur = -1;
+  for (int w = w0; w < w1; ++w) {
+    const WorkItem it = work[gr.begin + w];
     const SlotDesc& d = slots[it.slot];
-    if (!d.active) continue;
-    float* sw = s_tab[warp];
-    float* bf = s_buf[warp];
-    switch (d.P * 4 + d.coll) {
-#define NAT_SERVE_CASE(PP)                                                           \
-  case PP * 4 + COLL_BGK: serve_item<PP, COLL_BGK>(d, sw, bf, it.row, it.seg, lane, step); break; \
-  case PP * 4 + COLL_KBC: serve_item<PP, COLL_KBC>(d, sw, bf, it.row, it.seg, lane, step); break;
-      NAT_SERVE_CASE(1)
-      NAT_SERVE_CASE(2)
-      NAT_SERVE_CASE(3)
-      NAT_SERVE_CASE(4)
-      NAT_SERVE_CASE(5)
-      NAT_SERVE_CASE(6)
-#undef NAT_SERVE_CASE
-      default: break;
+    if (!d.active || step > d.last_step) continue;
+    if (it.slot != cur) {
+      __syncwarp();
+      fill_row_table<float, P, false>(s_tab[warp], d.W, lane, 32);
+      __syncwarp();
+      cur = it.slot;
+    }
+    serve_item<P, COLL>(d, s_tab[warp], s_buf[warp], it.row, it.seg, lane, step);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned t = atomicAdd(ticket, 1u);
+    if (t == total_ctas - 1) {
+      *ticket = 0u;
+      *step_ctr = step + 1;
+      __threadfence();
     }
   }
 }
 
-__global__ void k_serve_tick(long long* step_ctr) { *step_ctr += 1; }
+using GroupKernel = void (*)(const SlotDesc*, const WorkItem*, const GroupRange*, long long*, unsigned*, unsigned);
+
+GroupKernel group_kernel(int g) {
+  switch (g) {
+#define NAT_SERVE_G(PP)                                         \
+  case serve_group(PP, COLL_BGK): return k_serve_group<PP, COLL_BGK>; \
+  case serve_group(PP, COLL_KBC): return k_serve_group<PP, COLL_KBC>;
+    NAT_SERVE_G(1)
+    NAT_SERVE_G(2)
+    NAT_SERVE_G(3)
+    NAT_SERVE_G(4)
+    NAT_SERVE_G(5)
+    NAT_SERVE_G(6)
+#undef NAT_SERVE_G
+    default: return nullptr;
+  }
+}
 
 // Equilibrium initial state of one slot (CFDSolver::initializeDistributions,
 // EQUILIBRIUM option, solver/CFDSolver.cpp:1103-1130), FE_Q lattice with the
@@ -218,11 +255,28 @@ struct nat_server {
   std::vector<SlotDesc> h_slots;
   std::vector<int> slot_used;
   WorkItem* d_work = nullptr;
-  int* d_nwork = nullptr;
+  GroupRange* d_groups = nullptr;
   long long* d_step = nullptr;
+  unsigned* d_ticket = nullptr;
   int* d_status = nullptr;  // one per slot
   int max_work = 0;
-  std::vector<WorkItem> h_work;
+  int group_count[NGROUPS] = {};
+  // page-locked staging of the work list, group ranges and slot table, two
+  // sets used in turn; an event marks when a set's copies have been read
+  WorkItem* stage_work[2] = {nullptr, nullptr};
+  GroupRange* stage_groups[2] = {nullptr, nullptr};
+  SlotDesc* stage_slots[2] = {nullptr, nullptr};
+  int stage_cap[2] = {0, 0};
+  cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+  int stage_k = 0;
+  // bound on the host running ahead of the device: an event every
+  // RUNAHEAD_EVERY steps in a ring of RUNAHEAD_RING
+  cudaEvent_t ahead_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool ahead_used[4] = {false, false, false, false};
+  int ahead_k = 0;
+  unsigned graph_ctas = 0;
+  int graph_nodes = 0;
+  int sms = 0;
   std::deque<std::pair<int64_t, nat_request>> pending;
   std::vector<Live> live;
   std::vector<Completing*> completing;
@@ -231,7 +285,6 @@ struct nat_server {
   int64_t next_id = 1;
   bool dirty = true;
   cudaGraphExec_t graph = nullptr;
-  int grid = 0;
   std::string err;
   // statistics
   long long steps_run = 0, node_updates = 0, launches = 0;
@@ -278,46 +331,101 @@ int validate(nat_server* s, const nat_request& r) {
   return NAT_OK;
 }
 
-// rebuild the device work list from the active slots
+constexpr int RUNAHEAD_EVERY = 16;
+constexpr int RUNAHEAD_RING = 4;
+
+// rebuild the device work list from the live slots, grouped by (order,
+// collision); uploaded asynchronously from one of the two staging sets
 int upload_state(nat_server* s) {
-  s->h_work.clear();
+  std::vector<WorkItem> per[NGROUPS];
   for (const Live& L : s->live) {
     const SlotDesc& d = s->h_slots[L.slot];
+    std::vector<WorkItem>& v = per[serve_group(d.P, d.coll)];
     for (int y = 0; y < d.ny; ++y)
-      for (int g = 0; g < d.nseg; ++g) s->h_work.push_back({L.slot, y, g});
+      for (int g = 0; g < d.nseg; ++g) v.push_back({L.slot, y, g});
   }
-  const int nw = (int)s->h_work.size();
+  int nw = 0;
+  for (int g = 0; g < NGROUPS; ++g) nw += (int)per[g].size();
   if (nw > s->max_work) {
+    // in-flight steps may still read the old list: drain them first (rare)
+    SCK(cudaStreamSynchronize(s->stream), "work list drain");
     cudaFree(s->d_work);
     s->max_work = nw * 2;
     SCK(cudaMalloc(&s->d_work, sizeof(WorkItem) * s->max_work), "work list");
-    // the graph holds the old work-list pointer
-    if (s->graph) {
-      cudaGraphExecDestroy(s->graph);
-      s->graph = nullptr;
-    }
   }
+  const int k = s->stage_k;
+  SCK(cudaEventSynchronize(s->stage_ev[k]), "staging reuse");  // its last copies are done
+  if (nw > s->stage_cap[k]) {
+    cudaFreeHost(s->stage_work[k]);
+    s->stage_cap[k] = nw * 2;
+    SCK(cudaHostAlloc(&s->stage_work[k], sizeof(WorkItem) * s->stage_cap[k], cudaHostAllocDefault), "staging");
+  }
+  int off = 0;
+  for (int g = 0; g < NGROUPS; ++g) {
+    s->stage_groups[k][g] = {off, (int)per[g].size()};
+    s->group_count[g] = (int)per[g].size();
+    if (!per[g].empty()) memcpy(s->stage_work[k] + off, per[g].data(), sizeof(WorkItem) * per[g].size());
+    off += (int)per[g].size();
+  }
+  memcpy(s->stage_slots[k], s->h_slots.data(), sizeof(SlotDesc) * s->max_slots);
   if (nw)
-    SCK(cudaMemcpyAsync(s->d_work, s->h_work.data(), sizeof(WorkItem) * nw, cudaMemcpyHostToDevice, s->stream),
+    SCK(cudaMemcpyAsync(s->d_work, s->stage_work[k], sizeof(WorkItem) * nw, cudaMemcpyHostToDevice, s->stream),
         "work upload");
-  SCK(cudaMemcpyAsync(s->d_nwork, &nw, sizeof(int), cudaMemcpyHostToDevice, s->stream), "nwork upload");
-  SCK(cudaMemcpyAsync(s->d_slots, s->h_slots.data(), sizeof(SlotDesc) * s->max_slots, cudaMemcpyHostToDevice,
+  SCK(cudaMemcpyAsync(s->d_groups, s->stage_groups[k], sizeof(GroupRange) * NGROUPS, cudaMemcpyHostToDevice,
+                      s->stream),
+      "group upload");
+  SCK(cudaMemcpyAsync(s->d_slots, s->stage_slots[k], sizeof(SlotDesc) * s->max_slots, cudaMemcpyHostToDevice,
                       s->stream),
       "slot upload");
-  // the copies read host memory asynchronously: keep it stable until done
-  SCK(cudaStreamSynchronize(s->stream), "state sync");
+  SCK(cudaEventRecord(s->stage_ev[k], s->stream), "staging event");
+  s->stage_k ^= 1;
   s->dirty = false;
+  if (s->graph) {  // the groups or their sizes changed: a new graph
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
   return NAT_OK;
 }
 
+// One graph per live set: a kernel node per non-empty group, no
+// dependencies between them (independent solves), each with a grid of about
+// two items per warp, at most two CTAs per SM.
 int capture(nat_server* s) {
-  cudaGraph_t g;
-  SCK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-  k_serve_step<<<s->grid, 32 * SERVE_WARPS, 0, s->stream>>>(s->d_slots, s->d_work, s->d_nwork, s->d_step);
-  k_serve_tick<<<1, 1, 0, s->stream>>>(s->d_step);
-  SCK(cudaStreamEndCapture(s->stream, &g), "end capture");
-  SCK(cudaGraphInstantiate(&s->graph, g, 0), "instantiate");
-  cudaGraphDestroy(g);
+  int grid[NGROUPS] = {};
+  unsigned total = 0;
+  for (int g = 0; g < NGROUPS; ++g) {
+    if (!s->group_count[g]) continue;
+    const int want = (s->group_count[g] + 2 * SERVE_WARPS - 1) / (2 * SERVE_WARPS);
+    grid[g] = want < 1 ? 1 : (want > 2 * s->sms ? 2 * s->sms : want);
+    total += (unsigned)grid[g];
+  }
+  if (!total) return NAT_OK;
+  cudaGraph_t gr;
+  SCK(cudaGraphCreate(&gr, 0), "graph create");
+  for (int g = 0; g < NGROUPS; ++g) {
+    if (!grid[g]) continue;
+    void* args[] = {(void*)&s->d_slots, (void*)&s->d_work, (void*)&s->d_groups, (void*)&s->d_step,
+                    (void*)&s->d_ticket, (void*)&total};
+    cudaKernelNodeParams kp;
+    memset(&kp, 0, sizeof kp);
+    kp.func = (void*)group_kernel(g);
+    kp.gridDim = dim3(grid[g]);
+    kp.blockDim = dim3(32 * SERVE_WARPS);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    cudaGraphNode_t node;
+    cudaError_t e = cudaGraphAddKernelNode(&node, gr, nullptr, 0, &kp);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(gr);
+      return sfail(s, NAT_ERR_CUDA, "graph node: %s", cudaGetErrorString(e));
+    }
+  }
+  cudaError_t e = cudaGraphInstantiate(&s->graph, gr, 0);
+  cudaGraphDestroy(gr);
+  if (e != cudaSuccess) return sfail(s, NAT_ERR_CUDA, "instantiate: %s", cudaGetErrorString(e));
+  s->graph_ctas = total;
+  s->graph_nodes = 0;
+  for (int g = 0; g < NGROUPS; ++g) s->graph_nodes += grid[g] ? 1 : 0;
   return NAT_OK;
 }
 
@@ -498,14 +606,23 @@ int nat_server_create(size_t pool_bytes, int max_slots, nat_server** out) {
   s->slot_used.assign(max_slots, 0);
   SCK(cudaMalloc(&s->d_slots, sizeof(SlotDesc) * max_slots), "slots");
   SCK(cudaMalloc(&s->d_status, sizeof(int) * max_slots), "status");
-  SCK(cudaMalloc(&s->d_nwork, sizeof(int)), "nwork");
+  SCK(cudaMalloc(&s->d_groups, sizeof(GroupRange) * NGROUPS), "groups");
   SCK(cudaMalloc(&s->d_step, sizeof(long long)), "step");
   SCK(cudaMemsetAsync(s->d_step, 0, sizeof(long long), s->stream), "step clear");
+  SCK(cudaMalloc(&s->d_ticket, sizeof(unsigned)), "ticket");
+  SCK(cudaMemsetAsync(s->d_ticket, 0, sizeof(unsigned), s->stream), "ticket clear");
   s->max_work = 1 << 16;
   SCK(cudaMalloc(&s->d_work, sizeof(WorkItem) * s->max_work), "work list");
-  int sms = 0;
-  SCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device), "sm count");
-  s->grid = 2 * sms;  // persistent: two CTAs per SM
+  for (int k = 0; k < 2; ++k) {
+    s->stage_cap[k] = s->max_work;
+    SCK(cudaHostAlloc(&s->stage_work[k], sizeof(WorkItem) * s->stage_cap[k], cudaHostAllocDefault), "staging");
+    SCK(cudaHostAlloc(&s->stage_groups[k], sizeof(GroupRange) * NGROUPS, cudaHostAllocDefault), "staging");
+    SCK(cudaHostAlloc(&s->stage_slots[k], sizeof(SlotDesc) * max_slots, cudaHostAllocDefault), "staging");
+    SCK(cudaEventCreateWithFlags(&s->stage_ev[k], cudaEventDisableTiming), "staging event");
+  }
+  for (int k = 0; k < RUNAHEAD_RING; ++k)
+    SCK(cudaEventCreateWithFlags(&s->ahead_ev[k], cudaEventDisableTiming), "run-ahead event");
+  SCK(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device), "sm count");
   return NAT_OK;
 }
 
@@ -521,9 +638,18 @@ int nat_server_destroy(nat_server* s) {
   cudaFree(s->pool_base);
   cudaFree(s->d_slots);
   cudaFree(s->d_status);
-  cudaFree(s->d_nwork);
+  cudaFree(s->d_groups);
   cudaFree(s->d_step);
+  cudaFree(s->d_ticket);
   cudaFree(s->d_work);
+  for (int k = 0; k < 2; ++k) {
+    cudaFreeHost(s->stage_work[k]);
+    cudaFreeHost(s->stage_groups[k]);
+    cudaFreeHost(s->stage_slots[k]);
+    if (s->stage_ev[k]) cudaEventDestroy(s->stage_ev[k]);
+  }
+  for (int k = 0; k < RUNAHEAD_RING; ++k)
+    if (s->ahead_ev[k]) cudaEventDestroy(s->ahead_ev[k]);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return NAT_OK;
@@ -540,8 +666,15 @@ int nat_server_submit(nat_server* s, const nat_request* r, int64_t* id) {
   return NAT_OK;
 }
 
-int nat_server_step(nat_server* s) {
-  if (!s) return NAT_ERR_INVALID_ARG;
+}  // extern "C"
+
+namespace {
+
+// One server step: collect finished results, admit queued requests, advance
+// every live solve by one time step (one graph launch).  *ran = 0 when no
+// solve was live.
+int server_step(nat_server* s, int* ran) {
+  *ran = 0;
   int rc = harvest(s, false);
   if (rc) return rc;
   rc = admit(s);
@@ -556,11 +689,46 @@ int nat_server_step(nat_server* s) {
     if (rc) return rc;
   }
   SCK(cudaGraphLaunch(s->graph, s->stream), "graph launch");
-  s->launches += 2;
+  s->launches += s->graph_nodes;  // the graph's kernels, one per group
   const long long step = s->host_step++;
   s->steps_run++;
   for (const Live& L : s->live) s->node_updates += s->h_slots[L.slot].n;
+  // keep the host at most RUNAHEAD_EVERY * RUNAHEAD_RING steps ahead of the device
+  if (s->host_step % RUNAHEAD_EVERY == 0) {
+    const int k = s->ahead_k;
+    if (s->ahead_used[k]) SCK(cudaEventSynchronize(s->ahead_ev[k]), "run-ahead wait");
+    SCK(cudaEventRecord(s->ahead_ev[k], s->stream), "run-ahead event");
+    s->ahead_used[k] = true;
+    s->ahead_k = (k + 1) % RUNAHEAD_RING;
+  }
+  *ran = 1;
   return retire(s, step);
+}
+
+}  // namespace
+
+extern "C" {
+
+int nat_server_step(nat_server* s) {
+  if (!s) return NAT_ERR_INVALID_ARG;
+  int ran;
+  return server_step(s, &ran);
+}
+
+int nat_server_run(nat_server* s, int max_steps, int* steps_done) {
+  if (!s || max_steps < 0) return NAT_ERR_INVALID_ARG;
+  int k = 0;
+  for (; k < max_steps; ++k) {
+    int ran = 0;
+    const int rc = server_step(s, &ran);
+    if (rc) {
+      if (steps_done) *steps_done = k;
+      return rc;
+    }
+    if (!ran) break;
+  }
+  if (steps_done) *steps_done = k;
+  return NAT_OK;
 }
 
 int nat_server_poll(nat_server* s, int64_t* ids, int max_ids, int* n_done, int wait) {

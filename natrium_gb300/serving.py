@@ -94,6 +94,7 @@ def _bind(L):
     L.nat_server_destroy.argtypes = [vp]
     L.nat_server_submit.argtypes = [vp, C.POINTER(_Request), C.POINTER(C.c_int64)]
     L.nat_server_step.argtypes = [vp]
+    L.nat_server_run.argtypes = [vp, C.c_int, C.POINTER(C.c_int)]
     L.nat_server_poll.argtypes = [vp, C.POINTER(C.c_int64), C.c_int, C.POINTER(C.c_int), C.c_int]
     L.nat_server_result.argtypes = [vp, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_int64), C.POINTER(C.c_int)]
@@ -150,6 +151,13 @@ class Server:
     def step(self):
         self._check(self._L.nat_server_step(self._h))
 
+    def run(self, max_steps: int) -> int:
+        """Up to max_steps server steps in one call; returns the number run
+        (fewer when no solve is live)."""
+        done = C.c_int()
+        self._check(self._L.nat_server_run(self._h, int(max_steps), C.byref(done)))
+        return done.value
+
     def poll(self, wait: bool = False, max_ids: int = 4096):
         ids = (C.c_int64 * max_ids)()
         n = C.c_int()
@@ -195,14 +203,19 @@ def workload(n: int = 512, seed: int = 0, rate: float = 200.0, steps_range=(50, 
     return arrivals, reqs
 
 
-def run_workload(arrivals, reqs, pool_bytes: int = 8 << 30, max_slots: int = 512):
+def run_workload(arrivals, reqs, pool_bytes: int = 8 << 30, max_slots: int = 512, steps_per_call: int = 8):
     """Replay the request stream in wall-clock time through one server.
-    Returns throughput and latency statistics."""
+    Requests are submitted as their arrival time passes; between checks the
+    server runs up to steps_per_call steps in one C call.  Returns throughput
+    (over the whole run, and over the arrival window: completions while
+    requests were still arriving) and latency statistics (arrival to result
+    on the host)."""
     lat = {}
     with Server(pool_bytes, max_slots) as srv:
         t0 = time.perf_counter()
         nxt = 0
         submit_t = {}
+        done_t = {}
         id2req = {}
         n = len(reqs)
         while len(lat) < n:
@@ -212,23 +225,26 @@ def run_workload(arrivals, reqs, pool_bytes: int = 8 << 30, max_slots: int = 512
                 submit_t[rid] = t0 + arrivals[nxt]
                 id2req[rid] = reqs[nxt]
                 nxt += 1
-            if srv.busy:
-                srv.step()
-            elif nxt < n:
+            ran = srv.run(steps_per_call) if srv.busy else 0
+            if not ran and nxt < n:
                 time.sleep(max(0.0, min(1e-3, arrivals[nxt] - now)))
             for rid in srv.poll(wait=False):
                 rho, u, st = srv.result_arrays(rid, id2req[rid].nodes)
                 if st != 0:
                     raise NatError(st, f"request {rid} failed")
+                done_t[rid] = time.perf_counter() - t0
                 lat[rid] = time.perf_counter() - submit_t[rid]
         wall = time.perf_counter() - t0
         stats = srv.stats()
     l = np.array(sorted(lat.values()))
-    first = float(arrivals[0])
+    first, last = float(arrivals[0]), float(arrivals[-1])
+    in_window = sum(1 for t in done_t.values() if t <= last)
     return {
         "solves": n,
         "wall_s": wall,
         "solves_per_s": n / (wall - first),
+        "solves_per_s_arrival_window": in_window / (last - first) if last > first else None,
+        "offered_per_s": (n - 1) / (last - first) if last > first else None,
         "latency_p50_s": float(np.percentile(l, 50)),
         "latency_p99_s": float(np.percentile(l, 99)),
         "node_updates_per_s": stats["node_updates"] / (wall - first),

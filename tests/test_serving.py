@@ -1,9 +1,12 @@
 """Continuous-batching server: each result is the same alone and in the
 mix, matches the single-solve path, and admission by HBM footprint works."""
+import math
+
 import numpy as np
 import pytest
 
 import natrium_gb300 as N
+import oracle as O
 from natrium_gb300 import problems as P
 from natrium_gb300.serving import INIT_SHEAR_LAYER, INIT_TAYLOR_GREEN, Request, Server, workload
 
@@ -116,3 +119,60 @@ def test_invalid_request_rejected(gpu_lib):
             srv.submit(Request("BGK_STANDARD", 9, (4, 4)))
         with pytest.raises(N.NatError):
             srv.submit(Request("BGK_STANDARD", 4, (4096, 4096)))  # larger than the pool
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("req", [Request("BGK_STANDARD", 3, (8, 8), steps=40, Ma=0.05, Re=500),
+                                 Request("KBC_STANDARD", 4, (4, 8), steps=30, Ma=0.08, Re=300)],
+                         ids=["bgk-p3-8x8", "kbc-p4-4x8"])
+def test_served_matches_oracle(gpu_lib, req):
+    """A served solve (FP32 deviation storage, in a mix with another request)
+    against the CPU oracle's FP64 run of the same request: the reference's
+    copy + CSR SpMV + collide per step from the same Taylor-Green equilibrium
+    (TaylorGreenVortex2D.cpp:36-59).  Relative L2 of u within 1e-6, of rho
+    within 1e-7."""
+    other = Request("BGK_STANDARD", 2, (16, 16), steps=60, init=INIT_SHEAR_LAYER, length=(1.0, 1.0), Re=2000)
+    with Server(1 << 30, 8) as srv:
+        rho_s, u_s, st = _run(srv, [req, other])[0]
+    assert st == 0
+    so = O.stencil("D2Q9", req.scaling)
+    mesh = O.Mesh(2, req.cells, req.order, False, (req.length[0], req.length[1], 1.0))
+    dt = O.time_step(mesh.h_min(), req.order, so.max_speed, req.cfl)
+    tau = req.viscosity / (dt * so.cs2) + 0.5
+    rho0, u0 = O.tgv2d_init(mesh.coords(), req.Ma, L=req.length[0])
+    f = O.equilibrium(so, rho0, np.ascontiguousarray(u0))
+    S = O.SLOperator(mesh, so, dt)
+    rho = np.zeros(mesh.n_nodes)
+    u = np.zeros((2, mesh.n_nodes))
+    for _ in range(req.steps):
+        f = S.stream(f)
+        O.collide(so, req.collision, tau, f, rho, u)
+    # oracle lattice (N p + 1 per axis) -> the served lattice (periodic duplicates folded)
+    nx, ny = req.cells[0] * req.order, req.cells[1] * req.order
+    keep = np.ones((ny + 1, nx + 1), bool)
+    keep[-1, :] = False
+    keep[:, -1] = False
+    k = keep.ravel()
+    r1, v1 = rho[k], u[:, k]
+    assert np.sqrt(np.sum((rho_s - r1) ** 2) / np.sum(r1 ** 2)) <= 1e-7
+    assert np.sqrt(np.sum((u_s - v1) ** 2) / np.sum(v1 ** 2)) <= 1e-6
+
+
+@pytest.mark.gpu
+def test_server_run_batches_steps(gpu_lib):
+    """nat_server_run advances several steps per call and gives the same
+    results as single steps."""
+    reqs = [Request("BGK_STANDARD", 3, (8, 8), steps=33), Request("KBC_STANDARD", 2, (8, 4), steps=17)]
+    with Server(1 << 30, 8) as srv:
+        single = _run(srv, reqs)
+    with Server(1 << 30, 8) as srv:
+        ids = [srv.submit(r) for r in reqs]
+        out = {}
+        while len(out) < len(ids):
+            if srv.busy:
+                assert srv.run(7) >= 0
+            for rid in srv.poll(wait=not srv.stats()["live"]):
+                out[rid] = srv.result_arrays(rid, reqs[ids.index(rid)].nodes)
+        batched = [out[i] for i in ids]
+    for a, b in zip(single, batched):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
