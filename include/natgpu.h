@@ -156,7 +156,10 @@ int nat_download_macro(nat_solver* s, double* rho_host, double* u_host);
  * asynchronous copy) must stay valid and are filled once nat_wait(ticket)
  * returns.  The device status word is read and cleared with it, so the
  * ticket carries the status of the steps enqueued since the previous read of
- * it.  Used to pipeline host I/O: the upload of the next f runs while this
+ * it.  The conversion to the reference layout runs on the handle's stream,
+ * the copies to the host on the handle's own read-back stream, so they
+ * overlap the steps enqueued after this call.
+ * Used to pipeline host I/O: the upload of the next f runs while this
  * read-back is in flight. */
 int nat_download_macro_async(nat_solver* s, double* rho_host, double* u_host,
                              uint64_t* ticket);

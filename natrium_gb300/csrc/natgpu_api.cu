@@ -962,6 +962,15 @@ int nat_destroy(nat_solver* s) {
     cudaStreamSynchronize(s->h2d);
     cudaStreamDestroy(s->h2d);
   }
+  if (s->d2h) {
+    cudaStreamSynchronize(s->d2h);
+    cudaStreamDestroy(s->d2h);
+  }
+  for (int k = 0; k < 2; ++k) {
+    if (s->rb_done[k]) cudaEventDestroy(s->rb_done[k]);
+    cudaFree(s->rb_stage[k]);
+  }
+  if (s->rb_ready) cudaEventDestroy(s->rb_ready);
   for (int k = 0; k < 2; ++k) {
     if (s->in_free[k]) {
       cudaEventSynchronize(s->in_free[k]);
@@ -1394,12 +1403,40 @@ int nat_download_macro_async(nat_solver* s, double* rho_host, double* u_host, ui
     s->tk_status[k] = 0;
     s->tk_held[k] = 0;
   }
-  int rc = enqueue_macro_readback(s, rho_host, u_host);
-  if (rc) return rc;
+  // read-back stream and staging slots, created on first use
+  if (!s->rb_ready) {
+    if (!s->d2h) CK(cudaStreamCreateWithFlags(&s->d2h, cudaStreamNonBlocking), "read-back stream");
+    for (int b = 0; b < 2; ++b) {
+      if (!s->rb_stage[b])
+        CK(cudaMalloc((void**)&s->rb_stage[b], sizeof(double) * (1 + s->D) * s->n_ref), "read-back staging");
+      if (!s->rb_done[b]) {
+        CK(cudaEventCreateWithFlags(&s->rb_done[b], cudaEventDisableTiming), "read-back events");
+        CK(cudaEventRecord(s->rb_done[b], s->d2h), "read-back events");
+      }
+    }
+    CK(cudaEventCreateWithFlags(&s->rb_ready, cudaEventDisableTiming), "read-back events");
+  }
+  const int b = (int)(t & 1);
+  // the slot's previous copies must have left it before it is refilled
+  CK(cudaStreamWaitEvent(s->stream, s->rb_done[b], 0), "read-back slot reuse");
+  Dims d = dims_of(s);
+  k_fields_to_ref<<<grid_for(s->n_ref), 256, 0, s->stream>>>(s->rho, s->rb_stage[b], d, 1);
+  k_fields_to_ref<<<grid_for(s->n_ref * s->D), 256, 0, s->stream>>>(s->u, s->rb_stage[b] + s->n_ref, d, s->D);
+  CK(cudaGetLastError(), "macro kernel");
+  s->launches += 2;
   // the status of the steps since the previous read of it, then cleared
   CK(cudaMemcpyAsync(&s->tk_status[k], s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream), "status read");
   CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "status clear");
-  CK(cudaEventRecord(s->tk_ev[k], s->stream), "ticket event");
+  // the copies to the host on the read-back stream, overlapping later steps
+  CK(cudaEventRecord(s->rb_ready, s->stream), "read-back event");
+  CK(cudaStreamWaitEvent(s->d2h, s->rb_ready, 0), "read-back order");
+  CK(cudaMemcpyAsync(rho_host, s->rb_stage[b], sizeof(double) * s->n_ref, cudaMemcpyDeviceToHost, s->d2h),
+     "download rho");
+  CK(cudaMemcpyAsync(u_host, s->rb_stage[b] + s->n_ref, sizeof(double) * s->D * s->n_ref, cudaMemcpyDeviceToHost,
+                     s->d2h),
+     "download u");
+  CK(cudaEventRecord(s->rb_done[b], s->d2h), "read-back done");
+  CK(cudaEventRecord(s->tk_ev[k], s->d2h), "ticket event");
   s->tk_held[k] = t;
   s->tk_next = t + 1;
   *ticket = t;

@@ -118,6 +118,14 @@ struct nat_solver {
   cudaEvent_t tk_ev[NTICKET] = {};
   unsigned long long tk_held[NTICKET] = {};  // ticket issued in each slot (0 none)
   int* tk_status = nullptr;                  // page-locked, NTICKET words
+  // The device-to-host copies of an asynchronous read-back run on their own
+  // stream (d2h) from one of two read-back staging slots (rb_stage, (1 + D)
+  // n_ref doubles each), so they overlap the next step on the handle's
+  // stream; rb_done[b] marks when slot b's copies have finished.
+  cudaStream_t d2h = nullptr;
+  double* rb_stage[2] = {nullptr, nullptr};
+  cudaEvent_t rb_done[2] = {nullptr, nullptr};
+  cudaEvent_t rb_ready = nullptr;
   unsigned long long tk_next = 1;            // next ticket; 0 is never issued
   int tk_lost = 0;
   // limit of each wait of the bulk-copy kernels for a copy (polls of the
