@@ -60,29 +60,53 @@ __host__ __device__ inline void tg_cell_vertices(const TrackGeom& g, const int* 
   }
 }
 
-// x(u) of the cell with vertices cv, and the Jacobian dx_r/du_a when J is
-// not null
-__host__ __device__ inline void tg_q1_map_v(int D, const double (*cv)[3], const double* u, double* x,
-                                            double (*J)[3]) {
+// The multilinear cell map in polynomial form, x(u) = c0 + u cu + v cv +
+// w cw + uv cuv + uw cuw + vw cvw + uvw cuvw (2-D: the first, u, v, uv
+// terms), coefficients from the vertices in the numbering bx + 2 by + 4 bz.
+struct Q1Coef {
+  double c[8][3];  // c0, cu, cv, cw, cuv, cuw, cvw, cuvw
+};
+
+__host__ __device__ inline void tg_q1_coef(int D, const double (*v)[3], Q1Coef& q) {
   for (int r = 0; r < 3; ++r) {
-    x[r] = 0.0;
-    if (J)
-      for (int a = 0; a < 3; ++a) J[r][a] = 0.0;
-  }
-  for (int k = 0; k < (1 << D); ++k) {
-    const int b[3] = {k & 1, (k >> 1) & 1, (k >> 2) & 1};
-    double phi = 1.0, dphi[3];
-    for (int a = 0; a < D; ++a) phi *= b[a] ? u[a] : 1.0 - u[a];
-    for (int a = 0; a < D; ++a) {
-      dphi[a] = b[a] ? 1.0 : -1.0;
-      for (int q = 0; q < D; ++q)
-        if (q != a) dphi[a] *= b[q] ? u[q] : 1.0 - u[q];
+    q.c[0][r] = v[0][r];
+    q.c[1][r] = v[1][r] - v[0][r];
+    q.c[2][r] = v[2][r] - v[0][r];
+    q.c[4][r] = (v[3][r] - v[2][r]) - (v[1][r] - v[0][r]);
+    if (D == 3) {
+      q.c[3][r] = v[4][r] - v[0][r];
+      q.c[5][r] = (v[5][r] - v[4][r]) - (v[1][r] - v[0][r]);
+      q.c[6][r] = (v[6][r] - v[4][r]) - (v[2][r] - v[0][r]);
+      q.c[7][r] = ((v[7][r] - v[6][r]) - (v[5][r] - v[4][r])) - ((v[3][r] - v[2][r]) - (v[1][r] - v[0][r]));
+    } else {
+      q.c[3][r] = q.c[5][r] = q.c[6][r] = q.c[7][r] = 0.0;
     }
-    const double* v = cv[k];
-    for (int r = 0; r < D; ++r) {
-      x[r] += phi * v[r];
-      if (J)
-        for (int a = 0; a < D; ++a) J[r][a] += dphi[a] * v[r];
+  }
+}
+
+// x(u), and the Jacobian dx_r/du_a when J is not null
+__host__ __device__ inline void tg_q1_map_c(int D, const Q1Coef& q, const double* u, double* x, double (*J)[3]) {
+  const double uu = u[0], vv = u[1], ww = D == 3 ? u[2] : 0.0;
+  const double uv = uu * vv, uw = uu * ww, vw = vv * ww, uvw = uv * ww;
+  for (int r = 0; r < 3; ++r) x[r] = 0.0;
+  if (J)
+    for (int r = 0; r < 3; ++r)
+      for (int a = 0; a < 3; ++a) J[r][a] = 0.0;
+  for (int r = 0; r < D; ++r) {
+    if (D == 2) {
+      x[r] = q.c[0][r] + uu * q.c[1][r] + vv * q.c[2][r] + uv * q.c[4][r];
+      if (J) {
+        J[r][0] = q.c[1][r] + vv * q.c[4][r];
+        J[r][1] = q.c[2][r] + uu * q.c[4][r];
+      }
+    } else {
+      x[r] = q.c[0][r] + uu * q.c[1][r] + vv * q.c[2][r] + ww * q.c[3][r] + uv * q.c[4][r] + uw * q.c[5][r] +
+             vw * q.c[6][r] + uvw * q.c[7][r];
+      if (J) {
+        J[r][0] = q.c[1][r] + vv * q.c[4][r] + ww * q.c[5][r] + vw * q.c[7][r];
+        J[r][1] = q.c[2][r] + uu * q.c[4][r] + ww * q.c[6][r] + uw * q.c[7][r];
+        J[r][2] = q.c[3][r] + uu * q.c[5][r] + vv * q.c[6][r] + uv * q.c[7][r];
+      }
     }
   }
 }
@@ -92,7 +116,9 @@ __host__ __device__ inline void tg_q1_map(const TrackGeom& g, const int* c, cons
                                           double (*J)[3]) {
   double cv[8][3];
   tg_cell_vertices(g, c, cv);
-  tg_q1_map_v(g.D, cv, u, x, J);
+  Q1Coef q;
+  tg_q1_coef(g.D, cv, q);
+  tg_q1_map_c(g.D, q, u, x, J);
 }
 
 __host__ __device__ inline double tg_det3(const double (*M)[3]) {
@@ -126,14 +152,19 @@ __host__ __device__ inline bool tg_solve(int D, const double (*J)[3], const doub
 // MappingQ1::transform_real_to_unit_cell): Newton's method from the cell
 // centre, each step halved (up to 12 times) until the residual decreases;
 // converged once a step is below 1e-14.  False when it cannot converge (the
-// reference's ExcTransformationFailed).  The cell's vertices are read once.
+// reference's ExcTransformationFailed).  The cell's map coefficients are
+// computed once per inverse.
 __host__ __device__ inline bool tg_q1_inverse(const TrackGeom& g, const int* c, const double* x, double* u) {
   const int D = g.D;
-  double cv[8][3];
-  tg_cell_vertices(g, c, cv);
+  Q1Coef q;
+  {
+    double cv[8][3];
+    tg_cell_vertices(g, c, cv);
+    tg_q1_coef(D, cv, q);
+  }
   double y[3], J[3][3], r[3] = {0, 0, 0}, res = 0.0;
   for (int a = 0; a < 3; ++a) u[a] = a < D ? 0.5 : 0.0;
-  tg_q1_map_v(D, cv, u, y, J);
+  tg_q1_map_c(D, q, u, y, J);
   for (int a = 0; a < D; ++a) {
     r[a] = y[a] - x[a];
     res += r[a] * r[a];
@@ -146,7 +177,7 @@ __host__ __device__ inline bool tg_q1_inverse(const TrackGeom& g, const int* c, 
     for (int k = 0; k <= 12; ++k, step *= 0.5) {
       double un[3] = {u[0], u[1], u[2]}, yn[3], Jn[3][3], rn[3] = {0, 0, 0}, rs = 0.0;
       for (int a = 0; a < D; ++a) un[a] = u[a] - step * du[a];
-      tg_q1_map_v(D, cv, un, yn, Jn);
+      tg_q1_map_c(D, q, un, yn, Jn);
       for (int a = 0; a < D; ++a) {
         rn[a] = yn[a] - x[a];
         rs += rn[a] * rn[a];
@@ -156,8 +187,8 @@ __host__ __device__ inline bool tg_q1_inverse(const TrackGeom& g, const int* c, 
           u[a] = un[a];
           r[a] = rn[a];
         }
-        for (int q = 0; q < 3; ++q)
-          for (int a = 0; a < 3; ++a) J[q][a] = Jn[q][a];
+        for (int row = 0; row < 3; ++row)
+          for (int a = 0; a < 3; ++a) J[row][a] = Jn[row][a];
         res = rs;
         ok = true;
         break;
