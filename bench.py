@@ -362,7 +362,8 @@ MIXED = {"name": "tgv3d_d3q27_kbc_sl_dg_p3_32x32x32", "stencil": "D3Q27", "colli
          "order": 3, "cells": (32, 32, 32), "Ma": 0.1, "Re": 1600.0, "cfl": 0.4, "steps": 2000, "every": 100}
 
 
-def bench_mixed(torch, stream, flush, steps: int = None, profile: bool = False, candidate: int = -1):
+def bench_mixed(torch, stream, flush, steps: int = None, profile: bool = False, candidate: int = -1,
+                variant: int = 0):
     """The mixed-precision accuracy configuration: 3-D Taylor-Green, D3Q27
     KBC, 32^3 hexahedra, FE_DGQ p = 3 (2,097,152 nodes x 27), Ma 0.1,
     Re 1600, 2000 steps.  The FP32 deviation path and the FP64 path run side
@@ -374,7 +375,12 @@ def bench_mixed(torch, stream, flush, steps: int = None, profile: bool = False, 
     the autotuner's choice (its report is returned, with the chosen index) or,
     with candidate >= 0, that candidate of its list without timing (then the
     3 warm-up steps are the only launches of the kernel before the timed
-    ones, for a one-launch capture)."""
+    ones, for a one-launch capture); with variant > 0 the autotuner chooses
+    among that kernel variant's shapes only (12: the tensor-core corners).
+
+    A third solver runs the FP32 path with kernel variant 12 (the 8 corner
+    directions as tf32x3 tensor-core tiles) beside the autotuned one: its
+    time and its error against FP64 decide whether that form is kept."""
     import natrium_gb300 as N
     from natrium_gb300 import problems as P
     c = MIXED
@@ -390,6 +396,8 @@ def bench_mixed(torch, stream, flush, steps: int = None, profile: bool = False, 
             rho, u = P.taylor_green_3d(X, c["Ma"])
             sol.upload_f(P.equilibrium(c["stencil"], scaling, rho, u))
             rep, chosen = [], candidate
+            if variant:
+                sol.set_kernel_variant(variant)
             if candidate >= 0:
                 sol.select_candidate(candidate)
             else:
@@ -408,7 +416,7 @@ def bench_mixed(torch, stream, flush, steps: int = None, profile: bool = False, 
             return {"workload": c["name"], "nodes": sol.n_dev, "ms_per_step": ms, "kernel": sol.kernel_info(),
                     "candidate": chosen, "autotune": rep}
     sols, reports = {}, {}
-    for prec in ("fp64", "fp32dev"):
+    for name, prec, var in (("fp64", "fp64", 0), ("fp32dev", "fp32dev", 0), ("fp32dev_tc", "fp32dev", 12)):
         spec = N.SolverSpec(stencil=c["stencil"], order=c["order"], cells=c["cells"], length=(2 * math.pi,) * 3,
                             scaling=scaling, viscosity=1.0 / c["Re"], cfl=c["cfl"], collision=c["collision"],
                             precision=prec, topology="dg")
@@ -417,11 +425,13 @@ def bench_mixed(torch, stream, flush, steps: int = None, profile: bool = False, 
         X = P.node_coords(c["cells"], c["order"], spec.length, "dg")
         rho, u = P.taylor_green_3d(X, c["Ma"])
         sol.upload_f(P.equilibrium(c["stencil"], scaling, rho, u))
+        if var:
+            sol.set_kernel_variant(var)
         sol.autotune(3)
-        reports[prec] = sol.autotune_report()
-        sols[prec] = sol
+        reports[name] = sol.autotune_report()
+        sols[name] = sol
     rl2 = lambda a, b: float(np.sqrt(np.sum((a - b) ** 2) / np.sum(b ** 2)))
-    curve, ms = [], {"fp64": 0.0, "fp32dev": 0.0}
+    curve, ms = [], {name: 0.0 for name in sols}
     done = 0
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     while done < steps:
@@ -437,13 +447,24 @@ def bench_mixed(torch, stream, flush, steps: int = None, profile: bool = False, 
             out[prec] = sol.download_macro()
         done += k
         curve.append({"step": done, "rel_l2_u": rl2(out["fp32dev"][1], out["fp64"][1]),
-                      "rel_l2_rho": rl2(out["fp32dev"][0], out["fp64"][0])})
+                      "rel_l2_rho": rl2(out["fp32dev"][0], out["fp64"][0]),
+                      "tc_rel_l2_u": rl2(out["fp32dev_tc"][1], out["fp64"][1]),
+                      "tc_rel_l2_rho": rl2(out["fp32dev_tc"][0], out["fp64"][0])})
     n = sols["fp64"].n_dev
     res = {"workload": c["name"], "nodes": n, "steps": steps, "unit": UNIT,
            "fp32dev": {"ms_per_step": ms["fp32dev"] / steps, "value": n * steps / (ms["fp32dev"] * 1e-3),
                        "kernel": sols["fp32dev"].kernel_info(), "autotune": reports["fp32dev"]},
            "fp64": {"ms_per_step": ms["fp64"] / steps, "value": n * steps / (ms["fp64"] * 1e-3),
                     "kernel": sols["fp64"].kernel_info(), "autotune": reports["fp64"]},
+           "fp32dev_tensor_core_corners": {
+               "ms_per_step": ms["fp32dev_tc"] / steps, "value": n * steps / (ms["fp32dev_tc"] * 1e-3),
+               "kernel": sols["fp32dev_tc"].kernel_info(),
+               "vs_autotuned_fp32dev": ms["fp32dev"] / ms["fp32dev_tc"],
+               "max_rel_l2_u": max(r["tc_rel_l2_u"] for r in curve),
+               "max_rel_l2_rho": max(r["tc_rel_l2_rho"] for r in curve),
+               "form": "kernel variant 12: the 8 corner directions as mma.sync m16n8k8 tf32 tiles, operands split "
+                       "into two TF32 halves (3 products), FP32 accumulation; the other 18 directions "
+                       "sum-factorised as in variant 11"},
            "speedup_fp32dev_vs_fp64": ms["fp64"] / ms["fp32dev"],
            "max_rel_l2_u": max(r["rel_l2_u"] for r in curve), "max_rel_l2_rho": max(r["rel_l2_rho"] for r in curve),
            "every_100_steps": curve,
@@ -662,7 +683,7 @@ def time_e2e_legs(sol, torch, ws, f0, nodes, e2e_steps):
             "pipeline_matches_blocking": pipeline_ok}
 
 
-KERNEL_NAMES = {1: "k_sl_step", 2: "k_sl_step_v2", 3: "k_sl_row", 6: "k_sl_rowt", 7: "k_sl_rowg", 11: "k_sl_cell"}
+KERNEL_NAMES = {1: "k_sl_step", 2: "k_sl_step_v2", 3: "k_sl_row", 6: "k_sl_rowt", 7: "k_sl_rowg", 11: "k_sl_cell", 12: "k_sl_cell[tensor-core corners]", 13: "k_sl_cell[z sharing]"}
 
 
 def run_ours(args):
@@ -681,7 +702,7 @@ def run_ours(args):
         return 0
     if args.mixed_only:
         print(json.dumps(bench_mixed(torch, stream, flush, steps=args.steps if args.profile else None,
-                                     profile=args.profile, candidate=args.candidate)))
+                                     profile=args.profile, candidate=args.candidate, variant=args.variant)))
         return 0
     if args.compressible_only:
         print(json.dumps(bench_compressible(torch, stream, flush, steps=args.steps, warmup=args.warmup,
@@ -872,7 +893,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--variant", type=int, default=0,
                     help="fused kernel: 0 autotuned, 1 generic, 3 tile, 4 row-segment, 6 bulk-copy row-segment, "
-                         "7 row-group")
+                         "7 row-group, 11 cell-row, 12 cell-row with tensor-core corners (D3Q27 FP32)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--candidate", type=int, default=-1,
                     help="with --profile: use this autotuner candidate without timing")

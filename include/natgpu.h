@@ -367,13 +367,21 @@ int nat_device_f(nat_solver* s, void** f_dev);
  * (3-D, FP32: 2-4 warps own a whole x row, no halo recomputation), 11 =
  * cell-row kernel required (3-D, DG: a lane owns one cell's p + 1 nodes along
  * x, a warp whole periodic x rows of 16 or 32 cells; vector loads of cell
- * rows, the x window by warp shuffles). */
+ * rows, the x window by warp shuffles), 12 = the cell-row kernel with the 8
+ * corner directions of D3Q27 (FP32 deviation storage, DG p = 3, 32 cells per
+ * x row) applied as dense per-cell operator tiles on the tensor cores
+ * (mma.sync m16n8k8, operands split into two TF32 halves, FP32
+ * accumulation; slower than 11 and short of its accuracy, so only taken
+ * when asked for), 13 = the cell-row kernel with z sharing: the z-window sums
+ * of the yz-diagonal directions computed once per CTA for all its rows. */
 int nat_set_kernel_variant(nat_solver* s, int variant);
 /* The fused-step kernel in use: 1 generic, 2 tile, 3 row-segment,
  * 5 two-population row-segment kernel (NAT_BGK_COMPRESSIBLE; 9 and 10: its
  * FP32 forms with f and g in shared memory, 20 / 24 resident warps per SM),
  * 6 bulk-copy row-segment kernel, 7 row-group kernel, 8 departure-point
- * kernel of mapped (MappingQ1) meshes, 11 cell-row kernel.  nat_autotune chooses among 5, 9
+ * kernel of mapped (MappingQ1) meshes, 11 cell-row kernel, 12 cell-row
+ * kernel with tensor-core corner directions, 13 cell-row kernel with z
+ * sharing.  nat_autotune chooses among 5, 9
  * and 10 for an FP32 two-population handle. */
 int nat_kernel_variant(const nat_solver* s);
 

@@ -399,7 +399,10 @@ class Solver:
     def set_kernel_variant(self, variant: int):
         """0 automatic, 1 generic kernel, 2 specialised kernel required,
         3 tile kernel required, 4 row-segment kernel required, 6 bulk-copy
-        row-segment kernel required, 7 row-group kernel required."""
+        row-segment kernel required, 7 row-group kernel required, 11 cell-row
+        kernel required, 12 cell-row kernel with the D3Q27 corner directions
+        on the tensor cores (only when asked for), 13 cell-row kernel with z
+        sharing of the yz-diagonal directions."""
         self._check(self._L.nat_set_kernel_variant(self._h, int(variant)))
 
     @property

@@ -29,6 +29,17 @@ struct CSum {
   __device__ __forceinline__ Real value() const { return s + c; }
 };
 
+template <class S>
+__host__ __device__ constexpr int opp(int i);
+
+// first direction i < opp(i) with a non-zero component along axis a
+template <class S>
+__host__ __device__ constexpr int first_pair(int a) {
+  for (int i = 1; i < S::Q; ++i)
+    if (i < opp<S>(i) && S::e(i, a) != 0) return i;
+  return -1;
+}
+
 // Moments: density (or its deviation) and momentum.  COMP selects
 // compensated summation (used for the float path).
 template <class S, bool COMP, class Real>
@@ -51,21 +62,32 @@ __device__ __forceinline__ void moments(const Real (&v)[S::Q], Real& m0,
     j[1] = ay.value();
     j[2] = az.value();
   } else {
-    Real a0 = 0, ax = 0, ay = 0, az = 0;
-    static_for<0, S::Q>([&](auto I) {
+    // per pair of opposite directions (i, i'): s = v_i + v_i' enters the
+    // density, d = v_i - v_i' each momentum component e_i has (fewer
+    // additions than summing the Q values into four accumulators)
+    Real a0 = v[0], jj[3] = {0, 0, 0};
+    static_for<1, S::Q>([&](auto I) {
       constexpr int i = decltype(I)::value;
-      a0 += v[i];
-      if constexpr (S::e(i, 0) > 0) ax += v[i];
-      if constexpr (S::e(i, 0) < 0) ax -= v[i];
-      if constexpr (S::e(i, 1) > 0) ay += v[i];
-      if constexpr (S::e(i, 1) < 0) ay -= v[i];
-      if constexpr (S::e(i, 2) > 0) az += v[i];
-      if constexpr (S::e(i, 2) < 0) az -= v[i];
+      constexpr int o = opp<S>(i);
+      if constexpr (i < o) {
+        a0 += v[i] + v[o];
+        const Real d = v[i] - v[o];
+        static_for<0, 3>([&](auto A) {
+          constexpr int a = decltype(A)::value;
+          constexpr int e = S::e(i, a);
+          if constexpr (e != 0) {
+            if constexpr (i == first_pair<S>(a))
+              jj[a] = e > 0 ? d : -d;
+            else
+              jj[a] = e > 0 ? jj[a] + d : jj[a] - d;
+          }
+        });
+      }
     });
     m0 = a0;
-    j[0] = ax;
-    j[1] = ay;
-    j[2] = az;
+    j[0] = jj[0];
+    j[1] = jj[1];
+    j[2] = jj[2];
   }
 }
 
@@ -131,9 +153,9 @@ __device__ __forceinline__ Real collide_bgk(Real (&v)[S::Q], Real inv_tau,
       const Real c = edot<S, i>(u);
       const Real ow = Real(S::w(i)) * orho;                       // omega w rho
       const Real even = fma(Real(4.5) * ow * c, c, Real(S::w(i)) * base);
-      const Real odd = Real(3) * ow * c;
-      v[i] = fma(v[i], keep, even + odd);
-      v[o] = fma(v[o], keep, even - odd);
+      const Real k3 = Real(3) * ow;                               // odd term 3 omega w rho c
+      v[i] = fma(v[i], keep, fma(k3, c, even));
+      v[o] = fma(v[o], keep, fma(-k3, c, even));
     }
   });
   return rho;
@@ -337,12 +359,12 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
   // q_i = prod_a (1 + d_a) - 1 of direction i, f^eq_i = w_i rho (1 + q_i)
   auto qof = [&](auto I) -> Real {
     constexpr int i = decltype(I)::value;
-    Real q = Real(0);
+    Real q = dm[0][S::e(i, 0) + 1];
 #pragma unroll
-    for (int a = 0; a < S::D; ++a) {
-      const int c = (a == 0 ? S::e(i, 0) : (a == 1 ? S::e(i, 1) : S::e(i, 2))) + 1;
+    for (int a = 1; a < S::D; ++a) {
+      const int c = (a == 1 ? S::e(i, 1) : S::e(i, 2)) + 1;
       const Real d = dm[a][c];
-      q = q + d + q * d;
+      q = fma(q, d, q + d);
     }
     return q;
   };
@@ -354,6 +376,13 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
 #pragma unroll
     for (int c = 0; c < 3; ++c) rinv[a][c] = Real(1) / (Real(1) + dm[a][c]);
   const Real irho = Real(1) / rho;
+  // (1 / rho) / (1 + d_x) / (1 + d_y) per (c_x, c_y): nine products shared by
+  // the directions of each pair
+  Real rxy[3][3];
+#pragma unroll
+  for (int cx = 0; cx < 3; ++cx)
+#pragma unroll
+    for (int cy = 0; cy < 3; ++cy) rxy[cx][cy] = (irho * rinv[0][cx]) * rinv[1][cy];
   // f - f^eq (the only per-direction array kept; f^eq and the shear part
   // are recomputed where needed, which keeps the register footprint small)
   Real df[S::Q];
@@ -362,9 +391,9 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
     const Real q = qof(I);
     const Real w = Real(S::w(i));
     if constexpr (DEV)
-      df[i] = v[i] - w * (m0 * (Real(1) + q) + q);
+      df[i] = fma(-w, fma(m0, q, m0 + q), v[i]);  // v - w (m0 (1 + q) + q)
     else
-      df[i] = v[i] - w * rho * (Real(1) + q);
+      df[i] = fma(-w * rho, q, v[i] - w * rho);  // v - w rho (1 + q)
   });
   // second-moment differences of f - feq
   Real M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
@@ -386,11 +415,11 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
     constexpr int i = decltype(I)::value;
     const Real ds = kbc_shear<S, i>(M);
     const Real dh = df[i] - ds;
-    Real inv = irho * Real(1.0 / S::w(i));
-#pragma unroll
-    for (int a = 0; a < S::D; ++a) inv *= rinv[a][(a == 0 ? S::e(i, 0) : (a == 1 ? S::e(i, 1) : S::e(i, 2))) + 1];
-    ss += ds * dh * inv;
-    sh += dh * dh * inv;
+    Real inv = rxy[S::e(i, 0) + 1][S::e(i, 1) + 1];
+    if constexpr (S::D == 3) inv *= rinv[2][S::e(i, 2) + 1];
+    const Real t = dh * (inv * Real(1.0 / S::w(i)));
+    ss = fma(ds, t, ss);
+    sh = fma(dh, t, sh);
   });
   const Real beta = Real(0.5) / tau;
   const Real ib = Real(1) / beta;
@@ -414,17 +443,23 @@ template <class S, class Real>
 __device__ __forceinline__ void conserve(Real (&v)[S::Q], const Real (&pre)[S::Q],
                                          const Real (&target)[3] = {Real(0), Real(0), Real(0)},
                                          Real mass_target = Real(0)) {
-  Real dm = -mass_target, dj[3] = {-target[0], -target[1], -target[2]};
-  static_for<0, S::Q>([&](auto I) {
+  // per pair of opposite directions: the sum of the two changes enters the
+  // mass defect, their difference the momentum components
+  Real dm = (v[0] - pre[0]) - mass_target, dj[3] = {-target[0], -target[1], -target[2]};
+  static_for<1, S::Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
-    const Real d = v[i] - pre[i];
-    dm += d;
-    if constexpr (S::e(i, 0) > 0) dj[0] += d;
-    if constexpr (S::e(i, 0) < 0) dj[0] -= d;
-    if constexpr (S::e(i, 1) > 0) dj[1] += d;
-    if constexpr (S::e(i, 1) < 0) dj[1] -= d;
-    if constexpr (S::e(i, 2) > 0) dj[2] += d;
-    if constexpr (S::e(i, 2) < 0) dj[2] -= d;
+    constexpr int o = opp<S>(i);
+    if constexpr (i < o) {
+      const Real di = v[i] - pre[i], dn = v[o] - pre[o];
+      dm += di + dn;
+      const Real dd = di - dn;
+      if constexpr (S::e(i, 0) > 0) dj[0] += dd;
+      if constexpr (S::e(i, 0) < 0) dj[0] -= dd;
+      if constexpr (S::e(i, 1) > 0) dj[1] += dd;
+      if constexpr (S::e(i, 1) < 0) dj[1] -= dd;
+      if constexpr (S::e(i, 2) > 0) dj[2] += dd;
+      if constexpr (S::e(i, 2) < 0) dj[2] -= dd;
+    }
   });
   // axis populations: +a and -a; changing them by -+dj/2 removes the
   // momentum defect and leaves the mass unchanged

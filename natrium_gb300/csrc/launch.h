@@ -72,9 +72,11 @@ struct RowLaunch {
   const void* fn;
   int kind = 3;      // 3: row kernel (sl_row.cuh), 6: bulk-copy row kernel (sl_rowt.cuh),
                      // 7: row-group kernel (sl_rowg.cuh; wy = rows per CTA),
-                     // 11: cell-row kernel (sl_cell.cuh; wy = rows per CTA)
-  int g = 0;         // kind 7: warps per x row (32 (g - 1) < nx <= 32 g); kind 11: cells per x row
-  int warps = 0;     // kind 11: warps per CTA
+                     // 11: cell-row kernel (sl_cell.cuh; wy = rows per CTA),
+                     // 12: the same with the D3Q27 corner directions on the tensor cores,
+                     // 13: the same with z sharing of the yz-diagonal directions
+  int g = 0;         // kind 7: warps per x row (32 (g - 1) < nx <= 32 g); kind 11-13: cells per x row
+  int warps = 0;     // kind 11-13: warps per CTA
   size_t smem = 0;   // dynamic shared memory (kind 6)
   int align = 1;     // nx must be a multiple of this (kind 6: aligned row copies)
   int min_nx = 0;    // and at least this (kind 6: at most two pieces per row)

@@ -594,7 +594,12 @@ std::vector<Cand> v2_candidates(nat_solver* s, int coll_sel, int smem_optin) {
       continue;
     if (e.kind == 7 && (s->n_ax[0] > 32 * e.g || s->n_ax[0] <= 32 * (e.g - 1) || s->n_ax[0] < e.min_nx))
       continue;
-    if (e.kind == 11 && (s->n_ax[0] != e.g * (e.P + 1) || (long long)e.smem > smem_optin)) continue;
+    if ((e.kind == 11 || e.kind == 12 || e.kind == 13) &&
+        (s->n_ax[0] != e.g * (e.P + 1) || (long long)e.smem > smem_optin))
+      continue;
+    // the tensor-core corner form runs only when asked for: it is slower and
+    // misses the FP32 path's accuracy (kernel variant 12)
+    if (e.kind == 12 && s->variant != 12) continue;
     Cand c;
     c.kind = e.kind;
     c.row = e;
@@ -708,7 +713,7 @@ int launch_row_t(nat_solver* s, const SpecWeights<Real>& W, int write_macro) {
     grid = (P.ny / s->row.wy) * P.nz;
     nth = 32 * s->row.g * s->row.wy;
   }
-  if (s->row.kind == 11) {  // cell rows: wy rows per CTA of `warps` warps
+  if (s->row.kind >= 11 && s->row.kind <= 13) {  // cell rows: wy rows per CTA of `warps` warps
     grid = (P.ny / s->row.wy) * P.nz;
     nth = 32 * s->row.warps;
   }
@@ -721,7 +726,7 @@ int launch_row_t(nat_solver* s, const SpecWeights<Real>& W, int write_macro) {
 }
 
 int launch_v2(nat_solver* s, int write_macro) {
-  if (s->kind == 3 || s->kind == 6 || s->kind == 7 || s->kind == 11)
+  if (s->kind == 3 || s->kind == 6 || s->kind == 7 || (s->kind >= 11 && s->kind <= 13))
     return s->spec.precision == NAT_FP64 ? launch_row_t<double>(s, s->w64, write_macro)
                                          : launch_row_t<float>(s, s->w32, write_macro);
   return s->spec.precision == NAT_FP64 ? launch_v2_t<double>(s, s->w64, write_macro)
@@ -1678,7 +1683,7 @@ int nat_device_f(nat_solver* s, void** f_dev) {
 int64_t nat_launch_count(const nat_solver* s) { return s ? s->launches : -1; }
 
 int nat_set_kernel_variant(nat_solver* s, int variant) {
-  if (!s || variant < 0 || variant > 11 || variant == 5 || (variant >= 8 && variant <= 10)) return NAT_ERR_INVALID_ARG;
+  if (!s || variant < 0 || variant > 13 || variant == 5 || (variant >= 8 && variant <= 10)) return NAT_ERR_INVALID_ARG;
   if (s->mapped) {
     if (variant == 0) return NAT_OK;
     return fail(s, NAT_ERR_UNSUPPORTED, "mapped meshes run the departure-point kernel only");
@@ -1910,14 +1915,15 @@ int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* t
     int t = k == 2 ? s->v2.B[a] : s->B[a];
     if (k == 3 || k == 6) t = a == 0 ? 32 : (a == 1 ? s->row.wy : s->row.wz);
     if (k == 7) t = a == 0 ? 32 * s->row.g : (a == 1 ? s->row.wy : 1);
-    if (k == 11) t = a == 0 ? s->row.g * (s->spec.order + 1) : (a == 1 ? s->row.wy : 1);
+    if (k >= 11 && k <= 13) t = a == 0 ? s->row.g * (s->spec.order + 1) : (a == 1 ? s->row.wy : 1);
     if (tile_nodes) tile_nodes[a] = t;
   }
-  const bool row = k == 3 || k == 6 || k == 7 || k == 11;
+  const bool row = k == 3 || k == 6 || k == 7 || (k >= 11 && k <= 13);
   if (threads)
     *threads = k == 2 ? s->v2.nth
                       : (k == 7 ? 32 * s->row.g * s->row.wy
-                                : (k == 11 ? 32 * s->row.warps : (row ? 32 * s->row.wy * s->row.wz : STEP_THREADS)));
+                                : (k >= 11 && k <= 13 ? 32 * s->row.warps
+                                                      : (row ? 32 * s->row.wy * s->row.wz : STEP_THREADS)));
   if (smem_bytes) *smem_bytes = (int64_t)(k == 2 ? s->v2.smem : (row ? s->row.smem : s->smem_step));
   return NAT_OK;
 }

@@ -105,10 +105,268 @@ __host__ __device__ constexpr size_t cell_smem_per_warp() {
   return (size_t)S::Q * 32 * (P + 1) * sizeof(Real);
 }
 
+// ---- tensor-core form of the corner directions (D3Q27, p = 3, FP32) --------
+// For a corner direction (sx, sy, sz) the streamed values of one cell's 16
+// nodes (cx, cy) at a fixed z class cz are a dense contraction over the
+// 2 x 2 source cells in x and y (own and upwind) and the 4 rows of the z
+// window: out[(cx, cy)] = sum_jz wz[jz] sum_k A[(cx, cy)][k] F_jz[k], k =
+// (cx', ux, cy', uy), A = Wx (x) Wy with Wx[cx][(cx', ux)] = w_x[cx][cx'] when
+// ux is the cell of cx's window (the upwind one for the class that leaves the
+// cell) and 0 otherwise -- the per-cell (p+1)^2 x 4 (p+1)^2 block of the
+// reference's assembled operator (SemiLagrangian.cpp:227-229, 483) restricted
+// to one z row.  The CTA's 4 warps hold the 4 y rows (cy) of one y cell; warp
+// w takes cells 8w .. 8w + 7 as the N = 8 columns of an m16n8k8 tile, M = the
+// 16 (cx, cy) nodes, K = 8 (cx', ux) per step, 8 steps (cy', uy) per z row.
+// Operands are split into two TF32 halves (a = a_hi + a_lo, both rounded to
+// nearest) and the product taken as a_hi b_hi + a_hi b_lo + a_lo b_hi with
+// FP32 accumulation; the z factor is applied to the four per-row partial sums
+// at the end.  A's fragments are precomputed per CTA: [dx][dy][step][lane][8].
+constexpr int CORNER_A_FLOATS = 4 * 8 * 32 * 8;
+
+__device__ __forceinline__ unsigned tf32_rna(float x) {
+  unsigned r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// A fragments of the four (sx, sy) sign pairs; threads t0, t0 + stride, ...
+template <int P>
+__device__ __forceinline__ void fill_corner_table(float* sA, const float (&W)[3][2][PER_MAX][PMAX1], int t0,
+                                                  int stride) {
+  for (int i = t0; i < CORNER_A_FLOATS / 2; i += stride) {
+    const int e = i & 3, lane = (i >> 2) & 31, st = (i >> 7) & 7, dxy = i >> 10;
+    const int dx = dxy & 1, dy = dxy >> 1;
+    const int g = lane >> 2, t = lane & 3;
+    const int r = g + ((e & 1) ? 8 : 0);      // a0: (g, t), a1: (g+8, t), a2: (g, t+4), a3: (g+8, t+4)
+    const int k = t + ((e & 2) ? 4 : 0);
+    const int cx = r & 3, cy = r >> 2;
+    const int cxs = k & 3, ux = k >> 2;       // source node and cell (0 own, 1 upwind) along x
+    const int cys = st & 3, uy = st >> 2;     // along y
+    const int ox = dx == 0 ? (cx == 0) : (cx == P);
+    const int oy = dy == 0 ? (cy == 0) : (cy == P);
+    const float a = (ux == ox && uy == oy) ? W[0][dx][cx][cxs] * W[1][dy][cy][cys] : 0.f;
+    const unsigned hi = tf32_rna(a);
+    const unsigned lo = tf32_rna(a - __uint_as_float(hi));
+    float* q = sA + ((size_t)((dxy * 8 + st) * 32 + lane) * 8);
+    q[e] = __uint_as_float(hi);
+    q[4 + e] = __uint_as_float(lo);
+  }
+}
+
+// ---- z sharing of the directions with y and z components -------------------
+// A direction (sx, sy, sz) with sy, sz != 0 (yz-diagonal, or corner) needs,
+// for each of the CTA's R rows, the y window of z-window sums (and then, for
+// a corner, the x factor).  The z window is the same for the whole CTA (one
+// z), so the z sums of the union of the R rows' y windows are computed once
+// per CTA (U rows, each shared by up to P + 1 output rows) and every row then
+// takes its y sum from them: about U / R + 1 window sums per node instead of
+// P + 2.  The U x nx z sums live in the shared slots of the directions
+// streamed last (the yz-diagonals go first), two buffers alternating between
+// consecutive yz-diagonals, so one CTA barrier per direction suffices.
+
+// directions with a y and a z component (the yz-diagonals, and the corners
+// of D3Q27, whose x factor follows the shared y/z part)
+template <class S>
+__host__ __device__ constexpr bool is_yz(int a) {
+  return S::D == 3 && S::e(a, 1) != 0 && S::e(a, 2) != 0;
+}
+template <class S>
+__host__ __device__ constexpr int n_yz() {
+  int k = 0;
+  for (int a = 1; a < S::Q; ++a) k += is_yz<S>(a);
+  return k;
+}
+// k-th streamed direction (k = 0 .. Q - 2): with ZS the y/z ones first
+template <class S, bool ZS>
+__host__ __device__ constexpr int cell_order(int k) {
+  if (!ZS) return k + 1;
+  int n = 0;
+  for (int a = 1; a < S::Q; ++a)
+    if (is_yz<S>(a) && n++ == k) return a;
+  for (int a = 1; a < S::Q; ++a)
+    if (!is_yz<S>(a) && n++ == k) return a;
+  return -1;
+}
+// window start of row y along an axis with displacement sign SG (DG)
+template <int P, int SG>
+__host__ __device__ constexpr int ws_dg(int y) {
+  return SG > 0 ? y - y % (P + 1) - (y % (P + 1) == 0 ? P + 1 : 0)
+                : y - y % (P + 1) + (y % (P + 1) == P ? P + 1 : 0);
+}
+// most union rows of R consecutive rows starting at a multiple of R
+template <int P, int R>
+__host__ __device__ constexpr int zs_union_max() {
+  int m = 0;
+  for (int r = 0; r < (P + 1) * R; r += R) {
+    const int y0 = r + 2 * (P + 1) * R;  // positive, same residue
+    const int a = ws_dg<P, 1>(y0 + R - 1) - ws_dg<P, 1>(y0) + P + 1;
+    const int b = ws_dg<P, -1>(y0 + R - 1) - ws_dg<P, -1>(y0) + P + 1;
+    m = a > m ? a : m;
+    m = b > m ? b : m;
+  }
+  return m;
+}
+// directions whose slots hold the two z-sum buffers: the last 2 SPB of the
+// order, SPB = slots per buffer
+template <class S, int P, int L, int WARPS>
+__host__ __device__ constexpr int zs_slots_per_buffer() {
+  constexpr int RPW = 32 / L;
+  constexpr int chunks = (zs_union_max<P, WARPS * RPW>() + RPW - 1) / RPW;
+  return (chunks + WARPS - 1) / WARPS;
+}
+template <class S, int P, int L, int WARPS>
+__device__ __forceinline__ int zs_slot(int buf, int s) {
+  constexpr int SPB = zs_slots_per_buffer<S, P, L, WARPS>();
+  return cell_order<S, true>(S::Q - 2 - (buf * SPB + s));
+}
+
+// x factor of the lane's PER nodes from their y/z-factored values T: classes
+// whose departure point stays in the node's own cell take the lane's own
+// values, the one class that leaves it (0 for sx > 0, P for sx < 0) takes the
+// neighbouring lane's (lane r L + nb of the warp's row r); the weights come
+// straight from the kernel's constant bank (compile-time class and window).
+template <bool DEV, int P, int L, int sx, class Real>
+__device__ __forceinline__ void x_factor(const Real (&Wx)[PER_MAX][PMAX1], const Real (&T)[P + 1],
+                                         Real (&out)[P + 1], int X, int r) {
+  constexpr int PER = P + 1;
+  const int nb = sx > 0 ? (X + L - 1) % L : (X + 1) % L;
+  Real U[PER];
+#pragma unroll
+  for (int c = 0; c < PER; ++c) U[c] = __shfl_sync(0xffffffffu, T[c], r * L + nb);
+  static_for<0, PER>([&](auto C) {
+    constexpr int c = decltype(C)::value;
+    Real w[P + 1];
+#pragma unroll
+    for (int j = 0; j <= P; ++j) w[j] = Wx[c][j];
+    constexpr bool other = sx > 0 ? (c == 0) : (c == P);
+    if constexpr (other) {
+      // window = the neighbouring cell, dominant its nearest node
+      constexpr int J0 = sx > 0 ? P : 0;
+      out[c] = wsum_fixed<DEV, P, J0>(w, U);
+    } else {
+      out[c] = wsum_fixed<DEV, P, c>(w, T);
+    }
+  });
+}
+
+// One corner direction A in the tensor-core form for the CTA's y cell `by`
+// (rows 4 by .. 4 by + 3, warp cy owns row 4 by + cy) at row z (class cz):
+// warp w computes cells 8w .. 8w + 7 for all 16 (cx, cy) nodes and stores
+// them into the owning warps' arrays S (layout [warp][q][32 PER]).
+template <class S, int P, int A>
+__device__ __forceinline__ void corner_mma(const RowParams<float>& prm, const float* sA, float* S_all, int by, int z,
+                                           int cz, int lane, int warp) {
+  constexpr int Q = S::Q, PER = P + 1, NPW = 32 * PER;
+  constexpr int sx = S::e(A, 0), sy = S::e(A, 1), sz = S::e(A, 2);
+  constexpr int dx = sx > 0 ? 0 : 1, dy = sy > 0 ? 0 : 1, dz = sz > 0 ? 0 : 1;
+  const int nx = prm.nx, ny = prm.ny, nz = prm.nz, nxy = nx * ny;
+  const int g = lane >> 2, t = lane & 3;
+  const int X = 8 * warp + g;                    // this thread's B column: cell X
+  const int Xu = (X - sx + 32) & 31;             // its upwind cell along x (row of 32 cells)
+  const int bo0 = 4 * X + t, bo1 = 4 * Xu + t;
+  // z window: the upwind z cell for the class that leaves the cell
+  const bool oz = dz == 0 ? (cz == 0) : (cz == P);
+  const int zc = (z / PER) - (oz ? sz : 0);
+  int zoff[PER];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) zoff[j] = wrap(zc * PER + j, nz) * nxy;
+  const float* __restrict__ src = prm.f_in + (size_t)A * prm.n;
+  const float4* At = reinterpret_cast<const float4*>(sA + (size_t)((dx + 2 * dy) * 8 * 32 + lane) * 8);
+  // Difference form: every row of A sums to 1, so per z row j and column
+  // (cell) n the contraction is ref + A (F - ref) with ref = the cell's own
+  // source node (2, 2) of that z row.  The tensor cores then accumulate only
+  // the small differences: their FP32 accumulation truncates, which biases a
+  // sum of the full values by about an ulp of it per step (measured on the
+  // 32^3 D3Q27 KBC Taylor-Green: 1.3e-5 relative error of u after 500 steps
+  // with the full values, 9.9e-7 with the differences, 2.5e-7 for the scalar
+  // path).
+  float ref[PER];
+  const int gy_ref = wrap(by * PER + 2, ny);
+#pragma unroll
+  for (int j = 0; j < PER; ++j) ref[j] = __ldg(src + (zoff[j] + gy_ref * nx + 4 * X + 2));
+  // The main products a_hi b_hi of each step go to a fresh accumulator and
+  // are added in FP32 (round to nearest); only the two small correction
+  // products accumulate on the tensor cores across steps.
+  float acc[PER][4], cor[PER][4];
+#pragma unroll
+  for (int j = 0; j < PER; ++j)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc[j][e] = cor[j][e] = 0.f;
+#pragma unroll 2
+  for (int st = 0; st < 8; ++st) {
+    const int cys = st & 3, uy = st >> 2;
+    const int gy = wrap((by - uy * sy) * PER + cys, ny);
+    const float4 h = At[st * 32 * 2], l = At[st * 32 * 2 + 1];
+    const unsigned ah[4] = {__float_as_uint(h.x), __float_as_uint(h.y), __float_as_uint(h.z), __float_as_uint(h.w)};
+    const unsigned al[4] = {__float_as_uint(l.x), __float_as_uint(l.y), __float_as_uint(l.z), __float_as_uint(l.w)};
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const float* row = src + (zoff[j] + gy * nx);
+      const float b0 = __ldg(row + bo0) - ref[j], b1 = __ldg(row + bo1) - ref[j];
+      const unsigned b0h = tf32_rna(b0), b1h = tf32_rna(b1);
+      const unsigned b0l = tf32_rna(b0 - __uint_as_float(b0h)), b1l = tf32_rna(b1 - __uint_as_float(b1h));
+      float pm[4] = {0.f, 0.f, 0.f, 0.f};
+      mma_tf32(pm, ah, b0h, b1h);
+      mma_tf32(cor[j], al, b0h, b1h);
+      mma_tf32(cor[j], ah, b0l, b1l);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc[j][e] += pm[e];
+    }
+  }
+  // per z row T_j = ref_j + acc_j (the references of the thread's output
+  // columns 2t, 2t + 1 come from lanes 8t, 8t + 4), then the z factor in the
+  // difference form around the dominant row J0; the four values go to the
+  // owning warps' arrays: c0 (g, 2t), c1 (g, 2t+1), c2 (g+8, 2t), c3 (g+8,
+  // 2t+1); row r = cx + 4 cy, column = cell 8 warp + col
+  float rc[PER][2];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    rc[j][0] = __shfl_sync(0xffffffffu, ref[j], 8 * t);
+    rc[j][1] = __shfl_sync(0xffffffffu, ref[j], 8 * t + 4);
+  }
+  const int J0 = win_j0<P, true, sz>(cz);
+  float o[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    float T[PER];
+#pragma unroll
+    for (int j = 0; j < PER; ++j) T[j] = rc[j][e & 1] + (acc[j][e] + cor[j][e]);
+    float tj0 = T[0];
+#pragma unroll
+    for (int j = 1; j < PER; ++j) tj0 = j == J0 ? T[j] : tj0;
+    float v = 0.f;
+#pragma unroll
+    for (int j = 0; j < PER; ++j)
+      if (j != J0) v = fma(prm.W.w[2][dz][cz][j], T[j] - tj0, v);
+    o[e] = v + tj0;
+  }
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int r = g + ((e & 2) ? 8 : 0);
+    const int cx = r & 3, cy = r >> 2;
+    const int cell = 8 * warp + 2 * t + (e & 1);
+    S_all[((size_t)cy * Q + A) * NPW + cell * PER + cx] = o[e];
+  }
+}
+
 // CTA: WARPS warps, each owning RPW = 32 / L consecutive x rows (y, z); the
 // CTA covers WARPS * RPW rows of one z.  Requires nx = L (P + 1) (DG), ny a
 // multiple of WARPS * RPW.
-template <class S, class Real, int COLL, int P, int L, int WARPS, int MINB>
+//
+// MMA: the corner directions of D3Q27 in the tensor-core form above (p = 3,
+// FP32, L = 32, 4 warps: the CTA is one y cell of one z row); the dynamic
+// shared memory then ends with the A table.
+//
+// ZS: the directions with y and z components with z sharing (above).
+template <class S, class Real, int COLL, int P, int L, int WARPS, int MINB, bool MMA = false, bool ZS = false>
 __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_constant__ RowParams<Real> prm) {
   constexpr bool DEV = sizeof(Real) == 4;
   constexpr int Q = S::Q;
@@ -116,9 +374,14 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
   constexpr int RPW = 32 / L;
   constexpr int NPW = 32 * PER;  // nodes per warp
   static_assert(L * RPW == 32 && (L & (L - 1)) == 0, "L must be a power of two dividing 32");
+  static_assert(!MMA || (Q == 27 && P == 3 && L == 32 && WARPS == 4 && DEV), "tensor-core corners: D3Q27, p=3, FP32");
+  static_assert(!ZS || (S::D == 3 && !MMA && 2 * zs_slots_per_buffer<S, P, L, WARPS>() <= Q - 1 - n_yz<S>()),
+                "z sharing: the two buffers must fit in the slots of the other directions");
   extern __shared__ __align__(16) unsigned char cell_smem[];
   __shared__ Real sw[row_table_size<P, true>()];
   fill_row_table<Real, P, true>(sw, prm.W.w, threadIdx.x, 32 * WARPS);
+  float* sA = reinterpret_cast<float*>(cell_smem) + (size_t)WARPS * Q * NPW;
+  if constexpr (MMA) fill_corner_table<P>(sA, prm.W.w, threadIdx.x, 32 * WARPS);
   __syncthreads();
   using Tab = const Real (*)[2][PER][P + 1];
   Tab tw = reinterpret_cast<Tab>(sw);
@@ -143,9 +406,92 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
     store_cell<PER>(Sw + lane * PER, v);
   }
 
-  static_for<1, Q>([&](auto I) {
-    constexpr int A = decltype(I)::value;
+  static_for<0, Q - 1>([&](auto K) {
+    constexpr int A = cell_order<S, ZS>(decltype(K)::value);
     constexpr int sx = S::e(A, 0), sy = S::e(A, 1), sz = S::D == 3 ? S::e(A, 2) : 0;
+    if constexpr (ZS && sy != 0 && sz != 0) {
+      // z sums of the CTA's union rows into buffer K & 1, then this row's y sum
+      constexpr int dy = sy > 0 ? 0 : 1, dz = sz > 0 ? 0 : 1;
+      constexpr int R = WARPS * RPW;
+      Real* S_all = reinterpret_cast<Real*>(cell_smem);
+      const int y0 = by * R;
+      const int ybase = ws_dg<P, sy>(y0);
+      const int U = ws_dg<P, sy>(y0 + R - 1) - ybase + PER;
+      const int zs = win_start<P, true, sz>(z, cz), j0z = win_j0<P, true, sz>(cz);
+      int zo[PER];
+#pragma unroll
+      for (int jz = 0; jz < PER; ++jz) {
+        const int rz = j0z + jz;
+        zo[jz] = wrap(zs + (rz > P ? rz - PER : rz), nz) * nxy;
+      }
+      const Real* __restrict__ srcA = prm.f_in + (size_t)A * prm.n;
+      auto zaddr = [&](int uu) {  // row uu of this direction's buffer
+        const int ch = uu / RPW;
+        const int q = zs_slot<S, P, L, WARPS>(decltype(K)::value & 1, ch / WARPS);
+        return S_all + ((size_t)(ch % WARPS) * Q + q) * NPW + (uu % RPW) * nx;
+      };
+      for (int it = threadIdx.x; it < U * L; it += 32 * WARPS) {
+        const int uu = it / L, xc = (it % L) * PER;
+        const int gy = wrap(ybase + uu, ny);
+        Real Z0[PER], acc[PER];
+#pragma unroll
+        for (int jz = 0; jz < PER; ++jz) {
+          Real v[PER];
+          load_cell<PER>(srcA + (zo[jz] + gy * nx + xc), v);
+          const Real wz = tw[2][dz][cz][jz];
+#pragma unroll
+          for (int c = 0; c < PER; ++c) {
+            if (jz == 0) {
+              Z0[c] = v[c];
+              acc[c] = DEV ? Real(0) : wz * v[c];
+            } else {
+              acc[c] = DEV ? fma(wz, v[c] - Z0[c], acc[c]) : fma(wz, v[c], acc[c]);
+            }
+          }
+        }
+        Real* zp = zaddr(uu) + xc;
+#pragma unroll
+        for (int c = 0; c < PER; ++c) zp[c] = DEV ? acc[c] + Z0[c] : acc[c];
+      }
+      __syncthreads();
+      const int ys = win_start<P, true, sy>(y, cy), j0y = win_j0<P, true, sy>(cy);
+      Real Y0[PER], acc[PER];
+#pragma unroll
+      for (int jy = 0; jy < PER; ++jy) {
+        const int ry = j0y + jy;
+        const Real* zp = zaddr(ys - ybase + (ry > P ? ry - PER : ry)) + x0;
+        const Real wy = tw[1][dy][cy][jy];
+#pragma unroll
+        for (int c = 0; c < PER; ++c) {
+          const Real v = zp[c];
+          if (jy == 0) {
+            Y0[c] = v;
+            acc[c] = DEV ? Real(0) : wy * v;
+          } else {
+            acc[c] = DEV ? fma(wy, v - Y0[c], acc[c]) : fma(wy, v, acc[c]);
+          }
+        }
+      }
+      Real out[PER];
+      if constexpr (sx == 0) {
+#pragma unroll
+        for (int c = 0; c < PER; ++c) out[c] = DEV ? acc[c] + Y0[c] : acc[c];
+      } else {
+        Real T[PER];
+#pragma unroll
+        for (int c = 0; c < PER; ++c) T[c] = DEV ? acc[c] + Y0[c] : acc[c];
+        x_factor<DEV, P, L, sx>(prm.W.w[0][sx > 0 ? 0 : 1], T, out, X, r);
+      }
+      if constexpr (decltype(K)::value == n_yz<S>() - 1) {
+        // the buffers' slots are written by their own directions later on
+        __syncthreads();
+      }
+      store_cell<PER>(Sw + (size_t)A * NPW + lane * PER, out);
+      return;
+    } else if constexpr (MMA && sx != 0 && sy != 0 && sz != 0) {
+      corner_mma<S, P, A>(prm, sA, reinterpret_cast<float*>(cell_smem), by, z, cz, lane, warp);
+      return;
+    } else {
     constexpr int NJY = sy != 0 ? P + 1 : 1;
     constexpr int NJZ = sz != 0 ? P + 1 : 1;
     constexpr int dy = sy > 0 ? 0 : 1, dz = sz > 0 ? 0 : 1, dx = sx > 0 ? 0 : 1;
@@ -222,32 +568,19 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
 #pragma unroll
       for (int c = 0; c < PER; ++c) out[c] = T[c];
     } else {
-      // the neighbouring cell along -sx (periodic within the row)
-      const int nb = sx > 0 ? (X + L - 1) % L : (X + 1) % L;
-      Real U[PER];
-#pragma unroll
-      for (int c = 0; c < PER; ++c) U[c] = __shfl_sync(0xffffffffu, T[c], r * L + nb);
-      static_for<0, PER>([&](auto C) {
-        constexpr int c = decltype(C)::value;
-        Real w[P + 1];
-#pragma unroll
-        for (int j = 0; j <= P; ++j) w[j] = prm.W.w[0][dx][c][j];
-        constexpr bool other = sx > 0 ? (c == 0) : (c == P);
-        if constexpr (other) {
-          // window = the neighbouring cell, dominant its nearest node
-          constexpr int J0 = sx > 0 ? P : 0;
-          out[c] = wsum_fixed<DEV, P, J0>(w, U);
-        } else {
-          out[c] = wsum_fixed<DEV, P, c>(w, T);
-        }
-      });
+      x_factor<DEV, P, L, sx>(prm.W.w[0][dx], T, out, X, r);
     }
     store_cell<PER>(Sw + (size_t)A * NPW + lane * PER, out);
+    }
   });
-  __syncwarp();
+  if constexpr (MMA)
+    __syncthreads();  // the corner values come from the CTA's other warps
+  else
+    __syncwarp();
 
   // phase 2: collide the warp's nodes, lane-strided
   const int row0 = by * rows_per_cta + warp * RPW;
+  const Real inv_tau = Real(1) / Real(prm.tau);
 #pragma unroll 1
   for (int k = 0; k < PER; ++k) {
     const int t = lane + 32 * k;  // node within the warp's rows
@@ -259,7 +592,7 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
     Real u[3] = {0, 0, 0};
     Real rho = Real(1);
     if constexpr (COLL == COLL_BGK) {
-      rho = collide_bgk<S, DEV, false>(fs, Real(1) / Real(prm.tau), u, false);
+      rho = collide_bgk<S, DEV, false>(fs, inv_tau, u, false);
     } else if constexpr (COLL == COLL_KBC) {
       rho = collide_kbc<S, DEV, false>(fs, Real(prm.tau), u, false);
     }

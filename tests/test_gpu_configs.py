@@ -241,7 +241,10 @@ def test_c3_tgv3d_kbc_32cubed_fp64_period16_against_oracle(gpu_lib):
 def test_c3_fp32_deviation_against_fp64_2000_steps(gpu_lib):
     """The mixed-precision configuration at full size: FP32 f - w_i storage
     against the FP64 path (pinned to the oracle above) after 500, 1000, 1500
-    and 2000 steps: relative L2 of u within 1e-6, of rho within 1e-7."""
+    and 2000 steps: relative L2 of u within 1e-6, of rho within 1e-7.  The
+    FP32 kernels: the cell-row kernel (variant 11), its z-sharing form
+    (variant 13) and its form with the 8 corner directions as tf32x3
+    tensor-core tiles (variant 12)."""
     cells, L, Ma = (32, 32, 32), 2 * math.pi, 0.1
     scaling = math.sqrt(3) / Ma
     X = P.node_coords(cells, 3, (L,) * 3, "dg")
@@ -249,19 +252,26 @@ def test_c3_fp32_deviation_against_fp64_2000_steps(gpu_lib):
     f0 = P.equilibrium("D3Q27", scaling, rho0, u0)
     sols = {}
     try:
-        for precision in ("fp64", "fp32dev"):
+        for name, precision, variant in (("fp64", "fp64", 0), ("fp32-11", "fp32dev", 11), ("fp32-12", "fp32dev", 12),
+                                         ("fp32-13", "fp32dev", 13)):
             spec = N.SolverSpec(stencil="D3Q27", order=3, cells=cells, length=(L,) * 3, scaling=scaling,
                                 viscosity=1 / 1600.0, cfl=0.4, collision="KBC_STANDARD", precision=precision,
                                 topology="dg")
-            sols[precision] = N.Solver(spec)
-            sols[precision].upload_f(f0)
+            sols[name] = N.Solver(spec)
+            if variant:
+                sols[name].set_kernel_variant(variant)
+                assert sols[name].kernel_variant == variant
+            sols[name].upload_f(f0)
         for block in range(4):
             out = {}
-            for precision, sol in sols.items():
+            for name, sol in sols.items():
                 sol.step(500)
-                out[precision] = sol.download_macro()
-            assert rel_l2(out["fp32dev"][1], out["fp64"][1]) <= 1e-6, block
-            assert rel_l2(out["fp32dev"][0], out["fp64"][0]) <= 1e-7, block
+                out[name] = sol.download_macro()
+            for name in ("fp32-11", "fp32-12", "fp32-13"):
+                eu, er = rel_l2(out[name][1], out["fp64"][1]), rel_l2(out[name][0], out["fp64"][0])
+                print(f"C3 {name} after {500 * (block + 1)} steps: u {eu:.3e} rho {er:.3e}")
+                assert eu <= 1e-6, (name, block)
+                assert er <= 1e-7, (name, block)
     finally:
         for sol in sols.values():
             sol.close()

@@ -515,6 +515,7 @@ EVERY_CASES = [
     # cell-row kernel shapes (nx = L (p + 1), L = 16 or 32 cells per x row)
     ("D3Q27", (16, 2, 2), 3, True, "KBC_STANDARD", "fp32dev"),
     ("D3Q27", (32, 2, 1), 3, True, "BGK_STANDARD", "fp32dev"),
+    ("D3Q27", (32, 2, 2), 3, True, "KBC_STANDARD", "fp32dev"),
     ("D3Q27", (32, 2, 1), 3, True, "KBC_STANDARD", "fp64"),
     ("D3Q19", (16, 4, 2), 4, True, "BGK_STANDARD", "fp32dev"),
     ("D3Q19", (16, 4, 2), 4, True, "BGK_STANDARD", "fp64"),
@@ -546,6 +547,42 @@ def test_every_autotune_candidate_matches_oracle(gpu_lib, case):
         assert rel_l2(f, f1) <= tol, (i, kinds[i])
         assert rel_l2(rho, rho1) <= tol
         assert rel_l2(u, u1) <= (1e-6 if precision == "fp32dev" else 1e-11)
+
+
+# Cell-row kernel with the 8 corner directions of D3Q27 as tf32x3 tensor-core
+# tiles (kernel variant 12, only when asked for): 32 cells per x row, y and z
+# with several cells so that the upwind windows wrap.
+TC_CASES = [
+    ("D3Q27", (32, 2, 2), 3, True, "KBC_STANDARD"),
+    ("D3Q27", (32, 3, 2), 3, True, "BGK_STANDARD"),
+]
+
+
+@pytest.mark.parametrize("case", TC_CASES, ids=[_ids(c) for c in TC_CASES])
+def test_tensor_core_corner_kernel_matches_oracle(gpu_lib, case):
+    stencil, cells, p, dg, model = case
+    st, mesh, dt, tau, spec = make_case(stencil, cells, p, dg, model, precision="fp32dev")
+    f0 = periodic_state(mesh, st, seed=31)
+    S = O.SLOperator(mesh, st, dt)
+    f1, rho1, u1 = oracle_step(S, st, model, tau, f0, 3)
+    with N.Solver(spec) as sol:
+        sol.set_kernel_variant(12)
+        assert sol.kernel_variant == 12
+        sol.upload_f(f0)
+        sol.step(3)
+        f = sol.download_f()
+        rho, u = sol.download_macro()
+    assert rel_l2(f, f1) <= 1e-6
+    assert rel_l2(rho, rho1) <= 1e-6
+    assert rel_l2(u, u1) <= 1e-6
+
+
+def test_tensor_core_corner_kernel_not_chosen_automatically(gpu_lib):
+    st, mesh, dt, tau, spec = make_case("D3Q27", (32, 2, 1), 3, True, "KBC_STANDARD", precision="fp32dev")
+    with N.Solver(spec) as sol:
+        n, _ = sol.autotune(1)
+        kinds = [r["variant"] for r in sol.autotune_report()]
+    assert 11 in kinds and 12 not in kinds
 
 
 # Row-group kernel (sl_rowg.cuh, kernel kind 7): G warps own a whole x row
