@@ -281,17 +281,19 @@ __device__ __forceinline__ void corner_mma(const RowParams<float>& prm, const fl
   const float* __restrict__ src = prm.f_in + (size_t)A * prm.n;
   const float4* At = reinterpret_cast<const float4*>(sA + (size_t)((dx + 2 * dy) * 8 * 32 + lane) * 8);
   // Difference form: every row of A sums to 1, so per z row j and column
-  // (cell) n the contraction is ref + A (F - ref) with ref = the cell's own
-  // source node (2, 2) of that z row.  The tensor cores then accumulate only
-  // the small differences: their FP32 accumulation truncates, which biases a
-  // sum of the full values by about an ulp of it per step (measured on the
-  // 32^3 D3Q27 KBC Taylor-Green: 1.3e-5 relative error of u after 500 steps
-  // with the full values, 9.9e-7 with the differences, 2.5e-7 for the scalar
-  // path).
+  // (cell) n the contraction is ref + A (F - ref) with ref = the source value
+  // in the middle of the 2 x 2 cell window of that z row (the own cell's
+  // corner node that faces the upwind cells), so that the differences take
+  // both signs.  The tensor cores then accumulate only the small
+  // differences: their FP32 accumulation truncates, which biases a sum of the
+  // full values by about an ulp of it per step (measured on the 32^3 D3Q27
+  // KBC Taylor-Green: 1.3e-5 relative error of u after 500 steps with the
+  // full values, 9.9e-7 with the differences, 2.5e-7 for the scalar path).
   float ref[PER];
-  const int gy_ref = wrap(by * PER + 2, ny);
+  const int gy_ref = wrap(by * PER + (sy > 0 ? 0 : P), ny);
+  const int gx_ref = 4 * X + (sx > 0 ? 0 : P);
 #pragma unroll
-  for (int j = 0; j < PER; ++j) ref[j] = __ldg(src + (zoff[j] + gy_ref * nx + 4 * X + 2));
+  for (int j = 0; j < PER; ++j) ref[j] = __ldg(src + (zoff[j] + gy_ref * nx + gx_ref));
   // The main products a_hi b_hi of each step go to a fresh accumulator and
   // are added in FP32 (round to nearest); only the two small correction
   // products accumulate on the tensor cores across steps.
