@@ -353,7 +353,10 @@ int nat_write_vtu(nat_solver* s, const char* path);
 int nat_mapped_rows(nat_solver* s, int where, int32_t* base, void* u, void* c, uint8_t* flags);
 
 /* Device pointers of the current distribution buffer (Q blocks of n_dev
- * values, double for NAT_FP64 and float (f - w_i) for NAT_FP32_DEV). */
+ * values, double for NAT_FP64 and float (f - w_i) for NAT_FP32_DEV).  The
+ * buffer changes with every step and every nat_upload_f (which converts into
+ * a spare buffer on its own streams and then makes it the current one), so
+ * the pointer is valid until the next of those calls. */
 int nat_device_f(nat_solver* s, void** f_dev);
 
 /* Kernel choice for the fused step: 0 = automatic (a specialised kernel --

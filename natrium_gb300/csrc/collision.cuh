@@ -337,24 +337,31 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
   Real m0, j[3];
   moments<S, COMP>(v, m0, j);
   const Real rho = DEV ? (Real(1) + m0) : m0;
+  const Real irho = Real(1) / rho;
   if (!given_u) {
-    const Real inv = Real(1) / rho;
-    u[0] = j[0] * inv;
-    u[1] = j[1] * inv;
-    u[2] = (S::D == 3) ? j[2] * inv : Real(0);
+    u[0] = j[0] * irho;
+    u[1] = j[1] * irho;
+    u[2] = (S::D == 3) ? j[2] * irho : Real(0);
   }
   // per axis: factor - 1 for c = -1, 0, +1 (stable small-number form of
-  // base = 2 - sqrt(1 + 3u^2), post = (2u + sqrt(1+3u^2)) / (1 - u))
-  Real dm[3][3];
+  // base = 2 - sqrt(1 + 3u^2), post = (2u + sqrt(1+3u^2)) / (1 - u)), and
+  // the reciprocals of the factors, 1 / base, 1 / (base post), post / base,
+  // from the two reciprocals 1 / base and 1 / post
+  Real dm[3][3], rinv[3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const Real ua = u[a];
     const Real s = sqrt(Real(1) + Real(3) * ua * ua);
     const Real sm1 = Real(3) * ua * ua / (Real(1) + s);  // s - 1
     const Real pm1 = (Real(3) * ua + sm1) / (Real(1) - ua);  // post - 1
+    const Real rb = Real(1) / (Real(1) - sm1);             // 1 / base
+    const Real ip = Real(1) / (Real(1) + pm1);             // 1 / post
     dm[a][1] = -sm1;                                       // base - 1
     dm[a][2] = pm1 - sm1 - sm1 * pm1;                      // base*post - 1
-    dm[a][0] = (-sm1 - pm1) / (Real(1) + pm1);             // base/post - 1
+    dm[a][0] = (-sm1 - pm1) * ip;                          // base/post - 1
+    rinv[a][1] = rb;
+    rinv[a][2] = rb * ip;
+    rinv[a][0] = (Real(1) + pm1) * rb;
   }
   // q_i = prod_a (1 + d_a) - 1 of direction i, f^eq_i = w_i rho (1 + q_i)
   auto qof = [&](auto I) -> Real {
@@ -368,14 +375,8 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
     }
     return q;
   };
-  // 1 / f^eq_i = (1 / (w_i rho)) prod_a 1 / (1 + d_a): nine reciprocals
-  // instead of one division per direction
-  Real rinv[3][3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) rinv[a][c] = Real(1) / (Real(1) + dm[a][c]);
-  const Real irho = Real(1) / rho;
+  // 1 / f^eq_i = (1 / (w_i rho)) prod_a 1 / (1 + d_a) from the per-axis
+  // reciprocals above instead of one division per direction;
   // (1 / rho) / (1 + d_x) / (1 + d_y) per (c_x, c_y): nine products shared by
   // the directions of each pair
   Real rxy[3][3];

@@ -281,25 +281,47 @@ int build_tables(nat_solver* s, const HostStencil& hs) {
 
 // ---- conversion / reduction kernels ---------------------------------------
 
+// Layout conversions.  Grid: (chunks of one z plane, z, component); the
+// index arithmetic inside a plane is 32-bit (one division by the row length
+// per element), which keeps these copies memory-bound.
+//   device layout:    [comp][z][y][x], nx * ny * nz per component
+//   reference layout: [comp][z][y][x] over rx * ry * rz (FE_Q: the periodic
+//                     duplicate layer included, rx <= nx + 1, ...)
+
+__host__ __forceinline__ dim3 plane_grid(long long plane, int planes, int comps) {
+  long long gx = (plane + 1023) / 1024;  // 256 threads, about 4 elements each
+  if (gx < 1) gx = 1;
+  return dim3((unsigned)gx, (unsigned)planes, (unsigned)comps);
+}
+
+__device__ __forceinline__ int wrap_once(int v, int n) { return v >= n ? v - n : v; }
+
+// grids of the conversions: over the device lattice (k_upload,
+// k_fields_from_ref) and over the reference lattice (k_download,
+// k_fields_to_ref)
+__host__ __forceinline__ dim3 dev_grid(const Dims& d, int comps) {
+  return plane_grid((long long)d.nx * d.ny, d.nz, comps);
+}
+__host__ __forceinline__ dim3 ref_grid(const Dims& d, int comps) {
+  return plane_grid((long long)d.rx * d.ry, d.rz, comps);
+}
+
 // reference layout (double) -> device layout
 template <class Real>
 __global__ void k_upload(const double* __restrict__ src, Real* __restrict__ dst,
                          Dims d, int Q, const double* rest_dev) {
-  const long long n = (long long)d.nx * d.ny * d.nz;
-  const long long nr = (long long)d.rx * d.ry * d.rz;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n * Q;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int q = (int)(i / n);
-    const long long g = i - (long long)q * n;
-    const int x = (int)(g % d.nx);
-    const int y = (int)((g / d.nx) % d.ny);
-    const int z = (int)(g / ((long long)d.nx * d.ny));
-    const long long r = ((long long)z * d.ry + y) * d.rx + x;
-    const double v = src[(long long)q * nr + r];
+  const int z = blockIdx.y, q = blockIdx.z;
+  const int plane = d.nx * d.ny;
+  const double* __restrict__ s = src + ((size_t)q * d.rz + z) * ((size_t)d.ry * d.rx);
+  Real* __restrict__ o = dst + ((size_t)q * d.nz + z) * (size_t)plane;
+  const double rest = sizeof(Real) == 4 ? rest_dev[q] : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += gridDim.x * blockDim.x) {
+    const int y = i / d.nx, x = i - y * d.nx;
+    const double v = s[(size_t)y * d.rx + x];
     if constexpr (sizeof(Real) == 4)
-      dst[i] = (Real)(v - rest_dev[q]);
+      o[i] = (Real)(v - rest);
     else
-      dst[i] = (Real)v;
+      o[i] = (Real)v;
   }
 }
 
@@ -307,52 +329,42 @@ __global__ void k_upload(const double* __restrict__ src, Real* __restrict__ dst,
 template <class Real>
 __global__ void k_download(const Real* __restrict__ src, double* __restrict__ dst,
                            Dims d, int Q, const double* rest_dev) {
-  const long long n = (long long)d.nx * d.ny * d.nz;
-  const long long nr = (long long)d.rx * d.ry * d.rz;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nr * Q;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int q = (int)(i / nr);
-    const long long r = i - (long long)q * nr;
-    const int x = (int)(r % d.rx) % d.nx;
-    const int y = (int)((r / d.rx) % d.ry) % d.ny;
-    const int z = (int)(r / ((long long)d.rx * d.ry)) % d.nz;
-    const long long g = ((long long)z * d.ny + y) * d.nx + x;
-    const double v = (double)src[(long long)q * n + g];
-    if constexpr (sizeof(Real) == 4)
-      dst[i] = v + rest_dev[q];
-    else
-      dst[i] = v;
+  const int zr = blockIdx.y, q = blockIdx.z;
+  const int plane = d.rx * d.ry;
+  const int z = wrap_once(zr, d.nz);
+  const Real* __restrict__ s = src + ((size_t)q * d.nz + z) * ((size_t)d.ny * d.nx);
+  double* __restrict__ o = dst + ((size_t)q * d.rz + zr) * (size_t)plane;
+  const double rest = sizeof(Real) == 4 ? rest_dev[q] : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += gridDim.x * blockDim.x) {
+    const int yr = i / d.rx, xr = i - yr * d.rx;
+    const double v = (double)s[(size_t)wrap_once(yr, d.ny) * d.nx + wrap_once(xr, d.nx)];
+    o[i] = sizeof(Real) == 4 ? v + rest : v;
   }
 }
 
 // double fields: device layout <-> reference layout (ncomp blocks)
 __global__ void k_fields_to_ref(const double* __restrict__ src, double* __restrict__ dst,
                                 Dims d, int ncomp) {
-  const long long n = (long long)d.nx * d.ny * d.nz;
-  const long long nr = (long long)d.rx * d.ry * d.rz;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nr * ncomp;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int q = (int)(i / nr);
-    const long long r = i - (long long)q * nr;
-    const int x = (int)(r % d.rx) % d.nx;
-    const int y = (int)((r / d.rx) % d.ry) % d.ny;
-    const int z = (int)(r / ((long long)d.rx * d.ry)) % d.nz;
-    dst[i] = src[(long long)q * n + ((long long)z * d.ny + y) * d.nx + x];
+  const int zr = blockIdx.y, q = blockIdx.z;
+  const int plane = d.rx * d.ry;
+  const int z = wrap_once(zr, d.nz);
+  const double* __restrict__ s = src + ((size_t)q * d.nz + z) * ((size_t)d.ny * d.nx);
+  double* __restrict__ o = dst + ((size_t)q * d.rz + zr) * (size_t)plane;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += gridDim.x * blockDim.x) {
+    const int yr = i / d.rx, xr = i - yr * d.rx;
+    o[i] = s[(size_t)wrap_once(yr, d.ny) * d.nx + wrap_once(xr, d.nx)];
   }
 }
 
 __global__ void k_fields_from_ref(const double* __restrict__ src, double* __restrict__ dst,
                                   Dims d, int ncomp) {
-  const long long n = (long long)d.nx * d.ny * d.nz;
-  const long long nr = (long long)d.rx * d.ry * d.rz;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n * ncomp;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int q = (int)(i / n);
-    const long long g = i - (long long)q * n;
-    const int x = (int)(g % d.nx);
-    const int y = (int)((g / d.nx) % d.ny);
-    const int z = (int)(g / ((long long)d.nx * d.ny));
-    dst[i] = src[(long long)q * nr + ((long long)z * d.ry + y) * d.rx + x];
+  const int z = blockIdx.y, q = blockIdx.z;
+  const int plane = d.nx * d.ny;
+  const double* __restrict__ s = src + ((size_t)q * d.rz + z) * ((size_t)d.ry * d.rx);
+  double* __restrict__ o = dst + ((size_t)q * d.nz + z) * (size_t)plane;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < plane; i += gridDim.x * blockDim.x) {
+    const int y = i / d.nx, x = i - y * d.nx;
+    o[i] = s[(size_t)y * d.rx + x];
   }
 }
 
@@ -967,6 +979,12 @@ int nat_destroy(nat_solver* s) {
     cudaStreamSynchronize(s->h2d);
     cudaStreamDestroy(s->h2d);
   }
+  if (s->conv) {
+    cudaStreamSynchronize(s->conv);
+    cudaStreamDestroy(s->conv);
+  }
+  if (s->spare_free) cudaEventDestroy(s->spare_free);
+  cudaFree(s->f_spare);
   if (s->d2h) {
     cudaStreamSynchronize(s->d2h);
     cudaStreamDestroy(s->d2h);
@@ -1299,6 +1317,17 @@ int nat_set_stream(nat_solver* s, void* stream) {
 static int ensure_upload_path(nat_solver* s) {
   if (s->h2d) return NAT_OK;
   const size_t bytes = sizeof(double) * (size_t)s->Q * s->n_ref;
+  const size_t fbytes = (s->spec.precision == NAT_FP64 ? sizeof(double) : sizeof(float)) * (size_t)s->Q * s->n_dev;
+  if (!s->f_spare && cudaMalloc(&s->f_spare, fbytes) != cudaSuccess) {
+    cudaGetLastError();
+    s->f_spare = nullptr;
+    return fail(s, NAT_ERR_OOM, "cudaMalloc(%zu) failed (spare state buffer)", fbytes);
+  }
+  if (!s->spare_free) {
+    CK(cudaEventCreateWithFlags(&s->spare_free, cudaEventDisableTiming), "upload events");
+    CK(cudaEventRecord(s->spare_free, s->stream), "upload events");
+  }
+  if (!s->conv) CK(cudaStreamCreateWithFlags(&s->conv, cudaStreamNonBlocking), "conversion stream");
   for (int k = 0; k < 2; ++k) {
     if (!s->in_stage[k] && cudaMalloc((void**)&s->in_stage[k], bytes) != cudaSuccess) {
       cudaGetLastError();
@@ -1319,22 +1348,28 @@ int nat_upload_f(nat_solver* s, const double* f_host) {
   int rc = ensure_upload_path(s);
   if (rc) return rc;
   const int k = s->in_slot;
-  // the copy waits for the conversion that last read this buffer; the
-  // conversion below waits for the copy
+  // the copy waits for the conversion that last read this staging buffer;
+  // the conversion waits for the copy and for the spare's last use
   CK(cudaStreamWaitEvent(s->h2d, s->in_free[k], 0), "upload order");
   CK(cudaMemcpyAsync(s->in_stage[k], f_host, sizeof(double) * s->Q * s->n_ref, cudaMemcpyHostToDevice, s->h2d),
      "upload f");
   CK(cudaEventRecord(s->in_full[k], s->h2d), "upload event");
-  CK(cudaStreamWaitEvent(s->stream, s->in_full[k], 0), "upload order");
+  CK(cudaStreamWaitEvent(s->conv, s->in_full[k], 0), "upload order");
+  CK(cudaStreamWaitEvent(s->conv, s->spare_free, 0), "upload order");
   Dims d = dims_of(s);
-  const int g = grid_for(s->n_dev * s->Q);
   if (s->spec.precision == NAT_FP64)
-    k_upload<double><<<g, 256, 0, s->stream>>>(s->in_stage[k], (double*)s->f[s->cur], d, s->Q, s->red + 2);
+    k_upload<double><<<dev_grid(d, s->Q), 256, 0, s->conv>>>(s->in_stage[k], (double*)s->f_spare, d, s->Q, s->red + 2);
   else
-    k_upload<float><<<g, 256, 0, s->stream>>>(s->in_stage[k], (float*)s->f[s->cur], d, s->Q, s->red + 2);
+    k_upload<float><<<dev_grid(d, s->Q), 256, 0, s->conv>>>(s->in_stage[k], (float*)s->f_spare, d, s->Q, s->red + 2);
   CK(cudaGetLastError(), "upload kernel");
   s->launches++;
-  CK(cudaEventRecord(s->in_free[k], s->stream), "upload event");
+  CK(cudaEventRecord(s->in_free[k], s->conv), "upload event");
+  // the converted state becomes the current one; the previous current
+  // buffer is the spare once the work enqueued on the solver stream so far
+  // (the steps that read or wrote it) is done
+  CK(cudaStreamWaitEvent(s->stream, s->in_free[k], 0), "upload order");
+  std::swap(s->f[s->cur], s->f_spare);
+  CK(cudaEventRecord(s->spare_free, s->stream), "upload event");
   s->in_slot = 1 - k;
   return NAT_OK;
 }
@@ -1342,11 +1377,10 @@ int nat_upload_f(nat_solver* s, const double* f_host) {
 int nat_download_f(nat_solver* s, double* f_host) {
   if (!s || !f_host) return NAT_ERR_INVALID_ARG;
   Dims d = dims_of(s);
-  const int g = grid_for(s->n_ref * s->Q);
   if (s->spec.precision == NAT_FP64)
-    k_download<double><<<g, 256, 0, s->stream>>>((const double*)s->f[s->cur], s->staging, d, s->Q, s->red + 2);
+    k_download<double><<<ref_grid(d, s->Q), 256, 0, s->stream>>>((const double*)s->f[s->cur], s->staging, d, s->Q, s->red + 2);
   else
-    k_download<float><<<g, 256, 0, s->stream>>>((const float*)s->f[s->cur], s->staging, d, s->Q, s->red + 2);
+    k_download<float><<<ref_grid(d, s->Q), 256, 0, s->stream>>>((const float*)s->f[s->cur], s->staging, d, s->Q, s->red + 2);
   CK(cudaGetLastError(), "download kernel");
   s->launches++;
   CK(cudaMemcpyAsync(f_host, s->staging, sizeof(double) * s->Q * s->n_ref,
@@ -1359,8 +1393,8 @@ int nat_download_f(nat_solver* s, double* f_host) {
 // host, all enqueued on the handle's stream.
 static int enqueue_macro_readback(nat_solver* s, double* rho_host, double* u_host) {
   Dims d = dims_of(s);
-  k_fields_to_ref<<<grid_for(s->n_ref), 256, 0, s->stream>>>(s->rho, s->staging, d, 1);
-  k_fields_to_ref<<<grid_for(s->n_ref * s->D), 256, 0, s->stream>>>(s->u, s->staging + s->n_ref, d, s->D);
+  k_fields_to_ref<<<ref_grid(d, 1), 256, 0, s->stream>>>(s->rho, s->staging, d, 1);
+  k_fields_to_ref<<<ref_grid(d, s->D), 256, 0, s->stream>>>(s->u, s->staging + s->n_ref, d, s->D);
   CK(cudaGetLastError(), "macro kernel");
   s->launches += 2;
   CK(cudaMemcpyAsync(rho_host, s->staging, sizeof(double) * s->n_ref, cudaMemcpyDeviceToHost, s->stream),
@@ -1425,8 +1459,8 @@ int nat_download_macro_async(nat_solver* s, double* rho_host, double* u_host, ui
   // the slot's previous copies must have left it before it is refilled
   CK(cudaStreamWaitEvent(s->stream, s->rb_done[b], 0), "read-back slot reuse");
   Dims d = dims_of(s);
-  k_fields_to_ref<<<grid_for(s->n_ref), 256, 0, s->stream>>>(s->rho, s->rb_stage[b], d, 1);
-  k_fields_to_ref<<<grid_for(s->n_ref * s->D), 256, 0, s->stream>>>(s->u, s->rb_stage[b] + s->n_ref, d, s->D);
+  k_fields_to_ref<<<ref_grid(d, 1), 256, 0, s->stream>>>(s->rho, s->rb_stage[b], d, 1);
+  k_fields_to_ref<<<ref_grid(d, s->D), 256, 0, s->stream>>>(s->u, s->rb_stage[b] + s->n_ref, d, s->D);
   CK(cudaGetLastError(), "macro kernel");
   s->launches += 2;
   // the status of the steps since the previous read of it, then cleared
@@ -1473,8 +1507,8 @@ int nat_upload_macro(nat_solver* s, const double* rho_host, const double* u_host
   CK(cudaMemcpyAsync(s->staging + s->n_ref, u_host, sizeof(double) * s->D * s->n_ref,
                      cudaMemcpyHostToDevice, s->stream), "upload u");
   Dims d = dims_of(s);
-  k_fields_from_ref<<<grid_for(s->n_dev), 256, 0, s->stream>>>(s->staging, s->rho, d, 1);
-  k_fields_from_ref<<<grid_for(s->n_dev * s->D), 256, 0, s->stream>>>(s->staging + s->n_ref, s->u, d, s->D);
+  k_fields_from_ref<<<dev_grid(d, 1), 256, 0, s->stream>>>(s->staging, s->rho, d, 1);
+  k_fields_from_ref<<<dev_grid(d, s->D), 256, 0, s->stream>>>(s->staging + s->n_ref, s->u, d, s->D);
   CK(cudaGetLastError(), "macro upload kernel");
   s->launches += 2;
   return NAT_OK;
@@ -1980,11 +2014,10 @@ int nat_upload_g(nat_solver* s, const double* g_host) {
   if (!s->thermal) return fail(s, NAT_ERR_UNSUPPORTED, "not a NAT_BGK_COMPRESSIBLE handle");
   CK(cudaMemcpyAsync(s->staging, g_host, sizeof(double) * s->Q * s->n_ref, cudaMemcpyHostToDevice, s->stream),
      "upload g");
-  const int gr = grid_for(s->n_dev * s->Q);
   if (s->spec.precision == NAT_FP64)
-    k_upload<double><<<gr, 256, 0, s->stream>>>(s->staging, (double*)s->g[s->cur], dims_of(s), s->Q, s->red + 2 + 32);
+    k_upload<double><<<dev_grid(dims_of(s), s->Q), 256, 0, s->stream>>>(s->staging, (double*)s->g[s->cur], dims_of(s), s->Q, s->red + 2 + 32);
   else
-    k_upload<float><<<gr, 256, 0, s->stream>>>(s->staging, (float*)s->g[s->cur], dims_of(s), s->Q, s->red + 2 + 32);
+    k_upload<float><<<dev_grid(dims_of(s), s->Q), 256, 0, s->stream>>>(s->staging, (float*)s->g[s->cur], dims_of(s), s->Q, s->red + 2 + 32);
   CK(cudaGetLastError(), "upload kernel");
   s->launches++;
   return NAT_OK;
@@ -1993,12 +2026,11 @@ int nat_upload_g(nat_solver* s, const double* g_host) {
 int nat_download_g(nat_solver* s, double* g_host) {
   if (!s || !g_host) return NAT_ERR_INVALID_ARG;
   if (!s->thermal) return fail(s, NAT_ERR_UNSUPPORTED, "not a NAT_BGK_COMPRESSIBLE handle");
-  const int gr = grid_for(s->n_ref * s->Q);
   if (s->spec.precision == NAT_FP64)
-    k_download<double><<<gr, 256, 0, s->stream>>>((const double*)s->g[s->cur], s->staging, dims_of(s), s->Q,
+    k_download<double><<<ref_grid(dims_of(s), s->Q), 256, 0, s->stream>>>((const double*)s->g[s->cur], s->staging, dims_of(s), s->Q,
                                                   s->red + 2 + 32);
   else
-    k_download<float><<<gr, 256, 0, s->stream>>>((const float*)s->g[s->cur], s->staging, dims_of(s), s->Q,
+    k_download<float><<<ref_grid(dims_of(s), s->Q), 256, 0, s->stream>>>((const float*)s->g[s->cur], s->staging, dims_of(s), s->Q,
                                                  s->red + 2 + 32);
   CK(cudaGetLastError(), "download kernel");
   s->launches++;
@@ -2012,8 +2044,8 @@ int nat_download_thermal(nat_solver* s, double* T_host, double* mask_host) {
   if (!s || !T_host || !mask_host) return NAT_ERR_INVALID_ARG;
   if (!s->thermal) return fail(s, NAT_ERR_UNSUPPORTED, "not a NAT_BGK_COMPRESSIBLE handle");
   Dims d = dims_of(s);
-  k_fields_to_ref<<<grid_for(s->n_ref), 256, 0, s->stream>>>(s->T, s->staging, d, 1);
-  k_fields_to_ref<<<grid_for(s->n_ref), 256, 0, s->stream>>>(s->mask, s->staging + s->n_ref, d, 1);
+  k_fields_to_ref<<<ref_grid(d, 1), 256, 0, s->stream>>>(s->T, s->staging, d, 1);
+  k_fields_to_ref<<<ref_grid(d, 1), 256, 0, s->stream>>>(s->mask, s->staging + s->n_ref, d, 1);
   CK(cudaGetLastError(), "thermal fields kernel");
   s->launches += 2;
   CK(cudaMemcpyAsync(T_host, s->staging, sizeof(double) * s->n_ref, cudaMemcpyDeviceToHost, s->stream),
@@ -2032,8 +2064,8 @@ int nat_init_thermal(nat_solver* s, const double* rho_host, const double* u_host
   // the staging buffer is reused once the copies above are done (same stream)
   CK(cudaMemcpyAsync(s->staging + (1 + s->D) * s->n_ref, T_host, sizeof(double) * s->n_ref,
                      cudaMemcpyHostToDevice, s->stream), "upload T");
-  k_fields_from_ref<<<grid_for(s->n_dev), 256, 0, s->stream>>>(s->staging + (1 + s->D) * s->n_ref, s->T,
-                                                               dims_of(s), 1);
+  k_fields_from_ref<<<dev_grid(dims_of(s), 1), 256, 0, s->stream>>>(s->staging + (1 + s->D) * s->n_ref, s->T,
+                                                                     dims_of(s), 1);
   CK(cudaGetLastError(), "T upload kernel");
   s->launches++;
   CK(launch_thermal_init(thermal_point_params<double>(s, 0, s->tm), s->f[s->cur], s->g[s->cur],

@@ -101,15 +101,22 @@ struct nat_solver {
   std::vector<float> at_ms;
   std::vector<int> at_desc;  // 5 ints per candidate
   // Pipelined host transfers.  nat_upload_f copies into one of two input
-  // staging buffers on its own stream (h2d); the conversion kernel on the
-  // solver's stream waits for that copy, and the next copy into the same
-  // buffer waits for the conversion.  So the copy of the next state runs
-  // while the current one is stepped and read back.  Created on first use.
+  // staging buffers on its own stream (h2d), and a conversion stream turns
+  // it into the device layout in a spare state buffer (a third f buffer);
+  // the solver's stream waits for the conversion, and the spare and the
+  // current buffer swap roles (host-side pointers).  The next copy into the
+  // same staging buffer waits for its conversion, and the next conversion
+  // into the spare waits for the spare's last use on the solver's stream.
+  // So the copy and the conversion of the next state run while the current
+  // one is stepped and read back.  Created on first use.
   cudaStream_t h2d = nullptr;
+  cudaStream_t conv = nullptr;
   double* in_stage[2] = {nullptr, nullptr};  // Q * n_ref doubles each
   cudaEvent_t in_full[2] = {nullptr, nullptr};
   cudaEvent_t in_free[2] = {nullptr, nullptr};
   int in_slot = 0;
+  void* f_spare = nullptr;            // Q * n_dev values (the state's precision)
+  cudaEvent_t spare_free = nullptr;   // the spare's last use on the solver stream
   // Asynchronous read-backs (nat_download_macro_async): ticket t uses slot
   // t % NTICKET, an event on the solver's stream and a page-locked copy of
   // the device status word taken right before it.  Reusing a slot first
