@@ -312,6 +312,19 @@ __device__ __forceinline__ Real collide_bgk_inc(Real (&v)[9], Real inv_tau,
 //   gamma = 2 when <dh|dh> < 1e-16,  f_i -= beta (2 ds_i + gamma dh_i),
 //   beta = 1 / (2 tau).
 // ---------------------------------------------------------------------------
+// weights of a tensor-product stencil: w_i = prod_a w1(e_ia), w1(0) = 2/3,
+// w1(+-1) = 1/6 (D2Q9, D3Q27), to a relative 1e-14
+template <class S>
+__host__ __device__ constexpr bool tensor_weights() {
+  for (int i = 0; i < S::Q; ++i) {
+    double p = 1.0;
+    for (int a = 0; a < S::D; ++a) p *= S::e(i, a) == 0 ? 2.0 / 3.0 : 1.0 / 6.0;
+    const double d = p - S::w(i);
+    if (d > 1e-14 * p || -d > 1e-14 * p) return false;
+  }
+  return true;
+}
+
 template <class S, int i, class Real>
 __device__ __forceinline__ Real kbc_shear(const Real (&M)[3][3]) {
   constexpr int ex = S::e(i, 0), ey = S::e(i, 1), ez = S::e(i, 2);
@@ -378,7 +391,18 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
   // 1 / f^eq_i = (1 / (w_i rho)) prod_a 1 / (1 + d_a) from the per-axis
   // reciprocals above instead of one division per direction;
   // (1 / rho) / (1 + d_x) / (1 + d_y) per (c_x, c_y): nine products shared by
-  // the directions of each pair
+  // the directions of each pair.  With tensor-product weights (D2Q9, D3Q27:
+  // w_i = prod_a w1(e_ia), w1(0) = 2/3, w1(+-1) = 1/6) the 1 / w_i factor is
+  // folded into the per-axis reciprocals as well.
+  constexpr bool TW = tensor_weights<S>();
+  if constexpr (TW) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      rinv[a][0] *= Real(6);
+      rinv[a][1] *= Real(1.5);
+      rinv[a][2] *= Real(6);
+    }
+  }
   Real rxy[3][3];
 #pragma unroll
   for (int cx = 0; cx < 3; ++cx)
@@ -396,41 +420,64 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
     else
       df[i] = fma(-w * rho, q, v[i] - w * rho);  // v - w rho (1 + q)
   });
-  // second-moment differences of f - feq
+  // second-moment differences of f - feq, per pair of opposite directions
+  // (e_a e_b is even in e: one sum df_i + df_i' per pair)
   Real M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-  static_for<0, S::Q>([&](auto I) {
+  static_for<1, S::Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
-    constexpr int ex = S::e(i, 0), ey = S::e(i, 1), ez = S::e(i, 2);
-    if constexpr (ex != 0) M[0][0] += df[i];
-    if constexpr (ey != 0) M[1][1] += df[i];
-    if constexpr (ez != 0) M[2][2] += df[i];
-    if constexpr (ex * ey != 0) M[0][1] += Real(ex * ey) * df[i];
-    if constexpr (ex * ez != 0) M[0][2] += Real(ex * ez) * df[i];
-    if constexpr (ey * ez != 0) M[1][2] += Real(ey * ez) * df[i];
+    constexpr int o = opp<S>(i);
+    if constexpr (i < o) {
+      constexpr int ex = S::e(i, 0), ey = S::e(i, 1), ez = S::e(i, 2);
+      const Real sp = df[i] + df[o];
+      if constexpr (ex != 0) M[0][0] += sp;
+      if constexpr (ey != 0) M[1][1] += sp;
+      if constexpr (ez != 0) M[2][2] += sp;
+      if constexpr (ex * ey > 0) M[0][1] += sp;
+      if constexpr (ex * ey < 0) M[0][1] -= sp;
+      if constexpr (ex * ez > 0) M[0][2] += sp;
+      if constexpr (ex * ez < 0) M[0][2] -= sp;
+      if constexpr (ey * ez > 0) M[1][2] += sp;
+      if constexpr (ey * ez < 0) M[1][2] -= sp;
+    }
   });
   M[1][0] = M[0][1];
   M[2][0] = M[0][2];
   M[2][1] = M[1][2];
+  // the shear part ds is zero for the directions with three non-zero
+  // components (D3Q27's corners): there dh = df and ds drops out of the sums
   Real ss = Real(0), sh = Real(0);
   static_for<0, S::Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
-    const Real ds = kbc_shear<S, i>(M);
-    const Real dh = df[i] - ds;
+    constexpr bool DS0 = S::D == 3 && S::e(i, 0) != 0 && S::e(i, 1) != 0 && S::e(i, 2) != 0;
     Real inv = rxy[S::e(i, 0) + 1][S::e(i, 1) + 1];
     if constexpr (S::D == 3) inv *= rinv[2][S::e(i, 2) + 1];
-    const Real t = dh * (inv * Real(1.0 / S::w(i)));
-    ss = fma(ds, t, ss);
-    sh = fma(dh, t, sh);
+    if constexpr (!TW) inv *= Real(1.0 / S::w(i));
+    if constexpr (DS0) {
+      sh = fma(df[i], df[i] * inv, sh);
+    } else {
+      const Real ds = kbc_shear<S, i>(M);
+      const Real dh = df[i] - ds;
+      const Real t = dh * inv;
+      ss = fma(ds, t, ss);
+      sh = fma(dh, t, sh);
+    }
   });
   const Real beta = Real(0.5) / tau;
   const Real ib = Real(1) / beta;
   Real gamma = ib - (Real(2) - ib) * (ss / sh);
   if (sh < Real(1e-16)) gamma = Real(2);
+  // f - beta (2 ds + gamma dh)
+  const Real b2 = Real(2) * beta, bg = beta * gamma;
   static_for<0, S::Q>([&](auto I) {
     constexpr int i = decltype(I)::value;
-    const Real ds = kbc_shear<S, i>(M);
-    const Real dh = df[i] - ds;
-    v[i] = v[i] - beta * (Real(2) * ds + gamma * dh);
+    constexpr bool DS0 = S::D == 3 && S::e(i, 0) != 0 && S::e(i, 1) != 0 && S::e(i, 2) != 0;
+    if constexpr (DS0) {
+      v[i] = fma(-bg, df[i], v[i]);
+    } else {
+      const Real ds = kbc_shear<S, i>(M);
+      const Real dh = df[i] - ds;
+      v[i] = fma(-bg, dh, fma(-b2, ds, v[i]));
+    }
   });
   return rho;
 }

@@ -400,6 +400,26 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
   const int y = by * rows_per_cta + warp * RPW + r;
   const int cy = y % PER, cz = z % PER;
   const int x0 = X * PER;
+  // the lane's y and z window rows per displacement sign (0: positive, 1:
+  // negative) in the rotated order (slot 0 the dominant row), as element
+  // offsets: computed once for all directions instead of per direction
+  int yrow[2][PER], zrow[2][PER];
+  {
+    const int ws[4] = {win_start<P, true, 1>(y, cy), win_start<P, true, -1>(y, cy),
+                       win_start<P, true, 1>(z, cz), win_start<P, true, -1>(z, cz)};
+    const int j0[4] = {win_j0<P, true, 1>(cy), win_j0<P, true, -1>(cy), win_j0<P, true, 1>(cz),
+                       win_j0<P, true, -1>(cz)};
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+#pragma unroll
+      for (int d = 0; d < 2; ++d) {
+        const int ry = j0[d] + j, rz = j0[2 + d] + j;
+        yrow[d][j] = wrap(ws[d] + (ry > P ? ry - PER : ry), ny) * nx;
+        zrow[d][j] = wrap(ws[2 + d] + (rz > P ? rz - PER : rz), nz) * nxy;
+      }
+    }
+  }
+  const int yself = y * nx, zself = z * nxy;
 
   // rest population: copied
   {
@@ -419,13 +439,7 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
       const int y0 = by * R;
       const int ybase = ws_dg<P, sy>(y0);
       const int U = ws_dg<P, sy>(y0 + R - 1) - ybase + PER;
-      const int zs = win_start<P, true, sz>(z, cz), j0z = win_j0<P, true, sz>(cz);
-      int zo[PER];
-#pragma unroll
-      for (int jz = 0; jz < PER; ++jz) {
-        const int rz = j0z + jz;
-        zo[jz] = wrap(zs + (rz > P ? rz - PER : rz), nz) * nxy;
-      }
+      const int* zo = zrow[dz];
       const Real* __restrict__ srcA = prm.f_in + (size_t)A * prm.n;
       auto zaddr = [&](int uu) {  // row uu of this direction's buffer
         const int ch = uu / RPW;
@@ -498,17 +512,6 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
     constexpr int NJZ = sz != 0 ? P + 1 : 1;
     constexpr int dy = sy > 0 ? 0 : 1, dz = sz > 0 ? 0 : 1, dx = sx > 0 ? 0 : 1;
     const Real* __restrict__ src = prm.f_in + ((size_t)A * prm.n + x0);  // + 32-bit row offsets
-    int ys = y, zs = z, j0y = 0, j0z = 0;
-    if constexpr (sy != 0) {
-      ys = win_start<P, true, sy>(y, cy);
-      j0y = win_j0<P, true, sy>(cy);
-    }
-    if constexpr (sz != 0) {
-      zs = win_start<P, true, sz>(z, cz);
-      j0z = win_j0<P, true, sz>(cz);
-    }
-    (void)dy;
-    (void)dz;
     // y/z factors: T[c] for the lane's PER nodes.  The z rows are taken in
     // the rotated order (slot 0 the dominant one) and accumulated one at a
     // time: T = Y_0 + sum_{jz >= 1} w_jz (Y_jz - Y_0) in the deviation mode
@@ -519,17 +522,14 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
       Real Y0[PER], acc[PER];
 #pragma unroll
       for (int jz = 0; jz < NJZ; ++jz) {
-        const int rz = j0z + jz;
-        const int gz = wrap(zs + (rz > P ? rz - (P + 1) : rz), nz);
+        const int zo = sz != 0 ? zrow[dz][jz] : zself;
         Real Y[PER];
         if constexpr (sy != 0) {
           Real y0v[PER], yacc[PER];
 #pragma unroll
           for (int jy = 0; jy < NJY; ++jy) {
-            const int ry = j0y + jy;
-            const int gy = wrap(ys + (ry > P ? ry - (P + 1) : ry), ny);
             Real v[PER];
-            load_cell<PER>(src + (gz * nxy + gy * nx), v);
+            load_cell<PER>(src + (zo + yrow[dy][jy]), v);
             const Real wy = tw[1][dy][cy][jy];
 #pragma unroll
             for (int c = 0; c < PER; ++c) {
@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
 #pragma unroll
           for (int c = 0; c < PER; ++c) Y[c] = DEV ? yacc[c] + y0v[c] : yacc[c];
         } else {
-          load_cell<PER>(src + (gz * nxy + ys * nx), Y);
+          load_cell<PER>(src + (zo + yself), Y);
         }
         if constexpr (sz != 0) {
           const Real wz = tw[2][dz][cz][jz];
