@@ -464,11 +464,9 @@ int nat_server_submit(nat_server* s, const nat_request* r, int64_t* id);
  * live solves with the same order and collision model). */
 int nat_server_step(nat_server* s);
 /* Up to max_steps server steps in one call (no counterpart in the
- * reference); stops early when no solve is live.  Steps up to the next
- * retirement run as one graph launch of up to 16 chained steps; requests
- * submitted meanwhile are admitted at the next launch.  *steps_done (may be
- * NULL) receives the number run.  The host runs at most about 64 steps ahead
- * of the device. */
+ * reference); stops early when no solve is live.  *steps_done (may be NULL)
+ * receives the number run.  The host runs at most 64 steps ahead of the
+ * device. */
 int nat_server_run(nat_server* s, int max_steps, int* steps_done);
 /* Ids of finished requests (up to max_ids); wait != 0 blocks until every
  * solve that has run its last step is copied out. */

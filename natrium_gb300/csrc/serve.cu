@@ -10,16 +10,14 @@
 // device memory and the last CTA of the step advances it, so the graph needs
 // no separate tick.  Admissions and retirements rebuild the work list
 // (uploaded asynchronously from double-buffered page-locked memory) and the
-// graphs; steps in between relaunch them, up to 16 steps chained in one
-// graph when no solve retires before.  A solve's last step writes rho / u;
-// the host copies them out after an event and frees the slot.
+// graph; steps in between relaunch the same graph.  A solve's last step
+// writes rho / u; the host copies them out after an event and frees the slot.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
 
-#include <algorithm>
 #include <deque>
 #include <map>
 #include <string>
@@ -286,10 +284,7 @@ struct nat_server {
   long long host_step = 0;
   int64_t next_id = 1;
   bool dirty = true;
-  // graphs of the live set: graphs[l] advances it by 2^l steps (levels of
-  // the group kernels, each level after the previous one); built on first use
-  static constexpr int NLEVELS = 5;
-  cudaGraphExec_t graphs[NLEVELS] = {};
+  cudaGraphExec_t graph = nullptr;
   std::string err;
   // statistics
   long long steps_run = 0, node_updates = 0, launches = 0;
@@ -385,21 +380,17 @@ int upload_state(nat_server* s) {
   SCK(cudaEventRecord(s->stage_ev[k], s->stream), "staging event");
   s->stage_k ^= 1;
   s->dirty = false;
-  for (auto& g : s->graphs)  // the groups or their sizes changed: new graphs
-    if (g) {
-      cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  if (s->graph) {  // the groups or their sizes changed: a new graph
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
   return NAT_OK;
 }
 
-// Graphs of a live set: per step a kernel node per non-empty group, no
+// One graph per live set: a kernel node per non-empty group, no
 // dependencies between them (independent solves), each with a grid of about
-// two items per warp, at most two CTAs per SM; graphs[l] chains 2^l such
-// steps, every node of a step depending on every node of the step before (the
-// last CTA of a step advances the step counter for the next).  Several steps
-// per launch take the graph-launch latency off all but one of them.
-int capture(nat_server* s, int lvl) {
+// two items per warp, at most two CTAs per SM.
+int capture(nat_server* s) {
   int grid[NGROUPS] = {};
   unsigned total = 0;
   for (int g = 0; g < NGROUPS; ++g) {
@@ -411,31 +402,25 @@ int capture(nat_server* s, int lvl) {
   if (!total) return NAT_OK;
   cudaGraph_t gr;
   SCK(cudaGraphCreate(&gr, 0), "graph create");
-  std::vector<cudaGraphNode_t> prev, cur;
-  for (int step = 0; step < (1 << lvl); ++step) {
-    cur.clear();
-    for (int g = 0; g < NGROUPS; ++g) {
-      if (!grid[g]) continue;
-      void* args[] = {(void*)&s->d_slots, (void*)&s->d_work, (void*)&s->d_groups, (void*)&s->d_step,
-                      (void*)&s->d_ticket, (void*)&total};
-      cudaKernelNodeParams kp;
-      memset(&kp, 0, sizeof kp);
-      kp.func = (void*)group_kernel(g);
-      kp.gridDim = dim3(grid[g]);
-      kp.blockDim = dim3(32 * SERVE_WARPS);
-      kp.sharedMemBytes = 0;
-      kp.kernelParams = args;
-      cudaGraphNode_t node;
-      cudaError_t e = cudaGraphAddKernelNode(&node, gr, prev.empty() ? nullptr : prev.data(), prev.size(), &kp);
-      if (e != cudaSuccess) {
-        cudaGraphDestroy(gr);
-        return sfail(s, NAT_ERR_CUDA, "graph node: %s", cudaGetErrorString(e));
-      }
-      cur.push_back(node);
+  for (int g = 0; g < NGROUPS; ++g) {
+    if (!grid[g]) continue;
+    void* args[] = {(void*)&s->d_slots, (void*)&s->d_work, (void*)&s->d_groups, (void*)&s->d_step,
+                    (void*)&s->d_ticket, (void*)&total};
+    cudaKernelNodeParams kp;
+    memset(&kp, 0, sizeof kp);
+    kp.func = (void*)group_kernel(g);
+    kp.gridDim = dim3(grid[g]);
+    kp.blockDim = dim3(32 * SERVE_WARPS);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    cudaGraphNode_t node;
+    cudaError_t e = cudaGraphAddKernelNode(&node, gr, nullptr, 0, &kp);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(gr);
+      return sfail(s, NAT_ERR_CUDA, "graph node: %s", cudaGetErrorString(e));
     }
-    prev.swap(cur);
   }
-  cudaError_t e = cudaGraphInstantiate(&s->graphs[lvl], gr, 0);
+  cudaError_t e = cudaGraphInstantiate(&s->graph, gr, 0);
   cudaGraphDestroy(gr);
   if (e != cudaSuccess) return sfail(s, NAT_ERR_CUDA, "instantiate: %s", cudaGetErrorString(e));
   s->graph_ctas = total;
@@ -649,8 +634,7 @@ int nat_server_destroy(nat_server* s) {
     delete c;
   }
   for (auto& kv : s->done) delete kv.second;
-  for (auto g : s->graphs)
-    if (g) cudaGraphExecDestroy(g);
+  if (s->graph) cudaGraphExecDestroy(s->graph);
   cudaFree(s->pool_base);
   cudaFree(s->d_slots);
   cudaFree(s->d_status);
@@ -686,12 +670,10 @@ int nat_server_submit(nat_server* s, const nat_request* r, int64_t* id) {
 
 namespace {
 
-// Server steps: collect finished results, admit queued requests, then
-// advance every live solve by m = 2^l <= max_steps time steps in one graph
-// launch, m no more than the steps left to the next retirement (the live set
-// is fixed in between; requests that arrive meanwhile wait for the next
-// call).  *ran = the steps run, 0 when no solve was live.
-int server_step(nat_server* s, int max_steps, int* ran) {
+// One server step: collect finished results, admit queued requests, advance
+// every live solve by one time step (one graph launch).  *ran = 0 when no
+// solve was live.
+int server_step(nat_server* s, int* ran) {
   *ran = 0;
   int rc = harvest(s, false);
   if (rc) return rc;
@@ -702,31 +684,25 @@ int server_step(nat_server* s, int max_steps, int* ran) {
     rc = upload_state(s);
     if (rc) return rc;
   }
-  long long left = max_steps;
-  for (const Live& L : s->live) left = std::min(left, L.last_step - s->host_step + 1);
-  int lvl = 0;
-  while (lvl + 1 < nat_server::NLEVELS && (2LL << lvl) <= left) ++lvl;
-  const int m = 1 << lvl;
-  if (!s->graphs[lvl]) {
-    rc = capture(s, lvl);
+  if (!s->graph) {
+    rc = capture(s);
     if (rc) return rc;
   }
-  SCK(cudaGraphLaunch(s->graphs[lvl], s->stream), "graph launch");
-  s->launches += (long long)s->graph_nodes * m;  // the graph's kernels, one per group and step
-  const long long first = s->host_step;
-  s->host_step += m;
-  s->steps_run += m;
-  for (const Live& L : s->live) s->node_updates += (long long)m * s->h_slots[L.slot].n;
+  SCK(cudaGraphLaunch(s->graph, s->stream), "graph launch");
+  s->launches += s->graph_nodes;  // the graph's kernels, one per group
+  const long long step = s->host_step++;
+  s->steps_run++;
+  for (const Live& L : s->live) s->node_updates += s->h_slots[L.slot].n;
   // keep the host at most RUNAHEAD_EVERY * RUNAHEAD_RING steps ahead of the device
-  if (s->host_step / RUNAHEAD_EVERY != first / RUNAHEAD_EVERY) {
+  if (s->host_step % RUNAHEAD_EVERY == 0) {
     const int k = s->ahead_k;
     if (s->ahead_used[k]) SCK(cudaEventSynchronize(s->ahead_ev[k]), "run-ahead wait");
     SCK(cudaEventRecord(s->ahead_ev[k], s->stream), "run-ahead event");
     s->ahead_used[k] = true;
     s->ahead_k = (k + 1) % RUNAHEAD_RING;
   }
-  *ran = m;
-  return retire(s, s->host_step - 1);
+  *ran = 1;
+  return retire(s, step);
 }
 
 }  // namespace
@@ -736,21 +712,20 @@ extern "C" {
 int nat_server_step(nat_server* s) {
   if (!s) return NAT_ERR_INVALID_ARG;
   int ran;
-  return server_step(s, 1, &ran);
+  return server_step(s, &ran);
 }
 
 int nat_server_run(nat_server* s, int max_steps, int* steps_done) {
   if (!s || max_steps < 0) return NAT_ERR_INVALID_ARG;
   int k = 0;
-  while (k < max_steps) {
+  for (; k < max_steps; ++k) {
     int ran = 0;
-    const int rc = server_step(s, max_steps - k, &ran);
+    const int rc = server_step(s, &ran);
     if (rc) {
       if (steps_done) *steps_done = k;
       return rc;
     }
     if (!ran) break;
-    k += ran;
   }
   if (steps_done) *steps_done = k;
   return NAT_OK;

@@ -203,7 +203,7 @@ def workload(n: int = 512, seed: int = 0, rate: float = 200.0, steps_range=(50, 
     return arrivals, reqs
 
 
-def run_workload(arrivals, reqs, pool_bytes: int = 8 << 30, max_slots: int = 512, steps_per_call: int = 16):
+def run_workload(arrivals, reqs, pool_bytes: int = 8 << 30, max_slots: int = 512, steps_per_call: int = 8):
     """Replay the request stream in wall-clock time through one server.
     Requests are submitted as their arrival time passes; between checks the
     server runs up to steps_per_call steps in one C call.  Returns throughput
