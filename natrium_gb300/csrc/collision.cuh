@@ -312,6 +312,23 @@ __device__ __forceinline__ Real collide_bgk_inc(Real (&v)[9], Real inv_tau,
 //   gamma = 2 when <dh|dh> < 1e-16,  f_i -= beta (2 ds_i + gamma dh_i),
 //   beta = 1 / (2 tau).
 // ---------------------------------------------------------------------------
+// 1 / x and sqrt(x): IEEE in FP64; with FAST in FP32 the hardware
+// approximations (MUFU.RCP / MUFU.RSQ based, a few ulp, no special-case path)
+template <bool FAST, class Real>
+__device__ __forceinline__ Real approx_rcp(Real x) {
+  if constexpr (FAST && sizeof(Real) == 4)
+    return __fdividef(1.0f, x);
+  else
+    return Real(1) / x;
+}
+template <bool FAST, class Real>
+__device__ __forceinline__ Real approx_sqrt(Real x) {
+  if constexpr (FAST && sizeof(Real) == 4)
+    return x * rsqrtf(x);
+  else
+    return sqrt(x);
+}
+
 // weights of a tensor-product stencil: w_i = prod_a w1(e_ia), w1(0) = 2/3,
 // w1(+-1) = 1/6 (D2Q9, D3Q27), to a relative 1e-14
 template <class S>
@@ -359,16 +376,19 @@ __device__ __forceinline__ Real collide_kbc(Real (&v)[S::Q], Real tau,
   // per axis: factor - 1 for c = -1, 0, +1 (stable small-number form of
   // base = 2 - sqrt(1 + 3u^2), post = (2u + sqrt(1+3u^2)) / (1 - u)), and
   // the reciprocals of the factors, 1 / base, 1 / (base post), post / base,
-  // from the two reciprocals 1 / base and 1 / post
+  // from the two reciprocals 1 / base and 1 / post.  In the FP32 deviation
+  // path these use the hardware's approximate reciprocal and square root
+  // (a few ulp): the factors enter f^eq as corrections of order u and u^2,
+  // where that error stays below the storage's own rounding.
   Real dm[3][3], rinv[3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const Real ua = u[a];
-    const Real s = sqrt(Real(1) + Real(3) * ua * ua);
-    const Real sm1 = Real(3) * ua * ua / (Real(1) + s);  // s - 1
-    const Real pm1 = (Real(3) * ua + sm1) / (Real(1) - ua);  // post - 1
-    const Real rb = Real(1) / (Real(1) - sm1);             // 1 / base
-    const Real ip = Real(1) / (Real(1) + pm1);             // 1 / post
+    const Real s = approx_sqrt<DEV>(Real(1) + Real(3) * ua * ua);
+    const Real sm1 = Real(3) * ua * ua * approx_rcp<DEV>(Real(1) + s);     // s - 1
+    const Real pm1 = (Real(3) * ua + sm1) * approx_rcp<DEV>(Real(1) - ua);  // post - 1
+    const Real rb = approx_rcp<DEV>(Real(1) - sm1);                         // 1 / base
+    const Real ip = approx_rcp<DEV>(Real(1) + pm1);                         // 1 / post
     dm[a][1] = -sm1;                                       // base - 1
     dm[a][2] = pm1 - sm1 - sm1 * pm1;                      // base*post - 1
     dm[a][0] = (-sm1 - pm1) * ip;                          // base/post - 1
