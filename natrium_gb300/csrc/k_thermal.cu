@@ -3,30 +3,20 @@
 #include <cuda_runtime.h>
 
 #include "launch.h"
-#include "sl_thermal.cuh"
+#include "thermal_step.h"
 
 namespace natgpu {
 
-// form: 0 register form (TH_WARPS warps per CTA), 1 / 2 shared-memory forms
-// (TH_WARPS_SS warps per CTA, FP32 only; sl_thermal.cuh)
-template <class Real, int FORM>
-static cudaError_t step_form(const ThermalStepT<Real>& P, bool collide, cudaStream_t st) {
-  constexpr int W = FORM > 0 ? TH_WARPS_SS : TH_WARPS;
-  const int warps = P.nseg * P.ny;
-  const int grid = (warps + W - 1) / W;
-  void* args[] = {const_cast<ThermalStepT<Real>*>(&P)};
-  const void* fn = collide ? (const void*)k_thermal_step<Real, true, W, FORM>
-                           : (const void*)k_thermal_step<Real, false, W, FORM>;
-  return cudaLaunchKernel(fn, dim3(grid), dim3(32 * W), args, 0, st);
-}
-
 template <class Real>
 static cudaError_t step_t(const ThermalStepT<Real>& P, bool collide, cudaStream_t st, int form) {
+  // order 2 (the compressible benchmark's) has its own instantiations with
+  // compile-time window loops (k_thermal_p2.cu)
+  if (P.tb.p == 2) return launch_thermal_step_p2(P, collide, st, form);
   if constexpr (sizeof(Real) == 4) {
-    if (form == 1) return step_form<Real, 1>(P, collide, st);
-    if (form == 2) return step_form<Real, 2>(P, collide, st);
+    if (form == 1) return thermal_step_form<Real, 1, 0>(P, collide, st);
+    if (form == 2) return thermal_step_form<Real, 2, 0>(P, collide, st);
   }
-  return step_form<Real, 0>(P, collide, st);
+  return thermal_step_form<Real, 0, 0>(P, collide, st);
 }
 
 cudaError_t launch_thermal_step(const ThermalStepT<double>& P, bool collide, cudaStream_t st, int form) {

@@ -339,7 +339,9 @@ constexpr int th_minb() {
   return FORM == 1 ? 5 : (FORM == 2 ? 6 : (F32 ? 2 : 1));
 }
 
-template <class Real, bool COLLIDE, int W = TH_WARPS, int FORM = 0>
+// PC > 0: the order p as a compile-time constant (the window loops then run
+// over p + 1 slots instead of PMAX1 predicated ones); PC = 0: any order.
+template <class Real, bool COLLIDE, int W = TH_WARPS, int FORM = 0, int PC = 0>
 __global__ void __launch_bounds__(32 * W, (th_minb<FORM, sizeof(Real) == 4>()))
     k_thermal_step(const __grid_constant__ ThermalStepT<Real> P) {
   __shared__ Real swx[ND_MAX][PER_MAX][PMAX1];
@@ -360,7 +362,7 @@ __global__ void __launch_bounds__(32 * W, (th_minb<FORM, sizeof(Real) == 4>()))
   const int wid = blockIdx.x * W + warp;
   if (wid >= P.nseg * P.ny) return;  // warp-uniform
   const int nx = P.nx, ny = P.ny, n = P.n;
-  const int p = P.tb.p, per = P.tb.per;
+  const int p = PC > 0 ? PC : P.tb.p, per = P.tb.per;
   const int seg = wid % P.nseg, y = wid / P.nseg;
   const int x0 = seg * 32, x = x0 + lane;
   const bool valid = x < nx;
