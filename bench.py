@@ -841,6 +841,8 @@ def run_ours(args):
         serving["capacity"] = {"solves_per_s": cap["solves_per_s"], "wall_s": cap["wall_s"],
                                "latency_p50_s": cap["latency_p50_s"], "latency_p99_s": cap["latency_p99_s"],
                                "node_updates_per_s": cap["node_updates_per_s"],
+                               "server_steps": cap["server_steps"], "graph_builds": cap["graph_builds"],
+                               "graph_updates": cap["graph_updates"], "host_rebuild_s": cap["host_rebuild_s"],
                                "note": "all 512 requests submitted at t = 0 (saturated server)"}
         serving.update({"workload": "512 D2Q9 solves (TGV / shear layer, BGK / KBC, N in {4..64}, p 2-6, "
                                     "Ma 0.02-0.1, Re 100-5000, 50-2000 steps), Poisson 200 req/s, seed 0, "

@@ -448,6 +448,9 @@ typedef struct nat_server_stats_t {
   int64_t steps, node_updates;
   int64_t pool_used, pool_bytes;
   int64_t launches;
+  /* step graphs instantiated, step graphs updated in place (same non-empty
+   * groups), and host time spent rebuilding work lists and graphs (ns) */
+  int64_t graph_builds, graph_updates, rebuild_ns;
 } nat_server_stats_t;
 
 typedef struct nat_server nat_server;

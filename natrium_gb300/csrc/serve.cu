@@ -18,6 +18,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <chrono>
 #include <deque>
 #include <map>
 #include <string>
@@ -263,11 +264,15 @@ struct nat_server {
   int group_count[NGROUPS] = {};
   // page-locked staging of the work list, group ranges and slot table, two
   // sets used in turn; an event marks when a set's copies have been read
-  WorkItem* stage_work[2] = {nullptr, nullptr};
-  GroupRange* stage_groups[2] = {nullptr, nullptr};
-  SlotDesc* stage_slots[2] = {nullptr, nullptr};
-  int stage_cap[2] = {0, 0};
-  cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+  // a ring of NSTAGE page-locked staging sets for the work list uploads: a
+  // set is refilled once its copies (an event) are done, which with several
+  // sets rarely waits even when the device runs many steps behind
+  static constexpr int NSTAGE = 8;
+  WorkItem* stage_work[NSTAGE] = {};
+  GroupRange* stage_groups[NSTAGE] = {};
+  SlotDesc* stage_slots[NSTAGE] = {};
+  int stage_cap[NSTAGE] = {};
+  cudaEvent_t stage_ev[NSTAGE] = {};
   int stage_k = 0;
   // bound on the host running ahead of the device: an event every
   // RUNAHEAD_EVERY steps in a ring of RUNAHEAD_RING
@@ -284,7 +289,15 @@ struct nat_server {
   long long host_step = 0;
   int64_t next_id = 1;
   bool dirty = true;
+  // the step graph, its template and kernel nodes (one per non-empty group,
+  // graph_mask); a new live set with the same non-empty groups updates the
+  // nodes' grids and arguments in place instead of instantiating again
   cudaGraphExec_t graph = nullptr;
+  cudaGraph_t graph_tmpl = nullptr;
+  cudaGraphNode_t gnodes[NGROUPS] = {};
+  unsigned graph_mask = 0;
+  bool graph_stale = true;
+  long long graph_builds = 0, graph_updates = 0, rebuild_ns = 0;
   std::string err;
   // statistics
   long long steps_run = 0, node_updates = 0, launches = 0;
@@ -378,34 +391,31 @@ int upload_state(nat_server* s) {
                       s->stream),
       "slot upload");
   SCK(cudaEventRecord(s->stage_ev[k], s->stream), "staging event");
-  s->stage_k ^= 1;
+  s->stage_k = (k + 1) % nat_server::NSTAGE;
   s->dirty = false;
-  if (s->graph) {  // the groups or their sizes changed: a new graph
-    cudaGraphExecDestroy(s->graph);
-    s->graph = nullptr;
-  }
+  s->graph_stale = true;  // the groups or their sizes changed
   return NAT_OK;
 }
 
-// One graph per live set: a kernel node per non-empty group, no
+// The step graph of the live set: a kernel node per non-empty group, no
 // dependencies between them (independent solves), each with a grid of about
-// two items per warp, at most two CTAs per SM.
+// two items per warp, at most two CTAs per SM.  When the set of non-empty
+// groups is the one the graph was built for, the nodes' grids and the CTA
+// total are updated in the instantiated graph; otherwise it is built anew.
 int capture(nat_server* s) {
   int grid[NGROUPS] = {};
-  unsigned total = 0;
+  unsigned total = 0, mask = 0;
   for (int g = 0; g < NGROUPS; ++g) {
     if (!s->group_count[g]) continue;
     const int want = (s->group_count[g] + 2 * SERVE_WARPS - 1) / (2 * SERVE_WARPS);
     grid[g] = want < 1 ? 1 : (want > 2 * s->sms ? 2 * s->sms : want);
     total += (unsigned)grid[g];
+    mask |= 1u << g;
   }
   if (!total) return NAT_OK;
-  cudaGraph_t gr;
-  SCK(cudaGraphCreate(&gr, 0), "graph create");
-  for (int g = 0; g < NGROUPS; ++g) {
-    if (!grid[g]) continue;
-    void* args[] = {(void*)&s->d_slots, (void*)&s->d_work, (void*)&s->d_groups, (void*)&s->d_step,
-                    (void*)&s->d_ticket, (void*)&total};
+  void* args[] = {(void*)&s->d_slots, (void*)&s->d_work, (void*)&s->d_groups, (void*)&s->d_step,
+                  (void*)&s->d_ticket, (void*)&total};
+  auto params = [&](int g) {
     cudaKernelNodeParams kp;
     memset(&kp, 0, sizeof kp);
     kp.func = (void*)group_kernel(g);
@@ -413,19 +423,41 @@ int capture(nat_server* s) {
     kp.blockDim = dim3(32 * SERVE_WARPS);
     kp.sharedMemBytes = 0;
     kp.kernelParams = args;
-    cudaGraphNode_t node;
-    cudaError_t e = cudaGraphAddKernelNode(&node, gr, nullptr, 0, &kp);
-    if (e != cudaSuccess) {
-      cudaGraphDestroy(gr);
-      return sfail(s, NAT_ERR_CUDA, "graph node: %s", cudaGetErrorString(e));
+    return kp;
+  };
+  if (s->graph && mask == s->graph_mask) {
+    bool ok = true;
+    for (int g = 0; g < NGROUPS && ok; ++g) {
+      if (!grid[g]) continue;
+      const cudaKernelNodeParams kp = params(g);
+      ok = cudaGraphExecKernelNodeSetParams(s->graph, s->gnodes[g], &kp) == cudaSuccess;
     }
+    if (ok) {
+      s->graph_ctas = total;
+      s->graph_updates++;
+      return NAT_OK;
+    }
+    cudaGetLastError();  // an update the driver refused: build anew
   }
-  cudaError_t e = cudaGraphInstantiate(&s->graph, gr, 0);
-  cudaGraphDestroy(gr);
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->graph_tmpl) cudaGraphDestroy(s->graph_tmpl);
+  s->graph = nullptr;
+  s->graph_tmpl = nullptr;
+  SCK(cudaGraphCreate(&s->graph_tmpl, 0), "graph create");
+  for (int g = 0; g < NGROUPS; ++g) {
+    s->gnodes[g] = nullptr;
+    if (!grid[g]) continue;
+    const cudaKernelNodeParams kp = params(g);
+    cudaError_t e = cudaGraphAddKernelNode(&s->gnodes[g], s->graph_tmpl, nullptr, 0, &kp);
+    if (e != cudaSuccess) return sfail(s, NAT_ERR_CUDA, "graph node: %s", cudaGetErrorString(e));
+  }
+  cudaError_t e = cudaGraphInstantiate(&s->graph, s->graph_tmpl, 0);
   if (e != cudaSuccess) return sfail(s, NAT_ERR_CUDA, "instantiate: %s", cudaGetErrorString(e));
+  s->graph_mask = mask;
   s->graph_ctas = total;
   s->graph_nodes = 0;
   for (int g = 0; g < NGROUPS; ++g) s->graph_nodes += grid[g] ? 1 : 0;
+  s->graph_builds++;
   return NAT_OK;
 }
 
@@ -613,7 +645,7 @@ int nat_server_create(size_t pool_bytes, int max_slots, nat_server** out) {
   SCK(cudaMemsetAsync(s->d_ticket, 0, sizeof(unsigned), s->stream), "ticket clear");
   s->max_work = 1 << 16;
   SCK(cudaMalloc(&s->d_work, sizeof(WorkItem) * s->max_work), "work list");
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < nat_server::NSTAGE; ++k) {
     s->stage_cap[k] = s->max_work;
     SCK(cudaHostAlloc(&s->stage_work[k], sizeof(WorkItem) * s->stage_cap[k], cudaHostAllocDefault), "staging");
     SCK(cudaHostAlloc(&s->stage_groups[k], sizeof(GroupRange) * NGROUPS, cudaHostAllocDefault), "staging");
@@ -635,6 +667,7 @@ int nat_server_destroy(nat_server* s) {
   }
   for (auto& kv : s->done) delete kv.second;
   if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->graph_tmpl) cudaGraphDestroy(s->graph_tmpl);
   cudaFree(s->pool_base);
   cudaFree(s->d_slots);
   cudaFree(s->d_status);
@@ -642,7 +675,7 @@ int nat_server_destroy(nat_server* s) {
   cudaFree(s->d_step);
   cudaFree(s->d_ticket);
   cudaFree(s->d_work);
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < nat_server::NSTAGE; ++k) {
     cudaFreeHost(s->stage_work[k]);
     cudaFreeHost(s->stage_groups[k]);
     cudaFreeHost(s->stage_slots[k]);
@@ -680,13 +713,17 @@ int server_step(nat_server* s, int* ran) {
   rc = admit(s);
   if (rc) return rc;
   if (s->live.empty()) return NAT_OK;
-  if (s->dirty) {
-    rc = upload_state(s);
-    if (rc) return rc;
-  }
-  if (!s->graph) {
+  if (s->dirty || s->graph_stale || !s->graph) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (s->dirty) {
+      rc = upload_state(s);
+      if (rc) return rc;
+    }
     rc = capture(s);
     if (rc) return rc;
+    s->graph_stale = false;
+    s->rebuild_ns +=
+        std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
   }
   SCK(cudaGraphLaunch(s->graph, s->stream), "graph launch");
   s->launches += s->graph_nodes;  // the graph's kernels, one per group
@@ -770,6 +807,9 @@ int nat_server_stats(const nat_server* s, nat_server_stats_t* st) {
   st->pool_used = (int64_t)s->pool.used;
   st->pool_bytes = (int64_t)s->pool_bytes;
   st->launches = s->launches;
+  st->graph_builds = s->graph_builds;
+  st->graph_updates = s->graph_updates;
+  st->rebuild_ns = s->rebuild_ns;
   return NAT_OK;
 }
 

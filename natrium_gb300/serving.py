@@ -33,7 +33,8 @@ class _Request(C.Structure):
 
 class _Stats(C.Structure):
     _fields_ = [(k, C.c_int64) for k in ("pending", "live", "completing", "finished", "steps", "node_updates",
-                                         "pool_used", "pool_bytes", "launches")]
+                                         "pool_used", "pool_bytes", "launches", "graph_builds",
+                                         "graph_updates", "rebuild_ns")]
 
 
 @dataclass
@@ -250,6 +251,9 @@ def run_workload(arrivals, reqs, pool_bytes: int = 8 << 30, max_slots: int = 512
         "node_updates_per_s": stats["node_updates"] / (wall - first),
         "server_steps": stats["steps"],
         "launches": stats["launches"],
+        "graph_builds": stats["graph_builds"],
+        "graph_updates": stats["graph_updates"],
+        "host_rebuild_s": stats["rebuild_ns"] * 1e-9,
     }
 
 

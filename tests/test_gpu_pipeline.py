@@ -1,6 +1,7 @@
 """Pipelined host I/O through the C ABI: nat_upload_f on its own copy stream
-(two input staging buffers), asynchronous read-back tickets
-(nat_download_macro_async / nat_wait).
+(two input staging buffers) and conversion stream (into a spare state
+buffer), asynchronous read-back tickets (nat_download_macro_async /
+nat_wait).
 
 Each pipelined result must equal, bit for bit, the blocking
 upload -> step -> download of the same state, while the next state's upload
@@ -52,6 +53,41 @@ def test_pipelined_readback_equals_blocking(gpu_lib, stencil, cells, p, precisio
         for k, (r, v) in enumerate(expect):
             assert np.array_equal(rho[k], r), k
             assert np.array_equal(u[k], v), k
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
+@pytest.mark.parametrize("stencil,cells,p,dg", [("D2Q9", (6, 5), 3, False), ("D3Q19", (4, 4, 4), 4, True)])
+def test_upload_into_spare_buffer(gpu_lib, stencil, cells, p, dg, precision):
+    """nat_upload_f converts into a spare state buffer on its own streams and
+    then makes it the current one: two uploads in a row leave the second
+    state; an upload while steps are in flight replaces the state only for
+    the steps after it; the previous current buffer, now the spare, is
+    reused by the next upload without corrupting anything in flight."""
+    st, mesh, dt, tau, spec = make_case(stencil, cells, p, dg, "BGK_STANDARD", precision=precision)
+    states = [np.ascontiguousarray(periodic_state(mesh, st, seed=s)) for s in range(4)]
+    with N.Solver(spec) as sol:
+        # the reference for each: upload, read back f, one step, read back rho/u
+        ref_f, ref_m = [], []
+        for f in states:
+            sol.upload_f(f)
+            ref_f.append(sol.download_f())
+            sol.step(1)
+            ref_m.append(sol.download_macro())
+        # two uploads in a row: the second state is the current one
+        sol.upload_f(states[0])
+        sol.upload_f(states[1])
+        assert np.array_equal(sol.download_f(), ref_f[1])
+        # upload, step (async), upload, step, ... with no synchronisation
+        for k in range(4):
+            sol.upload_f(states[k])
+            sol.step_async(1, True)
+        r, u = sol.download_macro()
+        assert np.array_equal(r, ref_m[3][0]) and np.array_equal(u, ref_m[3][1])
+        # a step after an upload continues from the uploaded state
+        sol.upload_f(states[2])
+        sol.step(1)
+        r, u = sol.download_macro()
+        assert np.array_equal(r, ref_m[2][0]) and np.array_equal(u, ref_m[2][1])
 
 
 def test_ticket_ring_reuse(gpu_lib):
