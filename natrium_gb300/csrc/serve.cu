@@ -33,6 +33,7 @@ using namespace natgpu;
 namespace {
 
 constexpr int SERVE_WARPS = 8;  // warps per CTA of the batched kernel
+constexpr int SERVE_MINB = 3;   // resident CTAs per SM it is compiled for
 
 struct SlotDesc {
   float* f[2];  // ping-pong distribution buffers (FP32 deviation)
@@ -53,8 +54,8 @@ struct WorkItem {
 };
 
 template <int P, int COLL>
-__device__ __forceinline__ void serve_item(const SlotDesc& d, const float* sw, float* buf, int row, int seg,
-                                           int lane, long long step) {
+__device__ __forceinline__ void serve_item(const SlotDesc& d, const float* sw, float* buf, float* fs, int row,
+                                           int seg, int lane, long long step) {
   const int par = (int)((step - d.start_step) & 1);
   RowArgs<float> a;
   a.f_in = d.f[par];
@@ -69,7 +70,7 @@ __device__ __forceinline__ void serve_item(const SlotDesc& d, const float* sw, f
   a.tau = d.tau;
   a.scaling = d.scaling;
   a.write_macro = step == d.last_step;
-  row_body<SD2Q9, float, COLL, P, false>(a, sw, buf, row, 0, seg * 32, lane);
+  row_body<SD2Q9, float, COLL, P, false, true>(a, sw, buf, row, 0, seg * 32, lane, fs);
   __syncwarp();
 }
 
@@ -87,8 +88,11 @@ struct GroupRange {
 // The CTA that finishes last among all CTAs of the step's kernels
 // (total_ctas, counted on *ticket) advances the device step counter: every
 // CTA has read the counter before that.
+// The streamed values of a segment wait in the warp's shared array (the row
+// kernel's shared-state form): at most 80 registers, three resident CTAs
+// per SM (24 warps) instead of two at 128.
 template <int P, int COLL>
-__global__ void __launch_bounds__(32 * SERVE_WARPS, 2)
+__global__ void __launch_bounds__(32 * SERVE_WARPS, SERVE_MINB)
     k_serve_group(const SlotDesc* __restrict__ slots, const WorkItem* __restrict__ work,
                   const GroupRange* __restrict__ groups, long long* step_ctr, unsigned* ticket,
                   unsigned total_ctas) {
@@ -96,6 +100,7 @@ __global__ void __launch_bounds__(32 * SERVE_WARPS, 2)
   constexpr int BW = 32 + P + P + 1;
   __shared__ float s_tab[SERVE_WARPS][TAB];
   __shared__ float s_buf[SERVE_WARPS][2 * (BW + 1)];
+  __shared__ float s_fs[SERVE_WARPS][SD2Q9::Q * 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const GroupRange gr = groups[serve_group(P, COLL)];
   const long long step = *step_ctr;
@@ -114,7 +119,7 @@ __global__ void __launch_bounds__(32 * SERVE_WARPS, 2)
       __syncwarp();
       cur = it.slot;
     }
-    serve_item<P, COLL>(d, s_tab[warp], s_buf[warp], it.row, it.seg, lane, step);
+    serve_item<P, COLL>(d, s_tab[warp], s_buf[warp], s_fs[warp], it.row, it.seg, lane, step);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -399,7 +404,7 @@ int upload_state(nat_server* s) {
 
 // The step graph of the live set: a kernel node per non-empty group, no
 // dependencies between them (independent solves), each with a grid of about
-// two items per warp, at most two CTAs per SM.  When the set of non-empty
+// two items per warp, at most SERVE_MINB CTAs per SM.  When the set of non-empty
 // groups is the one the graph was built for, the nodes' grids and the CTA
 // total are updated in the instantiated graph; otherwise it is built anew.
 int capture(nat_server* s) {
@@ -408,7 +413,7 @@ int capture(nat_server* s) {
   for (int g = 0; g < NGROUPS; ++g) {
     if (!s->group_count[g]) continue;
     const int want = (s->group_count[g] + 2 * SERVE_WARPS - 1) / (2 * SERVE_WARPS);
-    grid[g] = want < 1 ? 1 : (want > 2 * s->sms ? 2 * s->sms : want);
+    grid[g] = want < 1 ? 1 : (want > SERVE_MINB * s->sms ? SERVE_MINB * s->sms : want);
     total += (unsigned)grid[g];
     mask |= 1u << g;
   }
