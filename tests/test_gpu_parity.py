@@ -354,6 +354,37 @@ def test_automatic_variant_choice(gpu_lib):
             sol.set_kernel_variant(2)
 
 
+def test_cell_variants_refused_where_they_do_not_apply(gpu_lib):
+    """Variants 11-13 need DG rows of 16 or 32 cells; 12 only exists for
+    D3Q27 FP32 and 13 not for D3Q27 FP32 BGK: asking for one where it does
+    not apply is refused (NAT_ERR_UNSUPPORTED), and the handle steps
+    correctly after the automatic choice is restored."""
+    st, mesh, dt, tau, spec = make_case("D3Q19", (16, 8, 1), 4, True, "BGK_STANDARD", precision="fp32dev")
+    with N.Solver(spec) as sol:
+        for v in (11, 13):
+            sol.set_kernel_variant(v)
+            assert sol.kernel_variant == v
+        with pytest.raises(N.NatError):
+            sol.set_kernel_variant(12)
+    st, mesh, dt, tau, spec = make_case("D3Q27", (32, 2, 1), 3, True, "BGK_STANDARD", precision="fp32dev")
+    with N.Solver(spec) as sol:
+        sol.set_kernel_variant(12)
+        assert sol.kernel_variant == 12
+        with pytest.raises(N.NatError):
+            sol.set_kernel_variant(13)
+    st, mesh, dt, tau, spec = make_case("D3Q19", (12, 2, 1), 4, True, "BGK_STANDARD", precision="fp32dev")
+    with N.Solver(spec) as sol:  # 12 cells per x row: no cell-row kernel
+        with pytest.raises(N.NatError):
+            sol.set_kernel_variant(11)
+        f0 = periodic_state(mesh, st, seed=5)
+        S = O.SLOperator(mesh, st, dt)
+        f1, rho1, u1 = oracle_step(S, st, "BGK_STANDARD", tau, f0, 2)
+        sol.set_kernel_variant(0)
+        sol.upload_f(f0)
+        sol.step(2)
+        assert rel_l2(sol.download_f(), f1) <= 1e-6
+
+
 @pytest.mark.parametrize("stencil,p,model", [("D3Q19", 4, "BGK_STANDARD"), ("D3Q27", 3, "KBC_STANDARD")])
 def test_fp32_tgv3d_long_run_against_fp64(gpu_lib, stencil, p, model):
     """3-D Taylor-Green (Ma 0.1, Re 1600), FP32 deviation storage against the
