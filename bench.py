@@ -70,14 +70,37 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def spec_for(precision: str):
+def spec_for(precision: str, topology: str = None):
     import natrium_gb300 as N
     w = WORKLOAD
     scaling = math.sqrt(3) / w["Ma"]
     nu = 1.0 / w["Re"]  # U = 1, characteristic length 1 (TaylorGreenVortex3D.cpp:21)
     return N.SolverSpec(stencil=w["stencil"], order=w["order"], cells=w["cells"], length=(w["L"],) * 3,
                         scaling=scaling, viscosity=nu, cfl=w["cfl"], collision=w["collision"],
-                        precision=precision, topology=w["topology"])
+                        precision=precision, topology=topology or w["topology"])
+
+
+def bench_feq(torch, stream, flush, steps: int = 50, warmup: int = 5):
+    """The same workload on the reference's own node topology, FE_Q p = 4
+    (16^3 cells: 64^3 = 262,144 device nodes, the periodic duplicates folded;
+    274,625 in the reference layout), FP64 and FP32 deviation, each with the
+    autotuner's kernel, device-timed like the headline (L2 flushed between
+    steps)."""
+    import natrium_gb300 as N
+    out = {"workload": WORKLOAD["name"].replace("_dg_", "_feq_"), "unit": UNIT}
+    for prec in ("fp64", "fp32dev"):
+        spec = spec_for(prec, "feq")
+        with N.Solver(spec) as sol:
+            sol.set_stream(stream.cuda_stream)
+            f0 = initial_state(spec)
+            sol.upload_f(f0)
+            sol.autotune(5)
+            sol.upload_f(f0)
+            per, launches = time_device(sol, torch, stream, flush, steps, warmup)
+            ms = sum(per) / steps
+            out[prec] = {"ms_per_step": ms, "value": sol.n_dev / (ms * 1e-3), "nodes": sol.n_dev,
+                         "kernel": sol.kernel_info(), "gpu_launches": launches}
+    return out
 
 
 def initial_state(spec):
@@ -831,6 +854,7 @@ def run_ours(args):
     compressible = None if args.no_compressible else bench_compressible(torch, stream, flush)
     mapped = None if args.no_mapped else bench_mapped(torch, stream, flush)
     mixed = None if args.no_mixed else bench_mixed(torch, stream, flush)
+    feq = None if args.no_mixed else bench_feq(torch, stream, flush)
     serving = None
     if not args.no_serving:
         from natrium_gb300 import serving as SV
@@ -887,6 +911,7 @@ def run_ours(args):
         "compressible": compressible,
         "mapped": mapped,
         "mixed_d3q27": mixed,
+        "feq_topology": feq,
         "state_ok": ok,
     }
     print(json.dumps(line))
