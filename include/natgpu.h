@@ -368,9 +368,9 @@ int nat_device_f(nat_solver* s, void** f_dev);
  * 6 = bulk-copy row-segment kernel required (3-D stencils; per-warp
  * cp.async.bulk pipeline of the source rows), 7 = row-group kernel required
  * (3-D, FP32: 2-4 warps own a whole x row, no halo recomputation), 11 =
- * cell-row kernel required (3-D, DG: a lane owns one cell's p + 1 nodes along
- * x, a warp whole periodic x rows of 16 or 32 cells; vector loads of cell
- * rows, the x window by warp shuffles), 12 = the cell-row kernel with the 8
+ * cell-row kernel required (3-D: a lane owns one cell's nodes along x, p + 1
+ * in DG, p in FE_Q, a warp whole periodic x rows of 16 or 32 cells; vector
+ * loads of cell rows, the x window by warp shuffles), 12 = the cell-row kernel with the 8
  * corner directions of D3Q27 (FP32 deviation storage, DG p = 3, 32 cells per
  * x row) applied as dense per-cell operator tiles on the tensor cores
  * (mma.sync m16n8k8, operands split into two TF32 halves, FP32

@@ -10,6 +10,7 @@ void cell_kernels(std::vector<RowLaunch>& v) {
   cell_kernels_q27d(v);
   cell_kernels_q19f(v);
   cell_kernels_q19d(v);
+  cell_kernels_q19feq(v);
 }
 
 }  // namespace natgpu

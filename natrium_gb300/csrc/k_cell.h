@@ -7,35 +7,36 @@
 
 namespace natgpu {
 namespace cellreg {
-template <class S, class Real, int COLL, int P, int L, int WARPS, int MINB, bool MMA = false, bool ZS = false>
+template <class S, class Real, int COLL, int P, int L, int WARPS, int MINB, bool MMA = false, bool ZS = false,
+          bool DG = true>
 RowLaunch centry(int coll) {
   RowLaunch e;
   e.stencil = S::ID;
   e.coll = coll;
   e.prec = sizeof(Real) == 8 ? 0 : 1;
   e.P = P;
-  e.dg = true;
+  e.dg = DG;
   e.wy = WARPS * (32 / L);  // rows per CTA
   e.wz = 1;
   e.kind = MMA ? 12 : (ZS ? 13 : 11);
-  e.g = L;                  // cells per x row: nx = L (P + 1)
+  e.g = L;                  // cells per x row: nx = L (P + 1) in DG, L P in FE_Q
   e.warps = WARPS;
-  e.smem = (size_t)WARPS * cell_smem_per_warp<S, Real, P>() + (MMA ? CORNER_A_FLOATS * sizeof(float) : 0);
-  e.fn = (const void*)&k_sl_cell<S, Real, COLL, P, L, WARPS, MINB, MMA, ZS>;
+  e.smem = (size_t)WARPS * cell_smem_per_warp<S, Real, P, DG>() + (MMA ? CORNER_A_FLOATS * sizeof(float) : 0);
+  e.fn = (const void*)&k_sl_cell<S, Real, COLL, P, L, WARPS, MINB, MMA, ZS, DG>;
   return e;
 }
 
-template <class S, class Real, int COLL, int P, int L, bool ZS = false>
+template <class S, class Real, int COLL, int P, int L, bool ZS = false, bool DG = true>
 void add_shapes(std::vector<RowLaunch>& v, int coll) {
-  constexpr size_t per_warp = cell_smem_per_warp<S, Real, P>();
+  constexpr size_t per_warp = cell_smem_per_warp<S, Real, P, DG>();
   // CTAs of 4 warps per SM within ~220 KB of shared memory; the same
   // register cap with CTAs of 2 warps; and one CTA fewer per SM (more
   // registers per thread, fewer spills)
   constexpr int M4 = (int)(220000 / (4 * per_warp)) > 0 ? (int)(220000 / (4 * per_warp)) : 1;
   constexpr int M4C = M4 > 8 ? 8 : M4;
-  v.push_back(centry<S, Real, COLL, P, L, 4, M4C, false, ZS>(coll));
-  v.push_back(centry<S, Real, COLL, P, L, 2, 2 * M4C, false, ZS>(coll));
-  if constexpr (M4C > 1) v.push_back(centry<S, Real, COLL, P, L, 4, M4C - 1, false, ZS>(coll));
+  v.push_back(centry<S, Real, COLL, P, L, 4, M4C, false, ZS, DG>(coll));
+  v.push_back(centry<S, Real, COLL, P, L, 2, 2 * M4C, false, ZS, DG>(coll));
+  if constexpr (M4C > 1) v.push_back(centry<S, Real, COLL, P, L, 4, M4C - 1, false, ZS, DG>(coll));
 }
 
 }  // namespace cellreg
@@ -45,5 +46,6 @@ void cell_kernels_q27fz(std::vector<RowLaunch>& v);
 void cell_kernels_q27d(std::vector<RowLaunch>& v);
 void cell_kernels_q19f(std::vector<RowLaunch>& v);
 void cell_kernels_q19d(std::vector<RowLaunch>& v);
+void cell_kernels_q19feq(std::vector<RowLaunch>& v);
 
 }  // namespace natgpu

@@ -607,7 +607,7 @@ std::vector<Cand> v2_candidates(nat_solver* s, int coll_sel, int smem_optin) {
     if (e.kind == 7 && (s->n_ax[0] > 32 * e.g || s->n_ax[0] <= 32 * (e.g - 1) || s->n_ax[0] < e.min_nx))
       continue;
     if ((e.kind == 11 || e.kind == 12 || e.kind == 13) &&
-        (s->n_ax[0] != e.g * (e.P + 1) || (long long)e.smem > smem_optin))
+        (s->n_ax[0] != e.g * (e.dg ? e.P + 1 : e.P) || (long long)e.smem > smem_optin))
       continue;
     // the tensor-core corner form runs only when asked for: it is slower and
     // misses the FP32 path's accuracy (kernel variant 12)
@@ -1949,7 +1949,7 @@ int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* t
     int t = k == 2 ? s->v2.B[a] : s->B[a];
     if (k == 3 || k == 6) t = a == 0 ? 32 : (a == 1 ? s->row.wy : s->row.wz);
     if (k == 7) t = a == 0 ? 32 * s->row.g : (a == 1 ? s->row.wy : 1);
-    if (k >= 11 && k <= 13) t = a == 0 ? s->row.g * (s->spec.order + 1) : (a == 1 ? s->row.wy : 1);
+    if (k >= 11 && k <= 13) t = a == 0 ? s->row.g * s->period : (a == 1 ? s->row.wy : 1);
     if (tile_nodes) tile_nodes[a] = t;
   }
   const bool row = k == 3 || k == 6 || k == 7 || (k >= 11 && k <= 13);

@@ -99,10 +99,11 @@ __device__ __forceinline__ Real wsum_fixed(const Real (&w)[P + 1], const Real (&
   }
 }
 
-// Shared memory per warp: Q * 32 * PER values.
-template <class S, class Real, int P>
+// Shared memory per warp: Q * 32 * PER values (PER = p + 1 nodes per cell
+// row in DG, p in FE_Q).
+template <class S, class Real, int P, bool DG = true>
 __host__ __device__ constexpr size_t cell_smem_per_warp() {
-  return (size_t)S::Q * 32 * (P + 1) * sizeof(Real);
+  return (size_t)S::Q * 32 * (DG ? P + 1 : P) * sizeof(Real);
 }
 
 // ---- tensor-core form of the corner directions (D3Q27, p = 3, FP32) --------
@@ -257,6 +258,39 @@ __device__ __forceinline__ void x_factor(const Real (&Wx)[PER_MAX][PMAX1], const
   });
 }
 
+// The x factor in FE_Q (a lane owns its cell's nodes 0 .. P - 1; node P is
+// node 0 of the next cell, the next lane's T[0]): for sx > 0 the class that
+// leaves the cell (0) takes the previous cell's P values and its own node 0,
+// the others the own cell [T_0 .. T_{P-1}, next T_0]; for sx < 0 every class
+// stays in the own cell.
+template <bool DEV, int P, int L, int sx, class Real>
+__device__ __forceinline__ void x_factor_feq(const Real (&Wx)[PER_MAX][PMAX1], const Real (&T)[P], Real (&out)[P],
+                                             int X, int r) {
+  const Real n0 = __shfl_sync(0xffffffffu, T[0], r * L + (X + 1) % L);
+  Real U[P];
+  if constexpr (sx > 0) {
+#pragma unroll
+    for (int c = 0; c < P; ++c) U[c] = __shfl_sync(0xffffffffu, T[c], r * L + (X + L - 1) % L);
+  }
+  static_for<0, P>([&](auto C) {
+    constexpr int c = decltype(C)::value;
+    Real w[P + 1], v[P + 1];
+#pragma unroll
+    for (int j = 0; j <= P; ++j) w[j] = Wx[c][j];
+    if constexpr (sx > 0 && c == 0) {
+#pragma unroll
+      for (int j = 0; j < P; ++j) v[j] = U[j];
+      v[P] = T[0];
+      out[c] = wsum_fixed<DEV, P, P>(w, v);  // dominant: the node itself, window slot P
+    } else {
+#pragma unroll
+      for (int j = 0; j < P; ++j) v[j] = T[j];
+      v[P] = n0;
+      out[c] = wsum_fixed<DEV, P, c>(w, v);
+    }
+  });
+}
+
 // One corner direction A in the tensor-core form for the CTA's y cell `by`
 // (rows 4 by .. 4 by + 3, warp cy owns row 4 by + cy) at row z (class cz):
 // warp w computes cells 8w .. 8w + 7 for all 16 (cx, cy) nodes and stores
@@ -368,20 +402,26 @@ __device__ __forceinline__ void corner_mma(const RowParams<float>& prm, const fl
 // shared memory then ends with the A table.
 //
 // ZS: the directions with y and z components with z sharing (above).
-template <class S, class Real, int COLL, int P, int L, int WARPS, int MINB, bool MMA = false, bool ZS = false>
+// DGT = false: FE_Q (continuous) nodes.  A lane owns its cell's nodes
+// 0 .. p - 1 (PER = p; node p is node 0 of the next cell), a window spans
+// p + 1 nodes, and the x window's extra node comes from the next lane.
+template <class S, class Real, int COLL, int P, int L, int WARPS, int MINB, bool MMA = false, bool ZS = false,
+          bool DGT = true>
 __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_constant__ RowParams<Real> prm) {
   constexpr bool DEV = sizeof(Real) == 4;
   constexpr int Q = S::Q;
-  constexpr int PER = P + 1;
+  constexpr int PER = DGT ? P + 1 : P;  // nodes per cell row (the node period)
+  constexpr int NW = P + 1;             // window length
   constexpr int RPW = 32 / L;
   constexpr int NPW = 32 * PER;  // nodes per warp
   static_assert(L * RPW == 32 && (L & (L - 1)) == 0, "L must be a power of two dividing 32");
   static_assert(!MMA || (Q == 27 && P == 3 && L == 32 && WARPS == 4 && DEV), "tensor-core corners: D3Q27, p=3, FP32");
-  static_assert(!ZS || (S::D == 3 && !MMA && 2 * zs_slots_per_buffer<S, P, L, WARPS>() <= Q - 1 - n_yz<S>()),
-                "z sharing: the two buffers must fit in the slots of the other directions");
+  static_assert(!ZS || (S::D == 3 && !MMA && DGT && 2 * zs_slots_per_buffer<S, P, L, WARPS>() <= Q - 1 - n_yz<S>()),
+                "z sharing: DG, and the two buffers must fit in the slots of the other directions");
+  static_assert(!MMA || DGT, "tensor-core corners: DG");
   extern __shared__ __align__(16) unsigned char cell_smem[];
-  __shared__ Real sw[row_table_size<P, true>()];
-  fill_row_table<Real, P, true>(sw, prm.W.w, threadIdx.x, 32 * WARPS);
+  __shared__ Real sw[row_table_size<P, DGT>()];
+  fill_row_table<Real, P, DGT>(sw, prm.W.w, threadIdx.x, 32 * WARPS);
   float* sA = reinterpret_cast<float*>(cell_smem) + (size_t)WARPS * Q * NPW;
   if constexpr (MMA) fill_corner_table<P>(sA, prm.W.w, threadIdx.x, 32 * WARPS);
   __syncthreads();
@@ -403,19 +443,19 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
   // the lane's y and z window rows per displacement sign (0: positive, 1:
   // negative) in the rotated order (slot 0 the dominant row), as element
   // offsets: computed once for all directions instead of per direction
-  int yrow[2][PER], zrow[2][PER];
+  int yrow[2][NW], zrow[2][NW];
   {
-    const int ws[4] = {win_start<P, true, 1>(y, cy), win_start<P, true, -1>(y, cy),
-                       win_start<P, true, 1>(z, cz), win_start<P, true, -1>(z, cz)};
-    const int j0[4] = {win_j0<P, true, 1>(cy), win_j0<P, true, -1>(cy), win_j0<P, true, 1>(cz),
-                       win_j0<P, true, -1>(cz)};
+    const int ws[4] = {win_start<P, DGT, 1>(y, cy), win_start<P, DGT, -1>(y, cy),
+                       win_start<P, DGT, 1>(z, cz), win_start<P, DGT, -1>(z, cz)};
+    const int j0[4] = {win_j0<P, DGT, 1>(cy), win_j0<P, DGT, -1>(cy), win_j0<P, DGT, 1>(cz),
+                       win_j0<P, DGT, -1>(cz)};
 #pragma unroll
-    for (int j = 0; j < PER; ++j) {
+    for (int j = 0; j < NW; ++j) {
 #pragma unroll
       for (int d = 0; d < 2; ++d) {
         const int ry = j0[d] + j, rz = j0[2 + d] + j;
-        yrow[d][j] = wrap(ws[d] + (ry > P ? ry - PER : ry), ny) * nx;
-        zrow[d][j] = wrap(ws[2 + d] + (rz > P ? rz - PER : rz), nz) * nxy;
+        yrow[d][j] = wrap(ws[d] + (ry > P ? ry - NW : ry), ny) * nx;
+        zrow[d][j] = wrap(ws[2 + d] + (rz > P ? rz - NW : rz), nz) * nxy;
       }
     }
   }
@@ -569,8 +609,10 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
     if constexpr (sx == 0) {
 #pragma unroll
       for (int c = 0; c < PER; ++c) out[c] = T[c];
-    } else {
+    } else if constexpr (DGT) {
       x_factor<DEV, P, L, sx>(prm.W.w[0][dx], T, out, X, r);
+    } else {
+      x_factor_feq<DEV, P, L, sx>(prm.W.w[0][dx], T, out, X, r);
     }
     store_cell<PER>(Sw + (size_t)A * NPW + lane * PER, out);
     }

@@ -551,6 +551,9 @@ EVERY_CASES = [
     ("D3Q19", (16, 4, 2), 4, True, "BGK_STANDARD", "fp32dev"),
     ("D3Q19", (16, 4, 2), 4, True, "BGK_STANDARD", "fp64"),
     ("D3Q19", (32, 2, 1), 3, True, "BGK_STANDARD", "fp32dev"),
+    # the cell-row kernel on FE_Q nodes (a lane owns its cell's p nodes)
+    ("D3Q19", (16, 4, 2), 4, False, "BGK_STANDARD", "fp32dev"),
+    ("D3Q19", (16, 4, 2), 4, False, "BGK_STANDARD", "fp64"),
 ]
 
 
