@@ -8,6 +8,7 @@ void cell_kernels_q19feq(std::vector<RowLaunch>& v) {
   using namespace cellreg;
   add_shapes<SD3Q19, float, COLL_BGK, 4, 16, false, false>(v, L_COLL_BGK);
   add_shapes<SD3Q19, double, COLL_BGK, 4, 16, false, false>(v, L_COLL_BGK);
+  add_shapes<SD3Q19, double, COLL_BGK, 4, 16, true, false>(v, L_COLL_BGK);  // z sharing
 }
 
 }  // namespace natgpu

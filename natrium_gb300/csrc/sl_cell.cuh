@@ -196,20 +196,23 @@ __host__ __device__ constexpr int cell_order(int k) {
     if (!is_yz<S>(a) && n++ == k) return a;
   return -1;
 }
-// window start of row y along an axis with displacement sign SG (DG)
-template <int P, int SG>
-__host__ __device__ constexpr int ws_dg(int y) {
-  return SG > 0 ? y - y % (P + 1) - (y % (P + 1) == 0 ? P + 1 : 0)
-                : y - y % (P + 1) + (y % (P + 1) == P ? P + 1 : 0);
+// window start of row y along an axis with displacement sign SG (the node
+// period PER = p + 1 in DG, p in FE_Q; the window spans p + 1 rows)
+template <int P, bool DG, int SG>
+__host__ __device__ constexpr int ws_row(int y) {
+  constexpr int PER = DG ? P + 1 : P;
+  return SG > 0 ? y - y % PER - (y % PER == 0 ? PER : 0)
+                : y - y % PER + (DG && y % PER == P ? PER : 0);
 }
 // most union rows of R consecutive rows starting at a multiple of R
-template <int P, int R>
+template <int P, bool DG, int R>
 __host__ __device__ constexpr int zs_union_max() {
+  constexpr int PER = DG ? P + 1 : P;
   int m = 0;
-  for (int r = 0; r < (P + 1) * R; r += R) {
-    const int y0 = r + 2 * (P + 1) * R;  // positive, same residue
-    const int a = ws_dg<P, 1>(y0 + R - 1) - ws_dg<P, 1>(y0) + P + 1;
-    const int b = ws_dg<P, -1>(y0 + R - 1) - ws_dg<P, -1>(y0) + P + 1;
+  for (int r = 0; r < PER * R; r += R) {
+    const int y0 = r + 2 * PER * R;  // positive, same residue
+    const int a = ws_row<P, DG, 1>(y0 + R - 1) - ws_row<P, DG, 1>(y0) + P + 1;
+    const int b = ws_row<P, DG, -1>(y0 + R - 1) - ws_row<P, DG, -1>(y0) + P + 1;
     m = a > m ? a : m;
     m = b > m ? b : m;
   }
@@ -217,15 +220,15 @@ __host__ __device__ constexpr int zs_union_max() {
 }
 // directions whose slots hold the two z-sum buffers: the last 2 SPB of the
 // order, SPB = slots per buffer
-template <class S, int P, int L, int WARPS>
+template <class S, int P, int L, int WARPS, bool DG>
 __host__ __device__ constexpr int zs_slots_per_buffer() {
   constexpr int RPW = 32 / L;
-  constexpr int chunks = (zs_union_max<P, WARPS * RPW>() + RPW - 1) / RPW;
+  constexpr int chunks = (zs_union_max<P, DG, WARPS * RPW>() + RPW - 1) / RPW;
   return (chunks + WARPS - 1) / WARPS;
 }
-template <class S, int P, int L, int WARPS>
+template <class S, int P, int L, int WARPS, bool DG>
 __device__ __forceinline__ int zs_slot(int buf, int s) {
-  constexpr int SPB = zs_slots_per_buffer<S, P, L, WARPS>();
+  constexpr int SPB = zs_slots_per_buffer<S, P, L, WARPS, DG>();
   return cell_order<S, true>(S::Q - 2 - (buf * SPB + s));
 }
 
@@ -416,8 +419,8 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
   constexpr int NPW = 32 * PER;  // nodes per warp
   static_assert(L * RPW == 32 && (L & (L - 1)) == 0, "L must be a power of two dividing 32");
   static_assert(!MMA || (Q == 27 && P == 3 && L == 32 && WARPS == 4 && DEV), "tensor-core corners: D3Q27, p=3, FP32");
-  static_assert(!ZS || (S::D == 3 && !MMA && DGT && 2 * zs_slots_per_buffer<S, P, L, WARPS>() <= Q - 1 - n_yz<S>()),
-                "z sharing: DG, and the two buffers must fit in the slots of the other directions");
+  static_assert(!ZS || (S::D == 3 && !MMA && 2 * zs_slots_per_buffer<S, P, L, WARPS, DGT>() <= Q - 1 - n_yz<S>()),
+                "z sharing: the two buffers must fit in the slots of the other directions");
   static_assert(!MMA || DGT, "tensor-core corners: DG");
   extern __shared__ __align__(16) unsigned char cell_smem[];
   __shared__ Real sw[row_table_size<P, DGT>()];
@@ -477,13 +480,13 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
       constexpr int R = WARPS * RPW;
       Real* S_all = reinterpret_cast<Real*>(cell_smem);
       const int y0 = by * R;
-      const int ybase = ws_dg<P, sy>(y0);
-      const int U = ws_dg<P, sy>(y0 + R - 1) - ybase + PER;
+      const int ybase = ws_row<P, DGT, sy>(y0);
+      const int U = ws_row<P, DGT, sy>(y0 + R - 1) - ybase + NW;
       const int* zo = zrow[dz];
       const Real* __restrict__ srcA = prm.f_in + (size_t)A * prm.n;
       auto zaddr = [&](int uu) {  // row uu of this direction's buffer
         const int ch = uu / RPW;
-        const int q = zs_slot<S, P, L, WARPS>(decltype(K)::value & 1, ch / WARPS);
+        const int q = zs_slot<S, P, L, WARPS, DGT>(decltype(K)::value & 1, ch / WARPS);
         return S_all + ((size_t)(ch % WARPS) * Q + q) * NPW + (uu % RPW) * nx;
       };
       for (int it = threadIdx.x; it < U * L; it += 32 * WARPS) {
@@ -491,7 +494,7 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
         const int gy = wrap(ybase + uu, ny);
         Real Z0[PER], acc[PER];
 #pragma unroll
-        for (int jz = 0; jz < PER; ++jz) {
+        for (int jz = 0; jz < NW; ++jz) {
           Real v[PER];
           load_cell<PER>(srcA + (zo[jz] + gy * nx + xc), v);
           const Real wz = tw[2][dz][cz][jz];
@@ -510,12 +513,12 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
         for (int c = 0; c < PER; ++c) zp[c] = DEV ? acc[c] + Z0[c] : acc[c];
       }
       __syncthreads();
-      const int ys = win_start<P, true, sy>(y, cy), j0y = win_j0<P, true, sy>(cy);
+      const int ys = win_start<P, DGT, sy>(y, cy), j0y = win_j0<P, DGT, sy>(cy);
       Real Y0[PER], acc[PER];
 #pragma unroll
-      for (int jy = 0; jy < PER; ++jy) {
+      for (int jy = 0; jy < NW; ++jy) {
         const int ry = j0y + jy;
-        const Real* zp = zaddr(ys - ybase + (ry > P ? ry - PER : ry)) + x0;
+        const Real* zp = zaddr(ys - ybase + (ry > P ? ry - NW : ry)) + x0;
         const Real wy = tw[1][dy][cy][jy];
 #pragma unroll
         for (int c = 0; c < PER; ++c) {
@@ -536,7 +539,10 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
         Real T[PER];
 #pragma unroll
         for (int c = 0; c < PER; ++c) T[c] = DEV ? acc[c] + Y0[c] : acc[c];
-        x_factor<DEV, P, L, sx>(prm.W.w[0][sx > 0 ? 0 : 1], T, out, X, r);
+        if constexpr (DGT)
+          x_factor<DEV, P, L, sx>(prm.W.w[0][sx > 0 ? 0 : 1], T, out, X, r);
+        else
+          x_factor_feq<DEV, P, L, sx>(prm.W.w[0][sx > 0 ? 0 : 1], T, out, X, r);
       }
       if constexpr (decltype(K)::value == n_yz<S>() - 1) {
         // the buffers' slots are written by their own directions later on
