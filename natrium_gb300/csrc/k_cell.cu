@@ -11,6 +11,7 @@ void cell_kernels(std::vector<RowLaunch>& v) {
   cell_kernels_q19f(v);
   cell_kernels_q19d(v);
   cell_kernels_q19feq(v);
+  cell_kernels_wide(v);
 }
 
 }  // namespace natgpu

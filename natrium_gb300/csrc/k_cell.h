@@ -16,7 +16,7 @@ RowLaunch centry(int coll) {
   e.prec = sizeof(Real) == 8 ? 0 : 1;
   e.P = P;
   e.dg = DG;
-  e.wy = WARPS * (32 / L);  // rows per CTA
+  e.wy = L > 32 ? WARPS / (L / 32) : WARPS * (32 / L);  // rows per CTA
   e.wz = 1;
   e.kind = MMA ? 12 : (ZS ? 13 : 11);
   e.g = L;                  // cells per x row: nx = L (P + 1) in DG, L P in FE_Q
@@ -47,5 +47,6 @@ void cell_kernels_q27d(std::vector<RowLaunch>& v);
 void cell_kernels_q19f(std::vector<RowLaunch>& v);
 void cell_kernels_q19d(std::vector<RowLaunch>& v);
 void cell_kernels_q19feq(std::vector<RowLaunch>& v);
+void cell_kernels_wide(std::vector<RowLaunch>& v);
 
 }  // namespace natgpu

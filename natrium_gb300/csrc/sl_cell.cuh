@@ -222,7 +222,7 @@ __host__ __device__ constexpr int zs_union_max() {
 // order, SPB = slots per buffer
 template <class S, int P, int L, int WARPS, bool DG>
 __host__ __device__ constexpr int zs_slots_per_buffer() {
-  constexpr int RPW = 32 / L;
+  constexpr int RPW = L >= 32 ? 1 : 32 / L;
   constexpr int chunks = (zs_union_max<P, DG, WARPS * RPW>() + RPW - 1) / RPW;
   return (chunks + WARPS - 1) / WARPS;
 }
@@ -232,55 +232,32 @@ __device__ __forceinline__ int zs_slot(int buf, int s) {
   return cell_order<S, true>(S::Q - 2 - (buf * SPB + s));
 }
 
-// x factor of the lane's PER nodes from their y/z-factored values T: classes
-// whose departure point stays in the node's own cell take the lane's own
-// values, the one class that leaves it (0 for sx > 0, P for sx < 0) takes the
-// neighbouring lane's (lane r L + nb of the warp's row r); the weights come
-// straight from the kernel's constant bank (compile-time class and window).
-template <bool DEV, int P, int L, int sx, class Real>
-__device__ __forceinline__ void x_factor(const Real (&Wx)[PER_MAX][PMAX1], const Real (&T)[P + 1],
-                                         Real (&out)[P + 1], int X, int r) {
-  constexpr int PER = P + 1;
-  const int nb = sx > 0 ? (X + L - 1) % L : (X + 1) % L;
-  Real U[PER];
-#pragma unroll
-  for (int c = 0; c < PER; ++c) U[c] = __shfl_sync(0xffffffffu, T[c], r * L + nb);
+// x factor of the lane's PER nodes from their y/z-factored values T and the
+// neighbouring cells' values U (previous cell, the one upwind for sx > 0) and
+// V (next cell).  DG: the classes whose departure point stays in the node's
+// own cell take T; the one class that leaves it (0 for sx > 0, P for
+// sx < 0) takes U or V, dominant its nearest node.  FE_Q (a lane owns nodes
+// 0 .. P - 1 of its cell, node P being V[0]): for sx > 0 class 0 takes
+// [U_0 .. U_{P-1}, T_0], the others [T_0 .. T_{P-1}, V_0]; for sx < 0 every
+// class takes the latter.  The weights come straight from the kernel's
+// constant bank (compile-time class and window).
+template <bool DEV, int P, bool DG, int sx, class Real, int PER>
+__device__ __forceinline__ void x_apply(const Real (&Wx)[PER_MAX][PMAX1], const Real (&T)[PER],
+                                        const Real (&U)[PER], const Real (&V)[PER], Real (&out)[PER]) {
   static_for<0, PER>([&](auto C) {
-    constexpr int c = decltype(C)::value;
-    Real w[P + 1];
-#pragma unroll
-    for (int j = 0; j <= P; ++j) w[j] = Wx[c][j];
-    constexpr bool other = sx > 0 ? (c == 0) : (c == P);
-    if constexpr (other) {
-      // window = the neighbouring cell, dominant its nearest node
-      constexpr int J0 = sx > 0 ? P : 0;
-      out[c] = wsum_fixed<DEV, P, J0>(w, U);
-    } else {
-      out[c] = wsum_fixed<DEV, P, c>(w, T);
-    }
-  });
-}
-
-// The x factor in FE_Q (a lane owns its cell's nodes 0 .. P - 1; node P is
-// node 0 of the next cell, the next lane's T[0]): for sx > 0 the class that
-// leaves the cell (0) takes the previous cell's P values and its own node 0,
-// the others the own cell [T_0 .. T_{P-1}, next T_0]; for sx < 0 every class
-// stays in the own cell.
-template <bool DEV, int P, int L, int sx, class Real>
-__device__ __forceinline__ void x_factor_feq(const Real (&Wx)[PER_MAX][PMAX1], const Real (&T)[P], Real (&out)[P],
-                                             int X, int r) {
-  const Real n0 = __shfl_sync(0xffffffffu, T[0], r * L + (X + 1) % L);
-  Real U[P];
-  if constexpr (sx > 0) {
-#pragma unroll
-    for (int c = 0; c < P; ++c) U[c] = __shfl_sync(0xffffffffu, T[c], r * L + (X + L - 1) % L);
-  }
-  static_for<0, P>([&](auto C) {
     constexpr int c = decltype(C)::value;
     Real w[P + 1], v[P + 1];
 #pragma unroll
     for (int j = 0; j <= P; ++j) w[j] = Wx[c][j];
-    if constexpr (sx > 0 && c == 0) {
+    if constexpr (DG) {
+      if constexpr (sx > 0 && c == 0) {
+        out[c] = wsum_fixed<DEV, P, P>(w, U);
+      } else if constexpr (sx < 0 && c == P) {
+        out[c] = wsum_fixed<DEV, P, 0>(w, V);
+      } else {
+        out[c] = wsum_fixed<DEV, P, c>(w, T);
+      }
+    } else if constexpr (sx > 0 && c == 0) {
 #pragma unroll
       for (int j = 0; j < P; ++j) v[j] = U[j];
       v[P] = T[0];
@@ -288,10 +265,89 @@ __device__ __forceinline__ void x_factor_feq(const Real (&Wx)[PER_MAX][PMAX1], c
     } else {
 #pragma unroll
       for (int j = 0; j < P; ++j) v[j] = T[j];
-      v[P] = n0;
+      v[P] = V[0];
       out[c] = wsum_fixed<DEV, P, c>(w, v);
     }
   });
+}
+
+// which neighbouring values a direction's x factor needs
+template <bool DG, int sx>
+__host__ __device__ constexpr bool x_needs_prev() {
+  return sx > 0;
+}
+template <bool DG, int sx>
+__host__ __device__ constexpr bool x_needs_next() {
+  return DG ? sx < 0 : sx != 0;
+}
+
+// x factor when the warp holds whole periodic rows of L <= 32 cells (lane
+// r L + X holds cell X of the warp's row r): the neighbours by shuffles
+template <bool DEV, int P, int L, bool DG, int sx, class Real, int PER>
+__device__ __forceinline__ void x_factor(const Real (&Wx)[PER_MAX][PMAX1], const Real (&T)[PER], Real (&out)[PER],
+                                         int X, int r) {
+  Real U[PER], V[PER];
+#pragma unroll
+  for (int c = 0; c < PER; ++c) {
+    U[c] = T[c];
+    V[c] = T[c];
+  }
+  if constexpr (x_needs_prev<DG, sx>()) {
+#pragma unroll
+    for (int c = 0; c < PER; ++c) U[c] = __shfl_sync(0xffffffffu, T[c], r * L + (X + L - 1) % L);
+  }
+  if constexpr (x_needs_next<DG, sx>()) {
+#pragma unroll
+    for (int c = 0; c < (DG ? PER : 1); ++c) V[c] = __shfl_sync(0xffffffffu, T[c], r * L + (X + 1) % L);
+  }
+  x_apply<DEV, P, DG, sx>(Wx, T, U, V, out);
+}
+
+// x factor when GW warps share a periodic row of 32 GW cells (warp g of the
+// row holds cells 32 g .. 32 g + 31): the neighbours by shuffles inside the
+// warp, and across the warps through shared memory: every warp leaves its
+// lanes 0 and 31's values in edge[warp][0 / 1], the row's warps meet at a
+// named barrier (id 1 + row, 32 GW threads; at most four rows per CTA), and
+// lane 0 / 31 take the
+// previous / next warp's.  edge alternates between two buffers from one
+// direction to the next, so one barrier per direction suffices.
+template <bool DEV, int P, int GW, bool DG, int sx, class Real, int PER>
+__device__ __forceinline__ void x_factor_mw(const Real (&Wx)[PER_MAX][PMAX1], const Real (&T)[PER],
+                                            Real (&out)[PER], int lane, int warp, Real (*edge)[2][PER]) {
+  const int g = warp % GW, row = warp / GW;
+  const int wprev = warp - g + (g + GW - 1) % GW, wnext = warp - g + (g + 1) % GW;
+  if (lane == 0 || lane == 31) {
+#pragma unroll
+    for (int c = 0; c < PER; ++c) edge[warp][lane == 0 ? 0 : 1][c] = T[c];
+  }
+  // a compile-time barrier id per row (a run-time id reserves all sixteen)
+  switch (row) {
+    case 0: asm volatile("bar.sync 1, %0;" ::"n"(32 * GW) : "memory"); break;
+    case 1: asm volatile("bar.sync 2, %0;" ::"n"(32 * GW) : "memory"); break;
+    case 2: asm volatile("bar.sync 3, %0;" ::"n"(32 * GW) : "memory"); break;
+    default: asm volatile("bar.sync 4, %0;" ::"n"(32 * GW) : "memory"); break;
+  }
+  Real U[PER], V[PER];
+#pragma unroll
+  for (int c = 0; c < PER; ++c) {
+    U[c] = T[c];
+    V[c] = T[c];
+  }
+  if constexpr (x_needs_prev<DG, sx>()) {
+#pragma unroll
+    for (int c = 0; c < PER; ++c) {
+      const Real sh = __shfl_sync(0xffffffffu, T[c], (lane + 31) & 31);
+      U[c] = lane == 0 ? edge[wprev][1][c] : sh;
+    }
+  }
+  if constexpr (x_needs_next<DG, sx>()) {
+#pragma unroll
+    for (int c = 0; c < (DG ? PER : 1); ++c) {
+      const Real sh = __shfl_sync(0xffffffffu, T[c], (lane + 1) & 31);
+      V[c] = lane == 31 ? edge[wnext][0][c] : sh;
+    }
+  }
+  x_apply<DEV, P, DG, sx>(Wx, T, U, V, out);
 }
 
 // One corner direction A in the tensor-core form for the CTA's y cell `by`
@@ -415,9 +471,12 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
   constexpr int Q = S::Q;
   constexpr int PER = DGT ? P + 1 : P;  // nodes per cell row (the node period)
   constexpr int NW = P + 1;             // window length
-  constexpr int RPW = 32 / L;
+  constexpr int GW = L > 32 ? L / 32 : 1;    // warps per x row
+  constexpr int RPW = L >= 32 ? 1 : 32 / L;  // x rows per warp
   constexpr int NPW = 32 * PER;  // nodes per warp
-  static_assert(L * RPW == 32 && (L & (L - 1)) == 0, "L must be a power of two dividing 32");
+  static_assert((L & (L - 1)) == 0 && L >= 8 && L <= 128, "L: a power of two, 8 .. 128 cells per x row");
+  static_assert(GW == 1 || (WARPS % GW == 0 && WARPS / GW <= 4 && !ZS && !MMA),
+                "several warps per row: whole rows per CTA, one named barrier per row, no z sharing");
   static_assert(!MMA || (Q == 27 && P == 3 && L == 32 && WARPS == 4 && DEV), "tensor-core corners: D3Q27, p=3, FP32");
   static_assert(!ZS || (S::D == 3 && !MMA && 2 * zs_slots_per_buffer<S, P, L, WARPS, DGT>() <= Q - 1 - n_yz<S>()),
                 "z sharing: the two buffers must fit in the slots of the other directions");
@@ -433,14 +492,17 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   Real* Sw = reinterpret_cast<Real*>(cell_smem) + (size_t)warp * Q * NPW;
+  // cell values at the warps' edges (several warps per row), two buffers
+  __shared__ Real s_edge[2][GW > 1 ? WARPS : 1][2][PER];
+  (void)s_edge;
   const int nx = prm.nx, ny = prm.ny, nz = prm.nz;
   const int nxy = nx * ny;
-  const int rows_per_cta = WARPS * RPW;
+  const int rows_per_cta = GW > 1 ? WARPS / GW : WARPS * RPW;
   const int by = blockIdx.x % (ny / rows_per_cta);
   const int z = blockIdx.x / (ny / rows_per_cta);
-  const int r = lane / L;  // row of this lane within the warp
-  const int X = lane % L;  // cell along x
-  const int y = by * rows_per_cta + warp * RPW + r;
+  const int r = GW > 1 ? 0 : lane / L;                        // row of this lane within the warp
+  const int X = GW > 1 ? (warp % GW) * 32 + lane : lane % L;  // cell along x
+  const int y = by * rows_per_cta + (GW > 1 ? warp / GW : warp * RPW + r);
   const int cy = y % PER, cz = z % PER;
   const int x0 = X * PER;
   // the lane's y and z window rows per displacement sign (0: positive, 1:
@@ -539,10 +601,7 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
         Real T[PER];
 #pragma unroll
         for (int c = 0; c < PER; ++c) T[c] = DEV ? acc[c] + Y0[c] : acc[c];
-        if constexpr (DGT)
-          x_factor<DEV, P, L, sx>(prm.W.w[0][sx > 0 ? 0 : 1], T, out, X, r);
-        else
-          x_factor_feq<DEV, P, L, sx>(prm.W.w[0][sx > 0 ? 0 : 1], T, out, X, r);
+        x_factor<DEV, P, L, DGT, sx>(prm.W.w[0][sx > 0 ? 0 : 1], T, out, X, r);
       }
       if constexpr (decltype(K)::value == n_yz<S>() - 1) {
         // the buffers' slots are written by their own directions later on
@@ -615,10 +674,10 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
     if constexpr (sx == 0) {
 #pragma unroll
       for (int c = 0; c < PER; ++c) out[c] = T[c];
-    } else if constexpr (DGT) {
-      x_factor<DEV, P, L, sx>(prm.W.w[0][dx], T, out, X, r);
+    } else if constexpr (GW > 1) {
+      x_factor_mw<DEV, P, GW, DGT, sx>(prm.W.w[0][dx], T, out, lane, warp, s_edge[xorder<S>(A) & 1]);
     } else {
-      x_factor_feq<DEV, P, L, sx>(prm.W.w[0][dx], T, out, X, r);
+      x_factor<DEV, P, L, DGT, sx>(prm.W.w[0][dx], T, out, X, r);
     }
     store_cell<PER>(Sw + (size_t)A * NPW + lane * PER, out);
     }
@@ -629,12 +688,13 @@ __global__ void __launch_bounds__(32 * WARPS, MINB) k_sl_cell(const __grid_const
     __syncwarp();
 
   // phase 2: collide the warp's nodes, lane-strided
-  const int row0 = by * rows_per_cta + warp * RPW;
+  const int row0 = GW > 1 ? y : by * rows_per_cta + warp * RPW;
+  const int xw = GW > 1 ? (warp % GW) * NPW : 0;  // the warp's first node along x
   const Real inv_tau = Real(1) / Real(prm.tau);
 #pragma unroll 1
   for (int k = 0; k < PER; ++k) {
-    const int t = lane + 32 * k;  // node within the warp's rows
-    const int rr = t / nx, xx = t % nx;
+    const int t = lane + 32 * k;  // node within the warp's rows (or row part)
+    const int rr = GW > 1 ? 0 : t / nx, xx = GW > 1 ? xw + t : t % nx;
     const int node = z * nxy + (row0 + rr) * nx + xx;
     Real fs[Q];
 #pragma unroll
