@@ -370,7 +370,7 @@ int nat_device_f(nat_solver* s, void** f_dev);
  * (3-D, FP32: 2-4 warps own a whole x row, no halo recomputation), 11 =
  * cell-row kernel required (3-D: a lane owns one cell's nodes along x, p + 1
  * in DG, p in FE_Q, a warp whole periodic x rows of 16 or 32 cells, or two
- * warps a row of 64; vector
+ * (four) warps a row of 64 (128); vector
  * loads of cell rows, the x window by warp shuffles), 12 = the cell-row kernel with the 8
  * corner directions of D3Q27 (FP32 deviation storage, DG p = 3, 32 cells per
  * x row) applied as dense per-cell operator tiles on the tensor cores

@@ -25,7 +25,8 @@ SOURCES = ["natgpu_api.cu", "k_d2q9.cu", "k_d3q19.cu", "k_d3q27.cu", "k_v2.cu", 
            "k_rowg_d3q19.cu", "k_rowg_d3q27.cu", "k_mapped_d2q9.cu", "k_mapped_d3q19.cu",
            "k_mapped_d3q27.cu", "tracker.cu", "io.cu", "k_cell.cu", "k_cell_q27f.cu", "k_cell_q27fz.cu",
            "k_cell_q27d.cu", "k_cell_q19f.cu", "k_cell_q19d.cu", "k_thermal_p2.cu",
-           "k_cell_q19feq.cu", "k_cell_wide.cu"]
+           "k_cell_q19feq.cu", "k_cell_wide.cu",
+           "k_cell_wide128.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 # the departure-path tracker runs on the host and on the device and must give

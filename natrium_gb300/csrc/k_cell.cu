@@ -12,6 +12,7 @@ void cell_kernels(std::vector<RowLaunch>& v) {
   cell_kernels_q19d(v);
   cell_kernels_q19feq(v);
   cell_kernels_wide(v);
+  cell_kernels_wide128(v);
 }
 
 }  // namespace natgpu

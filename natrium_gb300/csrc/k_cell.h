@@ -39,6 +39,19 @@ void add_shapes(std::vector<RowLaunch>& v, int coll) {
   if constexpr (M4C > 1) v.push_back(centry<S, Real, COLL, P, L, 4, M4C - 1, false, ZS, DG>(coll));
 }
 
+// x rows of 128 cells: four warps per row, CTAs of one or two rows
+template <class S, class Real, int COLL, int P, bool DG = true>
+void add_shapes_128(std::vector<RowLaunch>& v, int coll) {
+  constexpr size_t per_warp = cell_smem_per_warp<S, Real, P, DG>();
+  constexpr int M4 = (int)(220000 / (4 * per_warp)) > 0 ? (int)(220000 / (4 * per_warp)) : 1;
+  constexpr int M4C = M4 > 8 ? 8 : M4;
+  constexpr int M8 = (int)(220000 / (8 * per_warp)) > 0 ? (int)(220000 / (8 * per_warp)) : 1;
+  constexpr int M8C = M8 > 4 ? 4 : M8;
+  v.push_back(centry<S, Real, COLL, P, 128, 4, M4C, false, false, DG>(coll));
+  v.push_back(centry<S, Real, COLL, P, 128, 8, M8C, false, false, DG>(coll));
+  if constexpr (M4C > 1) v.push_back(centry<S, Real, COLL, P, 128, 4, M4C - 1, false, false, DG>(coll));
+}
+
 }  // namespace cellreg
 
 void cell_kernels_q27f(std::vector<RowLaunch>& v);
@@ -48,5 +61,6 @@ void cell_kernels_q19f(std::vector<RowLaunch>& v);
 void cell_kernels_q19d(std::vector<RowLaunch>& v);
 void cell_kernels_q19feq(std::vector<RowLaunch>& v);
 void cell_kernels_wide(std::vector<RowLaunch>& v);
+void cell_kernels_wide128(std::vector<RowLaunch>& v);
 
 }  // namespace natgpu

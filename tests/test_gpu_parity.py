@@ -556,6 +556,11 @@ EVERY_CASES = [
     ("D3Q19", (64, 2, 1), 4, True, "BGK_STANDARD", "fp64"),
     ("D3Q19", (64, 2, 2), 4, False, "BGK_STANDARD", "fp32dev"),
     ("D3Q27", (64, 2, 1), 3, True, "KBC_STANDARD", "fp32dev"),
+    # x rows of 128 cells: four warps per row
+    ("D3Q19", (128, 2, 1), 4, True, "BGK_STANDARD", "fp32dev"),
+    ("D3Q19", (128, 2, 1), 4, True, "BGK_STANDARD", "fp64"),
+    ("D3Q19", (128, 2, 2), 4, False, "BGK_STANDARD", "fp32dev"),
+    ("D3Q27", (128, 2, 1), 3, True, "KBC_STANDARD", "fp32dev"),
     # the cell-row kernel on FE_Q nodes (a lane owns its cell's p nodes)
     ("D3Q19", (16, 4, 2), 4, False, "BGK_STANDARD", "fp32dev"),
     ("D3Q19", (16, 4, 2), 4, False, "BGK_STANDARD", "fp64"),
