@@ -564,6 +564,7 @@ EVERY_CASES = [
     # the cell-row kernel on FE_Q nodes (a lane owns its cell's p nodes)
     ("D3Q19", (16, 4, 2), 4, False, "BGK_STANDARD", "fp32dev"),
     ("D3Q19", (16, 4, 2), 4, False, "BGK_STANDARD", "fp64"),
+    ("D3Q27", (32, 4, 2), 3, False, "KBC_STANDARD", "fp32dev"),
 ]
 
 
