@@ -612,7 +612,9 @@ def bench_config(nodes: int, ws: int) -> dict:
     w = WORKLOAD
     return {"workload": w["name"], "nodes": nodes, "stencil": w["stencil"], "collision": w["collision"],
             "order": w["order"], "topology": w["topology"], "cells": list(w["cells"]), "Ma": w["Ma"], "Re": w["Re"],
-            "cfl": w["cfl"], "storage": "fp64 (plain)", "parallelism": f"replicas x{ws}"}
+            "cfl": w["cfl"], "storage": "fp64 (plain)", "parallelism": f"replicas x{ws}",
+            "l2": "GPU arm: L2 flushed between timed steps (256 MiB write outside the timed events); "
+                  "CPU arm: no flush (host caches)"}
 
 
 def run_reference(args):
