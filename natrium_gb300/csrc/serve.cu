@@ -404,7 +404,8 @@ int upload_state(nat_server* s) {
 
 // The step graph of the live set: a kernel node per non-empty group, no
 // dependencies between them (independent solves), each with a grid of about
-// two items per warp, at most SERVE_MINB CTAs per SM.  When the set of non-empty
+// one item per warp (a short serial chain per step), at most SERVE_MINB CTAs
+// per SM.  When the set of non-empty
 // groups is the one the graph was built for, the nodes' grids and the CTA
 // total are updated in the instantiated graph; otherwise it is built anew.
 int capture(nat_server* s) {
@@ -412,7 +413,7 @@ int capture(nat_server* s) {
   unsigned total = 0, mask = 0;
   for (int g = 0; g < NGROUPS; ++g) {
     if (!s->group_count[g]) continue;
-    const int want = (s->group_count[g] + 2 * SERVE_WARPS - 1) / (2 * SERVE_WARPS);
+    const int want = (s->group_count[g] + SERVE_WARPS - 1) / SERVE_WARPS;  // one item per warp
     grid[g] = want < 1 ? 1 : (want > SERVE_MINB * s->sms ? SERVE_MINB * s->sms : want);
     total += (unsigned)grid[g];
     mask |= 1u << g;
