@@ -44,6 +44,12 @@ int main(void) {
   if (nat_download_macro_async(NULL, x, x, &ticket) != NAT_ERR_INVALID_ARG) return 15;
   if (nat_wait(NULL, 1) != NAT_ERR_INVALID_ARG) return 16;
   if (nat_destroy(NULL) != NAT_OK) return 17;
+  {
+    /* the server statistics the Python mirror reads field by field: twelve int64 */
+    nat_server_stats_t st;
+    if (sizeof st != 12 * sizeof(int64_t)) return 18;
+    if (nat_server_stats(NULL, &st) != NAT_ERR_INVALID_ARG) return 19;
+  }
   printf("ok %s\n", nat_version());
   return 0;
 }
@@ -66,3 +72,17 @@ def test_c99_program_includes_header_and_links(tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
     assert r.stdout.startswith("ok ")
+
+
+def test_server_stats_layout_matches_python_mirror():
+    """natrium_gb300.serving reads nat_server_stats_t through ctypes: the same
+    twelve int64 fields in the same order as include/natgpu.h."""
+    import ctypes
+    from natrium_gb300 import serving as SV
+    names = [f for f, _ in SV._Stats._fields_]
+    assert ctypes.sizeof(SV._Stats) == 12 * 8
+    hdr = open(os.path.join(ROOT, "include", "natgpu.h")).read()
+    body = hdr[hdr.index("typedef struct nat_server_stats_t {"):hdr.index("} nat_server_stats_t;")]
+    decl = " ".join(l.split("/*")[0] for l in body.splitlines()[1:] if "int64_t" in l)
+    fields = [f.strip(" ;") for f in decl.replace("int64_t", "").replace(";", ",").split(",") if f.strip(" ;")]
+    assert fields == names
