@@ -51,20 +51,22 @@ cudaError_t launch_thermal_init(const ThermalPointT<double>& P, void* f, void* g
 
 template <class Real>
 static cudaError_t wall_nodes_t(const ThermalStepT<Real>& P, int nbn, const int* node, const int* ptr,
-                                const int* col, const Real* w, const double* cst, cudaStream_t st) {
+                                const int* col, const Real* w, const double* cst, bool collide, cudaStream_t st) {
   const int nrows = nbn * (TH_Q - 1);
   k_thermal_rows<Real><<<(nrows + 255) / 256, 256, 0, st>>>(P, nrows, node, ptr, col, w, cst);
-  k_thermal_collide_nodes<Real><<<(nbn + 127) / 128, 128, 0, st>>>(P, nbn, node);
+  if (collide) k_thermal_collide_nodes<Real><<<(nbn + 127) / 128, 128, 0, st>>>(P, nbn, node);
   return cudaGetLastError();
 }
 
 cudaError_t launch_thermal_wall_nodes(const ThermalStepT<double>& P, int nbn, const int* node, const int* ptr,
-                                      const int* col, const double* w, const double* cst, cudaStream_t st) {
-  return wall_nodes_t(P, nbn, node, ptr, col, w, cst, st);
+                                      const int* col, const double* w, const double* cst, bool collide,
+                                      cudaStream_t st) {
+  return wall_nodes_t(P, nbn, node, ptr, col, w, cst, collide, st);
 }
 cudaError_t launch_thermal_wall_nodes(const ThermalStepT<float>& P, int nbn, const int* node, const int* ptr,
-                                      const int* col, const float* w, const double* cst, cudaStream_t st) {
-  return wall_nodes_t(P, nbn, node, ptr, col, w, cst, st);
+                                      const int* col, const float* w, const double* cst, bool collide,
+                                      cudaStream_t st) {
+  return wall_nodes_t(P, nbn, node, ptr, col, w, cst, collide, st);
 }
 
 }  // namespace natgpu

@@ -104,10 +104,13 @@ cudaError_t launch_thermal_collide(const ThermalPointT<float>& P, int grid, cuda
 cudaError_t launch_thermal_init(const ThermalPointT<double>& P, void* f, void* g, bool fp32, int grid,
                                 cudaStream_t st);
 // fused step of the wall nodes of the two-population model: rows as
-// k_wall_nodes, f and g through the same rows (constant slots f, g)
+// k_wall_nodes, f and g through the same rows (constant slots f, g);
+// collide = false: the rows only (the step kernel then collides the nodes)
 cudaError_t launch_thermal_wall_nodes(const ThermalStepT<double>& P, int nbn, const int* node, const int* ptr,
-                                      const int* col, const double* w, const double* cst, cudaStream_t st);
+                                      const int* col, const double* w, const double* cst, bool collide,
+                                      cudaStream_t st);
 cudaError_t launch_thermal_wall_nodes(const ThermalStepT<float>& P, int nbn, const int* node, const int* ptr,
-                                      const int* col, const float* w, const double* cst, cudaStream_t st);
+                                      const int* col, const float* w, const double* cst, bool collide,
+                                      cudaStream_t st);
 
 }  // namespace natgpu

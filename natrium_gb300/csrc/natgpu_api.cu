@@ -871,6 +871,7 @@ ThermalStepT<Real> thermal_step_params(nat_solver* s, int write_macro, const The
   P.ny = s->n_ax[1];
   P.nseg = (s->n_ax[0] + 31) / 32;
   P.write_macro = write_macro;
+  P.wall_bits = nullptr;
   P.tb = tb;
   P.M = M;
   return P;
@@ -892,13 +893,28 @@ ThermalPointT<Real> thermal_point_params(nat_solver* s, int in_init, const Therm
   return P;
 }
 
+// One fused step of the two-population lattice.  With walls (collide), the
+// wall nodes' sparse rows go first into the output buffers and the step kernel
+// collides those nodes with the rest (ThermalStepT::wall_bits).
+template <class Real>
+static cudaError_t thermal_launches(nat_solver* s, ThermalStepT<Real> P, const Real* wrow, bool collide, int form) {
+  if (collide && s->d_bn_bits && s->nbn > 0) {
+    cudaError_t e = launch_thermal_wall_nodes(P, s->nbn, s->d_bn_node, s->d_br_ptr, s->d_br_col, wrow, s->d_br_c,
+                                              false, s->stream);
+    if (e != cudaSuccess) return e;
+    s->launches++;
+    P.wall_bits = s->d_bn_bits;
+  }
+  return launch_thermal_step(P, collide, s->stream, form);
+}
+
 int launch_thermal(nat_solver* s, bool collide, int write_macro) {
   cudaError_t e;
   if (s->spec.precision == NAT_FP64)
-    e = launch_thermal_step(thermal_step_params<double>(s, write_macro, s->tt, s->tm), collide, s->stream, 0);
+    e = thermal_launches(s, thermal_step_params<double>(s, write_macro, s->tt, s->tm), s->d_br_w, collide, 0);
   else
-    e = launch_thermal_step(thermal_step_params<float>(s, write_macro, s->ttf, s->tmf), collide, s->stream,
-                            s->th_form);
+    e = thermal_launches(s, thermal_step_params<float>(s, write_macro, s->ttf, s->tmf), s->d_br_wf, collide,
+                         s->th_form);
   if (e != cudaSuccess) return cuda_fail(s, e, "two-population stream-collide launch");
   s->launches++;
   s->cur = 1 - s->cur;
@@ -1022,6 +1038,7 @@ int nat_destroy(nat_solver* s) {
   cudaFree(s->d_br_wf);
   cudaFree(s->d_br_c);
   cudaFree(s->d_bn_node);
+  cudaFree(s->d_bn_bits);
   cudaFree(s->d_mw);
   free_mapped_rows(s);
   delete s;
@@ -1573,6 +1590,7 @@ static int launch_collide(nat_solver* s, int in_init) {
 // same step (reads the pre-step buffer, overwrites the wall nodes).
 static int launch_wall_nodes(nat_solver* s, int write_macro) {
   if ((!s->walls && !s->mapped) || s->nbn == 0) return NAT_OK;
+  if (s->thermal && s->d_bn_bits) return NAT_OK;  // collided by the step kernel (launch_thermal)
   if (s->thermal) {
     // the step's buffers: launch_thermal toggled cur, so swap in and out
     cudaError_t e;
@@ -1583,7 +1601,7 @@ static int launch_wall_nodes(nat_solver* s, int write_macro) {
       P.f_out = static_cast<double*>(s->f[s->cur]);
       P.g_out = static_cast<double*>(s->g[s->cur]);
       e = launch_thermal_wall_nodes(P, s->nbn, s->d_bn_node, s->d_br_ptr, s->d_br_col, s->d_br_w, s->d_br_c,
-                                    s->stream);
+                                    true, s->stream);
     } else {
       ThermalStepT<float> P = thermal_step_params<float>(s, write_macro, s->ttf, s->tmf);
       P.f_in = static_cast<const float*>(s->f[1 - s->cur]);
@@ -1591,7 +1609,7 @@ static int launch_wall_nodes(nat_solver* s, int write_macro) {
       P.f_out = static_cast<float*>(s->f[s->cur]);
       P.g_out = static_cast<float*>(s->g[s->cur]);
       e = launch_thermal_wall_nodes(P, s->nbn, s->d_bn_node, s->d_br_ptr, s->d_br_col, s->d_br_wf, s->d_br_c,
-                                    s->stream);
+                                    true, s->stream);
     }
     if (e != cudaSuccess) return cuda_fail(s, e, "two-population wall nodes");
     s->launches += 2;  // rows, then the collision of the nodes

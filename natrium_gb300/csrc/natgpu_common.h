@@ -144,6 +144,10 @@ struct ThermalStepT {
   int* status;
   int n, nx, ny, nseg;
   int write_macro;
+  // wall nodes: one word per warp row segment (y nseg + x / 32), bit x % 32;
+  // their streamed values wait in f_out / g_out (written by k_thermal_rows
+  // before the step) and replace the lattice stencil's.  nullptr: no walls.
+  const unsigned* wall_bits;
   ThermalTablesT<Real> tb;
   ThermalModelT<Real> M;
 };

@@ -372,6 +372,8 @@ __global__ void __launch_bounds__(32 * W, (th_minb<FORM, sizeof(Real) == 4>()))
   // x position of this lane's first buffer slot (the buffer spans at most 64)
   const int gxa = ((x0 + P.tb.xl + lane) % nx + nx) % nx;
   const bool hasb = lane + 32 < P.tb.bw;
+  // wall node: its rows were streamed from the sparse rows into f_out / g_out
+  const bool wall = COLLIDE && P.wall_bits && ((__ldg(P.wall_bits + wid) >> lane) & 1u);
 
   // the step on the node's populations fs, gs (registers or shared memory)
   auto body = [&](auto& fs, auto& gs) {
@@ -446,6 +448,17 @@ __global__ void __launch_bounds__(32 * W, (th_minb<FORM, sizeof(Real) == 4>()))
 
   if (!valid) return;
   if constexpr (COLLIDE) {
+    if (wall) {
+      // the rows kernel's output: wait for that grid (a no-op unless this
+      // kernel was launched as its programmatic dependent); plain loads, this
+      // thread writes the same words below
+      asm volatile("griddepcontrol.wait;" ::: "memory");
+#pragma unroll
+      for (int q = 1; q < TH_Q; ++q) {
+        fs[q] = P.f_out[(long long)q * n + node];
+        gs[q] = P.g_out[(long long)q * n + node];
+      }
+    }
     Real ux = Real(0), uy = Real(0);
     double rho, T, kn;
     const int bad = thermal_relax<Real>(P.M, fs, gs, false, ux, uy, rho, T, kn);
@@ -473,14 +486,20 @@ __global__ void __launch_bounds__(32 * W, (th_minb<FORM, sizeof(Real) == 4>()))
   }
 }
 
-// Wall nodes of the two-population model, in two passes that keep the GPU
-// busy although the wall nodes are few:
+// Wall nodes of the two-population model:
 //  1. k_thermal_rows: one thread per sparse row (node, direction) streams f
 //     and g of that row into the output buffers (constant slots: f, g);
-//  2. k_thermal_collide_nodes: one thread per wall node collides its streamed
-//     values (rest population from the input) and writes f, g and the fields.
+//  2. the collision of those nodes: on the Cartesian lattice k_thermal_step
+//     itself (launched after the rows as their programmatic dependent, so
+//     the lattice streams while the rows run; ThermalStepT::wall_bits marks
+//     the nodes, whose lanes wait for the rows grid); on mapped cells, where every node is a wall node,
+//     k_thermal_collide_nodes, one thread per node, rest population from the
+//     input.
 // (One thread walking all 24 rows of its node, ~430 dependent loads, left
-// the few hundred warps latency-bound: ~50 us for 3,000 nodes.)
+// the few hundred warps latency-bound: ~50 us for 3,000 nodes.  A separate
+// collision pass after the step cost 11.7 us (FP32) / 31 us (FP64) per step
+// on the 128 x 128 cell, order-2 two-dimensional Riemann problem with four
+// open faces.)
 template <class Real>
 __global__ void __launch_bounds__(256) k_thermal_rows(const __grid_constant__ ThermalStepT<Real> P, int nrows,
                                                       const int* __restrict__ bnode, const int* __restrict__ ptr,
@@ -488,6 +507,8 @@ __global__ void __launch_bounds__(256) k_thermal_rows(const __grid_constant__ Th
                                                       const double* __restrict__ cst) {
   constexpr bool DEV = sizeof(Real) == 4;
   const int n = P.n;
+  // the step kernel may start now (its wall lanes wait for this grid)
+  asm volatile("griddepcontrol.launch_dependents;");
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
     const int node = bnode[r / (TH_Q - 1)];
     const int a = r % (TH_Q - 1) + 1;

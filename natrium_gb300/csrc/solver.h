@@ -81,6 +81,8 @@ struct nat_solver {
   double* d_br_c = nullptr;      // per row: f const, f const (deviation form), g const, g const (deviation)
   int nbn = 0;                   // wall nodes: nodes with a row that meets a wall; their
   int* d_bn_node = nullptr;      // Q - 1 rows are rows k (Q-1) .. k (Q-1) + Q - 2 above
+  unsigned* d_bn_bits = nullptr; // two-population Cartesian lattice: the wall nodes as bits,
+                                 // one word per 32-node x segment of a row (ThermalStepT)
   // MappingQ1 cells: every node is a "wall node" (all rows sparse), the
   // Cartesian fused kernels are not used
   bool mapped = false;

@@ -19,7 +19,19 @@ cudaError_t thermal_step_form(const ThermalStepT<Real>& P, bool collide, cudaStr
   void* args[] = {const_cast<ThermalStepT<Real>*>(&P)};
   const void* fn = collide ? (const void*)k_thermal_step<Real, true, W, FORM, PC>
                            : (const void*)k_thermal_step<Real, false, W, FORM, PC>;
-  return cudaLaunchKernel(fn, dim3(grid), dim3(32 * W), args, 0, st);
+  if (!P.wall_bits) return cudaLaunchKernel(fn, dim3(grid), dim3(32 * W), args, 0, st);
+  // after k_thermal_rows: programmatic dependent launch, the lattice streams
+  // while the rows run; the wall lanes wait for them (griddepcontrol.wait)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(32 * W);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 cudaError_t launch_thermal_step_p2(const ThermalStepT<double>& P, bool collide, cudaStream_t st, int form);

@@ -355,6 +355,8 @@ int build_wall_rows(nat_solver* s) {
   cudaFree(s->d_br_wf);
   cudaFree(s->d_br_c);
   cudaFree(s->d_bn_node);
+  cudaFree(s->d_bn_bits);
+  s->d_bn_bits = nullptr;
   s->d_br_dst = s->d_br_ptr = s->d_br_col = s->d_bn_node = nullptr;
   s->d_br_w = s->d_br_c = nullptr;
   s->d_br_wf = nullptr;
@@ -531,6 +533,23 @@ int build_wall_rows(nat_solver* s) {
   }
   CK(cudaMemcpy(s->d_br_c, cst.data(), sizeof(double) * cst.size(), cudaMemcpyHostToDevice), "wall rows");
   CK(cudaMemcpy(s->d_bn_node, bnodes.data(), sizeof(int) * bnodes.size(), cudaMemcpyHostToDevice), "wall nodes");
+  if (s->thermal && !s->mapped && !bnodes.empty()) {
+    // the two-population step collides the wall nodes itself: mark them per
+    // 32-node x segment of a row (node = y nx + x)
+    const int nx = s->n_ax[0], nseg = (nx + 31) / 32;
+    std::vector<unsigned> bits((size_t)nseg * s->n_ax[1], 0u);
+    for (int v : bnodes) {
+      const int y = v / nx, x = v % nx;
+      if (v < 0 || y >= s->n_ax[1]) return fail(s, NAT_ERR_CUDA, "internal error: wall node %d out of range", v);
+      bits[(size_t)y * nseg + x / 32] |= 1u << (x % 32);
+    }
+    if (cudaMalloc((void**)&s->d_bn_bits, sizeof(unsigned) * bits.size()) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(s, NAT_ERR_OOM, "cudaMalloc(%zu) failed", sizeof(unsigned) * bits.size());
+    }
+    CK(cudaMemcpy(s->d_bn_bits, bits.data(), sizeof(unsigned) * bits.size(), cudaMemcpyHostToDevice),
+       "wall node bits");
+  }
   return NAT_OK;
 }
 

@@ -205,6 +205,49 @@ def test_walls_compressible_model_matches_oracle(gpu_lib):
     assert rel_l2(T, T1) <= 1e-12
 
 
+THERMAL_WALL_FORMS = [("fp64", 0), ("fp32dev", 0), ("fp32dev", 1), ("fp32dev", 2)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bc", [(0, 0, 1, 1, 0, 0), (2, 2, 2, 2, 0, 0)], ids=["moving walls y", "do-nothing all"])
+@pytest.mark.parametrize("precision,form", THERMAL_WALL_FORMS,
+                         ids=["fp64", "fp32-registers", "fp32-smem-20-warps", "fp32-smem-24-warps"])
+def test_walls_compressible_model_fused_forms(gpu_lib, bc, precision, form):
+    """The step kernel collides the wall nodes of the two-population model
+    after their sparse rows: 36 nodes along x (two 32-node row segments, the
+    second partial) so the per-segment wall words of both segments are used,
+    in every kernel form."""
+    uw = ((0, 0, 0), (0, 0, 0), (0.05, 0, 0), (-0.05, 0, 0), (0, 0, 0), (0, 0, 0))
+    st = O.stencil("D2Q25H", 1.0)
+    m = O.Mesh(2, (12, 4), 2, True, (1.0, 1.0), bc=bc, uw=uw)
+    dt = O.time_step(m.h_min(), 2, st.max_speed, 0.4)
+    nu = 1e-3
+    tau = nu / (dt * st.cs2) + 0.5
+    from tests.gpu_cases import thermal_state
+    rho0, u0, T0, f0, g0 = thermal_state(m, st, seed=6)
+    S = O.SLOperator(m, st, dt)
+    f1, g1 = f0.copy(), g0.copy()
+    r1, u1, T1, m1 = S.step_compressible(f1, g1, tau, nsteps=3)
+    periodic = (bc[0] == 0, False, True)
+    spec = N.SolverSpec(stencil="D2Q25H", order=2, cells=(12, 4), length=(1.0, 1.0), scaling=1.0, viscosity=nu,
+                        dt=dt, collision="BGK_COMPRESSIBLE", precision=precision, topology="dg", periodic=periodic)
+    with N.Solver(spec) as sol:
+        _set_walls(sol, bc, uw, 1.0)
+        if precision == "fp32dev":
+            sol.select_candidate(form)
+        sol.upload_f(f0)
+        sol.upload_g(g0)
+        sol.step(3)
+        f, g = sol.download_f(), sol.download_g()
+        T, _ = sol.download_thermal()
+        r, _ = sol.download_macro()
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    assert rel_l2(f, f1) <= tol
+    assert rel_l2(g, g1) <= tol
+    assert rel_l2(T, T1) <= tol
+    assert rel_l2(r, r1) <= tol
+
+
 def test_walls_need_dg_topology():
     spec = N.SolverSpec(stencil="D2Q9", order=2, cells=(2, 2), length=(1, 1), scaling=1.0, viscosity=0.1,
                         topology="feq", periodic=(True, False, True))
