@@ -381,12 +381,15 @@ int nat_device_f(nat_solver* s, void** f_dev);
 int nat_set_kernel_variant(nat_solver* s, int variant);
 /* The fused-step kernel in use: 1 generic, 2 tile, 3 row-segment,
  * 5 two-population row-segment kernel (NAT_BGK_COMPRESSIBLE; 9 and 10: its
- * FP32 forms with f and g in shared memory, 20 / 24 resident warps per SM),
+ * FP32 forms with f and g in shared memory, 20 / 24 resident warps per SM;
+ * 14: its FP32 register form at order 2 with the window rows copied into
+ * shared memory asynchronously, one direction ahead),
  * 6 bulk-copy row-segment kernel, 7 row-group kernel, 8 departure-point
  * kernel of mapped (MappingQ1) meshes, 11 cell-row kernel, 12 cell-row
  * kernel with tensor-core corner directions, 13 cell-row kernel with z
- * sharing.  nat_autotune chooses among 5, 9
- * and 10 for an FP32 two-population handle. */
+ * sharing.  nat_autotune chooses among 5, 9 and 10 (and 14 at order 2) for
+ * an FP32 two-population handle; nat_select_candidate takes their index
+ * 0-2 (3). */
 int nat_kernel_variant(const nat_solver* s);
 
 /* Autotuner: times `steps` fused steps with every kernel that applies to

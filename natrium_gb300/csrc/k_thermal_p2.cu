@@ -10,6 +10,7 @@ static cudaError_t step_p2(const ThermalStepT<Real>& P, bool collide, cudaStream
   if constexpr (sizeof(Real) == 4) {
     if (form == 1) return thermal_step_form<Real, 1, 2>(P, collide, st);
     if (form == 2) return thermal_step_form<Real, 2, 2>(P, collide, st);
+    if (form == 3) return thermal_step_form<Real, 3, 2>(P, collide, st);
   }
   return thermal_step_form<Real, 0, 2>(P, collide, st);
 }

@@ -1752,10 +1752,17 @@ int nat_set_kernel_variant(nat_solver* s, int variant) {
   return select_v2(s, coll_selector(s->spec.collision), smem_optin);
 }
 
+// The two-population kernel's forms (sl_thermal.cuh) as kernel variants:
+// 0 -> 5 (registers), 1 / 2 -> 9 / 10 (shared memory), 3 -> 14 (registers,
+// staged rows); the forms an FP32 handle can choose from (form 3: order 2).
+static int th_variant(int form) { return form == 0 ? 5 : (form == 3 ? 14 : 8 + form); }
+static int th_forms(const nat_solver* s) { return s->ttf.p == 2 ? 4 : 3; }
+static int th_threads(int form) { return 32 * ((form == 1 || form == 2) ? TH_WARPS_SS : TH_WARPS); }
+
 int nat_kernel_variant(const nat_solver* s) {
   if (!s) return -1;
   if (s->mapped && !s->thermal) return 8;
-  if (s->thermal) return s->th_form == 0 ? 5 : 8 + s->th_form;
+  if (s->thermal) return th_variant(s->th_form);
   return s->use_v2 ? s->kind : 1;
 }
 
@@ -1782,7 +1789,8 @@ static int tune_candidates(nat_solver* s, std::vector<Cand>* cand, int* ncand) {
 int nat_select_candidate(nat_solver* s, int index) {
   if (!s) return NAT_ERR_INVALID_ARG;
   if (s->thermal && s->spec.precision != NAT_FP64 && !s->mapped) {
-    if (index < 0 || index > 2) return fail(s, NAT_ERR_INVALID_ARG, "candidate %d of 3", index);
+    if (index < 0 || index >= th_forms(s))
+      return fail(s, NAT_ERR_INVALID_ARG, "candidate %d of %d", index, th_forms(s));
     s->th_form = index;
     return NAT_OK;
   }
@@ -1798,9 +1806,9 @@ int nat_select_candidate(nat_solver* s, int index) {
   return NAT_OK;
 }
 
-// The two-population fused kernel in FP32: time its three forms (f and g
-// backed up in the staging buffer, which holds Q n_ref doubles >= 2 Q n_dev
-// floats) and keep the fastest.
+// The two-population fused kernel in FP32: time its forms (three; four at
+// order 2, which has the staged form), with f and g backed up in the staging
+// buffer (Q n_ref doubles >= 2 Q n_dev floats), and keep the fastest.
 static int autotune_thermal(nat_solver* s, int steps, int* n_candidates, int* chosen) {
   const size_t pop = sizeof(float) * (size_t)s->Q * s->n_dev;
   const int cur0 = s->cur, form0 = s->th_form;
@@ -1814,7 +1822,7 @@ static int autotune_thermal(nat_solver* s, int steps, int* n_candidates, int* ch
   s->at_desc.clear();
   float best = 1e30f;
   int best_i = -1, rc = NAT_OK;
-  for (int form = 0; form < 3 && !rc; ++form) {
+  for (int form = 0; form < th_forms(s) && !rc; ++form) {
     s->th_form = form;
     rc = nat_step_async(s, 1, 0);
     if (rc) break;
@@ -1828,7 +1836,7 @@ static int autotune_thermal(nat_solver* s, int steps, int* n_candidates, int* ch
     }
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
-    const int desc[5] = {form == 0 ? 5 : 8 + form, 32, 1, 1, 32 * (form == 0 ? TH_WARPS : TH_WARPS_SS)};
+    const int desc[5] = {th_variant(form), 32, 1, 1, th_threads(form)};
     s->at_ms.push_back(ms / steps);
     s->at_desc.insert(s->at_desc.end(), desc, desc + 5);
     if (ms < best) {
@@ -1849,7 +1857,7 @@ static int autotune_thermal(nat_solver* s, int steps, int* n_candidates, int* ch
     return rc;
   }
   s->th_form = best_i;
-  if (n_candidates) *n_candidates = 3;
+  if (n_candidates) *n_candidates = th_forms(s);
   if (chosen) *chosen = best_i;
   return NAT_OK;
 }
@@ -1957,7 +1965,7 @@ int nat_kernel_info(const nat_solver* s, int* variant, int tile_nodes[3], int* t
       tile_nodes[1] = 1;
       tile_nodes[2] = 1;
     }
-    if (threads) *threads = 32 * (s->th_form == 0 ? TH_WARPS : TH_WARPS_SS);
+    if (threads) *threads = th_threads(s->th_form);
     if (smem_bytes) *smem_bytes = 0;
     return NAT_OK;
   }

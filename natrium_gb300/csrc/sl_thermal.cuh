@@ -339,6 +339,28 @@ constexpr int th_minb() {
   return FORM == 1 ? 5 : (FORM == 2 ? 6 : (F32 ? 2 : 1));
 }
 
+// warps per CTA of each form (3: the register form with staged rows)
+template <int FORM>
+constexpr int th_warps() {
+  return (FORM == 1 || FORM == 2) ? TH_WARPS_SS : TH_WARPS;
+}
+
+// 4-byte asynchronous global -> shared copies (the staged form's rows)
+__device__ __forceinline__ void th_cp_async4(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void th_cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void th_cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// FORM 3 (FP32, compile-time order): the register form whose y-window rows
+// arrive by cp.async in a per-warp double buffer, one direction ahead: the
+// register form waits on its global loads (long-scoreboard stalls, 16
+// resident warps at 124 registers); the copies in flight hold no registers.
+//
 // PC > 0: the order p as a compile-time constant (the window loops then run
 // over p + 1 slots instead of PMAX1 predicated ones); PC = 0: any order.
 template <class Real, bool COLLIDE, int W = TH_WARPS, int FORM = 0, int PC = 0>
@@ -347,9 +369,17 @@ __global__ void __launch_bounds__(32 * W, (th_minb<FORM, sizeof(Real) == 4>()))
   __shared__ Real swx[ND_MAX][PER_MAX][PMAX1];
   __shared__ int soffx[ND_MAX][PER_MAX];
   __shared__ int sj0x[ND_MAX][PER_MAX];
-  constexpr bool SS = FORM > 0;
+  constexpr bool SS = FORM == 1 || FORM == 2;
+  constexpr bool STG = FORM == 3;
+  static_assert(!STG || (PC > 0 && PC < PMAX1 && sizeof(Real) == 4), "staged form: FP32, compile-time order");
+  constexpr int NR = STG ? PC + 1 : 1;  // rows of a y window
+  // stage buffers: directions in flight + 1 (three, two directions ahead,
+  // measured the same as two on the 128 x 128-cell order-2 problem)
+  constexpr int NB = STG ? 2 : 1;
   __shared__ Real bufs[W][4][TH_BWMAX + 1];
   __shared__ Real pops[SS ? W : 1][2][SS ? TH_Q : 1][32];
+  // [warp][buffer][f, g][window row][x slot]
+  __shared__ Real stg[STG ? W : 1][NB][2][NR][STG ? TH_BWMAX : 1];
   for (int i = threadIdx.x; i < ND_MAX * PER_MAX * PMAX1; i += blockDim.x)
     (&swx[0][0][0])[i] = (&P.tb.w[0][0][0][0])[i];
   for (int i = threadIdx.x; i < ND_MAX * PER_MAX; i += blockDim.x) {
@@ -372,11 +402,45 @@ __global__ void __launch_bounds__(32 * W, (th_minb<FORM, sizeof(Real) == 4>()))
   // x position of this lane's first buffer slot (the buffer spans at most 64)
   const int gxa = ((x0 + P.tb.xl + lane) % nx + nx) % nx;
   const bool hasb = lane + 32 < P.tb.bw;
+  int gxb = gxa + 32;  // x position of the lane's second buffer slot
+  while (gxb >= nx) gxb -= nx;
   // wall node: its rows were streamed from the sparse rows into f_out / g_out
   const bool wall = COLLIDE && P.wall_bits && ((__ldg(P.wall_bits + wid) >> lane) & 1u);
 
   // the step on the node's populations fs, gs (registers or shared memory)
+  // FORM 3: copy direction A's window rows (its lane slots: the node's own x,
+  // or the buffer slots gxa and gxb) into stage buffer A % NB; one commit
+  // group per direction (empty past the last)
+  auto stage = [&](auto Ac) {
+    if constexpr (STG) {
+      constexpr int A = decltype(Ac)::value;
+      if constexpr (A < TH_Q) {
+        constexpr int dx = SD2Q25H::dcls(A, 0), dy = SD2Q25H::dcls(A, 1);
+        constexpr int b = A % NB;
+        const Real* fsrc = P.f_in + (long long)A * n;
+        const Real* gsrc = P.g_in + (long long)A * n;
+        const int ys = dy >= 0 ? y + P.tb.offy[dy < 0 ? 0 : dy][cy] : y;
+        const int ca = dx < 0 ? xs : gxa;
+#pragma unroll
+        for (int j = 0; j < (dy >= 0 ? NR : 1); ++j) {
+          int rr = ys + j;
+          rr -= rr >= ny ? ny : 0;
+          rr -= rr >= ny ? ny : 0;
+          const int o = rr * nx;
+          th_cp_async4(&stg[warp][b][0][j][lane], fsrc + o + ca);
+          th_cp_async4(&stg[warp][b][1][j][lane], gsrc + o + ca);
+          if (dx >= 0 && hasb) {
+            th_cp_async4(&stg[warp][b][0][j][lane + 32], fsrc + o + gxb);
+            th_cp_async4(&stg[warp][b][1][j][lane + 32], gsrc + o + gxb);
+          }
+        }
+      }
+      th_cp_async_commit();
+    }
+  };
+
   auto body = [&](auto& fs, auto& gs) {
+  static_for<1, NB>([&](auto Sc) { stage(IC<decltype(Sc)::value>{}); });
   fs[0] = P.f_in[node];
   gs[0] = P.g_in[node];
 
@@ -388,8 +452,34 @@ __global__ void __launch_bounds__(32 * W, (th_minb<FORM, sizeof(Real) == 4>()))
     // warp-uniform y window start (y + offy + j < 2 ny + p < 3 ny: two
     // conditional subtractions wrap a row index)
     const int ys = dy >= 0 ? y + P.tb.offy[dy < 0 ? 0 : dy][cy] : y;
-    auto ysum = [&](int gx, Real& vf, Real& vg) {
-      if constexpr (dy >= 0) {
+    if constexpr (STG) {
+      // the next NB - 1 directions' rows in flight; this direction's rows
+      // (this lane's own copies) have landed
+      stage(IC<A + NB - 1>{});
+      th_cp_async_wait<NB - 1>();
+    }
+    // the y-window sums at x position gx (stage slot col in FORM 3)
+    auto ysum = [&](int gx, int col, Real& vf, Real& vg) {
+      if constexpr (STG) {
+        constexpr int b = A % NB;
+        if constexpr (dy >= 0) {
+          Real af[PMAX1], ag[PMAX1];
+#pragma unroll
+          for (int j = 0; j < PMAX1; ++j) {
+            af[j] = Real(0);
+            ag[j] = Real(0);
+            if (j < NR) {
+              af[j] = stg[warp][b][0][j < NR ? j : 0][col];
+              ag[j] = stg[warp][b][1][j < NR ? j : 0][col];
+            }
+          }
+          vf = th_wsum<Real>(P.tb.w[1][dy][cy], af, p, P.tb.j0[1][dy][cy]);
+          vg = th_wsum<Real>(P.tb.w[1][dy][cy], ag, p, P.tb.j0[1][dy][cy]);
+        } else {
+          vf = stg[warp][b][0][0][col];
+          vg = stg[warp][b][1][0][col];
+        }
+      } else if constexpr (dy >= 0) {
         Real af[PMAX1], ag[PMAX1];
 #pragma unroll
         for (int j = 0; j < PMAX1; ++j) {
@@ -412,19 +502,17 @@ __global__ void __launch_bounds__(32 * W, (th_minb<FORM, sizeof(Real) == 4>()))
       }
     };
     if constexpr (dx < 0) {
-      ysum(xs, fs[A], gs[A]);
+      ysum(xs, lane, fs[A], gs[A]);
     } else {
       Real* bf = &bufs[warp][(th_xorder(A) & 1) * 2][0];
       Real* bg = &bufs[warp][(th_xorder(A) & 1) * 2 + 1][0];
       {
         Real vf, vg;
-        ysum(gxa, vf, vg);
+        ysum(gxa, lane, vf, vg);
         bf[lane] = vf;
         bg[lane] = vg;
         if (hasb) {
-          int gxb = gxa + 32;
-          while (gxb >= nx) gxb -= nx;
-          ysum(gxb, vf, vg);
+          ysum(gxb, lane + 32, vf, vg);
           bf[lane + 32] = vf;
           bg[lane + 32] = vg;
         }

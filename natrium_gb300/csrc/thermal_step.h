@@ -9,11 +9,12 @@
 namespace natgpu {
 
 // form: 0 register form (TH_WARPS warps per CTA), 1 / 2 shared-memory forms
-// (TH_WARPS_SS warps per CTA, FP32 only; sl_thermal.cuh); PC: the order as a
-// compile-time constant, 0 for any
+// (TH_WARPS_SS warps per CTA, FP32 only), 3 the register form with staged
+// rows (FP32, order 2 only; sl_thermal.cuh); PC: the order as a compile-time
+// constant, 0 for any
 template <class Real, int FORM, int PC>
 cudaError_t thermal_step_form(const ThermalStepT<Real>& P, bool collide, cudaStream_t st) {
-  constexpr int W = FORM > 0 ? TH_WARPS_SS : TH_WARPS;
+  constexpr int W = th_warps<FORM>();
   const int warps = P.nseg * P.ny;
   const int grid = (warps + W - 1) / W;
   void* args[] = {const_cast<ThermalStepT<Real>*>(&P)};

@@ -277,6 +277,43 @@ def test_fp32_kernel_forms_close_to_oracle(gpu_lib, form, settings):
     assert rel_l2(T, T1) <= 1e-6
 
 
+STAGED_CASES = [((5, 4), True), ((12, 6), True), ((12, 6), False)]
+
+
+@pytest.mark.parametrize("cells,dg", STAGED_CASES, ids=["dg-15-nodes", "dg-36-nodes", "feq-24-nodes"])
+def test_fp32_staged_form_order2_close_to_oracle(gpu_lib, cells, dg):
+    """Order 2 has a fourth FP32 form (variant 14): the register form whose
+    y-window rows arrive by cp.async one direction ahead.  Rows narrower
+    than a warp (the buffer slots wrap more than once) and rows of two
+    32-node segments, DG and FE_Q; the same values as the register form, and
+    the autotuner offers all four forms."""
+    st, mesh, dt, tau, spec = thermal_case(cells, 2, dg, scaling=1.2)
+    rho0, u0, T0, f0, g0 = thermal_state(mesh, st, seed=21)
+    S = O.SLOperator(mesh, st, dt)
+    f1, g1 = f0.copy(), g0.copy()
+    r1, u1, T1, m1 = S.step_compressible(f1, g1, tau, nsteps=3)
+    out = {}
+    for form in (0, 3):
+        with N.Solver(_spec32(spec)) as sol:
+            sol.select_candidate(form)
+            assert sol.kernel_variant == (5 if form == 0 else 14)
+            sol.upload_f(f0)
+            sol.upload_g(g0)
+            sol.step(3)
+            out[form] = (sol.download_f(), sol.download_g(), sol.download_thermal()[0])
+            if form == 3:
+                n, ch = sol.autotune(2)
+                rep = sol.autotune_report()
+                assert n == 4 and [r["variant"] for r in rep] == [5, 9, 10, 14]
+                assert sol.kernel_variant == rep[ch]["variant"]
+    f, g, T = out[3]
+    assert rel_l2(f, f1) <= 1e-6
+    assert rel_l2(g, g1) <= 1e-6
+    assert rel_l2(T, T1) <= 1e-6
+    for a, b in zip(out[3], out[0]):
+        assert rel_l2(a, b) <= 1e-7
+
+
 def test_fp32_initialisation_and_uniform_state(gpu_lib):
     st, mesh, dt, tau, spec = thermal_case((4, 4), 2, False, scaling=1.1)
     n = mesh.n_nodes

@@ -205,13 +205,13 @@ def test_walls_compressible_model_matches_oracle(gpu_lib):
     assert rel_l2(T, T1) <= 1e-12
 
 
-THERMAL_WALL_FORMS = [("fp64", 0), ("fp32dev", 0), ("fp32dev", 1), ("fp32dev", 2)]
+THERMAL_WALL_FORMS = [("fp64", 0), ("fp32dev", 0), ("fp32dev", 1), ("fp32dev", 2), ("fp32dev", 3)]
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("bc", [(0, 0, 1, 1, 0, 0), (2, 2, 2, 2, 0, 0)], ids=["moving walls y", "do-nothing all"])
 @pytest.mark.parametrize("precision,form", THERMAL_WALL_FORMS,
-                         ids=["fp64", "fp32-registers", "fp32-smem-20-warps", "fp32-smem-24-warps"])
+                         ids=["fp64", "fp32-registers", "fp32-smem-20-warps", "fp32-smem-24-warps", "fp32-staged"])
 def test_walls_compressible_model_fused_forms(gpu_lib, bc, precision, form):
     """The step kernel collides the wall nodes of the two-population model
     after their sparse rows: 36 nodes along x (two 32-node row segments, the
