@@ -317,7 +317,11 @@ def open_boundaries(sol):
         sol.set_boundary(face, "DO_NOTHING")
 
 
-def _compressible_leg(torch, stream, flush, precision, steps, warmup, full_run):
+# the FP32 two-population kernel's forms by kernel variant (nat_select_candidate index)
+TH_FORMS = {5: 0, 9: 1, 10: 2, 14: 3}
+
+
+def _compressible_leg(torch, stream, flush, precision, steps, warmup, full_run, variant=0):
     import natrium_gb300 as N
     from natrium_gb300 import problems as P
     c = COMPRESSIBLE
@@ -329,7 +333,10 @@ def _compressible_leg(torch, stream, flush, precision, steps, warmup, full_run):
     sol.set_stream(stream.cuda_stream)
     sol.init_thermal(rho, u, T)
     if precision != "fp64":
-        sol.autotune(10)  # FP32: register or shared-memory form of the fused kernel
+        if variant:  # a pinned form (a launch list of the form the autotuner picks outside ncu)
+            sol.select_candidate(TH_FORMS[variant])
+        else:
+            sol.autotune(10)  # FP32: register, shared-memory or staged-row form of the fused kernel
     per, launches = time_device(sol, torch, stream, flush, steps, warmup)
     ms = sum(per) / steps
     n = sol.n_dev
@@ -363,16 +370,18 @@ def _compressible_leg(torch, stream, flush, precision, steps, warmup, full_run):
     return out, n, fields
 
 
-def bench_compressible(torch, stream, flush, steps: int = 200, warmup: int = 5, full_run: bool = True):
+def bench_compressible(torch, stream, flush, steps: int = 200, warmup: int = 5, full_run: bool = True,
+                       variant: int = 0):
     """The compressible two-population path (D2Q25H, quartic BGK with g) on
     the four-quadrant Riemann problem: 128^2 cells, FE_DGQ p = 2 (147,456
     nodes x 25 x 2 populations), do-nothing (extrapolation) boundaries.  FP32
     deviation storage (the configuration's storage) and plain FP64, each
     device-timed; with full_run
     both also run to t = 0.3 and the FP32 fields are compared with the FP64
-    ones (the FP64 path matches the oracle to 1e-12 per step)."""
+    ones (the FP64 path matches the oracle to 1e-12 per step).  variant
+    (5, 9, 10, 14) pins the FP32 kernel form instead of autotuning it."""
     c = COMPRESSIBLE
-    o32, n, F32 = _compressible_leg(torch, stream, flush, "fp32dev", steps, warmup, full_run)
+    o32, n, F32 = _compressible_leg(torch, stream, flush, "fp32dev", steps, warmup, full_run, variant)
     o64, _, F64 = _compressible_leg(torch, stream, flush, "fp64", max(20, steps // 4), warmup, full_run)
     out = {"workload": c["name"], "nodes": n, "dtype": "f32", "unit": UNIT, "value": o32["value"],
            "ms_per_step": o32["ms_per_step"], "fp32dev": o32, "fp64": o64,
@@ -739,7 +748,7 @@ def run_ours(args):
         return 0
     if args.compressible_only:
         print(json.dumps(bench_compressible(torch, stream, flush, steps=args.steps, warmup=args.warmup,
-                                            full_run=not args.profile)))
+                                            full_run=not args.profile, variant=args.variant)))
         return 0
 
     vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
@@ -930,7 +939,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--variant", type=int, default=0,
                     help="fused kernel: 0 autotuned, 1 generic, 3 tile, 4 row-segment, 6 bulk-copy row-segment, "
-                         "7 row-group, 11 cell-row, 12 cell-row with tensor-core corners (D3Q27 FP32)")
+                         "7 row-group, 11 cell-row, 12 cell-row with tensor-core corners (D3Q27 FP32); with "
+                         "--compressible-only the FP32 two-population form: 5 registers, 9 / 10 shared memory, "
+                         "14 staged rows")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--candidate", type=int, default=-1,
                     help="with --profile: use this autotuner candidate without timing")
