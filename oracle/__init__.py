@@ -74,6 +74,7 @@ def lib():
         L.orc_sl_lifetime_hits.argtypes = [C.c_void_p]
         L.orc_sl_csr.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int32), dp]
         L.orc_sl_stream.argtypes = [C.c_void_p, dp, dp, C.c_int]
+        L.orc_sl_stream_g.argtypes = [C.c_void_p, dp, dp, C.c_int]
         L.orc_sl_csr_dirs.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int32)]
         L.orc_sl_bconst.argtypes = [C.c_void_p, C.c_int, dp]
         L.orc_sl_wall_hits.argtypes = [C.c_void_p]
@@ -292,6 +293,15 @@ class SLOperator:
         f = np.ascontiguousarray(f, dtype=np.float64)
         out = np.empty_like(f)
         lib().orc_sl_stream(self._h, _dp(f), _dp(out), nthreads)
+        return out
+
+    def stream_g(self, g: np.ndarray, nthreads: int = 1) -> np.ndarray:
+        """The compressible model's second population through the same
+        operator without the wall-velocity terms (CompressibleCFDSolver::gStream,
+        CompressibleCFDSolver.h:279-314)."""
+        g = np.ascontiguousarray(g, dtype=np.float64)
+        out = np.empty_like(g)
+        lib().orc_sl_stream_g(self._h, _dp(g), _dp(out), nthreads)
         return out
 
     def step_bgk(self, f, tau, nsteps=1, nthreads=1):
