@@ -407,7 +407,6 @@ __global__ void __launch_bounds__(32 * W, (th_minb<FORM, sizeof(Real) == 4>()))
   // wall node: its rows were streamed from the sparse rows into f_out / g_out
   const bool wall = COLLIDE && P.wall_bits && ((__ldg(P.wall_bits + wid) >> lane) & 1u);
 
-  // the step on the node's populations fs, gs (registers or shared memory)
   // FORM 3: copy direction A's window rows (its lane slots: the node's own x,
   // or the buffer slots gxa and gxb) into stage buffer A % NB; one commit
   // group per direction (empty past the last)
@@ -439,6 +438,7 @@ __global__ void __launch_bounds__(32 * W, (th_minb<FORM, sizeof(Real) == 4>()))
     }
   };
 
+  // the step on the node's populations fs, gs (registers or shared memory)
   auto body = [&](auto& fs, auto& gs) {
   static_for<1, NB>([&](auto Sc) { stage(IC<decltype(Sc)::value>{}); });
   fs[0] = P.f_in[node];
